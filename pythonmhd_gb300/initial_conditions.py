@@ -1,0 +1,185 @@
+"""Host-side initial states for the 2D step (inputs, not part of the hot path).
+
+* ``orszag_tang``: the Orszag-Tang vortex of the reference's sample script
+  (InitializationFiles/SampleSimulations/2D_MHD/OrszagTang_InitializationFile.py:117-194),
+  optionally with face B taken from the corner vector potential (the form the
+  4096^2 / batched workloads use) instead of the cell-averaged faces the
+  reference's ``SimulationGrid`` builds when no faces are passed
+  (Source/SimulationGrid.py:147-156).
+* ``turbulence``: the seeded driven-free turbulence state (Gaussian random
+  density, velocity and vector-potential fields with power-law spectra).
+* ``prim_to_cons_mhd`` / ``prim_to_cons_hydro``: the conserved variables the
+  reference's grid derives at construction
+  (Source/PrimCons_HelperModule.py:23-35 and :314-340).
+
+Spectral convention (frozen): a field with "power ~ k^-a for k1 <= |k| <= k2"
+is ``irfft2`` of complex coefficients c(kx, ky) = (N(0,1) + i N(0,1)) * |k|^(-a/2)
+on the integer wavevectors of the periodic box with k1 <= |k| <= k2, zero
+elsewhere (per-mode power, not shell power), drawn from
+``numpy.random.default_rng(seed)`` in the order g, vx, vy, Az, then shifted to
+zero mean and scaled as each field requires.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+OUTFLOW = 0
+PERIODIC = 1
+
+
+def cell_centres(n, lo, hi):
+    d = (hi - lo) / n
+    return lo + (np.arange(n) + 0.5) * d, d
+
+
+def prim_to_cons_mhd(prim, gamma):
+    """Conserved 8-vector from the primitive 8-vector (same arithmetic order as the reference)."""
+    p = np.asarray(prim, dtype=np.float64)
+    c = np.empty_like(p)
+    c[0] = p[0]
+    c[1] = p[0] * p[1]
+    c[2] = p[0] * p[2]
+    c[3] = p[0] * p[3]
+    c[4] = p[4]
+    c[5] = p[5]
+    c[6] = p[6]
+    c[7] = p[7] / (gamma - 1.0) + 0.5 * p[0] * (p[1] * p[1] + p[2] * p[2] + p[3] * p[3])
+    c[7] += 0.5 * (p[4] * p[4] + p[5] * p[5] + p[6] * p[6])
+    return c
+
+
+def prim_to_cons_hydro(prim, gamma):
+    p = np.asarray(prim, dtype=np.float64)
+    c = np.empty_like(p)
+    c[0] = p[0]
+    c[1] = p[0] * p[1]
+    c[2] = p[0] * p[2]
+    c[3] = p[0] * p[3]
+    c[4] = (p[4] / (gamma - 1.0)) + 0.5 * p[0] * (np.square(p[1]) + np.square(p[2]) + np.square(p[3]))
+    return c
+
+
+def faces_from_cells(bx, by, bcx, bcy):
+    """Face B as the mean of the two neighbouring cell values (Source/CT_HelperModule.py:29-70)."""
+    if bcx == OUTFLOW:
+        lx = np.concatenate([bx[:, :1], bx], axis=1)
+        rx = np.concatenate([bx, bx[:, -1:]], axis=1)
+    else:
+        lx = np.concatenate([bx[:, -1:], bx], axis=1)
+        rx = np.concatenate([bx, bx[:, :1]], axis=1)
+    if bcy == OUTFLOW:
+        ty = np.concatenate([by[:1], by], axis=0)
+        by_ = np.concatenate([by, by[-1:]], axis=0)
+    else:
+        ty = np.concatenate([by[-1:], by], axis=0)
+        by_ = np.concatenate([by, by[:1]], axis=0)
+    return (lx + rx) / 2.0, (ty + by_) / 2.0
+
+
+def faces_from_potential(az):
+    """Periodic face B from a corner vector potential az[j, i] at (x_i - dx/2, y_j - dy/2).
+
+    Returns (faceBx (Ny, Nx+1), faceBy (Ny+1, Nx)) with dx = dy = 1 (callers scale),
+    the duplicate periodic faces equal bit for bit.
+    """
+    bxf = np.roll(az, -1, axis=0) - az            # Bx = dAz/dy at x-face i of row j
+    byf = -(np.roll(az, -1, axis=1) - az)          # By = -dAz/dx at y-face j of column i
+    fbx = np.concatenate([bxf, bxf[:, :1]], axis=1)
+    fby = np.concatenate([byf, byf[:1, :]], axis=0)
+    return fbx, fby
+
+
+def orszag_tang(nx, ny, gamma=5.0 / 3.0, b0_scale=1.0, faces="potential",
+                rho_perturb=0.0, seed=None):
+    """Orszag-Tang vortex on the periodic unit square.
+
+    Returns (prim (8,Ny,Nx), cons (8,Ny,Nx), faceBx (Ny,Nx+1), faceBy (Ny+1,Nx), dx, dy).
+    ``faces="potential"`` takes the faces from A_z (divergence-free to roundoff);
+    ``faces="cells"`` re-averages them from the cell values as the reference grid does.
+    ``rho_perturb`` multiplies the density by (1 + rho_perturb * N(0,1)) (seeded).
+    """
+    pi = math.pi
+    x, dx = cell_centres(nx, 0.0, 1.0)
+    y, dy = cell_centres(ny, 0.0, 1.0)
+    X, Y = np.meshgrid(x, y)
+    b0 = b0_scale / np.sqrt(4.0 * pi)
+    az = (b0 / (4.0 * pi)) * np.cos(4.0 * pi * (X - dx / 2.0)) \
+        + (b0 / (2.0 * pi)) * np.cos(2.0 * pi * (Y - dy / 2.0))
+    fbx_u, fby_u = faces_from_potential(az)
+    left_bx = fbx_u[:, :-1] / dy
+    top_by = fby_u[:-1, :] / dx
+    cbx = (left_bx + np.roll(left_bx, -1, axis=1)) / 2.0
+    cby = (top_by + np.roll(top_by, -1, axis=0)) / 2.0
+    prim = np.zeros((8, ny, nx))
+    prim[0] = 25.0 / (36.0 * pi)
+    if rho_perturb:
+        rng = np.random.default_rng(seed)
+        prim[0] *= 1.0 + rho_perturb * rng.standard_normal((ny, nx))
+    prim[1] = -np.sin(2.0 * pi * Y)
+    prim[2] = np.sin(2.0 * pi * X)
+    prim[4] = cbx
+    prim[5] = cby
+    prim[7] = 5.0 / (12.0 * pi)
+    if faces == "potential":
+        fbx = fbx_u / dy
+        fby = fby_u / dx
+    else:
+        fbx, fby = faces_from_cells(cbx, cby, PERIODIC, PERIODIC)
+    return prim, prim_to_cons_mhd(prim, gamma), fbx, fby, dx, dy
+
+
+def _gaussian_field(rng, n, slope, kmin, kmax):
+    kx = np.fft.rfftfreq(n, d=1.0 / n)
+    ky = np.fft.fftfreq(n, d=1.0 / n)
+    KX, KY = np.meshgrid(kx, ky)
+    k = np.sqrt(KX * KX + KY * KY)
+    mask = (k >= kmin) & (k <= kmax)
+    amp = np.zeros_like(k)
+    amp[mask] = k[mask] ** (-slope / 2.0)
+    c = (rng.standard_normal(k.shape) + 1j * rng.standard_normal(k.shape)) * amp
+    f = np.fft.irfft2(c, s=(n, n))
+    return f - f.mean()
+
+
+def turbulence(n, seed=1, gamma=5.0 / 3.0, kmax_v=32, kmax_a=16, mach=1.0, beta=1.0):
+    """Driven-free turbulence initial state on the periodic unit square, n x n cells.
+
+    rho = exp(0.1 g) with g a unit-variance field, power ~ k^-2 (1 <= k <= kmax_v);
+    vx, vy independent fields of the same spectrum scaled to rms Mach ``mach``
+    (sqrt(<(vx^2+vy^2)/c_s^2>) = mach, c_s^2 = gamma p / rho); p = 1/gamma;
+    A_z with power ~ k^-3 (1 <= k <= kmax_a) scaled so 2p/<B^2> = ``beta``.
+    Returns (prim, cons, faceBx, faceBy, dx, dy).
+    """
+    rng = np.random.default_rng(seed)
+    g = _gaussian_field(rng, n, 2.0, 1.0, kmax_v)
+    g /= g.std()
+    vx = _gaussian_field(rng, n, 2.0, 1.0, kmax_v)
+    vy = _gaussian_field(rng, n, 2.0, 1.0, kmax_v)
+    az = _gaussian_field(rng, n, 3.0, 1.0, kmax_a)
+    dx = dy = 1.0 / n
+    rho = np.exp(0.1 * g)
+    p = np.full((n, n), 1.0 / gamma)
+    cs2 = gamma * p / rho
+    vscale = mach / np.sqrt(np.mean((vx * vx + vy * vy) / cs2))
+    vx *= vscale
+    vy *= vscale
+    fbx_u, fby_u = faces_from_potential(az)
+    fbx = fbx_u / dy
+    fby = fby_u / dx
+    cbx = (fbx[:, :-1] + fbx[:, 1:]) / 2.0
+    cby = (fby[:-1, :] + fby[1:, :]) / 2.0
+    bscale = np.sqrt(2.0 * (1.0 / gamma) / beta / np.mean(cbx * cbx + cby * cby))
+    fbx *= bscale
+    fby *= bscale
+    cbx = (fbx[:, :-1] + fbx[:, 1:]) / 2.0
+    cby = (fby[:-1, :] + fby[1:, :]) / 2.0
+    prim = np.zeros((8, n, n))
+    prim[0] = rho
+    prim[1] = vx
+    prim[2] = vy
+    prim[4] = cbx
+    prim[5] = cby
+    prim[7] = p
+    return prim, prim_to_cons_mhd(prim, gamma), fbx, fby, dx, dy

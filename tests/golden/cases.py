@@ -1,0 +1,206 @@
+"""Seeded input states shared by the golden-fixture generator and the parity tests.
+
+Each case is (name, physics, builder); ``builder()`` returns a dict with the
+state arrays and the evolve parameters. The cases are chosen to drive every
+branch of the step: PPM and first-order reconstruction, both boundary
+conditions on each axis, the entropy fix, zero normal/transverse B, exactly
+zero mass flux at the corners, supersonic upwinding, the density/pressure
+floors, and the tEnd clip of dt.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from pythonmhd_gb300 import initial_conditions as ic
+
+G53 = 5.0 / 3.0
+
+
+def _params(**kw):
+    p = dict(t_start=0.0, t_end=10.0, start_cycle=0, max_cycles=2, gamma=G53, cfl=0.4,
+             min_d=1e-12, min_p=1e-12, min_e=1e-12, order=2, efix=False, eps=0.5,
+             bcx=ic.PERIODIC, bcy=ic.PERIODIC)
+    p.update(kw)
+    return p
+
+
+def _smooth_random(rng, ny, nx, kmax=3):
+    """A smooth random field on the grid (sum of a few Fourier modes)."""
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(x, y)
+    f = np.zeros((ny, nx))
+    for _ in range(4):
+        kx, ky = rng.integers(1, kmax + 1, size=2)
+        ph = rng.uniform(0, 2 * math.pi, size=2)
+        f += rng.standard_normal() * np.sin(2 * math.pi * kx * X + ph[0]) * np.cos(2 * math.pi * ky * Y + ph[1])
+    return f / 4.0
+
+
+def _mhd_state(prim, gamma, bcx, bcy):
+    fbx, fby = ic.faces_from_cells(prim[4], prim[5], bcx, bcy)
+    return prim, ic.prim_to_cons_mhd(prim, gamma), fbx, fby
+
+
+def mhd_cases():
+    out = []
+
+    def ot(nx, ny, faces, **kw):
+        prim, cons, fbx, fby, dx, dy = ic.orszag_tang(nx, ny, gamma=G53, faces=faces)
+        return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=dx, dy=dy, **_params(**kw))
+
+    out.append(("ot_ppm", lambda: ot(24, 16, "potential", max_cycles=3)))
+    out.append(("ot_order0", lambda: ot(24, 16, "potential", order=0, max_cycles=3)))
+    out.append(("ot_cellfaces_efix", lambda: ot(20, 20, "cells", efix=True, eps=0.5)))
+    out.append(("ot_tend_clip", lambda: ot(16, 16, "potential", t_end=0.012, max_cycles=50)))
+    out.append(("ot_no_cycle", lambda: ot(8, 8, "potential", start_cycle=5, max_cycles=5)))
+
+    def turb():
+        prim, cons, fbx, fby, dx, dy = ic.turbulence(32, seed=3, gamma=G53, kmax_v=8, kmax_a=4)
+        return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=dx, dy=dy, **_params())
+    out.append(("turb_ppm", turb))
+
+    def rand(seed, ny, nx, bcx, bcy, b_on=(1, 1, 1), v_scale=0.5, rho_lo=0.5, **kw):
+        rng = np.random.default_rng(seed)
+        prim = np.zeros((8, ny, nx))
+        prim[0] = rho_lo + np.abs(1.0 + _smooth_random(rng, ny, nx))
+        for k in (1, 2, 3):
+            prim[k] = v_scale * _smooth_random(rng, ny, nx)
+        for k, on in zip((4, 5, 6), b_on):
+            prim[k] = on * (0.7 * _smooth_random(rng, ny, nx) + 0.3 * rng.standard_normal())
+        prim[7] = 0.4 + np.abs(0.5 + _smooth_random(rng, ny, nx))
+        prim, cons, fbx, fby = _mhd_state(prim, G53, bcx, bcy)
+        return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=1.0 / nx, dy=1.0 / ny,
+                    **_params(bcx=bcx, bcy=bcy, **kw))
+
+    out.append(("rand_outflow_ppm", lambda: rand(11, 18, 22, 0, 0)))
+    out.append(("rand_px_oy_ppm", lambda: rand(12, 20, 14, 1, 0)))
+    out.append(("rand_ox_py_order0", lambda: rand(13, 14, 20, 0, 1, order=0)))
+    out.append(("rand_efix_small_eps", lambda: rand(14, 16, 16, 1, 1, efix=True, eps=0.05)))
+    out.append(("zero_b", lambda: rand(15, 16, 18, 0, 0, b_on=(0, 0, 0))))
+    out.append(("zero_bx", lambda: _zero_bx(16)))
+    out.append(("zero_btran", lambda: _zero_btran(17)))
+    out.append(("uniform_static", lambda: _uniform(static=True)))
+    out.append(("supersonic", lambda: _supersonic(18)))
+    out.append(("floors", lambda: rand(19, 16, 16, 0, 1, v_scale=2.0, rho_lo=0.01,
+                                      min_d=0.8, min_p=0.6, min_e=1.5)))
+    out.append(("tiny_outflow", lambda: rand(20, 3, 5, 0, 0)))
+    out.append(("tiny_periodic", lambda: rand(21, 2, 4, 1, 1)))
+    return out
+
+
+def _zero_bx(seed):
+    rng = np.random.default_rng(seed)
+    ny, nx = 16, 16
+    prim = np.zeros((8, ny, nx))
+    prim[0] = 1.0 + 0.2 * _smooth_random(rng, ny, nx)
+    prim[1] = 0.3 * _smooth_random(rng, ny, nx)
+    prim[2] = 0.3 * _smooth_random(rng, ny, nx)
+    prim[5] = 0.5 + 0.2 * _smooth_random(rng, ny, nx)
+    prim[6] = 0.2 * _smooth_random(rng, ny, nx)
+    prim[7] = 1.0 + 0.2 * _smooth_random(rng, ny, nx)
+    prim, cons, fbx, fby = _mhd_state(prim, G53, 1, 1)
+    return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=1 / nx, dy=1 / ny, **_params())
+
+
+def _zero_btran(seed):
+    """A 1D-invariant Brio-Wu-like state: only Bx (normal in x) is nonzero."""
+    rng = np.random.default_rng(seed)
+    ny, nx = 6, 24
+    prim = np.zeros((8, ny, nx))
+    left = np.arange(nx) < nx // 2
+    prim[0] = np.where(left, 1.0, 0.125)[None, :].repeat(ny, 0)
+    prim[7] = np.where(left, 1.0, 0.1)[None, :].repeat(ny, 0)
+    prim[4] = 0.75
+    prim[1] = 0.01 * rng.standard_normal((ny, nx))
+    prim, cons, fbx, fby = _mhd_state(prim, 2.0, 0, 1)
+    return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=1 / nx, dy=1 / nx,
+                **_params(gamma=2.0, bcx=0, bcy=1))
+
+
+def _uniform(static):
+    ny, nx = 8, 10
+    prim = np.zeros((8, ny, nx))
+    prim[0] = 1.0
+    prim[4] = 0.3
+    prim[5] = -0.2
+    prim[6] = 0.1
+    prim[7] = 0.6
+    if not static:
+        prim[1] = 0.2
+    prim, cons, fbx, fby = _mhd_state(prim, G53, 1, 0)
+    return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=0.1, dy=0.125, **_params(bcy=0))
+
+
+def _supersonic(seed):
+    rng = np.random.default_rng(seed)
+    ny, nx = 12, 12
+    prim = np.zeros((8, ny, nx))
+    prim[0] = 1.0 + 0.1 * _smooth_random(rng, ny, nx)
+    prim[1] = 6.0 + 0.2 * _smooth_random(rng, ny, nx)
+    prim[2] = -6.0 + 0.2 * _smooth_random(rng, ny, nx)
+    prim[4] = 0.2
+    prim[5] = 0.1 * _smooth_random(rng, ny, nx)
+    prim[7] = 0.5 + 0.05 * _smooth_random(rng, ny, nx)
+    prim, cons, fbx, fby = _mhd_state(prim, G53, 1, 1)
+    return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=1 / nx, dy=1 / ny, **_params())
+
+
+def hydro_cases():
+    out = []
+
+    def rand(seed, ny, nx, bcx, bcy, v_scale=0.5, rho_lo=0.5, **kw):
+        rng = np.random.default_rng(seed)
+        prim = np.zeros((5, ny, nx))
+        prim[0] = rho_lo + np.abs(1.0 + _smooth_random(rng, ny, nx))
+        for k in (1, 2, 3):
+            prim[k] = v_scale * _smooth_random(rng, ny, nx)
+        prim[4] = 0.4 + np.abs(0.5 + _smooth_random(rng, ny, nx))
+        return dict(prim=prim, cons=ic.prim_to_cons_hydro(prim, G53), dx=1.0 / nx, dy=1.0 / ny,
+                    **_params(bcx=bcx, bcy=bcy, **kw))
+
+    def blast():
+        ny, nx = 20, 24
+        x = (np.arange(nx) + 0.5) / nx - 0.5
+        y = (np.arange(ny) + 0.5) / ny - 0.5
+        X, Y = np.meshgrid(x, y)
+        prim = np.zeros((5, ny, nx))
+        prim[0] = 1.0
+        prim[4] = np.where(X * X + Y * Y < 0.04, 10.0, 0.1)
+        return dict(prim=prim, cons=ic.prim_to_cons_hydro(prim, 1.4), dx=1 / nx, dy=1 / ny,
+                    **_params(gamma=1.4, bcx=0, bcy=0, max_cycles=3))
+
+    out.append(("blast_ppm", blast))
+    out.append(("rand_periodic_ppm_efix", lambda: rand(31, 16, 20, 1, 1, efix=True, eps=0.3)))
+    out.append(("rand_order0", lambda: rand(32, 14, 18, 1, 0, order=0)))
+    out.append(("rand_outflow_ppm", lambda: rand(33, 18, 14, 0, 0)))
+    out.append(("supersonic", lambda: rand(34, 12, 12, 1, 1, v_scale=0.2) | {}))
+    out.append(("floors", lambda: rand(35, 16, 16, 0, 1, v_scale=2.0, rho_lo=0.01,
+                                       min_d=0.8, min_p=0.6)))
+    out.append(("tiny", lambda: rand(36, 3, 4, 1, 0)))
+    out.append(("tend_clip", lambda: rand(37, 10, 10, 1, 1, t_end=0.03, max_cycles=40)))
+    return out
+
+
+def supersonic_hydro_fix(case):
+    """Shift the hydro 'supersonic' case to |v| > c in both directions."""
+    prim = case["prim"].copy()
+    prim[1] += 4.0
+    prim[2] -= 4.0
+    case["prim"] = prim
+    case["cons"] = ic.prim_to_cons_hydro(prim, case["gamma"])
+    return case
+
+
+def build(physics, name):
+    table = dict(mhd_cases() if physics == "mhd" else hydro_cases())
+    case = table[name]()
+    if physics == "hydro" and name == "supersonic":
+        case = supersonic_hydro_fix(case)
+    return case
+
+
+def names(physics):
+    return [n for n, _ in (mhd_cases() if physics == "mhd" else hydro_cases())]

@@ -1,0 +1,77 @@
+"""Generate the golden fixtures by running the reference PythonMHD step itself.
+
+Run in a checkout that has the reference next to it (the fixtures are committed,
+so the tests do not need the reference):
+
+    python -B tests/golden/make_golden.py /root/reference/PythonMHD
+
+For every case in ``tests/golden/cases.py`` this imports the reference's own
+``Source.EvolveFunctions_MHD.evolve_2D_mhd`` / ``Source.EvolveFunctions_Hydro.evolve_2D_hydro``
+(which depend only on NumPy), calls it on a minimal grid object carrying the
+attributes the reference reads (Source/EvolveFunctions_MHD.py:396-444,
+Source/EvolveFunctions_Hydro.py:353-376), and stores inputs, parameters and the
+returned tuple in ``tests/golden/<physics>_<case>.npz``.
+"""
+from __future__ import annotations
+
+import contextlib
+import io
+import os
+import sys
+from types import SimpleNamespace
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.dont_write_bytecode = True
+
+from tests.golden import cases  # noqa: E402
+
+SCALARS = ("t_start", "t_end", "start_cycle", "max_cycles", "gamma", "cfl", "min_d", "min_p",
+           "min_e", "order", "efix", "eps", "bcx", "bcy", "dx", "dy")
+
+
+def run_reference(ref_root, physics, case):
+    sys.path.insert(0, ref_root)
+    import Source.EvolveFunctions_Hydro as ref_hydro  # noqa: E402
+    import Source.EvolveFunctions_MHD as ref_mhd  # noqa: E402
+    ny, nx = case["prim"].shape[1:]
+    grid = SimpleNamespace(primVars=case["prim"].copy(), consVars=case["cons"].copy(),
+                           dx=case["dx"], dy=case["dy"], BcX=case["bcx"], BcY=case["bcy"],
+                           numXCells=nx, numYCells=ny)
+    args = (grid, case["t_start"], case["t_end"], case["start_cycle"], case["max_cycles"],
+            case["gamma"], case["cfl"], case["min_d"], case["min_p"], case["min_e"],
+            case["order"], case["efix"], case["eps"])
+    with contextlib.redirect_stdout(io.StringIO()):
+        if physics == "mhd":
+            grid.faceBx = case["fbx"].copy()
+            grid.faceBy = case["fby"].copy()
+            res = ref_mhd.evolve_2D_mhd(*args)
+            keys = ("prim", "cons", "fbx", "fby", "t", "cycle", "sl_prim", "sl_cons", "sl_fbx",
+                    "sl_fby", "sl_t")
+        else:
+            res = ref_hydro.evolve_2D_hydro(*args)
+            keys = ("prim", "cons", "t", "cycle", "sl_prim", "sl_cons", "sl_t")
+    return {"out_" + k: np.asarray(v) for k, v in zip(keys, res)}
+
+
+def main(ref_root):
+    for physics in ("mhd", "hydro"):
+        for name in cases.names(physics):
+            case = cases.build(physics, name)
+            outs = run_reference(ref_root, physics, case)
+            arrays = {"in_prim": case["prim"], "in_cons": case["cons"]}
+            if physics == "mhd":
+                arrays.update(in_fbx=case["fbx"], in_fby=case["fby"])
+            for k in SCALARS:
+                arrays["p_" + k] = np.asarray(case[k])
+            arrays.update(outs)
+            path = os.path.join(HERE, f"{physics}_{name}.npz")
+            np.savez_compressed(path, **arrays)
+            print(f"{path}: cycles={int(outs['out_cycle'])} t={float(outs['out_t']):.6g}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/PythonMHD")

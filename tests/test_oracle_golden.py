@@ -1,0 +1,37 @@
+"""The CPU oracle reproduces the reference's own outputs bit for bit.
+
+The fixtures were produced by running the reference PythonMHD step
+(Source/EvolveFunctions_MHD.py:393, Source/EvolveFunctions_Hydro.py:350) with
+tests/golden/make_golden.py; this pins the oracle before anything is checked
+against it.
+"""
+import numpy as np
+import pytest
+
+from oracle import hydro2d, mhd2d
+from tests.golden_io import HYDRO_KEYS, MHD_KEYS, case_id, golden_files, load
+
+
+@pytest.mark.parametrize("path", golden_files("mhd"), ids=case_id)
+def test_oracle_mhd_matches_reference_bitwise(path):
+    p, i, o = load(path)
+    res = mhd2d.evolve(i["prim"], i["cons"], i["fbx"], i["fby"], p["dx"], p["dy"], p["bcx"], p["bcy"],
+                       p["t_start"], p["t_end"], p["start_cycle"], p["max_cycles"], p["gamma"],
+                       p["cfl"], p["min_d"], p["min_p"], p["min_e"], p["order"], p["efix"], p["eps"])
+    for k, v in zip(MHD_KEYS, res):
+        assert np.array_equal(np.asarray(v), o[k]), k
+
+
+@pytest.mark.parametrize("path", golden_files("hydro"), ids=case_id)
+def test_oracle_hydro_matches_reference_bitwise(path):
+    p, i, o = load(path)
+    res = hydro2d.evolve(i["prim"], i["cons"], p["dx"], p["dy"], p["bcx"], p["bcy"],
+                         p["t_start"], p["t_end"], p["start_cycle"], p["max_cycles"], p["gamma"],
+                         p["cfl"], p["min_d"], p["min_p"], p["min_e"], p["order"], p["efix"], p["eps"])
+    for k, v in zip(HYDRO_KEYS, res):
+        assert np.array_equal(np.asarray(v), o[k]), k
+
+
+def test_golden_set_is_complete():
+    assert len(golden_files("mhd")) >= 18
+    assert len(golden_files("hydro")) >= 8
