@@ -1,0 +1,103 @@
+/*
+ * C ABI of the GB300 2D unsplit Godunov step (adiabatic hydro / ideal MHD).
+ *
+ * One handle = one grid on one GPU with its own CUDA stream.  The handle owns
+ * the device state (two ping-pong state buffers, so the state at the start of
+ * the last cycle -- the reference's "second-last" state -- is always kept) and
+ * the scratch of a cycle.  Arrays crossing this boundary are C-contiguous
+ * float64 in the reference's layout:
+ *   prim, cons : (nvars, ny, nx)  nvars = 8 for MHD [rho,vx,vy,vz,Bx,By,Bz,p] /
+ *                                                  [rho,mx,my,mz,Bx,By,Bz,E],
+ *                                  5 for hydro [rho,vx,vy,vz,p] / [rho,mx,my,mz,E]
+ *   faceBx     : (ny, nx+1)       faceBy : (ny+1, nx)   (MHD only; NULL for hydro)
+ * Every call returns a status code (0 = MHD_OK); mhd2d_strerror() names it.
+ * A handle is not re-entrant: one host thread at a time per handle.
+ *
+ * These entry points replace the reference's Python evolve functions, which
+ * take the grid object and the same scalar parameters:
+ *   Source/EvolveFunctions_MHD.py:393-394    evolve_2D_mhd(simulationGrid, tStart, tEnd,
+ *                                            startCycle, maxCycles, gamma, cfl, minDens,
+ *                                            minPres, minEnergy, reconstructOrder,
+ *                                            entropyFix, epsilon)
+ *   Source/EvolveFunctions_Hydro.py:350-351  evolve_2D_hydro(...)  (same arguments)
+ * The reference crosses no native boundary; the Python mirror in
+ * pythonmhd_gb300/evolve.py binds these with ctypes and keeps those signatures.
+ */
+#ifndef PYTHONMHD_GB300_H
+#define PYTHONMHD_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum mhd2d_status {
+  MHD_OK = 0,
+  MHD_ERR_ARG = 1,         /* invalid argument (shape, BC code, null pointer, ...) */
+  MHD_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  MHD_ERR_NOMEM = 3,       /* device or pinned-host allocation failed */
+  MHD_ERR_STATE = 4,       /* call out of order (e.g. advance before upload) */
+  MHD_ERR_NONFINITE = 5,   /* the time or dt became NaN/Inf during advance */
+  MHD_ERR_TOO_LARGE = 6    /* size above a fixed limit of the entry point */
+};
+
+enum mhd2d_physics { MHD2D_HYDRO = 0, MHD2D_MHD = 1 };
+enum mhd2d_arith { MHD2D_ARITH_EXACT = 0, MHD2D_ARITH_FAST = 1 };
+
+/* Create a handle for an ny x nx grid.  bcx/bcy: 0 outflow, 1 periodic
+ * (Source/PythonMHD_Constants.py:11-12).  recon: 0 first order, 2 PPM
+ * (Source/EvolveFunctions_MHD.py:483-511).  arith: MHD2D_ARITH_EXACT reproduces
+ * the reference's float64 arithmetic bit for bit; MHD2D_ARITH_FAST lets the
+ * compiler fuse multiply-adds (results agree to rounding).  Requires nx, ny >= 2. */
+int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma,
+                 int physics, int recon, int entropy_fix, double eps, double min_d,
+                 double min_p, double min_e, int arith, void** handle);
+
+/* Copy a host state in (becomes the current state).  The reference reads
+ * grid.primVars, grid.consVars, grid.faceBx, grid.faceBy at the start of an
+ * evolve call (Source/EvolveFunctions_MHD.py:396-444). */
+int mhd2d_upload(void* handle, const double* prim, const double* cons,
+                 const double* faceBx, const double* faceBy);
+
+/* Run the evolve loop on the device: while t < t_end and cycle < max_cycles,
+ * one CTU(+CT) cycle with the CFL dt clipped to t_end
+ * (Source/EvolveFunctions_MHD.py:464-692).  Returns the final time/cycle and the
+ * time at the start of the last cycle (t0 when no cycle ran). */
+int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0,
+                  long long max_cycles, double cfl, double* t_out, long long* cycle_out,
+                  double* t_second_last);
+
+/* Copy a state out: which = 0 the current state, 1 the state at the start of
+ * the last cycle (the reference's secondLast* arrays).  Any pointer may be
+ * NULL to skip that array. */
+int mhd2d_download(void* handle, int which, double* prim, double* cons,
+                   double* faceBx, double* faceBy);
+
+/* Device pointers of the current state (for zero-copy use from a framework on
+ * the same device).  Pointers stay valid until the next advance/upload. */
+int mhd2d_state_ptrs(void* handle, int which, double** prim, double** cons,
+                     double** faceBx, double** faceBy);
+
+/* Debug view of a cycle's intermediates after an advance (in float64, row-major):
+ * what = 0..3 x-face left/right, y-face left/right states (prim, nvars-1 slots),
+ * 4/5 x/y fluxes, 6 corner EMF ((ny+1) x (nx+1)), 7/8 half-step faceBx/faceBy. */
+int mhd2d_peek(void* handle, int what, double* out, size_t count);
+
+/* Number of kernel launches the last mhd2d_advance call enqueued (graph nodes
+ * times graph launches; replays past the end of the run count too). */
+int mhd2d_last_launches(void* handle, long long* launches);
+
+/* Bytes of device memory the handle holds. */
+int mhd2d_device_bytes(void* handle, size_t* bytes);
+
+/* The CUDA stream the handle's work runs on (a cudaStream_t). */
+int mhd2d_stream(void* handle, void** stream);
+
+const char* mhd2d_strerror(int status);
+void mhd2d_destroy(void* handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYTHONMHD_GB300_H */

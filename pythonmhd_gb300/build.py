@@ -1,0 +1,88 @@
+"""Build the in-tree CUDA library ``pythonmhd_gb300/libpythonmhd_gb300.so`` for sm_103a.
+
+Three translation units are compiled in parallel with nvcc and linked into one
+shared library with a plain C ABI (``include/pythonmhd_gb300.h``):
+
+* ``csrc/kernels_exact.cu``  -- the step kernels with ``-fmad=false``
+* ``csrc/kernels_fast.cu``   -- the same kernels with FMA contraction
+* ``csrc/capi.cu``           -- handles, copies and the CUDA-graph evolve loop
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libpythonmhd_gb300.so")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+UNITS = [
+    ("kernels_exact.cu", ["-fmad=false"]),
+    ("kernels_fast.cu", ["-fmad=true"]),
+    ("capi.cu", []),
+]
+
+
+def nvcc_path() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build pythonmhd_gb300")
+
+
+def _sources():
+    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    srcs.append(os.path.join(ROOT, "include", "pythonmhd_gb300.h"))
+    srcs.append(os.path.abspath(__file__))
+    return srcs
+
+
+def is_stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    return any(os.path.getmtime(s) > t for s in _sources())
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile and link the library if it is missing or older than its sources."""
+    if not force and not is_stale():
+        return LIB
+    nvcc = nvcc_path()
+    os.makedirs(BUILD, exist_ok=True)
+    common = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+    procs = []
+    objs = []
+    for src, extra in UNITS:
+        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(obj)
+        cmd = common + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    errors = []
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            errors.append(" ".join(cmd) + "\n" + out.decode(errors="replace"))
+        elif verbose and out:
+            print(out.decode(errors="replace"), file=sys.stderr)
+    if errors:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
+    tmp = LIB + ".tmp"
+    link = [nvcc, ARCH, "-shared", "-cudart", "static", "-o", tmp] + objs
+    r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

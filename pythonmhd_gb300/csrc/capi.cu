@@ -1,0 +1,345 @@
+// C ABI of the 2D Godunov step: handle lifetime, host<->device copies and the
+// device-resident evolve loop (CUDA graphs of two cycles replayed in chunks).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/pythonmhd_gb300.h"
+#include "godunov2d_types.h"
+
+namespace mhdk {
+namespace exact { void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s); }
+namespace fast { void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s); }
+}  // namespace mhdk
+
+using mhdk::Grid;
+using mhdk::LoopState;
+
+namespace {
+
+struct Handle {
+  Grid g{};
+  int arith = 0;
+  int device = 0;
+  int nvars = 8;
+  cudaStream_t stream = nullptr;
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  LoopState* host_loop = nullptr;  // pinned
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // two cycles starting at parity p
+  int cur = 0;            // state buffer holding the current state
+  int have_state = 0;
+  long long last_cycles_run = 0;
+  long long last_launches = 0;
+  size_t graph_nodes[2] = {0, 0};
+  int dt_blocks = 0;
+};
+
+int cuda_fail(cudaError_t e) {
+  if (e == cudaErrorMemoryAllocation) return MHD_ERR_NOMEM;
+  return MHD_ERR_CUDA;
+}
+
+#define CK(call)                                  \
+  do {                                            \
+    cudaError_t _e = (call);                      \
+    if (_e != cudaSuccess) return cuda_fail(_e);  \
+  } while (0)
+
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+void enqueue(Handle* h, int parity) {
+  if (h->arith == MHD2D_ARITH_EXACT) mhdk::exact::enqueue_cycle(h->g, parity, h->dt_blocks, h->stream);
+  else mhdk::fast::enqueue_cycle(h->g, parity, h->dt_blocks, h->stream);
+}
+
+int build_graph(Handle* h, int parity) {
+  if (h->graph[parity]) return MHD_OK;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue(h, parity);
+  enqueue(h, parity ^ 1);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  if (e != cudaSuccess) return cuda_fail(e);
+  size_t nodes = 0;
+  cudaGraphGetNodes(graph, nullptr, &nodes);
+  h->graph_nodes[parity] = nodes;
+  e = cudaGraphInstantiate(&h->graph[parity], graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e);
+  return MHD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mhd2d_strerror(int status) {
+  switch (status) {
+    case MHD_OK: return "ok";
+    case MHD_ERR_ARG: return "invalid argument";
+    case MHD_ERR_CUDA: return "CUDA runtime error";
+    case MHD_ERR_NOMEM: return "out of memory";
+    case MHD_ERR_STATE: return "call out of order (no state uploaded)";
+    case MHD_ERR_NONFINITE: return "time or timestep became non-finite";
+    case MHD_ERR_TOO_LARGE: return "size above the entry point's fixed limit";
+    default: return "unknown status";
+  }
+}
+
+int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma, int physics,
+                 int recon, int entropy_fix, double eps, double min_d, double min_p, double min_e,
+                 int arith, void** handle) {
+  if (!handle) return MHD_ERR_ARG;
+  *handle = nullptr;
+  if (nx < 2 || ny < 2 || !(dx > 0.0) || !(dy > 0.0)) return MHD_ERR_ARG;
+  if ((bcx != 0 && bcx != 1) || (bcy != 0 && bcy != 1)) return MHD_ERR_ARG;
+  if (physics != MHD2D_HYDRO && physics != MHD2D_MHD) return MHD_ERR_ARG;
+  if (recon != 0 && recon != 2) return MHD_ERR_ARG;
+  if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST) return MHD_ERR_ARG;
+  if ((long long)nx * ny > (1LL << 31)) return MHD_ERR_TOO_LARGE;
+
+  Handle* h = new (std::nothrow) Handle();
+  if (!h) return MHD_ERR_NOMEM;
+  Grid& g = h->g;
+  g.nx = nx; g.ny = ny; g.dx = dx; g.dy = dy; g.bcx = bcx; g.bcy = bcy;
+  g.physics = physics; g.recon = recon; g.efix = entropy_fix ? 1 : 0;
+  g.gamma = gamma; g.eps = eps; g.min_d = min_d; g.min_p = min_p; g.min_e = min_e;
+  h->arith = arith;
+  h->nvars = physics == MHD2D_MHD ? 8 : 5;
+  const int nv = physics == MHD2D_MHD ? 7 : 5;
+  const int nw = physics == MHD2D_MHD ? 42 : 10;
+
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete h; return cuda_fail(e); }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  h->dt_blocks = std::max(1, sms) * 8;
+
+  const size_t cp = mhdk::cell_plane(g), xp = mhdk::xface_plane(g), yp = mhdk::yface_plane(g),
+               kp = mhdk::corner_plane(g);
+  g.ext_plane = std::max((size_t)(nx + 2) * ny, (size_t)nx * (ny + 2));
+  const bool mhd = physics == MHD2D_MHD;
+  // carve every buffer out of one allocation
+  struct Req { double** p; size_t n; };
+  Req reqs[32];
+  int nr = 0;
+  for (int b = 0; b < 2; ++b) {
+    reqs[nr++] = {&g.st[b].prim, (size_t)h->nvars * cp};
+    reqs[nr++] = {&g.st[b].cons, (size_t)h->nvars * cp};
+    if (mhd) { reqs[nr++] = {&g.st[b].fbx, xp}; reqs[nr++] = {&g.st[b].fby, yp}; }
+  }
+  reqs[nr++] = {&g.xl, nv * xp}; reqs[nr++] = {&g.xr, nv * xp};
+  reqs[nr++] = {&g.yl, nv * yp}; reqs[nr++] = {&g.yr, nv * yp};
+  reqs[nr++] = {&g.fx, nv * xp}; reqs[nr++] = {&g.fy, nv * yp};
+  if (mhd) {
+    reqs[nr++] = {&g.uxl, nv * xp}; reqs[nr++] = {&g.uxr, nv * xp};
+    reqs[nr++] = {&g.uyl, nv * yp}; reqs[nr++] = {&g.uyr, nv * yp};
+    reqs[nr++] = {&g.emf, kp}; reqs[nr++] = {&g.nfbx, xp}; reqs[nr++] = {&g.nfby, yp};
+    reqs[nr++] = {&g.hez, cp};
+  }
+  if (recon == 2) {
+    reqs[nr++] = {&g.slopes, nv * g.ext_plane};
+    reqs[nr++] = {&g.eig, nw * g.ext_plane};
+  }
+  size_t total = 0;
+  for (int i = 0; i < nr; ++i) total += align256(reqs[i].n * sizeof(double));
+  total += align256(sizeof(LoopState)) + align256(sizeof(int));
+  e = cudaMalloc(&h->arena, total);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return cuda_fail(e);
+  }
+  h->arena_bytes = total;
+  char* base = static_cast<char*>(h->arena);
+  size_t off = 0;
+  for (int i = 0; i < nr; ++i) {
+    *reqs[i].p = reinterpret_cast<double*>(base + off);
+    off += align256(reqs[i].n * sizeof(double));
+  }
+  g.loop = reinterpret_cast<LoopState*>(base + off);
+  off += align256(sizeof(LoopState));
+  g.status = reinterpret_cast<int*>(base + off);
+  e = cudaMemsetAsync(h->arena, 0, total, h->stream);
+  if (e == cudaSuccess) e = cudaMallocHost(&h->host_loop, sizeof(LoopState));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    if (h->host_loop) cudaFreeHost(h->host_loop);
+    cudaFree(h->arena);
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return cuda_fail(e);
+  }
+  *handle = h;
+  return MHD_OK;
+}
+
+void mhd2d_destroy(void* handle) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& ge : h->graph)
+    if (ge) cudaGraphExecDestroy(ge);
+  if (h->host_loop) cudaFreeHost(h->host_loop);
+  if (h->arena) cudaFree(h->arena);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int mhd2d_upload(void* handle, const double* prim, const double* cons, const double* faceBx,
+                 const double* faceBy) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !prim || !cons) return MHD_ERR_ARG;
+  const bool mhd = h->g.physics == MHD2D_MHD;
+  if (mhd && (!faceBx || !faceBy)) return MHD_ERR_ARG;
+  const mhdk::StateBuf& s = h->g.st[h->cur];
+  const size_t cb = (size_t)h->nvars * mhdk::cell_plane(h->g) * sizeof(double);
+  CK(cudaMemcpyAsync(s.prim, prim, cb, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(s.cons, cons, cb, cudaMemcpyHostToDevice, h->stream));
+  if (mhd) {
+    CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(h->g) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(h->g) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  h->have_state = 1;
+  h->last_cycles_run = 0;
+  return MHD_OK;
+}
+
+int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
+                  double* t_out, long long* cycle_out, double* t_second_last) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return MHD_ERR_ARG;
+  if (!h->have_state) return MHD_ERR_STATE;
+  if (!(t0 <= t_end) || cycle0 < 0) return MHD_ERR_ARG;
+  static_assert(sizeof(LoopState) % 8 == 0, "layout");
+  LoopState init{};
+  init.t = t0;
+  init.t_end = t_end;
+  init.t_prev = t0;
+  init.dt = 0.0;
+  init.cfl = cfl;
+  init.cycle = cycle0;
+  init.max_cycles = max_cycles;
+  init.cycles_run = 0;
+  init.active = 0;
+  init.cur = h->cur;
+  *h->host_loop = init;
+  CK(cudaMemcpyAsync(h->g.loop, h->host_loop, sizeof(LoopState), cudaMemcpyHostToDevice, h->stream));
+  long long budget_pairs = 1;
+  h->last_launches = 0;
+  LoopState st = init;
+  while (st.t < st.t_end && st.cycle < st.max_cycles) {
+    const int parity = st.cur;
+    int rc = build_graph(h, parity);
+    if (rc) return rc;
+    for (long long k = 0; k < budget_pairs; ++k) CK(cudaGraphLaunch(h->graph[parity], h->stream));
+    h->last_launches += budget_pairs * (long long)h->graph_nodes[parity];
+    CK(cudaMemcpyAsync(h->host_loop, h->g.loop, sizeof(LoopState), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    st = *h->host_loop;
+    if (!std::isfinite(st.t) || !std::isfinite(st.dt)) {
+      h->cur = st.cur;
+      h->last_cycles_run = st.cycles_run;
+      return MHD_ERR_NONFINITE;
+    }
+    // size the next chunk from the remaining cycles (graphs past the end are no-ops)
+    long long remaining = st.max_cycles - st.cycle;
+    if (st.dt > 0.0) {
+      const double est = std::ceil((st.t_end - st.t) / st.dt) + 1.0;
+      if (est < (double)remaining) remaining = (long long)est;
+    }
+    budget_pairs = std::max(1LL, std::min((remaining + 1) / 2, 256LL));
+  }
+  h->cur = st.cur;
+  h->last_cycles_run = st.cycles_run;
+  if (t_out) *t_out = st.t;
+  if (cycle_out) *cycle_out = st.cycle;
+  if (t_second_last) *t_second_last = st.cycles_run > 0 ? st.t_prev : t0;
+  return MHD_OK;
+}
+
+int mhd2d_download(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || (which != 0 && which != 1)) return MHD_ERR_ARG;
+  if (!h->have_state) return MHD_ERR_STATE;
+  int b = h->cur;
+  if (which == 1 && h->last_cycles_run > 0) b ^= 1;
+  const mhdk::StateBuf& s = h->g.st[b];
+  const size_t cb = (size_t)h->nvars * mhdk::cell_plane(h->g) * sizeof(double);
+  if (prim) CK(cudaMemcpyAsync(prim, s.prim, cb, cudaMemcpyDeviceToHost, h->stream));
+  if (cons) CK(cudaMemcpyAsync(cons, s.cons, cb, cudaMemcpyDeviceToHost, h->stream));
+  if (h->g.physics == MHD2D_MHD) {
+    if (faceBx) CK(cudaMemcpyAsync(faceBx, s.fbx, mhdk::xface_plane(h->g) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (faceBy) CK(cudaMemcpyAsync(faceBy, s.fby, mhdk::yface_plane(h->g) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd2d_state_ptrs(void* handle, int which, double** prim, double** cons, double** faceBx, double** faceBy) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || (which != 0 && which != 1)) return MHD_ERR_ARG;
+  int b = h->cur;
+  if (which == 1 && h->last_cycles_run > 0) b ^= 1;
+  const mhdk::StateBuf& s = h->g.st[b];
+  if (prim) *prim = s.prim;
+  if (cons) *cons = s.cons;
+  if (faceBx) *faceBx = s.fbx;
+  if (faceBy) *faceBy = s.fby;
+  return MHD_OK;
+}
+
+int mhd2d_peek(void* handle, int what, double* out, size_t count) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !out) return MHD_ERR_ARG;
+  const Grid& g = h->g;
+  const int nv = g.physics == MHD2D_MHD ? 7 : 5;
+  const double* src = nullptr;
+  size_t n = 0;
+  switch (what) {
+    case 0: src = g.xl; n = nv * mhdk::xface_plane(g); break;
+    case 1: src = g.xr; n = nv * mhdk::xface_plane(g); break;
+    case 2: src = g.yl; n = nv * mhdk::yface_plane(g); break;
+    case 3: src = g.yr; n = nv * mhdk::yface_plane(g); break;
+    case 4: src = g.fx; n = nv * mhdk::xface_plane(g); break;
+    case 5: src = g.fy; n = nv * mhdk::yface_plane(g); break;
+    case 6: src = g.emf; n = mhdk::corner_plane(g); break;
+    case 7: src = g.nfbx; n = mhdk::xface_plane(g); break;
+    case 8: src = g.nfby; n = mhdk::yface_plane(g); break;
+    default: return MHD_ERR_ARG;
+  }
+  if (!src || count < n) return MHD_ERR_ARG;
+  CK(cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd2d_last_launches(void* handle, long long* launches) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !launches) return MHD_ERR_ARG;
+  *launches = h->last_launches;
+  return MHD_OK;
+}
+
+int mhd2d_device_bytes(void* handle, size_t* bytes) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !bytes) return MHD_ERR_ARG;
+  *bytes = h->arena_bytes;
+  return MHD_OK;
+}
+
+int mhd2d_stream(void* handle, void** stream) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !stream) return MHD_ERR_ARG;
+  *stream = h->stream;
+  return MHD_OK;
+}
+
+}  // extern "C"

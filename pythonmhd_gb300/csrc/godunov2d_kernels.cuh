@@ -1,0 +1,945 @@
+// Kernels of one 2D CTU(+CT) cycle.  Included by two translation units that
+// define MHD_NS: `exact` (built with -fmad=false: reproduces the reference's
+// NumPy arithmetic bit for bit) and `fast` (FMA contraction allowed).
+//
+// A cycle (Source/EvolveFunctions_MHD.py:464-692, Source/EvolveFunctions_Hydro.py:390-513):
+//   dt_reduce -> begin -> [slopes_x -> faces_x -> slopes_y -> faces_y]
+//   -> roe_x(1) -> roe_y(1) -> [MHD: emf(1)] -> ctu_x -> ctu_y
+//   -> [MHD: half] -> roe_x(2) -> roe_y(2) -> [MHD: emf(2)] -> final -> end
+// Every kernel returns at once when the loop state says the cycle is not a real
+// one (t >= t_end or cycle >= max_cycles), so a captured graph can be replayed
+// past the end of a run without changing the state.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "godunov2d_types.h"
+#include "mhd_math.cuh"
+
+#ifndef MHD_NS
+#error "define MHD_NS"
+#endif
+
+namespace mhdk {
+namespace MHD_NS {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ int wrapc(int c, int L, int bc) {
+  if (bc == PERIODIC) {
+    int m = c % L;
+    return m < 0 ? m + L : m;
+  }
+  return c < 0 ? 0 : (c >= L ? L - 1 : c);
+}
+
+// ----------------------------------------------------------------------------
+// Sweep policies
+// ----------------------------------------------------------------------------
+template <int AX>
+struct MhdSweep {
+  static constexpr int NV = 7;
+  static constexpr int NW = kPrimEigWords;
+  static constexpr int N = AX == 0 ? 1 : 2;
+  static constexpr int T1 = AX == 0 ? 2 : 3;
+  static constexpr int T2 = AX == 0 ? 3 : 1;
+  static constexpr int BN = AX == 0 ? 4 : 5;   // prim8 slot of the cell normal B
+  static constexpr int SB = AX == 0 ? 4 : 5;   // sweep slot that gets the B source term
+  __device__ static constexpr int src(int k) {
+    return AX == 0 ? (k < 4 ? k : (k == 4 ? 5 : (k == 5 ? 6 : 7)))
+                   : (k < 4 ? k : (k == 4 ? 6 : (k == 5 ? 4 : 7)));
+  }
+  __device__ static constexpr int ord(int k) {
+    return k == 0 ? 0 : k == 1 ? N : k == 2 ? T1 : k == 3 ? T2 : k == 4 ? 6 : k == 5 ? 4 : 5;
+  }
+  using Eig = PrimEig;
+  __device__ static void eig(const double* w, double bn, double gamma, Eig& e) {
+    prim_eigensystem<N, T1, T2>(w, bn, gamma, e);
+  }
+  __device__ static bool Lnz(int i, int j) { return prim_L_nz<N, T1, T2>(i, j); }
+  __device__ static bool Rnz(int i, int j) { return prim_R_nz<N, T1, T2>(i, j); }
+  __device__ static double L(const Eig& e, int i, int j) { return prim_L<N, T1, T2>(e, i, j); }
+  __device__ static double R(const Eig& e, int i, int j) { return prim_R<N, T1, T2>(e, i, j); }
+  __device__ static double* lam(Eig& e) { return e.lam; }
+  __device__ static void store(const Eig& e, double* p, size_t stride) {
+    const double* s = reinterpret_cast<const double*>(&e);
+#pragma unroll
+    for (int k = 0; k < NW; ++k) p[k * stride] = s[k];
+  }
+  __device__ static void load(Eig& e, const double* p, size_t stride) {
+    double* s = reinterpret_cast<double*>(&e);
+#pragma unroll
+    for (int k = 0; k < NW; ++k) s[k] = p[k * stride];
+  }
+};
+
+template <int AX>
+struct HydroSweep {
+  static constexpr int NV = 5;
+  static constexpr int NW = 10;
+  static constexpr bool Y = AX == 1;
+  static constexpr int BN = -1;
+  static constexpr int SB = -1;
+  __device__ static constexpr int src(int k) { return k; }
+  __device__ static constexpr int ord(int k) { return k; }
+  using Eig = HPrimEig;
+  __device__ static void eig(const double* w, double, double gamma, Eig& e) { hprim_eigensystem<Y>(w, gamma, e); }
+  __device__ static bool Lnz(int i, int j) { return hprim_L_nz<Y>(i, j); }
+  __device__ static bool Rnz(int i, int j) { return hprim_R_nz<Y>(i, j); }
+  __device__ static double L(const Eig& e, int i, int j) { return hprim_L<Y>(e, i, j); }
+  __device__ static double R(const Eig& e, int i, int j) { return hprim_R<Y>(e, i, j); }
+  __device__ static double* lam(Eig& e) { return e.lam; }
+  __device__ static void store(const Eig& e, double* p, size_t stride) {
+    const double* s = reinterpret_cast<const double*>(&e);
+#pragma unroll
+    for (int k = 0; k < NW; ++k) p[k * stride] = s[k];
+  }
+  __device__ static void load(Eig& e, const double* p, size_t stride) {
+    double* s = reinterpret_cast<double*>(&e);
+#pragma unroll
+    for (int k = 0; k < NW; ++k) s[k] = p[k * stride];
+  }
+};
+
+// Row i of L times v in the reference's accumulation order.
+template <class S>
+__device__ __forceinline__ double project(const typename S::Eig& e, int i, const double* v) {
+  double acc = 0.0;
+  bool first = true;
+#pragma unroll
+  for (int k = 0; k < S::NV; ++k) {
+    const int j = S::ord(k);
+    if (S::Lnz(i, j)) {
+      const double t = S::L(e, i, j) * v[j];
+      acc = first ? t : acc + t;
+      first = false;
+    }
+  }
+  return acc;
+}
+
+struct SweepGeom {
+  int Ls, Lt, nx;  // sweep length, transverse length, row stride of the cell grid
+  int bc;
+};
+
+template <int AX>
+__device__ __forceinline__ size_t cell_index(int c, int t, int nx) {
+  return AX == 0 ? (size_t)t * nx + c : (size_t)c * nx + t;
+}
+template <int AX>
+__device__ __forceinline__ size_t ext_index(int c, int t, int nx) {
+  // c in [-1, Ls]; extended grid has Ls+2 cells along the sweep
+  return AX == 0 ? (size_t)t * (nx + 2) + (c + 1) : (size_t)(c + 1) * nx + t;
+}
+template <int AX>
+__device__ __forceinline__ size_t face_index(int f, int t, int nx) {
+  return AX == 0 ? (size_t)t * (nx + 1) + f : (size_t)f * nx + t;
+}
+
+template <class S, int AX>
+__device__ __forceinline__ void load_sweep_cell(const double* prim, size_t plane, int c, int t,
+                                                const SweepGeom& g, double* w) {
+  const size_t idx = cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx);
+#pragma unroll
+  for (int k = 0; k < S::NV; ++k) w[k] = __ldg(prim + S::src(k) * plane + idx);
+}
+
+// ----------------------------------------------------------------------------
+// PPM phase A: eigensystem + monotonised characteristic slopes for cells -1..Ls
+// (Source/Reconstruction_PPM_MHD_HelperModule.py:317-389, Hydro :86-200)
+// ----------------------------------------------------------------------------
+template <class S, int AX>
+__global__ void __launch_bounds__(kBlock) k_ppm_slopes(Grid G, StateBuf in) {
+  if (!G.loop->active) return;
+  SweepGeom g;
+  g.nx = G.nx;
+  g.Ls = AX == 0 ? G.nx : G.ny;
+  g.Lt = AX == 0 ? G.ny : G.nx;
+  g.bc = AX == 0 ? G.bcx : G.bcy;
+  int c, t;
+  if (AX == 0) { c = blockIdx.x * blockDim.x + threadIdx.x - 1; t = blockIdx.y; }
+  else { t = blockIdx.x * blockDim.x + threadIdx.x; c = (int)blockIdx.y - 1; }
+  if (c > g.Ls || t >= g.Lt) return;
+  const size_t plane = cell_plane(G);
+  constexpr int NV = S::NV;
+  double wl[NV], wc[NV], wr[NV];
+  load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
+  load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
+  load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
+  double bn = 0.0;
+  if (S::BN >= 0) bn = __ldg(in.prim + (size_t)(S::BN >= 0 ? S::BN : 0) * plane + cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx));
+  typename S::Eig e;
+  S::eig(wc, bn, G.gamma, e);
+
+  double dc[NV], dl[NV], dr[NV], wt[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    dc[k] = wr[k] - wl[k];
+    dl[k] = wc[k] - wl[k];
+    dr[k] = wr[k] - wc[k];
+    wt[k] = (dl[k] * dr[k] > 0.0) ? (2.0 * dl[k] * dr[k]) / (dl[k] + dr[k]) : 0.0;
+  }
+  double sc[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const double cc = project<S>(e, i, dc);
+    const double cl = project<S>(e, i, dl);
+    const double cr = project<S>(e, i, dr);
+    const double cw = project<S>(e, i, wt);
+    double s = 0.0;
+    if (cl * cr > 0.0) {
+      const double lim1 = dmin(fabs(cl), fabs(cr));
+      const double lim2 = dmin(0.5 * fabs(cc), fabs(cw));
+      s = signed_mag(cc, dmin(2.0 * lim1, lim2));
+    }
+    sc[i] = s;
+  }
+  const size_t xi = ext_index<AX>(c, t, g.nx);
+  const size_t es = G.ext_plane;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double acc = 0.0;
+    bool first = true;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      if (S::Rnz(i, j)) {
+        const double tt = sc[j] * S::R(e, i, j);
+        acc = first ? tt : acc + tt;
+        first = false;
+      }
+    }
+    G.slopes[i * es + xi] = acc;
+  }
+  S::store(e, G.eig + xi, es);
+}
+
+// Write one reconstructed state to a face: floors (Source/PrimCons_HelperModule.py:499-554),
+// then the transverse-B source term (Source/EvolveFunctions_MHD.py:524-535).
+template <class S>
+__device__ __forceinline__ void put_face(double* buf, size_t fplane, size_t fidx, const double* v,
+                                         double min_d, double min_p, double bsrc) {
+  constexpr int NV = S::NV;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = v[k];
+    if (k == 0 && x < min_d) x = min_d;
+    if (k == NV - 1 && x < min_p) x = min_p;
+    if (k == S::SB) x = x + bsrc;
+    buf[k * fplane + fidx] = x;
+  }
+}
+
+// B source term of one face state: half_dt * v_t(cell) * ((fb[f2] - fb[f1]) * inv_dn)
+// (Source/Reconstruction_PPM_MHD_HelperModule.py:1193-1239)
+template <int AX>
+__device__ __forceinline__ double bsource(const double* prim, const double* fb, size_t plane, int cell, int f1,
+                                          int f2, int t, int nx, double half_dt, double inv_dn) {
+  const int vslot = AX == 0 ? 2 : 1;
+  const double vt = __ldg(prim + vslot * plane + cell_index<AX>(cell, t, nx));
+  const double b2 = __ldg(fb + face_index<AX>(f2, t, nx));
+  const double b1 = __ldg(fb + face_index<AX>(f1, t, nx));
+  return half_dt * vt * ((b2 - b1) * inv_dn);
+}
+
+// ----------------------------------------------------------------------------
+// PPM phase B / first order: interface values, monotonicity, characteristic
+// tracing, face states (Source/Reconstruction_PPM_MHD_HelperModule.py:391-548)
+// ----------------------------------------------------------------------------
+template <class S, int AX, bool PPM>
+__global__ void __launch_bounds__(kBlock) k_faces(Grid G, StateBuf in) {
+  if (!G.loop->active) return;
+  SweepGeom g;
+  g.nx = G.nx;
+  g.Ls = AX == 0 ? G.nx : G.ny;
+  g.Lt = AX == 0 ? G.ny : G.nx;
+  g.bc = AX == 0 ? G.bcx : G.bcy;
+  int c, t;
+  if (AX == 0) { c = blockIdx.x * blockDim.x + threadIdx.x; t = blockIdx.y; }
+  else { t = blockIdx.x * blockDim.x + threadIdx.x; c = blockIdx.y; }
+  if (c >= g.Ls || t >= g.Lt) return;
+  const size_t plane = cell_plane(G);
+  constexpr int NV = S::NV;
+  const double dt = G.loop->dt;
+  const double dn = AX == 0 ? G.dx : G.dy;
+  double lia[NV], ria[NV];
+  double wc[NV];
+  load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
+  if (PPM) {
+    double wl[NV], wr[NV];
+    load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
+    load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
+    const size_t es = G.ext_plane;
+    const size_t xl = ext_index<AX>(c - 1, t, g.nx);
+    const size_t xc = ext_index<AX>(c, t, g.nx);
+    const size_t xr = ext_index<AX>(c + 1, t, g.nx);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double s_l = G.slopes[k * es + xl];
+      const double s_c = G.slopes[k * es + xc];
+      const double s_r = G.slopes[k * es + xr];
+      double a = 0.5 * (wc[k] + wl[k]) - (s_c - s_l) / 6.0;
+      double b = 0.5 * (wr[k] + wc[k]) - (s_r - s_c) / 6.0;
+      const double dprod = (b - wc[k]) * (wc[k] - a);
+      const double idiff = b - a;
+      const double adiff = 6.0 * (wc[k] - 0.5 * (a + b));
+      if (dprod <= 0.0) {
+        a = wc[k];
+        b = wc[k];
+      } else if ((idiff * adiff) > sq(idiff)) {
+        a = (6.0 * wc[k] - 4.0 * b) / 2.0;
+      } else if ((idiff * adiff) < (-1.0 * sq(idiff))) {
+        b = (6.0 * wc[k] - 4.0 * a) / 2.0;
+      }
+      a = dmax(dmin(wc[k], wl[k]), a);
+      a = dmin(dmax(wc[k], wl[k]), a);
+      b = dmax(dmin(wc[k], wr[k]), b);
+      b = dmin(dmax(wc[k], wr[k]), b);
+      lia[k] = a;
+      ria[k] = b;
+    }
+    typename S::Eig e;
+    S::load(e, G.eig + xc, es);
+    const double* lam = S::lam(e);
+    const double dtdx = dt / dn;
+    double c1[NV], c2[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      c1[k] = ria[k] - lia[k];
+      c2[k] = 6.0 * (wc[k] - 0.5 * (lia[k] + ria[k]));
+    }
+    const double c3 = 0.5 * dmax(lam[NV - 1], 0.0) * dtdx;
+    const double c4 = -0.5 * dmin(lam[0], 0.0) * dtdx;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      lia[k] = lia[k] + c4 * (c1[k] + (1.0 - FOUR_THIRDS * c4) * c2[k]);
+      ria[k] = ria[k] - c3 * (c1[k] - (1.0 - FOUR_THIRDS * c3) * c2[k]);
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      if (lam[i] <= 0.0) {
+        const double v1 = 0.5 * dtdx * lam[0];
+        const double v2 = 0.5 * dtdx * lam[i];
+        const double v3 = v1 - v2;
+        const double v4 = FOUR_THIRDS * (sq(v1) - sq(v2));
+        double fac = 0.0;
+        bool first = true;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          const int j = S::ord(k);
+          if (S::Lnz(i, j)) {
+            const double tt = S::L(e, i, j) * (v3 * (c1[j] + c2[j]) + v4 * c2[j]);
+            fac = first ? tt : fac + tt;
+            first = false;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < NV; ++j)
+          if (S::Rnz(j, i)) lia[j] = lia[j] + fac * S::R(e, j, i);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      if (lam[i] >= 0.0) {
+        const double v1 = 0.5 * dtdx * lam[NV - 1];
+        const double v2 = 0.5 * dtdx * lam[i];
+        const double v3 = v1 - v2;
+        const double v4 = FOUR_THIRDS * (sq(v1) - sq(v2));
+        double fac = 0.0;
+        bool first = true;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          const int j = S::ord(k);
+          if (S::Lnz(i, j)) {
+            const double tt = S::L(e, i, j) * (v3 * (c1[j] - c2[j]) + v4 * c2[j]);
+            fac = first ? tt : fac + tt;
+            first = false;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < NV; ++j)
+          if (S::Rnz(j, i)) ria[j] = ria[j] + fac * S::R(e, j, i);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) { lia[k] = wc[k]; ria[k] = wc[k]; }
+  }
+
+  // Face writes: cell c gives the right state of face c and the left state of face c+1;
+  // the boundary cells also fill face 0 / face Ls (reference :529-548).
+  double* outL = AX == 0 ? G.xl : G.yl;
+  double* outR = AX == 0 ? G.xr : G.yr;
+  const size_t fplane = AX == 0 ? xface_plane(G) : yface_plane(G);
+  const int Ls = g.Ls;
+  double s_mid = 0.0, s_lo = 0.0, s_hi = 0.0;
+  if (S::SB >= 0) {
+    const double* fb = AX == 0 ? in.fbx : in.fby;
+    const double half_dt = 0.5 * dt;
+    const double inv_dn = 1.0 / dn;
+    s_mid = bsource<AX>(in.prim, fb, plane, c, c, c + 1, t, g.nx, half_dt, inv_dn);
+    if (c == 0) {
+      if (g.bc == OUTFLOW) s_lo = bsource<AX>(in.prim, fb, plane, 0, 0, 0, t, g.nx, half_dt, inv_dn);
+      else s_hi = bsource<AX>(in.prim, fb, plane, 0, Ls, 1, t, g.nx, half_dt, inv_dn);
+    }
+    if (c == Ls - 1) {
+      if (g.bc == OUTFLOW) s_hi = bsource<AX>(in.prim, fb, plane, Ls - 1, Ls, Ls, t, g.nx, half_dt, inv_dn);
+      else s_lo = bsource<AX>(in.prim, fb, plane, Ls - 1, Ls - 1, 0, t, g.nx, half_dt, inv_dn);
+    }
+  }
+  put_face<S>(outR, fplane, face_index<AX>(c, t, g.nx), lia, G.min_d, G.min_p, s_mid);
+  put_face<S>(outL, fplane, face_index<AX>(c + 1, t, g.nx), ria, G.min_d, G.min_p, s_mid);
+  if (c == 0) {
+    if (g.bc == OUTFLOW) put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), lia, G.min_d, G.min_p, s_lo);
+    else put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), lia, G.min_d, G.min_p, s_hi);
+  }
+  if (c == Ls - 1) {
+    if (g.bc == OUTFLOW) put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), ria, G.min_d, G.min_p, s_hi);
+    else put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), ria, G.min_d, G.min_p, s_lo);
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Roe fluxes at every face of one direction.  Stage 1 converts the reconstructed
+// prim states with the current face B; stage 2 reads the CTU-corrected cons and
+// prim states (converted with the half-step face B in k_ctu_mhd).
+// ----------------------------------------------------------------------------
+template <int AX, int STAGE>
+__global__ void __launch_bounds__(kBlock) k_roe_mhd(Grid G, StateBuf in) {
+  if (!G.loop->active) return;
+  const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
+  const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  constexpr int N = AX == 0 ? 1 : 2, T1 = AX == 0 ? 2 : 3, T2 = AX == 0 ? 3 : 1;
+  const double* WL = AX == 0 ? G.xl : G.yl;
+  const double* WR = AX == 0 ? G.xr : G.yr;
+  double wl[7], wr[7], ul[7], ur[7];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) { wl[k] = WL[k * nf + f]; wr[k] = WR[k * nf + f]; }
+  double bn;
+  if (STAGE == 1) {
+    bn = (AX == 0 ? in.fbx : in.fby)[f];
+    prim_to_cons7(wl, bn, G.gamma, ul);
+    prim_to_cons7(wr, bn, G.gamma, ur);
+  } else {
+    bn = (AX == 0 ? G.nfbx : G.nfby)[f];
+    const double* UL = AX == 0 ? G.uxl : G.uyl;
+    const double* UR = AX == 0 ? G.uxr : G.uyr;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) { ul[k] = UL[k * nf + f]; ur[k] = UR[k * nf + f]; }
+  }
+  double flux[7];
+  roe_flux<N, T1, T2>(wl, wr, ul, ur, bn, G.gamma, G.efix != 0, G.eps, flux);
+  double* F = AX == 0 ? G.fx : G.fy;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) F[k * nf + f] = flux[k];
+}
+
+template <int AX>
+__global__ void __launch_bounds__(kBlock) k_roe_hydro(Grid G) {
+  if (!G.loop->active) return;
+  const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
+  const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const double* WL = AX == 0 ? G.xl : G.yl;
+  const double* WR = AX == 0 ? G.xr : G.yr;
+  double wl[5], wr[5], flux[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) { wl[k] = WL[k * nf + f]; wr[k] = WR[k * nf + f]; }
+  hroe_flux<AX == 1>(wl, wr, G.gamma, G.efix != 0, G.eps, flux);
+  double* F = AX == 0 ? G.fx : G.fy;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) F[k * nf + f] = flux[k];
+}
+
+// ----------------------------------------------------------------------------
+// Corner EMF (Source/CornerEMF_HelperModule.py:440-529)
+// STAGE 1 takes the cell Ez = vy*Bx - vx*By from the primitives
+// (Source/EvolveFunctions_MHD.py:541); STAGE 2 the half-step Ez.
+// ----------------------------------------------------------------------------
+template <int STAGE>
+__device__ __forceinline__ double cell_ez(const Grid& G, const StateBuf& in, int j, int i) {
+  const size_t idx = (size_t)j * G.nx + i;
+  if (STAGE == 2) return G.hez[idx];
+  const size_t plane = cell_plane(G);
+  return __ldg(in.prim + 2 * plane + idx) * __ldg(in.prim + 4 * plane + idx)
+       - __ldg(in.prim + 1 * plane + idx) * __ldg(in.prim + 5 * plane + idx);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock) k_emf(Grid G, StateBuf in) {
+  if (!G.loop->active) return;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y;
+  const int nx = G.nx, ny = G.ny;
+  if (I > nx || J > ny) return;
+  const int ic = wrapc(I, nx, G.bcx), im = wrapc(I - 1, nx, G.bcx);
+  const int jc = wrapc(J, ny, G.bcy), jm = wrapc(J - 1, ny, G.bcy);
+  const size_t yfp = yface_plane(G), xfp = xface_plane(G);
+  // y-face fluxes of row J at columns I (top) and I-1 (ltop)
+  const double top0 = G.fy[0 * yfp + (size_t)J * nx + ic];
+  const double top5 = G.fy[5 * yfp + (size_t)J * nx + ic];
+  const double lt0 = G.fy[0 * yfp + (size_t)J * nx + im];
+  const double lt5 = G.fy[5 * yfp + (size_t)J * nx + im];
+  // x-face fluxes of column I at rows J (left) and J-1 (uleft)
+  const double l0 = G.fx[0 * xfp + (size_t)jc * (nx + 1) + I];
+  const double l4 = G.fx[4 * xfp + (size_t)jc * (nx + 1) + I];
+  const double ul0 = G.fx[0 * xfp + (size_t)jm * (nx + 1) + I];
+  const double ul4 = G.fx[4 * xfp + (size_t)jm * (nx + 1) + I];
+  const double ec = cell_ez<STAGE>(G, in, jc, ic);
+  const double el = cell_ez<STAGE>(G, in, jc, im);
+  const double eu = cell_ez<STAGE>(G, in, jm, ic);
+  const double eul = cell_ez<STAGE>(G, in, jm, im);
+  double x1 = 0.0, x2 = 0.0, y1 = 0.0, y2 = 0.0;
+  if (lt0 > 0.0) x1 = lt5 - ul4 - eul;
+  else if (lt0 < 0.0) x1 = lt5 - l4 - el;
+  else if (lt0 == 0.0) x1 = lt5 - 0.5 * (l4 + ul4 + el + eul);
+  if (top0 > 0.0) x2 = top5 - ul4 - eu;
+  else if (top0 < 0.0) x2 = top5 - l4 - ec;
+  else if (top0 == 0.0) x2 = top5 - 0.5 * (l4 + ul4 + ec + eu);
+  if (ul0 > 0.0) y1 = -ul4 + lt5 - eul;
+  else if (ul0 < 0.0) y1 = -ul4 + top5 - eu;
+  else if (ul0 == 0.0) y1 = -ul4 + 0.5 * (lt5 + top5 - eul - eu);
+  if (l0 > 0.0) y2 = -l4 + lt5 - el;
+  else if (l0 < 0.0) y2 = -l4 + top5 - ec;
+  else if (l0 == 0.0) y2 = -l4 + 0.5 * (lt5 + top5 - el - ec);
+  G.emf[(size_t)J * (nx + 1) + I] = 0.25 * (x1 + x2 + y1 + y2);
+}
+
+// ----------------------------------------------------------------------------
+// CTU transverse predictor for MHD face states (Source/CTU_HelperModule.py:282-444,
+// Source/EvolveFunctions_MHD.py:557-592): cons += transverse flux difference +
+// source, cons floors, half-step face B, prim with the half-step face B.
+// ----------------------------------------------------------------------------
+template <int AX>
+__global__ void __launch_bounds__(kBlock) k_ctu_mhd(Grid G, StateBuf in) {
+  if (!G.loop->active) return;
+  const int nx = G.nx, ny = G.ny;
+  const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
+  const size_t fl = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (fl >= nf) return;
+  const int width = AX == 0 ? nx + 1 : nx;
+  const int row = (int)(fl / width), col = (int)(fl % width);
+  // sweep-face index f and transverse index t
+  const int f = AX == 0 ? col : row;
+  const int t = AX == 0 ? row : col;
+  const int Ls = AX == 0 ? nx : ny;
+  const int bc = AX == 0 ? G.bcx : G.bcy;
+  const double dt = G.loop->dt;
+  const double half_dt = 0.5 * dt;
+  const double inv_dn = 1.0 / (AX == 0 ? G.dx : G.dy);
+  const double half_dtdt = 0.5 * (dt / (AX == 0 ? G.dy : G.dx));   // transverse
+  const size_t plane = cell_plane(G);
+  const double* fb = AX == 0 ? in.fbx : in.fby;
+  auto fbv = [&](int ff) { return fb[face_index<AX>(ff, t, nx)]; };
+  const double bn = fb[fl];
+
+  // half-step face B from the stage-1 corner EMF (Source/EvolveFunctions_MHD.py:579-586)
+  double nb;
+  if (AX == 0) {
+    const double lo = G.emf[(size_t)(row + 1) * (nx + 1) + col];
+    const double up = G.emf[(size_t)row * (nx + 1) + col];
+    nb = bn - half_dtdt * (lo - up);
+    G.nfbx[fl] = nb;
+  } else {
+    const double r = G.emf[(size_t)row * (nx + 1) + col + 1];
+    const double l = G.emf[(size_t)row * (nx + 1) + col];
+    nb = bn + half_dtdt * (r - l);
+    G.nfby[fl] = nb;
+  }
+
+  double* Wout[2] = {AX == 0 ? G.xl : G.yl, AX == 0 ? G.xr : G.yr};
+  double* Uout[2] = {AX == 0 ? G.uxl : G.uyl, AX == 0 ? G.uxr : G.uyr};
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    double w[7], u[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) w[k] = Wout[side][k * nf + fl];
+    prim_to_cons7(w, bn, G.gamma, u);
+
+    // padded cell index kpad and its source cell / dB (Source/CTU_HelperModule.py:293-345, :377-430)
+    const int kpad = f + side;
+    int scell;
+    double lb, rb;
+    if (AX == 0) {
+      scell = wrapc(kpad - 1, Ls, bc);
+      if (bc == OUTFLOW) {
+        lb = fbv(kpad - 1 < 0 ? 0 : (kpad - 1 > Ls ? Ls : kpad - 1));
+        rb = fbv(kpad > Ls ? Ls : kpad);
+      } else {
+        lb = fbv(kpad == 0 ? Ls - 1 : kpad - 1);
+        rb = fbv(kpad == Ls + 1 ? 1 : kpad);
+      }
+    } else {
+      if (bc == OUTFLOW) {
+        scell = kpad == 0 ? 1 : (kpad - 1 > Ls - 1 ? Ls - 1 : kpad - 1);
+        lb = fbv(kpad == 0 ? 1 : kpad - 1);
+        rb = fbv(kpad == Ls + 1 ? Ls - 1 : kpad);
+      } else {
+        scell = wrapc(kpad - 1, Ls, bc);
+        lb = fbv(kpad == 0 ? Ls - 1 : kpad - 1);
+        rb = fbv(kpad == Ls + 1 ? 1 : kpad);
+      }
+    }
+    const double dB = rb - lb;
+    const size_t sidx = cell_index<AX>(scell, t, nx);
+    const double cbx = __ldg(in.prim + 4 * plane + sidx);
+    const double cby = __ldg(in.prim + 5 * plane + sidx);
+    const double cbz = __ldg(in.prim + 6 * plane + sidx);
+    const double cvz = __ldg(in.prim + 3 * plane + sidx);
+    double src[7];
+    src[0] = 0.0;
+    src[1] = cbx * dB * inv_dn;
+    src[2] = cby * dB * inv_dn;
+    src[3] = cbz * dB * inv_dn;
+    src[4] = AX == 0 ? 0.0 : cvz * dB * inv_dn;
+    src[5] = AX == 0 ? cvz * dB * inv_dn : 0.0;
+    src[6] = (cbz * cvz) * dB * inv_dn;
+
+    // transverse flux difference of the cell on this side (standard wrap/clamp)
+    const int fc = wrapc(f - 1 + side, Ls, bc);
+    const double* F = AX == 0 ? G.fy : G.fx;
+    const size_t tfp = AX == 0 ? yface_plane(G) : xface_plane(G);
+    size_t i_lo, i_hi;  // lower/upper transverse face of cell (fc, t)
+    if (AX == 0) { i_lo = (size_t)t * nx + fc; i_hi = (size_t)(t + 1) * nx + fc; }
+    else { i_lo = (size_t)fc * (nx + 1) + t; i_hi = (size_t)fc * (nx + 1) + t + 1; }
+    double fh[7], flo[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) { fh[k] = F[k * tfp + i_hi]; flo[k] = F[k * tfp + i_lo]; }
+    // remap: x-sweep takes the y-flux Bz (slot 4) into slot 5 and zeroes slot 4;
+    // y-sweep takes the x-flux Bz (slot 5) into slot 4 and zeroes slot 5
+    if (AX == 0) { fh[5] = fh[4]; fh[4] = 0.0; flo[5] = flo[4]; flo[4] = 0.0; }
+    else { fh[4] = fh[5]; fh[5] = 0.0; flo[4] = flo[5]; flo[5] = 0.0; }
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      const bool zero_src = (k == 0) || (AX == 0 ? k == 4 : k == 5);
+      const double corr = zero_src ? (-half_dtdt * (fh[k] - flo[k]))
+                                   : (-half_dtdt * (fh[k] - flo[k]) + half_dt * src[k]);
+      u[k] = u[k] + corr;
+    }
+    if (u[0] < G.min_d) u[0] = G.min_d;
+    if (u[6] < G.min_e) u[6] = G.min_e;
+    double w2[7];
+    cons_to_prim7(u, nb, G.gamma, w2);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      Uout[side][k * nf + fl] = u[k];
+      Wout[side][k * nf + fl] = w2[k];
+    }
+  }
+}
+
+// Hydro CTU (Source/EvolveFunctions_Hydro.py:460-489): cons -= half dt/dn * transverse
+// flux difference, back to prim.
+template <int AX>
+__global__ void __launch_bounds__(kBlock) k_ctu_hydro(Grid G) {
+  if (!G.loop->active) return;
+  const int nx = G.nx;
+  const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
+  const size_t fl = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (fl >= nf) return;
+  const int width = AX == 0 ? nx + 1 : nx;
+  const int row = (int)(fl / width), col = (int)(fl % width);
+  const int f = AX == 0 ? col : row;
+  const int t = AX == 0 ? row : col;
+  const int Ls = AX == 0 ? G.nx : G.ny;
+  const int bc = AX == 0 ? G.bcx : G.bcy;
+  const double dt = G.loop->dt;
+  const double half_dtdt = 0.5 * (dt / (AX == 0 ? G.dy : G.dx));
+  double* Wout[2] = {AX == 0 ? G.xl : G.yl, AX == 0 ? G.xr : G.yr};
+  const double* F = AX == 0 ? G.fy : G.fx;
+  const size_t tfp = AX == 0 ? yface_plane(G) : xface_plane(G);
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    double w[5], u[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) w[k] = Wout[side][k * nf + fl];
+    hprim_to_cons<AX == 1>(w, G.gamma, u);
+    const int fc = wrapc(f - 1 + side, Ls, bc);
+    size_t i_lo, i_hi;
+    if (AX == 0) { i_lo = (size_t)t * nx + fc; i_hi = (size_t)(t + 1) * nx + fc; }
+    else { i_lo = (size_t)fc * (nx + 1) + t; i_hi = (size_t)fc * (nx + 1) + t + 1; }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) u[k] = u[k] - half_dtdt * (F[k * tfp + i_hi] - F[k * tfp + i_lo]);
+    hcons_to_prim<AX == 1>(u, G.gamma, w);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) Wout[side][k * nf + fl] = w[k];
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Half-step cell Ez (Source/EvolveFunctions_MHD.py:594-624)
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_half_ez(Grid G, StateBuf in) {
+  if (!G.loop->active) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  const int nx = G.nx;
+  if (i >= nx || j >= G.ny) return;
+  const double dt = G.loop->dt;
+  const double hx = 0.5 * (dt / G.dx), hy = 0.5 * (dt / G.dy);
+  const size_t plane = cell_plane(G), xfp = xface_plane(G), yfp = yface_plane(G);
+  const size_t idx = (size_t)j * nx + i;
+  const size_t xr = (size_t)j * (nx + 1) + i + 1, xlf = (size_t)j * (nx + 1) + i;
+  const size_t yb = (size_t)(j + 1) * nx + i, yt = (size_t)j * nx + i;
+  double hu[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double u = __ldg(in.cons + k * plane + idx);
+    u = u - hx * (G.fx[k * xfp + xr] - G.fx[k * xfp + xlf]);
+    u = u - hy * (G.fy[k * yfp + yb] - G.fy[k * yfp + yt]);
+    hu[k] = u;
+  }
+  const double hbx = (G.nfbx[xlf] + G.nfbx[xr]) / 2.0;
+  const double hby = (G.nfby[yt] + G.nfby[yb]) / 2.0;
+  const double hvx = hu[1] / hu[0];
+  const double hvy = hu[2] / hu[0];
+  G.hez[idx] = hvy * hbx - hvx * hby;
+}
+
+// ----------------------------------------------------------------------------
+// Final update (Source/EvolveFunctions_MHD.py:643-687; Hydro :502-506)
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_final_mhd(Grid G, StateBuf in, StateBuf out) {
+  if (!G.loop->active) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  const int nx = G.nx, ny = G.ny;
+  if (i >= nx || j >= ny) return;
+  const double dt = G.loop->dt;
+  const double dtdy = dt / G.dy, dtdx = dt / G.dx;
+  const size_t plane = cell_plane(G), xfp = xface_plane(G), yfp = yface_plane(G);
+  const size_t idx = (size_t)j * nx + i;
+  const size_t xlf = (size_t)j * (nx + 1) + i, xr = xlf + 1;
+  const size_t yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
+  const size_t cw = nx + 1;
+  const double* E = G.emf;
+  // full-step face B (Source/EvolveFunctions_MHD.py:644-645)
+  const double bxl = in.fbx[xlf] - dtdy * (E[(size_t)(j + 1) * cw + i] - E[(size_t)j * cw + i]);
+  const double bxr = in.fbx[xr] - dtdy * (E[(size_t)(j + 1) * cw + i + 1] - E[(size_t)j * cw + i + 1]);
+  const double byt = in.fby[yt] + dtdx * (E[(size_t)j * cw + i + 1] - E[(size_t)j * cw + i]);
+  const double byb = in.fby[yb] + dtdx * (E[(size_t)(j + 1) * cw + i + 1] - E[(size_t)(j + 1) * cw + i]);
+  out.fbx[xlf] = bxl;
+  if (i == nx - 1) out.fbx[xr] = bxr;
+  out.fby[yt] = byt;
+  if (j == ny - 1) out.fby[yb] = byb;
+  const double cbx = (bxl + bxr) / 2.0;
+  const double cby = (byt + byb) / 2.0;
+  // conservative update of the x-sweep cons vector [rho, mx, my, mz, By, Bz, E]
+  const int cslot[7] = {0, 1, 2, 3, 5, 6, 7};
+  double u[7];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) u[k] = __ldg(in.cons + cslot[k] * plane + idx);
+  const double bz = u[5] - dtdx * (G.fx[5 * xfp + xr] - G.fx[5 * xfp + xlf])
+                         - dtdy * (G.fy[4 * yfp + yb] - G.fy[4 * yfp + yt]);
+  const int upd[5] = {0, 1, 2, 3, 6};
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    const int k = upd[q];
+    double v = u[k] - dtdx * (G.fx[k * xfp + xr] - G.fx[k * xfp + xlf]);
+    v = v - dtdy * (G.fy[k * yfp + yb] - G.fy[k * yfp + yt]);
+    u[k] = v;
+  }
+  u[5] = bz;
+  u[4] = cby;
+  double w[7];
+  cons_to_prim7(u, cbx, G.gamma, w);
+  const double po[8] = {w[0], w[1], w[2], w[3], cbx, w[4], w[5], w[6]};
+  const double co[8] = {u[0], u[1], u[2], u[3], cbx, u[4], u[5], u[6]};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    out.prim[k * plane + idx] = po[k];
+    out.cons[k * plane + idx] = co[k];
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_final_hydro(Grid G, StateBuf in, StateBuf out) {
+  if (!G.loop->active) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  const int nx = G.nx;
+  if (i >= nx || j >= G.ny) return;
+  const double dt = G.loop->dt;
+  const double dtdx = dt / G.dx, dtdy = dt / G.dy;
+  const size_t plane = cell_plane(G), xfp = xface_plane(G), yfp = yface_plane(G);
+  const size_t idx = (size_t)j * nx + i;
+  const size_t xlf = (size_t)j * (nx + 1) + i, xr = xlf + 1;
+  const size_t yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
+  double u[5], w[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    double v = __ldg(in.cons + k * plane + idx);
+    v = v - dtdx * (G.fx[k * xfp + xr] - G.fx[k * xfp + xlf]);
+    v = v - dtdy * (G.fy[k * yfp + yb] - G.fy[k * yfp + yt]);
+    u[k] = v;
+  }
+  hcons_to_prim<false>(u, G.gamma, w);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    out.prim[k * plane + idx] = w[k];
+    out.cons[k * plane + idx] = u[k];
+  }
+}
+
+// ----------------------------------------------------------------------------
+// CFL reduction (Source/TimestepCalculations_HelperModule.py:67-109, :239-289):
+// per-cell max signal speeds, warp-shuffle + block max, one atomicMax per block on
+// the bit pattern (non-negative doubles order like their 64-bit integers).
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = dmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <int PHYS>
+__global__ void __launch_bounds__(256) k_dt_reduce(Grid G, StateBuf in) {
+  LoopState* L = G.loop;
+  if (!(L->t < L->t_end && L->cycle < L->max_cycles)) return;
+  const int nx = G.nx;
+  const size_t n = cell_plane(G);
+  const size_t plane = n;
+  const double gamma = G.gamma;
+  double mx = 0.0, my = 0.0;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const double* c = in.cons;
+    const double inv_d = 1.0 / c[idx];
+    const double vx = c[plane + idx] * inv_d;
+    const double vy = c[2 * plane + idx] * inv_d;
+    const double vz = c[3 * plane + idx] * inv_d;
+    const double vsq = vx * vx + vy * vy + vz * vz;
+    if (PHYS == MHD) {
+      const int j = (int)(idx / nx), i = (int)(idx % nx);
+      const double c4 = c[4 * plane + idx], c5 = c[5 * plane + idx];
+      const double bx = c4 + fabs(in.fbx[(size_t)j * (nx + 1) + i] - c4);
+      const double by = c5 + fabs(in.fby[(size_t)j * nx + i] - c5);
+      const double bz = c[6 * plane + idx];
+      const double bsq = bx * bx + by * by + bz * bz;
+      const double p = dmax((gamma - 1.0) * (c[7 * plane + idx] - 0.5 * c[idx] * vsq - 0.5 * bsq), SMALL_VALUE);
+      const double a2 = gamma * p * inv_d;
+      const double ssum = bsq * inv_d + a2;
+      const double sdiff = bsq * inv_d - a2;
+      const double cfx2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (by * by + bz * bz) * inv_d));
+      const double cfy2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (bx * bx + bz * bz) * inv_d));
+      mx = dmax(mx, fabs(vx) + sqrt(cfx2));
+      my = dmax(my, fabs(vy) + sqrt(cfy2));
+    } else {
+      const double p = dmax((gamma - 1.0) * (c[4 * plane + idx] - 0.5 * c[idx] * vsq), SMALL_VALUE);
+      const double a = sqrt(gamma * p * inv_d);
+      mx = dmax(mx, fabs(vx) + a);
+      my = dmax(my, fabs(vy) + a);
+    }
+  }
+  __shared__ double sx[8], sy[8];
+  mx = warp_max(mx);
+  my = warp_max(my);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sx[wid] = mx; sy[wid] = my; }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    mx = lane < nw ? sx[lane] : 0.0;
+    my = lane < nw ? sy[lane] : 0.0;
+    mx = warp_max(mx);
+    my = warp_max(my);
+    if (lane == 0) {
+      atomicMax(&L->max_sx, (unsigned long long)__double_as_longlong(mx));
+      atomicMax(&L->max_sy, (unsigned long long)__double_as_longlong(my));
+    }
+  }
+}
+
+// dt from the reduced speeds, the tEnd clip, and the loop condition
+// (Source/EvolveFunctions_MHD.py:466-479).
+template <int PHYS>
+__global__ void k_begin(Grid G) {
+  LoopState* L = G.loop;
+  const int act = (L->t < L->t_end && L->cycle < L->max_cycles) ? 1 : 0;
+  L->active = act;
+  if (act) {
+    const double mx = __longlong_as_double((long long)L->max_sx);
+    const double my = __longlong_as_double((long long)L->max_sy);
+    double dt;
+    if (PHYS == MHD) {
+      const double inv = dmax(mx / G.dx, my / G.dy);
+      dt = L->cfl / inv;
+    } else {
+      const double dtx = L->cfl / (mx / G.dx);
+      const double dty = L->cfl / (my / G.dy);
+      dt = dmin(dtx, dty);
+    }
+    if (L->t + dt > L->t_end) dt = L->t_end - L->t;
+    L->dt = dt;
+  }
+  L->max_sx = 0ull;
+  L->max_sy = 0ull;
+}
+
+__global__ void k_end(Grid G) {
+  LoopState* L = G.loop;
+  if (!L->active) return;
+  L->t_prev = L->t;
+  L->t = L->t + L->dt;
+  L->cycle = L->cycle + 1;
+  L->cycles_run = L->cycles_run + 1;
+  L->cur ^= 1;
+  L->active = 0;
+}
+
+// ----------------------------------------------------------------------------
+// Host-side enqueue of one cycle reading state buffer `parity`.
+// ----------------------------------------------------------------------------
+inline dim3 row_grid(int n, int rows) { return dim3((unsigned)((n + kBlock - 1) / kBlock), (unsigned)rows); }
+inline unsigned lin_grid(size_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+template <int PHYS>
+void enqueue_recon(const Grid& g, const StateBuf& in, cudaStream_t s) {
+  using SX = typename std::conditional<PHYS == MHD, MhdSweep<0>, HydroSweep<0>>::type;
+  using SY = typename std::conditional<PHYS == MHD, MhdSweep<1>, HydroSweep<1>>::type;
+  if (g.recon == 2) {
+    k_ppm_slopes<SX, 0><<<row_grid(g.nx + 2, g.ny), kBlock, 0, s>>>(g, in);
+    k_faces<SX, 0, true><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_ppm_slopes<SY, 1><<<row_grid(g.nx, g.ny + 2), kBlock, 0, s>>>(g, in);
+    k_faces<SY, 1, true><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+  } else {
+    k_faces<SX, 0, false><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_faces<SY, 1, false><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+  }
+}
+
+void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s) {
+  const StateBuf in = g.st[parity];
+  const StateBuf out = g.st[parity ^ 1];
+  const size_t nxf = xface_plane(g), nyf = yface_plane(g);
+  if (g.physics == MHD) {
+    k_dt_reduce<MHD><<<dt_blocks, 256, 0, s>>>(g, in);
+    k_begin<MHD><<<1, 1, 0, s>>>(g);
+    enqueue_recon<MHD>(g, in, s);
+    k_roe_mhd<0, 1><<<lin_grid(nxf), kBlock, 0, s>>>(g, in);
+    k_roe_mhd<1, 1><<<lin_grid(nyf), kBlock, 0, s>>>(g, in);
+    k_emf<1><<<row_grid(g.nx + 1, g.ny + 1), kBlock, 0, s>>>(g, in);
+    k_ctu_mhd<0><<<lin_grid(nxf), kBlock, 0, s>>>(g, in);
+    k_ctu_mhd<1><<<lin_grid(nyf), kBlock, 0, s>>>(g, in);
+    k_half_ez<<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_roe_mhd<0, 2><<<lin_grid(nxf), kBlock, 0, s>>>(g, in);
+    k_roe_mhd<1, 2><<<lin_grid(nyf), kBlock, 0, s>>>(g, in);
+    k_emf<2><<<row_grid(g.nx + 1, g.ny + 1), kBlock, 0, s>>>(g, in);
+    k_final_mhd<<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in, out);
+  } else {
+    k_dt_reduce<HYDRO><<<dt_blocks, 256, 0, s>>>(g, in);
+    k_begin<HYDRO><<<1, 1, 0, s>>>(g);
+    enqueue_recon<HYDRO>(g, in, s);
+    k_roe_hydro<0><<<lin_grid(nxf), kBlock, 0, s>>>(g);
+    k_roe_hydro<1><<<lin_grid(nyf), kBlock, 0, s>>>(g);
+    k_ctu_hydro<0><<<lin_grid(nxf), kBlock, 0, s>>>(g);
+    k_ctu_hydro<1><<<lin_grid(nyf), kBlock, 0, s>>>(g);
+    k_roe_hydro<0><<<lin_grid(nxf), kBlock, 0, s>>>(g);
+    k_roe_hydro<1><<<lin_grid(nyf), kBlock, 0, s>>>(g);
+    k_final_hydro<<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in, out);
+  }
+  k_end<<<1, 1, 0, s>>>(g);
+}
+
+}  // namespace MHD_NS
+}  // namespace mhdk

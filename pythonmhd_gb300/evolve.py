@@ -1,0 +1,124 @@
+"""Drop-in replacements for the reference's 2D evolve functions.
+
+``evolve_2D_mhd`` and ``evolve_2D_hydro`` keep the reference signatures, the
+preconditions they assert, their return tuples and their aliasing:
+
+* Source/EvolveFunctions_MHD.py:393-697  evolve_2D_mhd(simulationGrid, tStart, tEnd,
+  startCycle, maxCycles, gamma, cfl, minDens, minPres, minEnergy,
+  reconstructOrder=0, entropyFix=False, epsilon=0.5)
+  -> (prim, cons, faceBx, faceBy, time, cycle, secondLastPrim, secondLastCons,
+      secondLastFaceBx, secondLastFaceBy, secondLastTime);
+  faceBx/faceBy are updated in place in the grid's arrays and returned,
+  prim/cons are new arrays (the grid's own objects when no cycle runs).
+* Source/EvolveFunctions_Hydro.py:350-516 evolve_2D_hydro(...) (same arguments)
+  -> (prim, cons, time, cycle, secondLastPrim, secondLastCons, secondLastTime);
+  the grid's primVars/consVars are updated in place and returned.
+
+The cycles run on the GPU (``Grid2D.advance``); the host uploads the grid once
+per call and downloads the result.  Handles are cached per grid geometry and
+parameters, so the driver's repeated calls reuse device memory and CUDA graphs.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .solver import Grid2D, default_arith
+
+OUTFLOW = 0
+PERIODIC = 1
+
+_cache: dict = {}
+_CACHE_MAX = 4
+
+
+def _handle(key, make):
+    h = _cache.get(key)
+    if h is None:
+        while len(_cache) >= _CACHE_MAX:
+            _cache.pop(next(iter(_cache))).close()
+        h = make()
+        _cache[key] = h
+    return h
+
+
+def clear_cache():
+    while _cache:
+        _cache.popitem()[1].close()
+
+
+def evolve_2D_mhd(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cfl, minDens, minPres,
+                  minEnergy, reconstructOrder=0, entropyFix=False, epsilon=0.5, arith=None):
+    prim = simulationGrid.primVars
+    bcx = simulationGrid.BcX
+    assert (bcx == OUTFLOW or bcx == PERIODIC)
+    bcy = simulationGrid.BcY
+    assert (bcy == OUTFLOW or bcy == PERIODIC)
+    assert (len(prim.shape) == 3)
+    assert (prim.shape[0] == 8)
+    assert (prim.shape[1] > 0)
+    fbx = simulationGrid.faceBx
+    fby = simulationGrid.faceBy
+    cons = simulationGrid.consVars
+    assert (prim.shape == cons.shape)
+    dx = simulationGrid.dx
+    assert (dx > 0)
+    dy = simulationGrid.dy
+    assert (dy > 0)
+    assert (tStart <= tEnd)
+    assert (startCycle >= 0)
+    ny, nx = prim.shape[1:]
+    order = 2 if reconstructOrder == 2 else 0
+    mode = arith or default_arith()
+    key = ("mhd", ny, nx, float(dx), float(dy), bcx, bcy, float(gamma), order, bool(entropyFix),
+           float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)
+    g = _handle(key, lambda: Grid2D(ny, nx, dx, dy, bcx, bcy, gamma, mhd=True, recon=order,
+                                    entropy_fix=entropyFix, eps=epsilon, min_d=minDens, min_p=minPres,
+                                    min_e=minEnergy, arith=mode))
+    g.upload(prim, cons, fbx, fby)
+    t, cyc, t_sl = g.advance(tStart, tEnd, startCycle, maxCycles, cfl)
+    if g.last_cycles == 0:
+        return (prim, cons, fbx, fby, tStart, startCycle, np.copy(prim), np.copy(cons), np.copy(fbx),
+                np.copy(fby), tStart)
+    new_prim, new_cons, new_fbx, new_fby = g.download(0)
+    sl_prim, sl_cons, sl_fbx, sl_fby = g.download(1)
+    np.copyto(fbx, new_fbx)
+    np.copyto(fby, new_fby)
+    return (new_prim, new_cons, fbx, fby, t, cyc, sl_prim, sl_cons, sl_fbx, sl_fby, t_sl)
+
+
+def evolve_2D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cfl, minDens, minPres,
+                    minEnergy, reconstructOrder=0, entropyFix=False, epsilon=0.5, arith=None):
+    prim = simulationGrid.primVars
+    assert (len(prim.shape) == 3)
+    cons = simulationGrid.consVars
+    assert (prim.shape == cons.shape)
+    nx = simulationGrid.numXCells
+    assert (nx > 1)
+    ny = simulationGrid.numYCells
+    assert (ny > 1)
+    dx = simulationGrid.dx
+    assert (dx > 0)
+    dy = simulationGrid.dy
+    assert (dy > 0)
+    bcx = simulationGrid.BcX
+    assert (bcx == OUTFLOW or bcx == PERIODIC)
+    bcy = simulationGrid.BcY
+    assert (bcy == OUTFLOW or bcy == PERIODIC)
+    assert (tStart <= tEnd)
+    assert (startCycle >= 0 and maxCycles > 0)
+    order = 2 if reconstructOrder == 2 else 0
+    mode = arith or default_arith()
+    key = ("hydro", ny, nx, float(dx), float(dy), bcx, bcy, float(gamma), order, bool(entropyFix),
+           float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)
+    g = _handle(key, lambda: Grid2D(ny, nx, dx, dy, bcx, bcy, gamma, mhd=False, recon=order,
+                                    entropy_fix=entropyFix, eps=epsilon, min_d=minDens, min_p=minPres,
+                                    min_e=minEnergy, arith=mode))
+    g.upload(prim, cons)
+    t, cyc, t_sl = g.advance(tStart, tEnd, startCycle, maxCycles, cfl)
+    if g.last_cycles == 0:
+        return prim, cons, tStart, startCycle, np.copy(prim), np.copy(cons), tStart
+    sl_prim, sl_cons = g.download(1)
+    new_prim, new_cons = g.download(0)
+    np.copyto(prim, new_prim)
+    np.copyto(cons, new_cons)
+    return prim, cons, t, cyc, sl_prim, sl_cons, t_sl

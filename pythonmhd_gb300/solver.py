@@ -1,0 +1,147 @@
+"""Host-side handle of one 2D grid on the GPU (thin wrapper over the C ABI)."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _lib
+
+ARITH = {"exact": 0, "fast": 1}
+
+
+def default_arith() -> str:
+    """Arithmetic mode used when none is given: ``PYTHONMHD_GB300_ARITH`` or "exact"."""
+    mode = os.environ.get("PYTHONMHD_GB300_ARITH", "exact").lower()
+    if mode not in ARITH:
+        raise ValueError(f"PYTHONMHD_GB300_ARITH must be one of {sorted(ARITH)}, got {mode!r}")
+    return mode
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_lib.c_double_p) if a is not None else None
+
+
+def _as_f64c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Grid2D:
+    """One ny x nx grid (hydro or MHD) resident on the current CUDA device.
+
+    The state is uploaded with :meth:`upload`, advanced on the device with
+    :meth:`advance` (the reference's evolve loop) and copied back with
+    :meth:`download`.  ``arith="exact"`` reproduces the reference's float64
+    arithmetic bit for bit; ``"fast"`` allows fused multiply-adds.
+    """
+
+    def __init__(self, ny, nx, dx, dy, bcx, bcy, gamma, mhd=True, recon=2, entropy_fix=False,
+                 eps=0.5, min_d=1e-12, min_p=1e-12, min_e=1e-12, arith=None):
+        self.lib = _lib.load()
+        self.ny, self.nx = int(ny), int(nx)
+        self.mhd = bool(mhd)
+        self.nvars = 8 if self.mhd else 5
+        self.arith = arith or default_arith()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.mhd2d_create(self.ny, self.nx, float(dx), float(dy), int(bcx), int(bcy),
+                                         float(gamma), 1 if self.mhd else 0, int(recon),
+                                         1 if entropy_fix else 0, float(eps), float(min_d),
+                                         float(min_p), float(min_e), ARITH[self.arith], ctypes.byref(h)),
+                   "mhd2d_create")
+        self._h = h
+        self.last_cycles = 0
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.lib.mhd2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- shapes -----------------------------------------------------------
+    def cell_shape(self):
+        return (self.nvars, self.ny, self.nx)
+
+    def check_shapes(self, prim, cons, fbx=None, fby=None):
+        if prim.shape != self.cell_shape() or cons.shape != self.cell_shape():
+            raise ValueError(f"prim/cons must have shape {self.cell_shape()}, got {prim.shape}, {cons.shape}")
+        if self.mhd:
+            if fbx is None or fby is None:
+                raise ValueError("MHD grids need faceBx and faceBy")
+            if fbx.shape != (self.ny, self.nx + 1) or fby.shape != (self.ny + 1, self.nx):
+                raise ValueError(f"faceBx/faceBy must be {(self.ny, self.nx + 1)}/{(self.ny + 1, self.nx)}")
+
+    # -- data movement ----------------------------------------------------
+    def upload(self, prim, cons, fbx=None, fby=None):
+        prim, cons = _as_f64c(prim), _as_f64c(cons)
+        fbx = _as_f64c(fbx) if fbx is not None else None
+        fby = _as_f64c(fby) if fby is not None else None
+        self.check_shapes(prim, cons, fbx, fby)
+        _lib.check(self.lib.mhd2d_upload(self._h, _ptr(prim), _ptr(cons), _ptr(fbx), _ptr(fby)),
+                   "mhd2d_upload")
+
+    def download(self, which=0, prim=None, cons=None, fbx=None, fby=None):
+        """Copy the current (which=0) or second-last (which=1) state into new or given arrays."""
+        prim = np.empty(self.cell_shape()) if prim is None else prim
+        cons = np.empty(self.cell_shape()) if cons is None else cons
+        if self.mhd:
+            fbx = np.empty((self.ny, self.nx + 1)) if fbx is None else fbx
+            fby = np.empty((self.ny + 1, self.nx)) if fby is None else fby
+        for a in (prim, cons, fbx, fby):
+            if a is not None and not (a.dtype == np.float64 and a.flags.c_contiguous):
+                raise ValueError("download targets must be C-contiguous float64")
+        _lib.check(self.lib.mhd2d_download(self._h, int(which), _ptr(prim), _ptr(cons), _ptr(fbx), _ptr(fby)),
+                   "mhd2d_download")
+        return (prim, cons, fbx, fby) if self.mhd else (prim, cons)
+
+    def advance(self, t0, t_end, cycle0, max_cycles, cfl):
+        t = ctypes.c_double()
+        c = ctypes.c_longlong()
+        tsl = ctypes.c_double()
+        _lib.check(self.lib.mhd2d_advance(self._h, float(t0), float(t_end), int(cycle0), int(max_cycles),
+                                          float(cfl), ctypes.byref(t), ctypes.byref(c), ctypes.byref(tsl)),
+                   "mhd2d_advance")
+        self.last_cycles = c.value - int(cycle0)
+        return t.value, c.value, tsl.value
+
+    def peek(self, what):
+        """Intermediates of the last cycle (see mhd2d_peek in include/pythonmhd_gb300.h)."""
+        nv = 7 if self.mhd else 5
+        nx, ny = self.nx, self.ny
+        shapes = {0: (nv, ny, nx + 1), 1: (nv, ny, nx + 1), 2: (nv, ny + 1, nx), 3: (nv, ny + 1, nx),
+                  4: (nv, ny, nx + 1), 5: (nv, ny + 1, nx), 6: (ny + 1, nx + 1), 7: (ny, nx + 1),
+                  8: (ny + 1, nx)}
+        out = np.empty(shapes[what])
+        _lib.check(self.lib.mhd2d_peek(self._h, int(what), _ptr(out), out.size), "mhd2d_peek")
+        return out
+
+    def last_launches(self):
+        n = ctypes.c_longlong()
+        _lib.check(self.lib.mhd2d_last_launches(self._h, ctypes.byref(n)), "mhd2d_last_launches")
+        return n.value
+
+    def device_bytes(self):
+        n = ctypes.c_size_t()
+        _lib.check(self.lib.mhd2d_device_bytes(self._h, ctypes.byref(n)), "mhd2d_device_bytes")
+        return n.value
+
+    def state_ptrs(self, which=0):
+        ptrs = [ctypes.c_void_p() for _ in range(4)]
+        _lib.check(self.lib.mhd2d_state_ptrs(self._h, int(which), *[ctypes.byref(p) for p in ptrs]),
+                   "mhd2d_state_ptrs")
+        return [p.value for p in ptrs]
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _lib.check(self.lib.mhd2d_stream(self._h, ctypes.byref(s)), "mhd2d_stream")
+        return s.value

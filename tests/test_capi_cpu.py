@@ -1,0 +1,71 @@
+"""CPU-side checks of the C ABI library: it builds for sm_103a, loads, and
+exports every entry point that include/pythonmhd_gb300.h declares.  No compute
+call is made here (there is no GPU in this environment)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from pythonmhd_gb300 import _lib, build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "pythonmhd_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mhd2d_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    for n in ("mhd2d_create", "mhd2d_upload", "mhd2d_advance", "mhd2d_download", "mhd2d_destroy",
+              "mhd2d_strerror"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_signatures_cover_the_header():
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+def test_strerror_names_every_status(lib):
+    for code in range(0, 7):
+        assert lib.mhd2d_strerror(code).decode() not in ("", "unknown status")
+    assert lib.mhd2d_strerror(99).decode() == "unknown status"
+
+
+def test_create_rejects_bad_arguments_before_touching_the_device(lib):
+    h = ctypes.c_void_p()
+    bad = [
+        (1, 16, 0.1, 0.1, 1, 1),     # ny < 2
+        (16, 1, 0.1, 0.1, 1, 1),     # nx < 2
+        (16, 16, 0.0, 0.1, 1, 1),    # dx <= 0
+        (16, 16, 0.1, 0.1, 2, 1),    # bad BC code
+    ]
+    for ny, nx, dx, dy, bx, by in bad:
+        rc = lib.mhd2d_create(ny, nx, dx, dy, bx, by, 1.4, 1, 2, 0, 0.5, 1e-12, 1e-12, 1e-12, 0, ctypes.byref(h))
+        assert rc == 1 and not h.value
+    rc = lib.mhd2d_create(16, 16, 0.1, 0.1, 1, 1, 1.4, 1, 1, 0, 0.5, 1e-12, 1e-12, 1e-12, 0, ctypes.byref(h))
+    assert rc == 1  # recon=1 (PLM) is not a reference order
+    assert lib.mhd2d_upload(None, None, None, None, None) == 1
+    lib.mhd2d_destroy(None)
+
+
+def test_null_handle_calls_fail_cleanly(lib):
+    t = ctypes.c_double()
+    c = ctypes.c_longlong()
+    assert lib.mhd2d_advance(None, 0.0, 1.0, 0, 1, 0.4, ctypes.byref(t), ctypes.byref(c), ctypes.byref(t)) == 1
+    assert lib.mhd2d_download(None, 0, None, None, None, None) == 1
