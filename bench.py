@@ -171,11 +171,23 @@ def measured_peaks():
         return {}
 
 
-def profile_summary():
-    """Per-launch DRAM traffic / FP64 instruction counts from the committed ncu summary."""
+def profile_summary(arith):
+    """Per-cycle DRAM traffic / FP64 instruction counts from the committed ncu summary."""
     try:
-        with open(os.path.join(ROOT, "profiles", "mhd_ppm_cycle_ncu.json")) as f:
+        with open(os.path.join(ROOT, "profiles", f"mhd_ppm_cycle_ncu_{arith}.json")) as f:
             return json.load(f)
+    except Exception:
+        return None
+
+
+def fp64_peak():
+    """DFMA lane-ops/s of this GPU from the FP64 probe (pythonmhd_gb300/csrc/fp64_probe.cu)."""
+    try:
+        from pythonmhd_gb300 import build as _build
+        exe = _build.build_probe()
+        out = subprocess.run([exe, "--json"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=120).stdout
+        return json.loads(out.strip().splitlines()[-1])
     except Exception:
         return None
 
@@ -271,7 +283,8 @@ def run_ours(a):
     peak_src = "measured" if hbm_peak else "fallback"
     hbm_peak = hbm_peak or 6800.0
     achieved = ALG_BYTES_PER_ZONE * zones / (ms_per * 1e-3) / 1e9
-    prof = profile_summary()
+    prof = profile_summary(a.arith)
+    probe = fp64_peak() if rank == 0 else None
     traffic = None
     fp64 = None
     if prof:
@@ -280,12 +293,12 @@ def run_ours(a):
             traffic = prof["dram_bytes_per_cycle"] * scale
         if prof.get("fp64_lane_ops_per_zone"):
             ops = prof["fp64_lane_ops_per_zone"] * zones
-            fp64 = {"achieved_gops": ops / (ms_per * 1e-3) / 1e9,
-                    "peak_gops": prof.get("fp64_peak_gops"),
-                    "unit": "G FP64 lane-instr/s (DFMA/DADD/DMUL counted once)",
-                    "ops_per_zone": prof["fp64_lane_ops_per_zone"],
-                    "frac": (ops / (ms_per * 1e-3) / 1e9) / prof["fp64_peak_gops"] if prof.get("fp64_peak_gops") else None,
-                    "source": prof.get("source")}
+            ach = ops / (ms_per * 1e-3) / 1e9
+            peak = probe["dfma_gops"] if probe else None
+            fp64 = {"achieved": ach, "peak": peak, "unit": "G FP64 lane-instr/s",
+                    "frac": ach / peak if peak else None, "ops_per_zone": prof["fp64_lane_ops_per_zone"],
+                    "peak_source": "measured DFMA rate (fp64_probe, same box)" if probe else None,
+                    "ops_source": prof.get("source")}
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "traffic": traffic,
             "kernel": "one full cycle (CUDA graph of 17 kernels), 128 algorithmic B/zone",

@@ -1,0 +1,86 @@
+"""GPU checks at sizes where the golden fixtures stop: bitwise agreement with the
+oracle on larger grids, and size-independent properties of the CTU+CT step at
+the full 4096^2 workload (periodic duplicate faces bitwise equal, conservation
+to roundoff, div B at roundoff, Orszag-Tang point symmetry)."""
+import numpy as np
+import pytest
+
+from oracle import mhd2d
+from pythonmhd_gb300 import initial_conditions as ic
+from pythonmhd_gb300.solver import Grid2D
+from tests.gpu_util import field_rel_err
+
+pytestmark = pytest.mark.gpu
+G = 5.0 / 3.0
+
+
+def _run(prim, cons, fbx, fby, dx, dy, cycles, arith="exact", recon=2, bc=(1, 1)):
+    ny, nx = prim.shape[1:]
+    g = Grid2D(ny, nx, dx, dy, bc[0], bc[1], G, mhd=True, recon=recon, arith=arith)
+    g.upload(prim, cons, fbx, fby)
+    t, c, tsl = g.advance(0.0, 1e30, 0, cycles, 0.4)
+    out = g.download(0)
+    g.close()
+    return out, t
+
+
+def _div_b(fbx, fby, dx, dy):
+    return (fbx[:, 1:] - fbx[:, :-1]) / dx + (fby[1:, :] - fby[:-1, :]) / dy
+
+
+@pytest.mark.parametrize("n,cycles", [(128, 3)])
+def test_turbulence_bitwise_vs_oracle(n, cycles):
+    prim, cons, fbx, fby, dx, dy = ic.turbulence(n, seed=5, gamma=G)
+    (gp, gc, gbx, gby), t = _run(prim, cons, fbx, fby, dx, dy, cycles)
+    want = mhd2d.evolve(prim, cons, fbx, fby, dx, dy, 1, 1, 0.0, 1e30, 0, cycles, G, 0.4,
+                        1e-12, 1e-12, 1e-12, 2, False, 0.5)
+    for a, b in zip((gp, gc, gbx, gby, t), want[:4] + (want[4],)):
+        assert np.array_equal(np.asarray(a), np.asarray(b))
+
+
+def test_orszag_tang_bitwise_vs_oracle_10_cycles():
+    prim, cons, fbx, fby, dx, dy = ic.orszag_tang(96, 96, gamma=G)
+    (gp, gc, gbx, gby), t = _run(prim, cons, fbx, fby, dx, dy, 10)
+    want = mhd2d.evolve(prim, cons, fbx, fby, dx, dy, 1, 1, 0.0, 1e30, 0, 10, G, 0.4,
+                        1e-12, 1e-12, 1e-12, 2, False, 0.5)
+    for a, b in zip((gp, gc, gbx, gby, t), want[:4] + (want[4],)):
+        assert np.array_equal(np.asarray(a), np.asarray(b))
+
+
+def test_fast_mode_within_1e12_on_turbulence_512():
+    """The FMA build on the benchmark's state (non-degenerate) agrees with the exact build per cycle."""
+    prim, cons, fbx, fby, dx, dy = ic.turbulence(512, seed=2, gamma=G)
+    (ep, ec, ebx, eby), _ = _run(prim, cons, fbx, fby, dx, dy, 1, "exact")
+    (fp, fc, fbx2, fby2), _ = _run(prim, cons, fbx, fby, dx, dy, 1, "fast")
+    assert field_rel_err(fp, ep) <= 1e-12
+    assert field_rel_err(fc, ec) <= 1e-12
+    assert field_rel_err(fbx2, ebx) <= 1e-12
+    assert field_rel_err(fby2, eby) <= 1e-12
+
+
+@pytest.mark.parametrize("n,cycles", [(4096, 2)])
+def test_full_size_invariants(n, cycles):
+    prim, cons, fbx, fby, dx, dy = ic.turbulence(n, seed=1, gamma=G)
+    (p, c, bx, by), t = _run(prim, cons, fbx, fby, dx, dy, cycles)
+    assert np.isfinite(c).all() and t > 0.0
+    # periodic duplicate faces stay bitwise equal
+    assert np.array_equal(bx[:, 0], bx[:, -1])
+    assert np.array_equal(by[0, :], by[-1, :])
+    # conservation of mass, momentum, energy and Bz (volume totals)
+    for k in (0, 1, 2, 3, 6, 7):
+        ref = np.sum(np.abs(cons[k]))
+        assert abs(np.sum(c[k]) - np.sum(cons[k])) <= 1e-12 * ref + 1e-12, k
+    # div B at roundoff, relative to |B|/dx
+    d0 = np.max(np.abs(_div_b(fbx, fby, dx, dy))) * dx
+    d1 = np.max(np.abs(_div_b(bx, by, dx, dy))) * dx
+    bmax = np.max(np.abs(fbx))
+    assert d1 <= max(10 * d0, 1e-13 * bmax)
+
+
+def test_orszag_tang_point_symmetry():
+    n = 256
+    prim, cons, fbx, fby, dx, dy = ic.orszag_tang(n, n, gamma=G)
+    (p, c, bx, by), t = _run(prim, cons, fbx, fby, dx, dy, 20)
+    rho = p[0]
+    sym = rho[::-1, ::-1]
+    assert np.max(np.abs(rho - sym)) <= 1e-12 * np.max(rho)
