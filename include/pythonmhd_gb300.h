@@ -94,6 +94,30 @@ int mhd2d_device_bytes(void* handle, size_t* bytes);
 /* The CUDA stream the handle's work runs on (a cudaStream_t). */
 int mhd2d_stream(void* handle, void** stream);
 
+/* Largest ny accepted by mhd2d_cfl_dt_noalloc (its static scratch holds two
+ * doubles per grid row). */
+#define MHD2D_NOALLOC_MAX_ROWS 16384
+
+/* CFL timestep of one state without allocating anything.  No counterpart in the
+ * reference: it is the reference's CFL formula (calcDt_2D_mhd / calcDt_2D_hydro)
+ * offered to callers that cannot allocate device memory -- code whose device
+ * memory is owned by another framework's caching allocator, or a stepping loop
+ * that must not call cudaMalloc/cudaFree each step (cudaFree synchronises the
+ * device).  The caller passes device pointers: cons (nvars, ny, nx), faceBx
+ * (ny, nx+1) and faceBy (ny+1, nx) for MHD (NULL for hydro), and dt_out (one
+ * double); the work is queued on `stream` (NULL = the default stream) and the
+ * call returns without waiting.  Scratch is a static device array of
+ * 2 * MHD2D_NOALLOC_MAX_ROWS doubles (256 KB) that every GPU loading the library
+ * holds until exit; ny > MHD2D_NOALLOC_MAX_ROWS returns MHD_ERR_TOO_LARGE.  The
+ * first call on each device looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU (different streams, or different
+ * host threads with the same device) race and may return a wrong dt.  The result
+ * equals the dt the exact-arithmetic step uses, bit for bit. */
+int mhd2d_cfl_dt_noalloc(int physics, int ny, int nx, double dx, double dy, double gamma,
+                         double cfl, const double* cons, const double* faceBx,
+                         const double* faceBy, double* dt_out, void* stream);
+
 const char* mhd2d_strerror(int status);
 void mhd2d_destroy(void* handle);
 

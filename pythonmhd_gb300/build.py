@@ -6,6 +6,7 @@ shared library with a plain C ABI (``include/pythonmhd_gb300.h``):
 * ``csrc/kernels_exact.cu``  -- the step kernels with ``-fmad=false``
 * ``csrc/kernels_fast.cu``   -- the same kernels with FMA contraction
 * ``csrc/capi.cu``           -- handles, copies and the CUDA-graph evolve loop
+* ``csrc/noalloc.cu``        -- the CFL timestep for callers that cannot allocate
 """
 from __future__ import annotations
 
@@ -26,6 +27,7 @@ UNITS = [
     ("kernels_exact.cu", ["-fmad=false"]),
     ("kernels_fast.cu", ["-fmad=true"]),
     ("capi.cu", []),
+    ("noalloc.cu", ["-fmad=false"]),
 ]
 
 
