@@ -47,7 +47,8 @@ enum mhd2d_arith { MHD2D_ARITH_EXACT = 0, MHD2D_ARITH_FAST = 1 };
 
 /* Create a handle for an ny x nx grid.  bcx/bcy: 0 outflow, 1 periodic
  * (Source/PythonMHD_Constants.py:11-12).  recon: 0 first order, 2 PPM
- * (Source/EvolveFunctions_MHD.py:483-511).  arith: MHD2D_ARITH_EXACT reproduces
+ * (Source/EvolveFunctions_MHD.py:483-511), 1 PLM (an addition: the reference's
+ * PLM branches are commented out, Source/EvolveFunctions_MHD.py:487-488).  arith: MHD2D_ARITH_EXACT reproduces
  * the reference's float64 arithmetic bit for bit; MHD2D_ARITH_FAST lets the
  * compiler fuse multiply-adds (results agree to rounding).  Requires nx, ny >= 2. */
 int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma,

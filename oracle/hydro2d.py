@@ -107,9 +107,10 @@ def _project(L, i, vec):
     return acc
 
 
-def ppm_sweep(w, gamma, dt, dn, bc, yaxis):
+def ppm_sweep(w, gamma, dt, dn, bc, yaxis, linear=False):
     """ppmReconstructX/Y_hydro (Source/Reconstruction_PPM_Hydro_HelperModule.py:86-371, :387-620)
-    along the last axis of ``w`` (5, M, N)."""
+    along the last axis of ``w`` (5, M, N); ``linear=True`` gives the PLM variant
+    (no reference counterpart, see ``oracle.mhd2d.plm_edges``)."""
     N = w.shape[-1]
     g = wrap_index(np.arange(-2, N + 2), N, bc)
     we = take_x(w, g)
@@ -148,6 +149,13 @@ def ppm_sweep(w, gamma, dt, dn, bc, yaxis):
     wc = wc[..., 1:-1]
     wl = wl[..., 1:-1]
     wr = wr[..., 1:-1]
+    if linear:
+        from .mhd2d import plm_edges
+        lam = [x[..., 1:-1] for x in lam]
+        L = {k: v[..., 1:-1] for k, v in L.items()}
+        R = {k: v[..., 1:-1] for k, v in R.items()}
+        lia, ria = plm_edges(wc, wl, wr, s_c, lam, L, R, dt / dn, tuple(range(5)), 5)
+        return faces_from_cells(lia, ria, bc)
     lia = 0.5 * (wc + wl) - (s_c - s_l) / 6.0
     ria = 0.5 * (wr + wc) - (s_r - s_c) / 6.0
     dprod = (ria - wc) * (wc - lia)
@@ -360,9 +368,10 @@ def cycle(prim, cons, dt, dx, dy, bcx, bcy, gamma, min_d, min_p, min_e, order, e
     Ny, Nx = prim.shape[1:]
     half_dtdx = 0.5 * (dt / dx)
     half_dtdy = 0.5 * (dt / dy)
-    if order == 2:
-        xl, xr = ppm_sweep(prim, gamma, dt, dx, bcx, False)
-        tl, tr = ppm_sweep(swap_xy(prim), gamma, dt, dy, bcy, True)
+    if order in (1, 2):
+        lin = order == 1
+        xl, xr = ppm_sweep(prim, gamma, dt, dx, bcx, False, linear=lin)
+        tl, tr = ppm_sweep(swap_xy(prim), gamma, dt, dy, bcy, True, linear=lin)
     else:
         xl, xr = faces_from_cells(prim, prim, bcx)
         tl, tr = faces_from_cells(swap_xy(prim), swap_xy(prim), bcy)

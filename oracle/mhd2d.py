@@ -236,10 +236,11 @@ def _project(L, i, vec, order):
 # PPM reconstruction along the last axis
 # (Source/Reconstruction_PPM_MHD_HelperModule.py:189-551 for x, :570-871 for y)
 # ----------------------------------------------------------------------------
-def ppm_sweep(w, bn_cell, gamma, dt, dn, bc, fr: Frame):
+def ppm_sweep(w, bn_cell, gamma, dt, dn, bc, fr: Frame, linear=False):
     """Return (left_state, right_state) at the N+1 interfaces along the last axis.
 
     ``w`` is (7, M, N) sweep ordered, ``bn_cell`` (M, N) the cell-centred normal B.
+    ``linear=True`` gives the PLM variant (no reference counterpart, see ``plm_edges``).
     """
     N = w.shape[-1]
     idx = np.arange(-2, N + 2)
@@ -287,6 +288,12 @@ def ppm_sweep(w, bn_cell, gamma, dt, dn, bc, fr: Frame):
     wc = wc[..., 1:-1]
     wl = wl[..., 1:-1]
     wr = wr[..., 1:-1]
+    if linear:
+        lam = [x[..., 1:-1] for x in lam]
+        L = {k: v[..., 1:-1] for k, v in L.items()}
+        R = {k: v[..., 1:-1] for k, v in R.items()}
+        lia, ria = plm_edges(wc, wl, wr, s_c, lam, L, R, dt / dn, order, 7)
+        return _faces_from_cells(lia, ria, bc)
 
     lia = 0.5 * (wc + wl) - (s_c - s_l) / 6.0
     ria = 0.5 * (wr + wc) - (s_r - s_c) / 6.0
@@ -350,6 +357,56 @@ def ppm_sweep(w, bn_cell, gamma, dt, dn, bc, fr: Frame):
                 ria[j] = ria[j] + fac * e
 
     return _faces_from_cells(lia, ria, bc)
+
+
+def plm_edges(wc, wl, wr, s, lam, L, R, dtdx, order, nv):
+    """PLM edge states of each cell with dt/2 characteristic tracing.
+
+    No counterpart in the reference (its PLM branches are commented out,
+    Source/EvolveFunctions_MHD.py:487-488).  The limited slope ``s`` is the
+    reference's characteristic-limited slope (primMonSlopes,
+    Source/Reconstruction_PPM_MHD_HelperModule.py:317-389); the edge values are
+    W -/+ s/2 kept between the neighbours, and the tracing is the reference's
+    own (:460-524) applied to the linear profile, i.e. with the parabolic
+    coefficient zero -- the PLM tracing of Stone et al. (2008) eqs. 38-42 with the
+    reference's <= / >= wave tests.
+    """
+    lia = wc - 0.5 * s
+    ria = wc + 0.5 * s
+    lia = np.maximum(np.minimum(wc, wl), lia)
+    lia = np.minimum(np.maximum(wc, wl), lia)
+    ria = np.maximum(np.minimum(wc, wr), ria)
+    ria = np.minimum(np.maximum(wc, wr), ria)
+    c1 = ria - lia
+    c3 = 0.5 * np.maximum(lam[nv - 1], 0.0) * dtdx
+    c4 = -0.5 * np.minimum(lam[0], 0.0) * dtdx
+    lia = lia + c4 * c1
+    ria = ria - c3 * c1
+    for i in range(nv):
+        ind = lam[i] <= 0.0
+        v3 = 0.5 * dtdx * lam[0] - 0.5 * dtdx * lam[i]
+        fac = np.zeros_like(v3)
+        for j in order:
+            e = L.get((i, j))
+            if e is not None:
+                fac = fac + ind * e * (v3 * c1[j])
+        for j in range(nv):
+            e = R.get((j, i))
+            if e is not None:
+                lia[j] = lia[j] + fac * e
+    for i in range(nv):
+        ind = lam[i] >= 0.0
+        v3 = 0.5 * dtdx * lam[nv - 1] - 0.5 * dtdx * lam[i]
+        fac = np.zeros_like(v3)
+        for j in order:
+            e = L.get((i, j))
+            if e is not None:
+                fac = fac + ind * e * (v3 * c1[j])
+        for j in range(nv):
+            e = R.get((j, i))
+            if e is not None:
+                ria[j] = ria[j] + fac * e
+    return lia, ria
 
 
 def _faces_from_cells(lia, ria, bc):
@@ -791,6 +848,7 @@ def cycle(prim, cons, fbx, fby, dt, dx, dy, bcx, bcy, gamma, min_d, min_p, min_e
           order, efix, eps, trace=None):
     """Advance (prim, cons, faceBx, faceBy) by one cycle of size dt.
 
+    order: 0 first order, 1 PLM (no reference counterpart), 2 PPM.
     Returns new (prim8, cons8, faceBx, faceBy); inputs are not modified.
     ``trace`` (a dict) receives the stage intermediates when given.
     """
@@ -800,9 +858,10 @@ def cycle(prim, cons, fbx, fby, dt, dx, dy, bcx, bcy, gamma, min_d, min_p, min_e
     half_dtdx = 0.5 * (dt / dx)
     half_dtdy = 0.5 * (dt / dy)
 
-    if order == 2:
-        xl, xr = ppm_sweep(wx, wy[5], gamma, dt, dx, bcx, FRAME_X)
-        tl, tr = ppm_sweep(swap_xy(wy), swap_xy(wx[4]), gamma, dt, dy, bcy, FRAME_Y)
+    if order in (1, 2):
+        lin = order == 1
+        xl, xr = ppm_sweep(wx, wy[5], gamma, dt, dx, bcx, FRAME_X, linear=lin)
+        tl, tr = ppm_sweep(swap_xy(wy), swap_xy(wx[4]), gamma, dt, dy, bcy, FRAME_Y, linear=lin)
         yl, yr = swap_xy(tl), swap_xy(tr)
     else:
         xl, xr = first_order_sweep(wx, bcx)

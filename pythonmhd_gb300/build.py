@@ -60,6 +60,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     common = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+    # extra nvcc flags for tuning builds (e.g. -DMHD_MIN_BLOCKS=3)
+    common += os.environ.get("PYTHONMHD_GB300_NVCC_FLAGS", "").split()
     procs = []
     objs = []
     for src, extra in UNITS:

@@ -99,7 +99,7 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
   if (nx < 2 || ny < 2 || !(dx > 0.0) || !(dy > 0.0)) return MHD_ERR_ARG;
   if ((bcx != 0 && bcx != 1) || (bcy != 0 && bcy != 1)) return MHD_ERR_ARG;
   if (physics != MHD2D_HYDRO && physics != MHD2D_MHD) return MHD_ERR_ARG;
-  if (recon != 0 && recon != 2) return MHD_ERR_ARG;
+  if (recon != 0 && recon != 1 && recon != 2) return MHD_ERR_ARG;
   if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST) return MHD_ERR_ARG;
   if ((long long)nx * ny > (1LL << 31)) return MHD_ERR_TOO_LARGE;
 
@@ -143,7 +143,7 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
     reqs[nr++] = {&g.emf, kp}; reqs[nr++] = {&g.nfbx, xp}; reqs[nr++] = {&g.nfby, yp};
     reqs[nr++] = {&g.hez, cp};
   }
-  if (recon == 2) {
+  if (recon >= 1) {
     reqs[nr++] = {&g.slopes, nv * g.ext_plane};
     reqs[nr++] = {&g.eig, nw * g.ext_plane};
   }

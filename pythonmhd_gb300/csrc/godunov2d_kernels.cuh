@@ -3,7 +3,7 @@
 // NumPy arithmetic bit for bit) and `fast` (FMA contraction allowed).
 //
 // A cycle (Source/EvolveFunctions_MHD.py:464-692, Source/EvolveFunctions_Hydro.py:390-513):
-//   dt_reduce -> begin -> [slopes_x -> faces_x -> slopes_y -> faces_y]
+//   dt_reduce -> begin -> [slopes_x] -> faces_x -> [slopes_y] -> faces_y   (slopes: PLM/PPM)
 //   -> roe_x(1) -> roe_y(1) -> [MHD: emf(1)] -> ctu_x -> ctu_y
 //   -> [MHD: half] -> roe_x(2) -> roe_y(2) -> [MHD: emf(2)] -> final -> end
 // Every kernel returns at once when the loop state says the cycle is not a real
@@ -25,6 +25,11 @@ namespace mhdk {
 namespace MHD_NS {
 
 constexpr int kBlock = 128;
+#ifndef MHD_MIN_BLOCKS
+#define MHD_MIN_BLOCKS 2
+#endif
+// resident blocks per SM the heavy FP64 kernels are compiled for (caps registers)
+constexpr int kMinBlocks = MHD_MIN_BLOCKS;
 
 __device__ __forceinline__ int wrapc(int c, int L, int bc) {
   if (bc == PERIODIC) {
@@ -151,7 +156,7 @@ __device__ __forceinline__ void load_sweep_cell(const double* prim, size_t plane
 // (Source/Reconstruction_PPM_MHD_HelperModule.py:317-389, Hydro :86-200)
 // ----------------------------------------------------------------------------
 template <class S, int AX>
-__global__ void __launch_bounds__(kBlock) k_ppm_slopes(Grid G, StateBuf in) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_ppm_slopes(Grid G, StateBuf in) {
   if (!G.loop->active) return;
   SweepGeom g;
   g.nx = G.nx;
@@ -244,11 +249,15 @@ __device__ __forceinline__ double bsource(const double* prim, const double* fb, 
 }
 
 // ----------------------------------------------------------------------------
-// PPM phase B / first order: interface values, monotonicity, characteristic
-// tracing, face states (Source/Reconstruction_PPM_MHD_HelperModule.py:391-548)
+// Reconstruction phase B: edge values, monotonicity, characteristic tracing and
+// face states.  MODE 2 = PPM (Source/Reconstruction_PPM_MHD_HelperModule.py:391-548),
+// MODE 1 = PLM (no reference counterpart: the reference's limited slope taken as a
+// linear profile W -/+ s/2, clamped to the neighbours, traced with the reference's
+// own tracing with the parabolic coefficient zero -- Stone et al. 2008 eqs. 38-42),
+// MODE 0 = first order (cell values copied to both faces, :489-511).
 // ----------------------------------------------------------------------------
-template <class S, int AX, bool PPM>
-__global__ void __launch_bounds__(kBlock) k_faces(Grid G, StateBuf in) {
+template <class S, int AX, int MODE>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_faces(Grid G, StateBuf in) {
   if (!G.loop->active) return;
   SweepGeom g;
   g.nx = G.nx;
@@ -266,7 +275,63 @@ __global__ void __launch_bounds__(kBlock) k_faces(Grid G, StateBuf in) {
   double lia[NV], ria[NV];
   double wc[NV];
   load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
-  if (PPM) {
+  if (MODE == 1) {
+    double wl[NV], wr[NV];
+    load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
+    load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
+    const size_t es = G.ext_plane;
+    const size_t xc = ext_index<AX>(c, t, g.nx);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double s_c = G.slopes[k * es + xc];
+      double a = wc[k] - 0.5 * s_c;
+      double b = wc[k] + 0.5 * s_c;
+      a = dmax(dmin(wc[k], wl[k]), a);
+      a = dmin(dmax(wc[k], wl[k]), a);
+      b = dmax(dmin(wc[k], wr[k]), b);
+      b = dmin(dmax(wc[k], wr[k]), b);
+      lia[k] = a;
+      ria[k] = b;
+    }
+    typename S::Eig e;
+    S::load(e, G.eig + xc, es);
+    const double* lam = S::lam(e);
+    const double dtdx = dt / dn;
+    double c1[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) c1[k] = ria[k] - lia[k];
+    const double c3 = 0.5 * dmax(lam[NV - 1], 0.0) * dtdx;
+    const double c4 = -0.5 * dmin(lam[0], 0.0) * dtdx;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      lia[k] = lia[k] + c4 * c1[k];
+      ria[k] = ria[k] - c3 * c1[k];
+    }
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        if (side == 0 ? lam[i] <= 0.0 : lam[i] >= 0.0) {
+          const double v3 = 0.5 * dtdx * lam[side == 0 ? 0 : NV - 1] - 0.5 * dtdx * lam[i];
+          double fac = 0.0;
+          bool first = true;
+#pragma unroll
+          for (int k = 0; k < NV; ++k) {
+            const int j = S::ord(k);
+            if (S::Lnz(i, j)) {
+              const double tt = S::L(e, i, j) * (v3 * c1[j]);
+              fac = first ? tt : fac + tt;
+              first = false;
+            }
+          }
+          double* edge = side == 0 ? lia : ria;
+#pragma unroll
+          for (int j = 0; j < NV; ++j)
+            if (S::Rnz(j, i)) edge[j] = edge[j] + fac * S::R(e, j, i);
+        }
+      }
+    }
+  } else if (MODE == 2) {
     double wl[NV], wr[NV];
     load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
     load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
@@ -406,7 +471,7 @@ __global__ void __launch_bounds__(kBlock) k_faces(Grid G, StateBuf in) {
 // prim states (converted with the half-step face B in k_ctu_mhd).
 // ----------------------------------------------------------------------------
 template <int AX, int STAGE>
-__global__ void __launch_bounds__(kBlock) k_roe_mhd(Grid G, StateBuf in) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_mhd(Grid G, StateBuf in) {
   if (!G.loop->active) return;
   const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
   const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -437,7 +502,7 @@ __global__ void __launch_bounds__(kBlock) k_roe_mhd(Grid G, StateBuf in) {
 }
 
 template <int AX>
-__global__ void __launch_bounds__(kBlock) k_roe_hydro(Grid G) {
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_hydro(Grid G) {
   if (!G.loop->active) return;
   const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
   const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -899,12 +964,17 @@ void enqueue_recon(const Grid& g, const StateBuf& in, cudaStream_t s) {
   using SY = typename std::conditional<PHYS == MHD, MhdSweep<1>, HydroSweep<1>>::type;
   if (g.recon == 2) {
     k_ppm_slopes<SX, 0><<<row_grid(g.nx + 2, g.ny), kBlock, 0, s>>>(g, in);
-    k_faces<SX, 0, true><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_faces<SX, 0, 2><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
     k_ppm_slopes<SY, 1><<<row_grid(g.nx, g.ny + 2), kBlock, 0, s>>>(g, in);
-    k_faces<SY, 1, true><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_faces<SY, 1, 2><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+  } else if (g.recon == 1) {
+    k_ppm_slopes<SX, 0><<<row_grid(g.nx + 2, g.ny), kBlock, 0, s>>>(g, in);
+    k_faces<SX, 0, 1><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_ppm_slopes<SY, 1><<<row_grid(g.nx, g.ny + 2), kBlock, 0, s>>>(g, in);
+    k_faces<SY, 1, 1><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
   } else {
-    k_faces<SX, 0, false><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
-    k_faces<SY, 1, false><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_faces<SX, 0, 0><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
+    k_faces<SY, 1, 0><<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in);
   }
 }
 

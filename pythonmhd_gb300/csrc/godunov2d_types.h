@@ -47,7 +47,7 @@ struct Grid {
   double dx, dy;
   int bcx, bcy;
   int physics;   // HYDRO / MHD
-  int recon;     // 0 first order, 2 PPM
+  int recon;     // 0 first order, 1 PLM, 2 PPM
   int efix;
   double gamma, eps, min_d, min_p, min_e;
 

@@ -67,7 +67,7 @@ def evolve_2D_mhd(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cf
     assert (tStart <= tEnd)
     assert (startCycle >= 0)
     ny, nx = prim.shape[1:]
-    order = 2 if reconstructOrder == 2 else 0
+    order = reconstructOrder if reconstructOrder in (1, 2) else 0
     mode = arith or default_arith()
     key = ("mhd", ny, nx, float(dx), float(dy), bcx, bcy, float(gamma), order, bool(entropyFix),
            float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)
@@ -106,7 +106,7 @@ def evolve_2D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, 
     assert (bcy == OUTFLOW or bcy == PERIODIC)
     assert (tStart <= tEnd)
     assert (startCycle >= 0 and maxCycles > 0)
-    order = 2 if reconstructOrder == 2 else 0
+    order = reconstructOrder if reconstructOrder in (1, 2) else 0
     mode = arith or default_arith()
     key = ("hydro", ny, nx, float(dx), float(dy), bcx, bcy, float(gamma), order, bool(entropyFix),
            float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)

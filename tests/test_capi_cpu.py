@@ -58,8 +58,8 @@ def test_create_rejects_bad_arguments_before_touching_the_device(lib):
     for ny, nx, dx, dy, bx, by in bad:
         rc = lib.mhd2d_create(ny, nx, dx, dy, bx, by, 1.4, 1, 2, 0, 0.5, 1e-12, 1e-12, 1e-12, 0, ctypes.byref(h))
         assert rc == 1 and not h.value
-    rc = lib.mhd2d_create(16, 16, 0.1, 0.1, 1, 1, 1.4, 1, 1, 0, 0.5, 1e-12, 1e-12, 1e-12, 0, ctypes.byref(h))
-    assert rc == 1  # recon=1 (PLM) is not a reference order
+    rc = lib.mhd2d_create(16, 16, 0.1, 0.1, 1, 1, 1.4, 1, 3, 0, 0.5, 1e-12, 1e-12, 1e-12, 0, ctypes.byref(h))
+    assert rc == 1  # recon must be 0 (first order), 1 (PLM) or 2 (PPM)
     assert lib.mhd2d_upload(None, None, None, None, None) == 1
     lib.mhd2d_destroy(None)
 
