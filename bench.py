@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=0, help="0 = same as --steps")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=10,
+                    help="cycles of the 256-instance batched workload (0 = skip it)")
+    ap.add_argument("--batch-count", type=int, default=256)
     return ap.parse_args()
 
 
@@ -193,6 +196,59 @@ def fp64_peak():
 
 
 # ----------------------------------------------------------------------------
+# batched form vs a per-instance loop of the single-grid path
+# ----------------------------------------------------------------------------
+def run_batch(a, torch):
+    """256 uneven Orszag-Tang instances (Nx, Ny in {64..512}, PLM): one batched
+    handle vs a loop of single-grid handles advancing each instance in turn."""
+    from pythonmhd_gb300 import initial_conditions as ic
+    from pythonmhd_gb300.solver import Batch2D, Grid2D
+    insts = ic.orszag_tang_batch(count=a.batch_count, seed=0)
+    zones = sum(i["nx"] * i["ny"] for i in insts)
+    k, w = a.batch_steps, 1
+    b = Batch2D(insts, mhd=True, recon=1, arith=a.arith)
+    for n, i in enumerate(insts):
+        b.upload(n, i["prim"], i["cons"], i["fbx"], i["fby"])
+    b.advance(0.0, 1e30, 0, w, 0.4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.advance(0.0, 1e30, w, w + k, 0.4)
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - t0
+    launches = b.info()["last_launches"]
+    b.close()
+    singles = []
+    for i in insts:
+        g = Grid2D(i["ny"], i["nx"], i["dx"], i["dy"], 1, 1, i["gamma"], mhd=True, recon=1, arith=a.arith)
+        g.upload(i["prim"], i["cons"], i["fbx"], i["fby"])
+        g.advance(0.0, 1e30, 0, w, 0.4)
+        singles.append(g)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for g in singles:
+        g.advance(0.0, 1e30, w, w + k, 0.4)
+    torch.cuda.synchronize()
+    tl = time.perf_counter() - t0
+    # step-major loop: every instance advanced one cycle per call, instance after instance
+    t0 = time.perf_counter()
+    for s in range(k):
+        for g in singles:
+            g.advance(0.0, 1e30, w + k + s, w + k + s + 1, 0.4)
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - t0
+    for g in singles:
+        g.close()
+    return {"workload": f"{len(insts)} Orszag-Tang instances, Nx,Ny uniform in 64..512 step 32, gamma in "
+                        f"[1.4,5/3], B0 x U[0.5,2], 1% density perturbation, PLM+Roe+CTU+CT, per-instance dt",
+            "zones_per_step": zones, "steps": k,
+            "batched_zone_updates_per_s": zones * k / tb, "looped_zone_updates_per_s": zones * k / tl,
+            "speedup_vs_loop": tl / tb, "batched_launches": launches,
+            "loop": "one single-grid handle per instance, each advanced k cycles in turn (CUDA graphs)",
+            "step_major_loop_zone_updates_per_s": zones * k / ts, "speedup_vs_step_major_loop": ts / tb,
+            "timing": "host wall clock around device-synchronised calls"}
+
+
+# ----------------------------------------------------------------------------
 # our arm
 # ----------------------------------------------------------------------------
 def run_ours(a):
@@ -263,6 +319,7 @@ def run_ours(a):
     e3.synchronize()
     ms_e2e = e2.elapsed_time(e3)
     clk = clocks.stop()
+    dev_bytes = g.device_bytes()
     if not np.isfinite(hp).all():
         raise RuntimeError("non-finite state after the timed cycles")
 
@@ -307,6 +364,10 @@ def run_ours(a):
     cpu = None
     if rank == 0 and not a.no_cpu:
         cpu = cpu_baseline(a.cpu_sample, a.cpu_steps)
+    batched = None
+    if a.batch_steps > 0:
+        g.close()
+        batched = run_batch(a, torch)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_per, "higher_is_better": True, "scaling": "weak",
@@ -318,7 +379,7 @@ def run_ours(a):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps, "ms_per_step": ms_e2e_per},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
-            "device_bytes": g.device_bytes(), "final_cycle": cyc, "final_time": t}
+            "device_bytes": dev_bytes, "final_cycle": cyc, "final_time": t, "batched": batched}
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()

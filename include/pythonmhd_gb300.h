@@ -119,6 +119,32 @@ int mhd2d_cfl_dt_noalloc(int physics, int ny, int nx, double dx, double dy, doub
                          double cfl, const double* cons, const double* faceBx,
                          const double* faceBy, double* dt_out, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched form: many independent grids (uneven sizes, per-instance gamma, dx,
+ * dy, boundary conditions, dt, time and cycle count) advanced together with one
+ * persistent-kernel launch per stage over a work list of row tiles; a whole
+ * cycle of all instances is one CUDA graph.  No counterpart in the reference,
+ * which advances one grid per evolve call; per instance the result equals the
+ * single-grid entry points' result bit for bit.
+ * ------------------------------------------------------------------------- */
+int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const double* dy,
+                const int* bcx, const int* bcy, const double* gamma, int physics, int recon,
+                int entropy_fix, double eps, double min_d, double min_p, double min_e,
+                int arith, void** handle);
+int mhdb_upload(void* handle, int instance, const double* prim, const double* cons,
+                const double* faceBx, const double* faceBy);
+/* Per-instance t0/t_end/cycle0/max_cycles arrays; every instance runs the
+ * reference loop (while t < t_end and cycle < max_cycles) with its own dt. */
+int mhdb_advance(void* handle, const double* t0, const double* t_end, const long long* cycle0,
+                 const long long* max_cycles, double cfl, double* t_out, long long* cycle_out);
+int mhdb_download(void* handle, int instance, int which, double* prim, double* cons,
+                  double* faceBx, double* faceBy);
+/* Blocks of each persistent launch (tuning knob; default 2 per SM). */
+int mhdb_set_blocks(void* handle, int blocks);
+int mhdb_info(void* handle, long long* last_launches, size_t* device_bytes, int* blocks,
+              void** stream);
+void mhdb_destroy(void* handle);
+
 const char* mhd2d_strerror(int status);
 void mhd2d_destroy(void* handle);
 

@@ -38,6 +38,18 @@ SIGNATURES = {
     "mhd2d_cfl_dt_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mhdb_create": (ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 7 + [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "mhdb_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, c_double_p, c_double_p, c_double_p]),
+    "mhdb_advance": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_void_p,
+                                    ctypes.c_void_p]),
+    "mhdb_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p, c_double_p,
+                                     c_double_p]),
+    "mhdb_set_blocks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "mhdb_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t),
+                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]),
+    "mhdb_destroy": (None, [ctypes.c_void_p]),
     "mhd2d_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "mhd2d_destroy": (None, [ctypes.c_void_p]),
 }

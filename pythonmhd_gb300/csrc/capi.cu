@@ -7,13 +7,20 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "../../include/pythonmhd_gb300.h"
 #include "godunov2d_types.h"
 
 namespace mhdk {
-namespace exact { void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s); }
-namespace fast { void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s); }
+namespace exact {
+void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
+void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, cudaStream_t s);
+}  // namespace exact
+namespace fast {
+void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
+void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, cudaStream_t s);
+}  // namespace fast
 }  // namespace mhdk
 
 using mhdk::Grid;
@@ -52,6 +59,41 @@ int cuda_fail(cudaError_t e) {
 
 size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
+// Lay out every buffer of one grid from `base` (256-byte aligned pieces) and
+// return the bytes used; with base == nullptr only the size is computed.
+size_t carve_grid(Grid& g, int nvars, char* base) {
+  const int nv = g.physics == MHD2D_MHD ? 7 : 5;
+  const int nw = g.physics == MHD2D_MHD ? 42 : 10;
+  const size_t cp = mhdk::cell_plane(g), xp = mhdk::xface_plane(g), yp = mhdk::yface_plane(g),
+               kp = mhdk::corner_plane(g);
+  g.ext_plane = std::max((size_t)(g.nx + 2) * g.ny, (size_t)g.nx * (g.ny + 2));
+  const bool mhd = g.physics == MHD2D_MHD;
+  size_t off = 0;
+  auto take = [&](double** p, size_t n) {
+    if (base) *p = reinterpret_cast<double*>(base + off);
+    off += align256(n * sizeof(double));
+  };
+  for (int b = 0; b < 2; ++b) {
+    take(&g.st[b].prim, (size_t)nvars * cp);
+    take(&g.st[b].cons, (size_t)nvars * cp);
+    if (mhd) { take(&g.st[b].fbx, xp); take(&g.st[b].fby, yp); }
+  }
+  take(&g.xl, nv * xp); take(&g.xr, nv * xp);
+  take(&g.yl, nv * yp); take(&g.yr, nv * yp);
+  take(&g.fx, nv * xp); take(&g.fy, nv * yp);
+  if (mhd) {
+    take(&g.uxl, nv * xp); take(&g.uxr, nv * xp);
+    take(&g.uyl, nv * yp); take(&g.uyr, nv * yp);
+    take(&g.emf, kp); take(&g.nfbx, xp); take(&g.nfby, yp);
+    take(&g.hez, cp);
+  }
+  if (g.recon >= 1) {
+    take(&g.slopes, nv * g.ext_plane);
+    take(&g.eig, nw * g.ext_plane);
+  }
+  return off;
+}
+
 void enqueue(Handle* h, int parity) {
   if (h->arith == MHD2D_ARITH_EXACT) mhdk::exact::enqueue_cycle(h->g, parity, h->dt_blocks, h->stream);
   else mhdk::fast::enqueue_cycle(h->g, parity, h->dt_blocks, h->stream);
@@ -72,6 +114,61 @@ int build_graph(Handle* h, int parity) {
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_fail(e);
   return MHD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched handles: many independent grids advanced by one launch per stage.
+// ---------------------------------------------------------------------------
+struct BatchHandle {
+  int count = 0;
+  int physics = 1, recon = 2, arith = 0, nvars = 8;
+  int device = 0;
+  std::vector<Grid> grids;         // host copies (device pointers inside)
+  Grid* d_grids = nullptr;
+  int4* d_tiles = nullptr;         // all work lists, one after the other
+  mhdk::BatchView view{};
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  LoopState* d_loops = nullptr;
+  LoopState* h_loops = nullptr;    // pinned
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  size_t graph_nodes = 0;
+  unsigned blocks = 0;
+  long long last_launches = 0;
+  std::vector<int> uploaded;
+};
+
+void enqueue_batch(BatchHandle* b) {
+  if (b->arith == MHD2D_ARITH_EXACT)
+    mhdk::exact::enqueue_cycle_batch(b->view, b->physics, b->recon, b->blocks, b->stream);
+  else
+    mhdk::fast::enqueue_cycle_batch(b->view, b->physics, b->recon, b->blocks, b->stream);
+}
+
+int build_batch_graph(BatchHandle* b) {
+  if (b->graph) return MHD_OK;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_batch(b);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  if (e != cudaSuccess) return cuda_fail(e);
+  size_t nodes = 0;
+  cudaGraphGetNodes(graph, nullptr, &nodes);
+  b->graph_nodes = nodes;
+  e = cudaGraphInstantiate(&b->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e);
+  return MHD_OK;
+}
+
+void free_batch(BatchHandle* b) {
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->h_loops) cudaFreeHost(b->h_loops);
+  if (b->arena) cudaFree(b->arena);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
 }
 
 }  // namespace
@@ -111,8 +208,6 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
   g.gamma = gamma; g.eps = eps; g.min_d = min_d; g.min_p = min_p; g.min_e = min_e;
   h->arith = arith;
   h->nvars = physics == MHD2D_MHD ? 8 : 5;
-  const int nv = physics == MHD2D_MHD ? 7 : 5;
-  const int nw = physics == MHD2D_MHD ? 42 : 10;
 
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
@@ -121,35 +216,7 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   h->dt_blocks = std::max(1, sms) * 8;
 
-  const size_t cp = mhdk::cell_plane(g), xp = mhdk::xface_plane(g), yp = mhdk::yface_plane(g),
-               kp = mhdk::corner_plane(g);
-  g.ext_plane = std::max((size_t)(nx + 2) * ny, (size_t)nx * (ny + 2));
-  const bool mhd = physics == MHD2D_MHD;
-  // carve every buffer out of one allocation
-  struct Req { double** p; size_t n; };
-  Req reqs[32];
-  int nr = 0;
-  for (int b = 0; b < 2; ++b) {
-    reqs[nr++] = {&g.st[b].prim, (size_t)h->nvars * cp};
-    reqs[nr++] = {&g.st[b].cons, (size_t)h->nvars * cp};
-    if (mhd) { reqs[nr++] = {&g.st[b].fbx, xp}; reqs[nr++] = {&g.st[b].fby, yp}; }
-  }
-  reqs[nr++] = {&g.xl, nv * xp}; reqs[nr++] = {&g.xr, nv * xp};
-  reqs[nr++] = {&g.yl, nv * yp}; reqs[nr++] = {&g.yr, nv * yp};
-  reqs[nr++] = {&g.fx, nv * xp}; reqs[nr++] = {&g.fy, nv * yp};
-  if (mhd) {
-    reqs[nr++] = {&g.uxl, nv * xp}; reqs[nr++] = {&g.uxr, nv * xp};
-    reqs[nr++] = {&g.uyl, nv * yp}; reqs[nr++] = {&g.uyr, nv * yp};
-    reqs[nr++] = {&g.emf, kp}; reqs[nr++] = {&g.nfbx, xp}; reqs[nr++] = {&g.nfby, yp};
-    reqs[nr++] = {&g.hez, cp};
-  }
-  if (recon >= 1) {
-    reqs[nr++] = {&g.slopes, nv * g.ext_plane};
-    reqs[nr++] = {&g.eig, nw * g.ext_plane};
-  }
-  size_t total = 0;
-  for (int i = 0; i < nr; ++i) total += align256(reqs[i].n * sizeof(double));
-  total += align256(sizeof(LoopState)) + align256(sizeof(int));
+  const size_t total = carve_grid(g, h->nvars, nullptr) + align256(sizeof(LoopState)) + align256(sizeof(int));
   e = cudaMalloc(&h->arena, total);
   if (e != cudaSuccess) {
     cudaStreamDestroy(h->stream);
@@ -158,11 +225,7 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
   }
   h->arena_bytes = total;
   char* base = static_cast<char*>(h->arena);
-  size_t off = 0;
-  for (int i = 0; i < nr; ++i) {
-    *reqs[i].p = reinterpret_cast<double*>(base + off);
-    off += align256(reqs[i].n * sizeof(double));
-  }
+  size_t off = carve_grid(g, h->nvars, base);
   g.loop = reinterpret_cast<LoopState*>(base + off);
   off += align256(sizeof(LoopState));
   g.status = reinterpret_cast<int*>(base + off);
@@ -339,6 +402,215 @@ int mhd2d_stream(void* handle, void** stream) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !stream) return MHD_ERR_ARG;
   *stream = h->stream;
+  return MHD_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const double* dy, const int* bcx,
+                const int* bcy, const double* gamma, int physics, int recon, int entropy_fix, double eps,
+                double min_d, double min_p, double min_e, int arith, void** handle) {
+  if (!handle) return MHD_ERR_ARG;
+  *handle = nullptr;
+  if (count < 1 || !ny || !nx || !dx || !dy || !bcx || !bcy || !gamma) return MHD_ERR_ARG;
+  if (physics != MHD2D_HYDRO && physics != MHD2D_MHD) return MHD_ERR_ARG;
+  if (recon != 0 && recon != 1 && recon != 2) return MHD_ERR_ARG;
+  if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST) return MHD_ERR_ARG;
+  for (int i = 0; i < count; ++i) {
+    if (nx[i] < 2 || ny[i] < 2 || !(dx[i] > 0.0) || !(dy[i] > 0.0)) return MHD_ERR_ARG;
+    if ((bcx[i] != 0 && bcx[i] != 1) || (bcy[i] != 0 && bcy[i] != 1)) return MHD_ERR_ARG;
+    if ((long long)nx[i] * ny[i] > (1LL << 31)) return MHD_ERR_TOO_LARGE;
+  }
+  BatchHandle* b = new (std::nothrow) BatchHandle();
+  if (!b) return MHD_ERR_NOMEM;
+  b->count = count;
+  b->physics = physics;
+  b->recon = recon;
+  b->arith = arith;
+  b->nvars = physics == MHD2D_MHD ? 8 : 5;
+  b->grids.resize(count);
+  b->uploaded.assign(count, 0);
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  b->blocks = (unsigned)std::max(1, sms) * 2;
+
+  // work lists: row segments of kTileWidth items per index space and instance
+  constexpr int kTileWidth = 128;
+  std::vector<int4> tiles[mhdk::kNumSpaces];
+  size_t grid_bytes = 0;
+  for (int i = 0; i < count; ++i) {
+    Grid& g = b->grids[i];
+    g = Grid{};
+    g.nx = nx[i]; g.ny = ny[i]; g.dx = dx[i]; g.dy = dy[i]; g.bcx = bcx[i]; g.bcy = bcy[i];
+    g.physics = physics; g.recon = recon; g.efix = entropy_fix ? 1 : 0;
+    g.gamma = gamma[i]; g.eps = eps; g.min_d = min_d; g.min_p = min_p; g.min_e = min_e;
+    grid_bytes += carve_grid(g, b->nvars, nullptr);
+    const int w[mhdk::kNumSpaces] = {g.nx, g.nx + 2, g.nx, g.nx + 1, g.nx, g.nx + 1};
+    const int hgt[mhdk::kNumSpaces] = {g.ny, g.ny, g.ny + 2, g.ny, g.ny + 1, g.ny + 1};
+    for (int sp = 0; sp < mhdk::kNumSpaces; ++sp)
+      for (int r = 0; r < hgt[sp]; ++r)
+        for (int x0 = 0; x0 < w[sp]; x0 += kTileWidth) tiles[sp].push_back(make_int4(i, r, x0, 0));
+  }
+  size_t ntiles_total = 0;
+  for (auto& t : tiles) ntiles_total += t.size();
+  const size_t total = grid_bytes + align256(count * sizeof(LoopState)) + align256(count * sizeof(Grid)) +
+                       align256(ntiles_total * sizeof(int4)) + align256(sizeof(int));
+  e = cudaMalloc(&b->arena, total);
+  if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
+  b->arena_bytes = total;
+  char* base = static_cast<char*>(b->arena);
+  size_t off = 0;
+  for (int i = 0; i < count; ++i) off += carve_grid(b->grids[i], b->nvars, base + off);
+  b->d_loops = reinterpret_cast<LoopState*>(base + off);
+  off += align256(count * sizeof(LoopState));
+  b->d_grids = reinterpret_cast<Grid*>(base + off);
+  off += align256(count * sizeof(Grid));
+  b->d_tiles = reinterpret_cast<int4*>(base + off);
+  off += align256(ntiles_total * sizeof(int4));
+  int* status = reinterpret_cast<int*>(base + off);
+  for (int i = 0; i < count; ++i) {
+    b->grids[i].loop = b->d_loops + i;
+    b->grids[i].status = status;
+  }
+  e = cudaMemsetAsync(b->arena, 0, total, b->stream);
+  size_t toff = 0;
+  b->view.grids = b->d_grids;
+  b->view.ninst = count;
+  for (int sp = 0; sp < mhdk::kNumSpaces && e == cudaSuccess; ++sp) {
+    b->view.tiles[sp] = b->d_tiles + toff;
+    b->view.ntiles[sp] = (int)tiles[sp].size();
+    e = cudaMemcpyAsync(b->d_tiles + toff, tiles[sp].data(), tiles[sp].size() * sizeof(int4),
+                        cudaMemcpyHostToDevice, b->stream);
+    toff += tiles[sp].size();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_grids, b->grids.data(), count * sizeof(Grid), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_loops, count * sizeof(LoopState));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
+  std::memset(b->h_loops, 0, count * sizeof(LoopState));
+  *handle = b;
+  return MHD_OK;
+}
+
+void mhdb_destroy(void* handle) {
+  if (handle) free_batch(static_cast<BatchHandle*>(handle));
+}
+
+int mhdb_upload(void* handle, int inst, const double* prim, const double* cons, const double* faceBx,
+                const double* faceBy) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || inst < 0 || inst >= b->count || !prim || !cons) return MHD_ERR_ARG;
+  const Grid& g = b->grids[inst];
+  const bool mhd = b->physics == MHD2D_MHD;
+  if (mhd && (!faceBx || !faceBy)) return MHD_ERR_ARG;
+  const mhdk::StateBuf& s = g.st[b->h_loops[inst].cur];
+  const size_t cb = (size_t)b->nvars * mhdk::cell_plane(g) * sizeof(double);
+  CK(cudaMemcpyAsync(s.prim, prim, cb, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(s.cons, cons, cb, cudaMemcpyHostToDevice, b->stream));
+  if (mhd) {
+    CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(g) * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(g) * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  b->uploaded[inst] = 1;
+  b->h_loops[inst].cycles_run = 0;
+  return MHD_OK;
+}
+
+int mhdb_advance(void* handle, const double* t0, const double* t_end, const long long* cycle0,
+                 const long long* max_cycles, double cfl, double* t_out, long long* cycle_out) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || !t0 || !t_end || !cycle0 || !max_cycles) return MHD_ERR_ARG;
+  for (int i = 0; i < b->count; ++i) {
+    if (!b->uploaded[i]) return MHD_ERR_STATE;
+    if (!(t0[i] <= t_end[i]) || cycle0[i] < 0) return MHD_ERR_ARG;
+  }
+  for (int i = 0; i < b->count; ++i) {
+    LoopState& L = b->h_loops[i];
+    const int cur = L.cur;
+    L = LoopState{};
+    L.t = t0[i]; L.t_end = t_end[i]; L.t_prev = t0[i]; L.cfl = cfl;
+    L.cycle = cycle0[i]; L.max_cycles = max_cycles[i]; L.cur = cur;
+  }
+  CK(cudaMemcpyAsync(b->d_loops, b->h_loops, b->count * sizeof(LoopState), cudaMemcpyHostToDevice, b->stream));
+  int rc = build_batch_graph(b);
+  if (rc) return rc;
+  b->last_launches = 0;
+  long long budget = 1;
+  for (;;) {
+    bool running = false;
+    long long remaining = 0;
+    for (int i = 0; i < b->count; ++i) {
+      const LoopState& L = b->h_loops[i];
+      if (L.t < L.t_end && L.cycle < L.max_cycles) {
+        running = true;
+        long long r = L.max_cycles - L.cycle;
+        if (L.dt > 0.0) {
+          const double est = std::ceil((L.t_end - L.t) / L.dt) + 1.0;
+          if (est < (double)r) r = (long long)est;
+        }
+        remaining = std::max(remaining, r);
+      }
+    }
+    if (!running) break;
+    for (long long k = 0; k < budget; ++k) CK(cudaGraphLaunch(b->graph, b->stream));
+    b->last_launches += budget * (long long)b->graph_nodes;
+    CK(cudaMemcpyAsync(b->h_loops, b->d_loops, b->count * sizeof(LoopState), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < b->count; ++i)
+      if (!std::isfinite(b->h_loops[i].t) || !std::isfinite(b->h_loops[i].dt)) return MHD_ERR_NONFINITE;
+    budget = std::max(1LL, std::min(remaining - budget, 512LL));
+  }
+  for (int i = 0; i < b->count; ++i) {
+    if (t_out) t_out[i] = b->h_loops[i].t;
+    if (cycle_out) cycle_out[i] = b->h_loops[i].cycle;
+  }
+  return MHD_OK;
+}
+
+int mhdb_download(void* handle, int inst, int which, double* prim, double* cons, double* faceBx,
+                  double* faceBy) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || inst < 0 || inst >= b->count || (which != 0 && which != 1)) return MHD_ERR_ARG;
+  if (!b->uploaded[inst]) return MHD_ERR_STATE;
+  const Grid& g = b->grids[inst];
+  int buf = b->h_loops[inst].cur;
+  if (which == 1 && b->h_loops[inst].cycles_run > 0) buf ^= 1;
+  const mhdk::StateBuf& s = g.st[buf];
+  const size_t cb = (size_t)b->nvars * mhdk::cell_plane(g) * sizeof(double);
+  if (prim) CK(cudaMemcpyAsync(prim, s.prim, cb, cudaMemcpyDeviceToHost, b->stream));
+  if (cons) CK(cudaMemcpyAsync(cons, s.cons, cb, cudaMemcpyDeviceToHost, b->stream));
+  if (b->physics == MHD2D_MHD) {
+    if (faceBx) CK(cudaMemcpyAsync(faceBx, s.fbx, mhdk::xface_plane(g) * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    if (faceBy) CK(cudaMemcpyAsync(faceBy, s.fby, mhdk::yface_plane(g) * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  return MHD_OK;
+}
+
+int mhdb_set_blocks(void* handle, int blocks) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || blocks < 1) return MHD_ERR_ARG;
+  if ((unsigned)blocks != b->blocks) {
+    b->blocks = (unsigned)blocks;
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  }
+  return MHD_OK;
+}
+
+int mhdb_info(void* handle, long long* launches, size_t* device_bytes, int* blocks, void** stream) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b) return MHD_ERR_ARG;
+  if (launches) *launches = b->last_launches;
+  if (device_bytes) *device_bytes = b->arena_bytes;
+  if (blocks) *blocks = (int)b->blocks;
+  if (stream) *stream = b->stream;
   return MHD_OK;
 }
 

@@ -155,8 +155,9 @@ __device__ __forceinline__ void load_sweep_cell(const double* prim, size_t plane
 // PPM phase A: eigensystem + monotonised characteristic slopes for cells -1..Ls
 // (Source/Reconstruction_PPM_MHD_HelperModule.py:317-389, Hydro :86-200)
 // ----------------------------------------------------------------------------
+// work item (x, y) of the sweep-extended cell space: (Ls+2) x Lt along the sweep
 template <class S, int AX>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_ppm_slopes(Grid G, StateBuf in) {
+__device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, int x, int y) {
   if (!G.loop->active) return;
   SweepGeom g;
   g.nx = G.nx;
@@ -164,8 +165,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_ppm_slopes(Grid G, State
   g.Lt = AX == 0 ? G.ny : G.nx;
   g.bc = AX == 0 ? G.bcx : G.bcy;
   int c, t;
-  if (AX == 0) { c = blockIdx.x * blockDim.x + threadIdx.x - 1; t = blockIdx.y; }
-  else { t = blockIdx.x * blockDim.x + threadIdx.x; c = (int)blockIdx.y - 1; }
+  if (AX == 0) { c = x - 1; t = y; }
+  else { t = x; c = y - 1; }
   if (c > g.Ls || t >= g.Lt) return;
   const size_t plane = cell_plane(G);
   constexpr int NV = S::NV;
@@ -256,8 +257,9 @@ __device__ __forceinline__ double bsource(const double* prim, const double* fb, 
 // own tracing with the parabolic coefficient zero -- Stone et al. 2008 eqs. 38-42),
 // MODE 0 = first order (cell values copied to both faces, :489-511).
 // ----------------------------------------------------------------------------
+// work item (x, y) of the cell space nx x ny
 template <class S, int AX, int MODE>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_faces(Grid G, StateBuf in) {
+__device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x, int y) {
   if (!G.loop->active) return;
   SweepGeom g;
   g.nx = G.nx;
@@ -265,8 +267,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_faces(Grid G, StateBuf i
   g.Lt = AX == 0 ? G.ny : G.nx;
   g.bc = AX == 0 ? G.bcx : G.bcy;
   int c, t;
-  if (AX == 0) { c = blockIdx.x * blockDim.x + threadIdx.x; t = blockIdx.y; }
-  else { t = blockIdx.x * blockDim.x + threadIdx.x; c = blockIdx.y; }
+  if (AX == 0) { c = x; t = y; }
+  else { t = x; c = y; }
   if (c >= g.Ls || t >= g.Lt) return;
   const size_t plane = cell_plane(G);
   constexpr int NV = S::NV;
@@ -470,11 +472,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_faces(Grid G, StateBuf i
 // prim states with the current face B; stage 2 reads the CTU-corrected cons and
 // prim states (converted with the half-step face B in k_ctu_mhd).
 // ----------------------------------------------------------------------------
+// work item: linear face index f of the x-face (AX 0) or y-face (AX 1) space
 template <int AX, int STAGE>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_mhd(Grid G, StateBuf in) {
+__device__ __forceinline__ void b_roe_mhd(const Grid& G, const StateBuf& in, size_t f) {
   if (!G.loop->active) return;
   const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
-  const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   constexpr int N = AX == 0 ? 1 : 2, T1 = AX == 0 ? 2 : 3, T2 = AX == 0 ? 3 : 1;
   const double* WL = AX == 0 ? G.xl : G.yl;
@@ -502,10 +504,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_mhd(Grid G, StateBuf
 }
 
 template <int AX>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_hydro(Grid G) {
+__device__ __forceinline__ void b_roe_hydro(const Grid& G, size_t f) {
   if (!G.loop->active) return;
   const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
-  const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const double* WL = AX == 0 ? G.xl : G.yl;
   const double* WR = AX == 0 ? G.xr : G.yr;
@@ -532,11 +533,10 @@ __device__ __forceinline__ double cell_ez(const Grid& G, const StateBuf& in, int
        - __ldg(in.prim + 1 * plane + idx) * __ldg(in.prim + 5 * plane + idx);
 }
 
+// work item (I, J) of the corner space (nx+1) x (ny+1)
 template <int STAGE>
-__global__ void __launch_bounds__(kBlock) k_emf(Grid G, StateBuf in) {
+__device__ __forceinline__ void b_emf(const Grid& G, const StateBuf& in, int I, int J) {
   if (!G.loop->active) return;
-  const int I = blockIdx.x * blockDim.x + threadIdx.x;
-  const int J = blockIdx.y;
   const int nx = G.nx, ny = G.ny;
   if (I > nx || J > ny) return;
   const int ic = wrapc(I, nx, G.bcx), im = wrapc(I - 1, nx, G.bcx);
@@ -578,11 +578,10 @@ __global__ void __launch_bounds__(kBlock) k_emf(Grid G, StateBuf in) {
 // source, cons floors, half-step face B, prim with the half-step face B.
 // ----------------------------------------------------------------------------
 template <int AX>
-__global__ void __launch_bounds__(kBlock) k_ctu_mhd(Grid G, StateBuf in) {
+__device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, size_t fl) {
   if (!G.loop->active) return;
   const int nx = G.nx, ny = G.ny;
   const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
-  const size_t fl = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (fl >= nf) return;
   const int width = AX == 0 ? nx + 1 : nx;
   const int row = (int)(fl / width), col = (int)(fl % width);
@@ -698,11 +697,10 @@ __global__ void __launch_bounds__(kBlock) k_ctu_mhd(Grid G, StateBuf in) {
 // Hydro CTU (Source/EvolveFunctions_Hydro.py:460-489): cons -= half dt/dn * transverse
 // flux difference, back to prim.
 template <int AX>
-__global__ void __launch_bounds__(kBlock) k_ctu_hydro(Grid G) {
+__device__ __forceinline__ void b_ctu_hydro(const Grid& G, size_t fl) {
   if (!G.loop->active) return;
   const int nx = G.nx;
   const size_t nf = AX == 0 ? xface_plane(G) : yface_plane(G);
-  const size_t fl = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (fl >= nf) return;
   const int width = AX == 0 ? nx + 1 : nx;
   const int row = (int)(fl / width), col = (int)(fl % width);
@@ -736,10 +734,8 @@ __global__ void __launch_bounds__(kBlock) k_ctu_hydro(Grid G) {
 // ----------------------------------------------------------------------------
 // Half-step cell Ez (Source/EvolveFunctions_MHD.py:594-624)
 // ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_half_ez(Grid G, StateBuf in) {
+__device__ __forceinline__ void b_half_ez(const Grid& G, const StateBuf& in, int i, int j) {
   if (!G.loop->active) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
   const int nx = G.nx;
   if (i >= nx || j >= G.ny) return;
   const double dt = G.loop->dt;
@@ -766,10 +762,9 @@ __global__ void __launch_bounds__(kBlock) k_half_ez(Grid G, StateBuf in) {
 // ----------------------------------------------------------------------------
 // Final update (Source/EvolveFunctions_MHD.py:643-687; Hydro :502-506)
 // ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_final_mhd(Grid G, StateBuf in, StateBuf out) {
+__device__ __forceinline__ void b_final_mhd(const Grid& G, const StateBuf& in, const StateBuf& out, int i,
+                                            int j) {
   if (!G.loop->active) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
   const int nx = G.nx, ny = G.ny;
   if (i >= nx || j >= ny) return;
   const double dt = G.loop->dt;
@@ -819,10 +814,9 @@ __global__ void __launch_bounds__(kBlock) k_final_mhd(Grid G, StateBuf in, State
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_final_hydro(Grid G, StateBuf in, StateBuf out) {
+__device__ __forceinline__ void b_final_hydro(const Grid& G, const StateBuf& in, const StateBuf& out, int i,
+                                              int j) {
   if (!G.loop->active) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
   const int nx = G.nx;
   if (i >= nx || j >= G.ny) return;
   const double dt = G.loop->dt;
@@ -858,45 +852,44 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// largest signal speeds of cell idx folded into (mx, my)
 template <int PHYS>
-__global__ void __launch_bounds__(256) k_dt_reduce(Grid G, StateBuf in) {
-  LoopState* L = G.loop;
-  if (!(L->t < L->t_end && L->cycle < L->max_cycles)) return;
+__device__ __forceinline__ void b_dt_cell(const Grid& G, const StateBuf& in, size_t idx, double& mx, double& my) {
   const int nx = G.nx;
-  const size_t n = cell_plane(G);
-  const size_t plane = n;
+  const size_t plane = cell_plane(G);
   const double gamma = G.gamma;
-  double mx = 0.0, my = 0.0;
-  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
-    const double* c = in.cons;
-    const double inv_d = 1.0 / c[idx];
-    const double vx = c[plane + idx] * inv_d;
-    const double vy = c[2 * plane + idx] * inv_d;
-    const double vz = c[3 * plane + idx] * inv_d;
-    const double vsq = vx * vx + vy * vy + vz * vz;
-    if (PHYS == MHD) {
-      const int j = (int)(idx / nx), i = (int)(idx % nx);
-      const double c4 = c[4 * plane + idx], c5 = c[5 * plane + idx];
-      const double bx = c4 + fabs(in.fbx[(size_t)j * (nx + 1) + i] - c4);
-      const double by = c5 + fabs(in.fby[(size_t)j * nx + i] - c5);
-      const double bz = c[6 * plane + idx];
-      const double bsq = bx * bx + by * by + bz * bz;
-      const double p = dmax((gamma - 1.0) * (c[7 * plane + idx] - 0.5 * c[idx] * vsq - 0.5 * bsq), SMALL_VALUE);
-      const double a2 = gamma * p * inv_d;
-      const double ssum = bsq * inv_d + a2;
-      const double sdiff = bsq * inv_d - a2;
-      const double cfx2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (by * by + bz * bz) * inv_d));
-      const double cfy2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (bx * bx + bz * bz) * inv_d));
-      mx = dmax(mx, fabs(vx) + sqrt(cfx2));
-      my = dmax(my, fabs(vy) + sqrt(cfy2));
-    } else {
-      const double p = dmax((gamma - 1.0) * (c[4 * plane + idx] - 0.5 * c[idx] * vsq), SMALL_VALUE);
-      const double a = sqrt(gamma * p * inv_d);
-      mx = dmax(mx, fabs(vx) + a);
-      my = dmax(my, fabs(vy) + a);
-    }
+  const double* c = in.cons;
+  const double inv_d = 1.0 / c[idx];
+  const double vx = c[plane + idx] * inv_d;
+  const double vy = c[2 * plane + idx] * inv_d;
+  const double vz = c[3 * plane + idx] * inv_d;
+  const double vsq = vx * vx + vy * vy + vz * vz;
+  if (PHYS == MHD) {
+    const int j = (int)(idx / nx), i = (int)(idx % nx);
+    const double c4 = c[4 * plane + idx], c5 = c[5 * plane + idx];
+    const double bx = c4 + fabs(in.fbx[(size_t)j * (nx + 1) + i] - c4);
+    const double by = c5 + fabs(in.fby[(size_t)j * nx + i] - c5);
+    const double bz = c[6 * plane + idx];
+    const double bsq = bx * bx + by * by + bz * bz;
+    const double p = dmax((gamma - 1.0) * (c[7 * plane + idx] - 0.5 * c[idx] * vsq - 0.5 * bsq), SMALL_VALUE);
+    const double a2 = gamma * p * inv_d;
+    const double ssum = bsq * inv_d + a2;
+    const double sdiff = bsq * inv_d - a2;
+    const double cfx2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (by * by + bz * bz) * inv_d));
+    const double cfy2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (bx * bx + bz * bz) * inv_d));
+    mx = dmax(mx, fabs(vx) + sqrt(cfx2));
+    my = dmax(my, fabs(vy) + sqrt(cfy2));
+  } else {
+    const double p = dmax((gamma - 1.0) * (c[4 * plane + idx] - 0.5 * c[idx] * vsq), SMALL_VALUE);
+    const double a = sqrt(gamma * p * inv_d);
+    mx = dmax(mx, fabs(vx) + a);
+    my = dmax(my, fabs(vy) + a);
   }
-  __shared__ double sx[8], sy[8];
+}
+
+// block max of (mx, my), then one atomicMax per block on the loop state
+__device__ __forceinline__ void block_max_to_loop(double mx, double my, LoopState* L) {
+  __shared__ double sx[32], sy[32];
   mx = warp_max(mx);
   my = warp_max(my);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -913,14 +906,19 @@ __global__ void __launch_bounds__(256) k_dt_reduce(Grid G, StateBuf in) {
       atomicMax(&L->max_sy, (unsigned long long)__double_as_longlong(my));
     }
   }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool loop_running(const LoopState* L) {
+  return L->t < L->t_end && L->cycle < L->max_cycles;
 }
 
 // dt from the reduced speeds, the tEnd clip, and the loop condition
 // (Source/EvolveFunctions_MHD.py:466-479).
 template <int PHYS>
-__global__ void k_begin(Grid G) {
+__device__ __forceinline__ void b_begin(const Grid& G) {
   LoopState* L = G.loop;
-  const int act = (L->t < L->t_end && L->cycle < L->max_cycles) ? 1 : 0;
+  const int act = loop_running(L) ? 1 : 0;
   L->active = act;
   if (act) {
     const double mx = __longlong_as_double((long long)L->max_sx);
@@ -941,7 +939,7 @@ __global__ void k_begin(Grid G) {
   L->max_sy = 0ull;
 }
 
-__global__ void k_end(Grid G) {
+__device__ __forceinline__ void b_end(const Grid& G) {
   LoopState* L = G.loop;
   if (!L->active) return;
   L->t_prev = L->t;
@@ -950,6 +948,60 @@ __global__ void k_end(Grid G) {
   L->cycles_run = L->cycles_run + 1;
   L->cur ^= 1;
   L->active = 0;
+}
+
+// ============================================================================
+// Plain kernels: one grid per launch, work item from the block/thread index.
+// ============================================================================
+template <int PHYS>
+__global__ void __launch_bounds__(256) k_dt_reduce(Grid G, StateBuf in) {
+  if (!loop_running(G.loop)) return;
+  const size_t n = cell_plane(G);
+  double mx = 0.0, my = 0.0;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x)
+    b_dt_cell<PHYS>(G, in, idx, mx, my);
+  block_max_to_loop(mx, my, G.loop);
+}
+template <int PHYS>
+__global__ void k_begin(Grid G) { b_begin<PHYS>(G); }
+__global__ void k_end(Grid G) { b_end(G); }
+
+template <class S, int AX>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_ppm_slopes(Grid G, StateBuf in) {
+  b_ppm_slopes<S, AX>(G, in, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+template <class S, int AX, int MODE>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_faces(Grid G, StateBuf in) {
+  b_faces<S, AX, MODE>(G, in, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+template <int AX, int STAGE>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_mhd(Grid G, StateBuf in) {
+  b_roe_mhd<AX, STAGE>(G, in, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <int AX>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_hydro(Grid G) {
+  b_roe_hydro<AX>(G, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock) k_emf(Grid G, StateBuf in) {
+  b_emf<STAGE>(G, in, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+template <int AX>
+__global__ void __launch_bounds__(kBlock) k_ctu_mhd(Grid G, StateBuf in) {
+  b_ctu_mhd<AX>(G, in, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <int AX>
+__global__ void __launch_bounds__(kBlock) k_ctu_hydro(Grid G) {
+  b_ctu_hydro<AX>(G, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(kBlock) k_half_ez(Grid G, StateBuf in) {
+  b_half_ez(G, in, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+__global__ void __launch_bounds__(kBlock) k_final_mhd(Grid G, StateBuf in, StateBuf out) {
+  b_final_mhd(G, in, out, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+__global__ void __launch_bounds__(kBlock) k_final_hydro(Grid G, StateBuf in, StateBuf out) {
+  b_final_hydro(G, in, out, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 // ----------------------------------------------------------------------------
@@ -1009,6 +1061,169 @@ void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s) {
     k_final_hydro<<<row_grid(g.nx, g.ny), kBlock, 0, s>>>(g, in, out);
   }
   k_end<<<1, 1, 0, s>>>(g);
+}
+
+// ============================================================================
+// Batched persistent kernels: many grids (instances) in one launch per stage.
+// Each launch walks a work list of tiles -- int4 {instance, row, x0, 0}: one
+// row segment of kBlock work items of one instance's index space -- with a
+// grid of resident blocks striding through the list.  The per-item bodies are
+// the ones above, so a batched cycle computes exactly what the plain cycle
+// computes for every instance.  Instances keep their own dt, time, cycle count
+// and current state buffer in their own LoopState.
+// ============================================================================
+#define MHD_TILE_LOOP(space)                                                  \
+  for (int ti = blockIdx.x; ti < V.ntiles[space]; ti += gridDim.x)           \
+    if (const int4 tl = V.tiles[space][ti]; true)
+
+template <int PHYS>
+__global__ void __launch_bounds__(kBlock) kb_dt_reduce(BatchView V) {
+  MHD_TILE_LOOP(SPACE_CELL) {
+    const Grid& G = V.grids[tl.x];
+    if (!loop_running(G.loop)) continue;   // uniform across the block
+    double mx = 0.0, my = 0.0;
+    const int i = tl.z + threadIdx.x;
+    if (i < G.nx) b_dt_cell<PHYS>(G, G.st[G.loop->cur], (size_t)tl.y * G.nx + i, mx, my);
+    block_max_to_loop(mx, my, G.loop);
+  }
+}
+template <int PHYS>
+__global__ void kb_begin(BatchView V) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < V.ninst) b_begin<PHYS>(V.grids[k]);
+}
+__global__ void kb_end(BatchView V) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < V.ninst) b_end(V.grids[k]);
+}
+template <class S, int AX>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_ppm_slopes(BatchView V) {
+  MHD_TILE_LOOP(AX == 0 ? SPACE_EXT_X : SPACE_EXT_Y) {
+    const Grid& G = V.grids[tl.x];
+    b_ppm_slopes<S, AX>(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+  }
+}
+template <class S, int AX, int MODE>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_faces(BatchView V) {
+  MHD_TILE_LOOP(SPACE_CELL) {
+    const Grid& G = V.grids[tl.x];
+    b_faces<S, AX, MODE>(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+  }
+}
+template <int AX, int STAGE>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_roe_mhd(BatchView V) {
+  MHD_TILE_LOOP(AX == 0 ? SPACE_XFACE : SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int w = AX == 0 ? G.nx + 1 : G.nx;
+    const int x = tl.z + threadIdx.x;
+    if (x < w) b_roe_mhd<AX, STAGE>(G, G.st[G.loop->cur], (size_t)tl.y * w + x);
+  }
+}
+template <int AX>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_roe_hydro(BatchView V) {
+  MHD_TILE_LOOP(AX == 0 ? SPACE_XFACE : SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int w = AX == 0 ? G.nx + 1 : G.nx;
+    const int x = tl.z + threadIdx.x;
+    if (x < w) b_roe_hydro<AX>(G, (size_t)tl.y * w + x);
+  }
+}
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock) kb_emf(BatchView V) {
+  MHD_TILE_LOOP(SPACE_CORNER) {
+    const Grid& G = V.grids[tl.x];
+    b_emf<STAGE>(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+  }
+}
+template <int AX>
+__global__ void __launch_bounds__(kBlock) kb_ctu_mhd(BatchView V) {
+  MHD_TILE_LOOP(AX == 0 ? SPACE_XFACE : SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int w = AX == 0 ? G.nx + 1 : G.nx;
+    const int x = tl.z + threadIdx.x;
+    if (x < w) b_ctu_mhd<AX>(G, G.st[G.loop->cur], (size_t)tl.y * w + x);
+  }
+}
+template <int AX>
+__global__ void __launch_bounds__(kBlock) kb_ctu_hydro(BatchView V) {
+  MHD_TILE_LOOP(AX == 0 ? SPACE_XFACE : SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int w = AX == 0 ? G.nx + 1 : G.nx;
+    const int x = tl.z + threadIdx.x;
+    if (x < w) b_ctu_hydro<AX>(G, (size_t)tl.y * w + x);
+  }
+}
+__global__ void __launch_bounds__(kBlock) kb_half_ez(BatchView V) {
+  MHD_TILE_LOOP(SPACE_CELL) {
+    const Grid& G = V.grids[tl.x];
+    b_half_ez(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+  }
+}
+__global__ void __launch_bounds__(kBlock) kb_final_mhd(BatchView V) {
+  MHD_TILE_LOOP(SPACE_CELL) {
+    const Grid& G = V.grids[tl.x];
+    b_final_mhd(G, G.st[G.loop->cur], G.st[G.loop->cur ^ 1], tl.z + threadIdx.x, tl.y);
+  }
+}
+__global__ void __launch_bounds__(kBlock) kb_final_hydro(BatchView V) {
+  MHD_TILE_LOOP(SPACE_CELL) {
+    const Grid& G = V.grids[tl.x];
+    b_final_hydro(G, G.st[G.loop->cur], G.st[G.loop->cur ^ 1], tl.z + threadIdx.x, tl.y);
+  }
+}
+
+template <int PHYS>
+void enqueue_recon_batch(const BatchView& V, int recon, unsigned blocks, cudaStream_t s) {
+  using SX = typename std::conditional<PHYS == MHD, MhdSweep<0>, HydroSweep<0>>::type;
+  using SY = typename std::conditional<PHYS == MHD, MhdSweep<1>, HydroSweep<1>>::type;
+  if (recon == 2) {
+    kb_ppm_slopes<SX, 0><<<blocks, kBlock, 0, s>>>(V);
+    kb_faces<SX, 0, 2><<<blocks, kBlock, 0, s>>>(V);
+    kb_ppm_slopes<SY, 1><<<blocks, kBlock, 0, s>>>(V);
+    kb_faces<SY, 1, 2><<<blocks, kBlock, 0, s>>>(V);
+  } else if (recon == 1) {
+    kb_ppm_slopes<SX, 0><<<blocks, kBlock, 0, s>>>(V);
+    kb_faces<SX, 0, 1><<<blocks, kBlock, 0, s>>>(V);
+    kb_ppm_slopes<SY, 1><<<blocks, kBlock, 0, s>>>(V);
+    kb_faces<SY, 1, 1><<<blocks, kBlock, 0, s>>>(V);
+  } else {
+    kb_faces<SX, 0, 0><<<blocks, kBlock, 0, s>>>(V);
+    kb_faces<SY, 1, 0><<<blocks, kBlock, 0, s>>>(V);
+  }
+}
+
+// One batched cycle of every instance; each instance reads the state buffer its
+// loop state names as current.  `blocks` = blocks of a persistent launch (a
+// multiple of the SM count).
+void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, cudaStream_t s) {
+  const unsigned ib = (unsigned)((V.ninst + 127) / 128);
+  if (physics == MHD) {
+    kb_dt_reduce<MHD><<<blocks, kBlock, 0, s>>>(V);
+    kb_begin<MHD><<<ib, 128, 0, s>>>(V);
+    enqueue_recon_batch<MHD>(V, recon, blocks, s);
+    kb_roe_mhd<0, 1><<<blocks, kBlock, 0, s>>>(V);
+    kb_roe_mhd<1, 1><<<blocks, kBlock, 0, s>>>(V);
+    kb_emf<1><<<blocks, kBlock, 0, s>>>(V);
+    kb_ctu_mhd<0><<<blocks, kBlock, 0, s>>>(V);
+    kb_ctu_mhd<1><<<blocks, kBlock, 0, s>>>(V);
+    kb_half_ez<<<blocks, kBlock, 0, s>>>(V);
+    kb_roe_mhd<0, 2><<<blocks, kBlock, 0, s>>>(V);
+    kb_roe_mhd<1, 2><<<blocks, kBlock, 0, s>>>(V);
+    kb_emf<2><<<blocks, kBlock, 0, s>>>(V);
+    kb_final_mhd<<<blocks, kBlock, 0, s>>>(V);
+  } else {
+    kb_dt_reduce<HYDRO><<<blocks, kBlock, 0, s>>>(V);
+    kb_begin<HYDRO><<<ib, 128, 0, s>>>(V);
+    enqueue_recon_batch<HYDRO>(V, recon, blocks, s);
+    kb_roe_hydro<0><<<blocks, kBlock, 0, s>>>(V);
+    kb_roe_hydro<1><<<blocks, kBlock, 0, s>>>(V);
+    kb_ctu_hydro<0><<<blocks, kBlock, 0, s>>>(V);
+    kb_ctu_hydro<1><<<blocks, kBlock, 0, s>>>(V);
+    kb_roe_hydro<0><<<blocks, kBlock, 0, s>>>(V);
+    kb_roe_hydro<1><<<blocks, kBlock, 0, s>>>(V);
+    kb_final_hydro<<<blocks, kBlock, 0, s>>>(V);
+  }
+  kb_end<<<ib, 128, 0, s>>>(V);
 }
 
 }  // namespace MHD_NS

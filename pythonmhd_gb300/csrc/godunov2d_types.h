@@ -4,6 +4,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include <vector_types.h>
+
 #ifdef __CUDACC__
 #define MHD_HD __host__ __device__
 #else
@@ -66,6 +68,18 @@ struct Grid {
   size_t ext_plane;            // plane stride of slopes / eig (max of x/y extended sizes)
   LoopState* loop;             // device
   int* status;                 // device error word (0 = ok)
+};
+
+// index spaces of the batched work lists
+enum Space : int { SPACE_CELL = 0, SPACE_EXT_X, SPACE_EXT_Y, SPACE_XFACE, SPACE_YFACE, SPACE_CORNER, kNumSpaces };
+
+// Device view of a batch: the per-instance grids and one work list of tiles per
+// index space (tile = int4 {instance, row, x0, 0}, a row segment of work items).
+struct BatchView {
+  const Grid* grids;
+  const int4* tiles[kNumSpaces];
+  int ntiles[kNumSpaces];
+  int ninst;
 };
 
 MHD_HD inline size_t cell_plane(const Grid& g) { return (size_t)g.nx * g.ny; }

@@ -183,3 +183,27 @@ def turbulence(n, seed=1, gamma=5.0 / 3.0, kmax_v=32, kmax_a=16, mach=1.0, beta=
     prim[5] = cby
     prim[7] = p
     return prim, prim_to_cons_mhd(prim, gamma), fbx, fby, dx, dy
+
+
+def orszag_tang_batch(count=256, seed=0, sizes=tuple(range(64, 513, 32)), gamma_range=(1.4, 5.0 / 3.0),
+                      b0_range=(0.5, 2.0), rho_perturb=0.01):
+    """The uneven batch of Orszag-Tang instances (the batched workload).
+
+    Each instance draws Nx and Ny independently and uniformly from ``sizes``,
+    gamma uniformly from ``gamma_range``, a B0 scale uniformly from ``b0_range``,
+    and gets a seeded ``rho_perturb`` Gaussian density perturbation (its own seed
+    ``seed * 100003 + k``).  Returns a list of dicts with the state arrays and
+    grid parameters.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        nx = int(rng.choice(sizes))
+        ny = int(rng.choice(sizes))
+        gamma = float(rng.uniform(*gamma_range))
+        b0 = float(rng.uniform(*b0_range))
+        prim, cons, fbx, fby, dx, dy = orszag_tang(nx, ny, gamma=gamma, b0_scale=b0, faces="potential",
+                                                   rho_perturb=rho_perturb, seed=seed * 100003 + k)
+        out.append(dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=dx, dy=dy, nx=nx, ny=ny, gamma=gamma,
+                        bcx=PERIODIC, bcy=PERIODIC))
+    return out

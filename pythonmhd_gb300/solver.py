@@ -145,3 +145,91 @@ class Grid2D:
         s = ctypes.c_void_p()
         _lib.check(self.lib.mhd2d_stream(self._h, ctypes.byref(s)), "mhd2d_stream")
         return s.value
+
+
+class Batch2D:
+    """Many independent grids advanced together (one persistent launch per stage).
+
+    ``grids`` is a list of dicts with keys ny, nx, dx, dy, bcx, bcy, gamma; all
+    instances share physics, reconstruction, entropy fix, floors and arithmetic.
+    """
+
+    def __init__(self, grids, mhd=True, recon=2, entropy_fix=False, eps=0.5, min_d=1e-12, min_p=1e-12,
+                 min_e=1e-12, arith=None):
+        self.lib = _lib.load()
+        self.mhd = bool(mhd)
+        self.nvars = 8 if self.mhd else 5
+        self.arith = arith or default_arith()
+        self.shapes = [(int(g["ny"]), int(g["nx"])) for g in grids]
+        n = len(grids)
+        ny = np.array([s[0] for s in self.shapes], dtype=np.int32)
+        nx = np.array([s[1] for s in self.shapes], dtype=np.int32)
+        dx = np.array([g["dx"] for g in grids], dtype=np.float64)
+        dy = np.array([g["dy"] for g in grids], dtype=np.float64)
+        bcx = np.array([g.get("bcx", 1) for g in grids], dtype=np.int32)
+        bcy = np.array([g.get("bcy", 1) for g in grids], dtype=np.int32)
+        gam = np.array([g["gamma"] for g in grids], dtype=np.float64)
+        self._keep = (ny, nx, dx, dy, bcx, bcy, gam)
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.mhdb_create(n, ny.ctypes.data, nx.ctypes.data, dx.ctypes.data, dy.ctypes.data,
+                                        bcx.ctypes.data, bcy.ctypes.data, gam.ctypes.data, 1 if self.mhd else 0,
+                                        int(recon), 1 if entropy_fix else 0, float(eps), float(min_d),
+                                        float(min_p), float(min_e), ARITH[self.arith], ctypes.byref(h)),
+                   "mhdb_create")
+        self._h = h
+        self.count = n
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.lib.mhdb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, k, prim, cons, fbx=None, fby=None):
+        prim, cons = _as_f64c(prim), _as_f64c(cons)
+        fbx = _as_f64c(fbx) if fbx is not None else None
+        fby = _as_f64c(fby) if fby is not None else None
+        ny, nx = self.shapes[k]
+        if prim.shape != (self.nvars, ny, nx) or cons.shape != prim.shape:
+            raise ValueError(f"instance {k}: prim/cons must be {(self.nvars, ny, nx)}")
+        _lib.check(self.lib.mhdb_upload(self._h, int(k), _ptr(prim), _ptr(cons), _ptr(fbx), _ptr(fby)),
+                   "mhdb_upload")
+
+    def advance(self, t0, t_end, cycle0, max_cycles, cfl):
+        n = self.count
+        t0 = np.broadcast_to(np.asarray(t0, dtype=np.float64), (n,)).copy()
+        te = np.broadcast_to(np.asarray(t_end, dtype=np.float64), (n,)).copy()
+        c0 = np.broadcast_to(np.asarray(cycle0, dtype=np.int64), (n,)).copy()
+        mc = np.broadcast_to(np.asarray(max_cycles, dtype=np.int64), (n,)).copy()
+        t_out = np.empty(n)
+        c_out = np.empty(n, dtype=np.int64)
+        _lib.check(self.lib.mhdb_advance(self._h, t0.ctypes.data, te.ctypes.data, c0.ctypes.data, mc.ctypes.data,
+                                         float(cfl), t_out.ctypes.data, c_out.ctypes.data), "mhdb_advance")
+        return t_out, c_out
+
+    def download(self, k, which=0):
+        ny, nx = self.shapes[k]
+        prim = np.empty((self.nvars, ny, nx))
+        cons = np.empty((self.nvars, ny, nx))
+        fbx = np.empty((ny, nx + 1)) if self.mhd else None
+        fby = np.empty((ny + 1, nx)) if self.mhd else None
+        _lib.check(self.lib.mhdb_download(self._h, int(k), int(which), _ptr(prim), _ptr(cons), _ptr(fbx), _ptr(fby)),
+                   "mhdb_download")
+        return (prim, cons, fbx, fby) if self.mhd else (prim, cons)
+
+    def set_blocks(self, blocks):
+        _lib.check(self.lib.mhdb_set_blocks(self._h, int(blocks)), "mhdb_set_blocks")
+
+    def info(self):
+        n = ctypes.c_longlong()
+        b = ctypes.c_size_t()
+        blk = ctypes.c_int()
+        s = ctypes.c_void_p()
+        _lib.check(self.lib.mhdb_info(self._h, ctypes.byref(n), ctypes.byref(b), ctypes.byref(blk), ctypes.byref(s)),
+                   "mhdb_info")
+        return {"last_launches": n.value, "device_bytes": b.value, "blocks": blk.value, "stream": s.value}
