@@ -206,9 +206,9 @@ def run_batch(a, torch):
     insts = ic.orszag_tang_batch(count=a.batch_count, seed=0)
     zones = sum(i["nx"] * i["ny"] for i in insts)
     k, w = a.batch_steps, 1
+    from pythonmhd_gb300 import autotune
     b = Batch2D(insts, mhd=True, recon=1, arith=a.arith)
-    for n, i in enumerate(insts):
-        b.upload(n, i["prim"], i["cons"], i["fbx"], i["fby"])
+    tuned = autotune.tune_batch(b, insts, recon=1, cycles=1)
     b.advance(0.0, 1e30, 0, w, 0.4)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -243,6 +243,8 @@ def run_batch(a, torch):
             "zones_per_step": zones, "steps": k,
             "batched_zone_updates_per_s": zones * k / tb, "looped_zone_updates_per_s": zones * k / tl,
             "speedup_vs_loop": tl / tb, "batched_launches": launches,
+            "launch_shape": {"tile_width": tuned["tile_width"], "fuse": tuned["fuse"], "blocks": tuned["blocks"],
+                             "autotuned": True, "from_cache": tuned["cached"]},
             "loop": "one single-grid handle per instance, each advanced k cycles in turn (CUDA graphs)",
             "step_major_loop_zone_updates_per_s": zones * k / ts, "speedup_vs_step_major_loop": ts / tb,
             "timing": "host wall clock around device-synchronised calls"}

@@ -139,8 +139,12 @@ int mhdb_advance(void* handle, const double* t0, const double* t_end, const long
                  const long long* max_cycles, double cfl, double* t_out, long long* cycle_out);
 int mhdb_download(void* handle, int instance, int which, double* prim, double* cons,
                   double* faceBx, double* faceBy);
-/* Blocks of each persistent launch (tuning knob; default 2 per SM). */
-int mhdb_set_blocks(void* handle, int blocks);
+/* Launch shape of a batched cycle (the autotuner's knobs): tile_width work
+ * items per tile = threads per block (32, 64 or 128; default 128), fuse = 1
+ * for one launch per stage and direction or 2 to run the independent x and y
+ * launches of a stage as one launch, blocks = blocks of each persistent launch
+ * (default 2 per SM).  Results do not depend on these. */
+int mhdb_configure(void* handle, int tile_width, int fuse, int blocks);
 int mhdb_info(void* handle, long long* last_launches, size_t* device_bytes, int* blocks,
               void** stream);
 void mhdb_destroy(void* handle);

@@ -46,7 +46,7 @@ SIGNATURES = {
                                     ctypes.c_void_p]),
     "mhdb_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p, c_double_p,
                                      c_double_p]),
-    "mhdb_set_blocks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "mhdb_configure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "mhdb_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t),
                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]),
     "mhdb_destroy": (None, [ctypes.c_void_p]),

@@ -15,11 +15,13 @@
 namespace mhdk {
 namespace exact {
 void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
-void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, cudaStream_t s);
+void enqueue_cycle_batch_tuned(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, int fuse,
+                               cudaStream_t s);
 }  // namespace exact
 namespace fast {
 void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
-void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, cudaStream_t s);
+void enqueue_cycle_batch_tuned(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, int fuse,
+                               cudaStream_t s);
 }  // namespace fast
 }  // namespace mhdk
 
@@ -90,6 +92,8 @@ size_t carve_grid(Grid& g, int nvars, char* base) {
   if (g.recon >= 1) {
     take(&g.slopes, nv * g.ext_plane);
     take(&g.eig, nw * g.ext_plane);
+    take(&g.slopes_y, nv * g.ext_plane);
+    take(&g.eig_y, nw * g.ext_plane);
   }
   return off;
 }
@@ -125,7 +129,9 @@ struct BatchHandle {
   int device = 0;
   std::vector<Grid> grids;         // host copies (device pointers inside)
   Grid* d_grids = nullptr;
-  int4* d_tiles = nullptr;         // all work lists, one after the other
+  int4* d_tiles = nullptr;         // all work lists, one after the other (own allocation)
+  int tile_width = 128;            // work items per tile = threads per block
+  int fuse = 1;                    // 1: one launch per stage and direction; 2: x+y fused
   mhdk::BatchView view{};
   void* arena = nullptr;
   size_t arena_bytes = 0;
@@ -141,9 +147,45 @@ struct BatchHandle {
 
 void enqueue_batch(BatchHandle* b) {
   if (b->arith == MHD2D_ARITH_EXACT)
-    mhdk::exact::enqueue_cycle_batch(b->view, b->physics, b->recon, b->blocks, b->stream);
+    mhdk::exact::enqueue_cycle_batch_tuned(b->view, b->physics, b->recon, b->blocks, (unsigned)b->tile_width, b->fuse,
+                                           b->stream);
   else
-    mhdk::fast::enqueue_cycle_batch(b->view, b->physics, b->recon, b->blocks, b->stream);
+    mhdk::fast::enqueue_cycle_batch_tuned(b->view, b->physics, b->recon, b->blocks, (unsigned)b->tile_width, b->fuse,
+                                          b->stream);
+}
+
+// (Re)build the per-space work lists for tiles of `width` items.
+int build_tiles(BatchHandle* b, int width) {
+  std::vector<int4> tiles[mhdk::kNumSpaces];
+  for (int i = 0; i < b->count; ++i) {
+    const Grid& g = b->grids[i];
+    const int w[mhdk::kNumSpaces] = {g.nx, g.nx + 2, g.nx, g.nx + 1, g.nx, g.nx + 1};
+    const int hgt[mhdk::kNumSpaces] = {g.ny, g.ny, g.ny + 2, g.ny, g.ny + 1, g.ny + 1};
+    for (int sp = 0; sp < mhdk::kNumSpaces; ++sp)
+      for (int r = 0; r < hgt[sp]; ++r)
+        for (int x0 = 0; x0 < w[sp]; x0 += width) tiles[sp].push_back(make_int4(i, r, x0, 0));
+  }
+  size_t total = 0;
+  for (auto& t : tiles) total += t.size();
+  int4* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, total * sizeof(int4));
+  if (e != cudaSuccess) return cuda_fail(e);
+  size_t off = 0;
+  mhdk::BatchView v = b->view;
+  for (int sp = 0; sp < mhdk::kNumSpaces && e == cudaSuccess; ++sp) {
+    v.tiles[sp] = d + off;
+    v.ntiles[sp] = (int)tiles[sp].size();
+    e = cudaMemcpyAsync(d + off, tiles[sp].data(), tiles[sp].size() * sizeof(int4), cudaMemcpyHostToDevice,
+                        b->stream);
+    off += tiles[sp].size();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) { cudaFree(d); return cuda_fail(e); }
+  if (b->d_tiles) cudaFree(b->d_tiles);
+  b->d_tiles = d;
+  b->view = v;
+  b->tile_width = width;
+  return MHD_OK;
 }
 
 int build_batch_graph(BatchHandle* b) {
@@ -165,6 +207,7 @@ int build_batch_graph(BatchHandle* b) {
 void free_batch(BatchHandle* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->d_tiles) cudaFree(b->d_tiles);
   if (b->h_loops) cudaFreeHost(b->h_loops);
   if (b->arena) cudaFree(b->arena);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -439,9 +482,6 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   b->blocks = (unsigned)std::max(1, sms) * 2;
 
-  // work lists: row segments of kTileWidth items per index space and instance
-  constexpr int kTileWidth = 128;
-  std::vector<int4> tiles[mhdk::kNumSpaces];
   size_t grid_bytes = 0;
   for (int i = 0; i < count; ++i) {
     Grid& g = b->grids[i];
@@ -450,16 +490,9 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
     g.physics = physics; g.recon = recon; g.efix = entropy_fix ? 1 : 0;
     g.gamma = gamma[i]; g.eps = eps; g.min_d = min_d; g.min_p = min_p; g.min_e = min_e;
     grid_bytes += carve_grid(g, b->nvars, nullptr);
-    const int w[mhdk::kNumSpaces] = {g.nx, g.nx + 2, g.nx, g.nx + 1, g.nx, g.nx + 1};
-    const int hgt[mhdk::kNumSpaces] = {g.ny, g.ny, g.ny + 2, g.ny, g.ny + 1, g.ny + 1};
-    for (int sp = 0; sp < mhdk::kNumSpaces; ++sp)
-      for (int r = 0; r < hgt[sp]; ++r)
-        for (int x0 = 0; x0 < w[sp]; x0 += kTileWidth) tiles[sp].push_back(make_int4(i, r, x0, 0));
   }
-  size_t ntiles_total = 0;
-  for (auto& t : tiles) ntiles_total += t.size();
   const size_t total = grid_bytes + align256(count * sizeof(LoopState)) + align256(count * sizeof(Grid)) +
-                       align256(ntiles_total * sizeof(int4)) + align256(sizeof(int));
+                       align256(sizeof(int));
   e = cudaMalloc(&b->arena, total);
   if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
   b->arena_bytes = total;
@@ -470,30 +503,22 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
   off += align256(count * sizeof(LoopState));
   b->d_grids = reinterpret_cast<Grid*>(base + off);
   off += align256(count * sizeof(Grid));
-  b->d_tiles = reinterpret_cast<int4*>(base + off);
-  off += align256(ntiles_total * sizeof(int4));
   int* status = reinterpret_cast<int*>(base + off);
   for (int i = 0; i < count; ++i) {
     b->grids[i].loop = b->d_loops + i;
     b->grids[i].status = status;
   }
   e = cudaMemsetAsync(b->arena, 0, total, b->stream);
-  size_t toff = 0;
   b->view.grids = b->d_grids;
   b->view.ninst = count;
-  for (int sp = 0; sp < mhdk::kNumSpaces && e == cudaSuccess; ++sp) {
-    b->view.tiles[sp] = b->d_tiles + toff;
-    b->view.ntiles[sp] = (int)tiles[sp].size();
-    e = cudaMemcpyAsync(b->d_tiles + toff, tiles[sp].data(), tiles[sp].size() * sizeof(int4),
-                        cudaMemcpyHostToDevice, b->stream);
-    toff += tiles[sp].size();
-  }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(b->d_grids, b->grids.data(), count * sizeof(Grid), cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_loops, count * sizeof(LoopState));
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
   std::memset(b->h_loops, 0, count * sizeof(LoopState));
+  const int rc = build_tiles(b, 128);
+  if (rc != MHD_OK) { free_batch(b); return rc; }
   *handle = b;
   return MHD_OK;
 }
@@ -594,17 +619,22 @@ int mhdb_download(void* handle, int inst, int which, double* prim, double* cons,
   return MHD_OK;
 }
 
-int mhdb_set_blocks(void* handle, int blocks) {
+int mhdb_configure(void* handle, int tile_width, int fuse, int blocks) {
   BatchHandle* b = static_cast<BatchHandle*>(handle);
-  if (!b || blocks < 1) return MHD_ERR_ARG;
-  if ((unsigned)blocks != b->blocks) {
-    b->blocks = (unsigned)blocks;
-    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  if (!b || blocks < 1 || (fuse != 1 && fuse != 2)) return MHD_ERR_ARG;
+  if (tile_width != 32 && tile_width != 64 && tile_width != 128) return MHD_ERR_ARG;
+  if (tile_width != b->tile_width) {
+    const int rc = build_tiles(b, tile_width);
+    if (rc != MHD_OK) return rc;
   }
+  b->fuse = fuse;
+  b->blocks = (unsigned)blocks;
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
   return MHD_OK;
 }
 
 int mhdb_info(void* handle, long long* launches, size_t* device_bytes, int* blocks, void** stream) {
+  // blocks of each persistent launch; see mhdb_configure for the other knobs
   BatchHandle* b = static_cast<BatchHandle*>(handle);
   if (!b) return MHD_ERR_ARG;
   if (launches) *launches = b->last_launches;

@@ -216,9 +216,9 @@ __device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, 
         first = false;
       }
     }
-    G.slopes[i * es + xi] = acc;
+    (AX == 0 ? G.slopes : G.slopes_y)[i * es + xi] = acc;
   }
-  S::store(e, G.eig + xi, es);
+  S::store(e, (AX == 0 ? G.eig : G.eig_y) + xi, es);
 }
 
 // Write one reconstructed state to a face: floors (Source/PrimCons_HelperModule.py:499-554),
@@ -285,7 +285,7 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
     const size_t xc = ext_index<AX>(c, t, g.nx);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const double s_c = G.slopes[k * es + xc];
+      const double s_c = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xc];
       double a = wc[k] - 0.5 * s_c;
       double b = wc[k] + 0.5 * s_c;
       a = dmax(dmin(wc[k], wl[k]), a);
@@ -296,7 +296,7 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
       ria[k] = b;
     }
     typename S::Eig e;
-    S::load(e, G.eig + xc, es);
+    S::load(e, (AX == 0 ? G.eig : G.eig_y) + xc, es);
     const double* lam = S::lam(e);
     const double dtdx = dt / dn;
     double c1[NV];
@@ -343,9 +343,9 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
     const size_t xr = ext_index<AX>(c + 1, t, g.nx);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const double s_l = G.slopes[k * es + xl];
-      const double s_c = G.slopes[k * es + xc];
-      const double s_r = G.slopes[k * es + xr];
+      const double s_l = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xl];
+      const double s_c = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xc];
+      const double s_r = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xr];
       double a = 0.5 * (wc[k] + wl[k]) - (s_c - s_l) / 6.0;
       double b = 0.5 * (wr[k] + wc[k]) - (s_r - s_c) / 6.0;
       const double dprod = (b - wc[k]) * (wc[k] - a);
@@ -367,7 +367,7 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
       ria[k] = b;
     }
     typename S::Eig e;
-    S::load(e, G.eig + xc, es);
+    S::load(e, (AX == 0 ? G.eig : G.eig_y) + xc, es);
     const double* lam = S::lam(e);
     const double dtdx = dt / dn;
     double c1[NV], c2[NV];
@@ -1172,56 +1172,169 @@ __global__ void __launch_bounds__(kBlock) kb_final_hydro(BatchView V) {
   }
 }
 
+// ---- fusion depth 2: the independent x and y launches of a stage in one launch,
+// walking the x work list and then the y work list.
+#define MHD_PAIR_LOOP(SA, SB)                                                       \
+  for (int ti = blockIdx.x; ti < V.ntiles[SA] + V.ntiles[SB]; ti += gridDim.x)      \
+    if (const bool first = ti < V.ntiles[SA]; true)                                 \
+      if (const int4 tl = first ? V.tiles[SA][ti] : V.tiles[SB][ti - V.ntiles[SA]]; true)
+
+template <class SX, class SY>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_ppm_slopes_xy(BatchView V) {
+  MHD_PAIR_LOOP(SPACE_EXT_X, SPACE_EXT_Y) {
+    const Grid& G = V.grids[tl.x];
+    if (first) b_ppm_slopes<SX, 0>(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+    else b_ppm_slopes<SY, 1>(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+  }
+}
+template <class SX, class SY, int MODE>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_faces_xy(BatchView V) {
+  MHD_PAIR_LOOP(SPACE_CELL, SPACE_CELL) {
+    const Grid& G = V.grids[tl.x];
+    if (first) b_faces<SX, 0, MODE>(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+    else b_faces<SY, 1, MODE>(G, G.st[G.loop->cur], tl.z + threadIdx.x, tl.y);
+  }
+}
+template <int STAGE>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_roe_mhd_xy(BatchView V) {
+  MHD_PAIR_LOOP(SPACE_XFACE, SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int x = tl.z + threadIdx.x;
+    if (first) {
+      if (x < G.nx + 1) b_roe_mhd<0, STAGE>(G, G.st[G.loop->cur], (size_t)tl.y * (G.nx + 1) + x);
+    } else {
+      if (x < G.nx) b_roe_mhd<1, STAGE>(G, G.st[G.loop->cur], (size_t)tl.y * G.nx + x);
+    }
+  }
+}
+__global__ void __launch_bounds__(kBlock, kMinBlocks) kb_roe_hydro_xy(BatchView V) {
+  MHD_PAIR_LOOP(SPACE_XFACE, SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int x = tl.z + threadIdx.x;
+    if (first) {
+      if (x < G.nx + 1) b_roe_hydro<0>(G, (size_t)tl.y * (G.nx + 1) + x);
+    } else {
+      if (x < G.nx) b_roe_hydro<1>(G, (size_t)tl.y * G.nx + x);
+    }
+  }
+}
+__global__ void __launch_bounds__(kBlock) kb_ctu_mhd_xy(BatchView V) {
+  MHD_PAIR_LOOP(SPACE_XFACE, SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int x = tl.z + threadIdx.x;
+    if (first) {
+      if (x < G.nx + 1) b_ctu_mhd<0>(G, G.st[G.loop->cur], (size_t)tl.y * (G.nx + 1) + x);
+    } else {
+      if (x < G.nx) b_ctu_mhd<1>(G, G.st[G.loop->cur], (size_t)tl.y * G.nx + x);
+    }
+  }
+}
+__global__ void __launch_bounds__(kBlock) kb_ctu_hydro_xy(BatchView V) {
+  MHD_PAIR_LOOP(SPACE_XFACE, SPACE_YFACE) {
+    const Grid& G = V.grids[tl.x];
+    const int x = tl.z + threadIdx.x;
+    if (first) {
+      if (x < G.nx + 1) b_ctu_hydro<0>(G, (size_t)tl.y * (G.nx + 1) + x);
+    } else {
+      if (x < G.nx) b_ctu_hydro<1>(G, (size_t)tl.y * G.nx + x);
+    }
+  }
+}
+
 template <int PHYS>
-void enqueue_recon_batch(const BatchView& V, int recon, unsigned blocks, cudaStream_t s) {
+void enqueue_recon_batch(const BatchView& V, int recon, unsigned blocks, unsigned tw, cudaStream_t s) {
   using SX = typename std::conditional<PHYS == MHD, MhdSweep<0>, HydroSweep<0>>::type;
   using SY = typename std::conditional<PHYS == MHD, MhdSweep<1>, HydroSweep<1>>::type;
   if (recon == 2) {
-    kb_ppm_slopes<SX, 0><<<blocks, kBlock, 0, s>>>(V);
-    kb_faces<SX, 0, 2><<<blocks, kBlock, 0, s>>>(V);
-    kb_ppm_slopes<SY, 1><<<blocks, kBlock, 0, s>>>(V);
-    kb_faces<SY, 1, 2><<<blocks, kBlock, 0, s>>>(V);
+    kb_ppm_slopes<SX, 0><<<blocks, tw, 0, s>>>(V);
+    kb_faces<SX, 0, 2><<<blocks, tw, 0, s>>>(V);
+    kb_ppm_slopes<SY, 1><<<blocks, tw, 0, s>>>(V);
+    kb_faces<SY, 1, 2><<<blocks, tw, 0, s>>>(V);
   } else if (recon == 1) {
-    kb_ppm_slopes<SX, 0><<<blocks, kBlock, 0, s>>>(V);
-    kb_faces<SX, 0, 1><<<blocks, kBlock, 0, s>>>(V);
-    kb_ppm_slopes<SY, 1><<<blocks, kBlock, 0, s>>>(V);
-    kb_faces<SY, 1, 1><<<blocks, kBlock, 0, s>>>(V);
+    kb_ppm_slopes<SX, 0><<<blocks, tw, 0, s>>>(V);
+    kb_faces<SX, 0, 1><<<blocks, tw, 0, s>>>(V);
+    kb_ppm_slopes<SY, 1><<<blocks, tw, 0, s>>>(V);
+    kb_faces<SY, 1, 1><<<blocks, tw, 0, s>>>(V);
   } else {
-    kb_faces<SX, 0, 0><<<blocks, kBlock, 0, s>>>(V);
-    kb_faces<SY, 1, 0><<<blocks, kBlock, 0, s>>>(V);
+    kb_faces<SX, 0, 0><<<blocks, tw, 0, s>>>(V);
+    kb_faces<SY, 1, 0><<<blocks, tw, 0, s>>>(V);
   }
+}
+
+void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, cudaStream_t s);
+
+template <int PHYS>
+void enqueue_recon_batch_xy(const BatchView& V, int recon, unsigned blocks, unsigned tw, cudaStream_t s) {
+  using SX = typename std::conditional<PHYS == MHD, MhdSweep<0>, HydroSweep<0>>::type;
+  using SY = typename std::conditional<PHYS == MHD, MhdSweep<1>, HydroSweep<1>>::type;
+  if (recon >= 1) kb_ppm_slopes_xy<SX, SY><<<blocks, tw, 0, s>>>(V);
+  if (recon == 2) kb_faces_xy<SX, SY, 2><<<blocks, tw, 0, s>>>(V);
+  else if (recon == 1) kb_faces_xy<SX, SY, 1><<<blocks, tw, 0, s>>>(V);
+  else kb_faces_xy<SX, SY, 0><<<blocks, tw, 0, s>>>(V);
 }
 
 // One batched cycle of every instance; each instance reads the state buffer its
 // loop state names as current.  `blocks` = blocks of a persistent launch (a
-// multiple of the SM count).
-void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, cudaStream_t s) {
+// multiple of the SM count); `tw` = tile width = threads per block (the work
+// lists must be built for it); `fuse` = 2 runs the x and y launches of a stage
+// as one launch.
+void enqueue_cycle_batch_tuned(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw,
+                               int fuse, cudaStream_t s) {
+  const unsigned ib = (unsigned)((V.ninst + 127) / 128);
+  if (fuse == 2) {
+    if (physics == MHD) {
+      kb_dt_reduce<MHD><<<blocks, tw, 0, s>>>(V);
+      kb_begin<MHD><<<ib, 128, 0, s>>>(V);
+      enqueue_recon_batch_xy<MHD>(V, recon, blocks, tw, s);
+      kb_roe_mhd_xy<1><<<blocks, tw, 0, s>>>(V);
+      kb_emf<1><<<blocks, tw, 0, s>>>(V);
+      kb_ctu_mhd_xy<<<blocks, tw, 0, s>>>(V);
+      kb_half_ez<<<blocks, tw, 0, s>>>(V);
+      kb_roe_mhd_xy<2><<<blocks, tw, 0, s>>>(V);
+      kb_emf<2><<<blocks, tw, 0, s>>>(V);
+      kb_final_mhd<<<blocks, tw, 0, s>>>(V);
+    } else {
+      kb_dt_reduce<HYDRO><<<blocks, tw, 0, s>>>(V);
+      kb_begin<HYDRO><<<ib, 128, 0, s>>>(V);
+      enqueue_recon_batch_xy<HYDRO>(V, recon, blocks, tw, s);
+      kb_roe_hydro_xy<<<blocks, tw, 0, s>>>(V);
+      kb_ctu_hydro_xy<<<blocks, tw, 0, s>>>(V);
+      kb_roe_hydro_xy<<<blocks, tw, 0, s>>>(V);
+      kb_final_hydro<<<blocks, tw, 0, s>>>(V);
+    }
+    kb_end<<<ib, 128, 0, s>>>(V);
+    return;
+  }
+  enqueue_cycle_batch(V, physics, recon, blocks, tw, s);
+}
+
+void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, cudaStream_t s) {
   const unsigned ib = (unsigned)((V.ninst + 127) / 128);
   if (physics == MHD) {
-    kb_dt_reduce<MHD><<<blocks, kBlock, 0, s>>>(V);
+    kb_dt_reduce<MHD><<<blocks, tw, 0, s>>>(V);
     kb_begin<MHD><<<ib, 128, 0, s>>>(V);
-    enqueue_recon_batch<MHD>(V, recon, blocks, s);
-    kb_roe_mhd<0, 1><<<blocks, kBlock, 0, s>>>(V);
-    kb_roe_mhd<1, 1><<<blocks, kBlock, 0, s>>>(V);
-    kb_emf<1><<<blocks, kBlock, 0, s>>>(V);
-    kb_ctu_mhd<0><<<blocks, kBlock, 0, s>>>(V);
-    kb_ctu_mhd<1><<<blocks, kBlock, 0, s>>>(V);
-    kb_half_ez<<<blocks, kBlock, 0, s>>>(V);
-    kb_roe_mhd<0, 2><<<blocks, kBlock, 0, s>>>(V);
-    kb_roe_mhd<1, 2><<<blocks, kBlock, 0, s>>>(V);
-    kb_emf<2><<<blocks, kBlock, 0, s>>>(V);
-    kb_final_mhd<<<blocks, kBlock, 0, s>>>(V);
+    enqueue_recon_batch<MHD>(V, recon, blocks, tw, s);
+    kb_roe_mhd<0, 1><<<blocks, tw, 0, s>>>(V);
+    kb_roe_mhd<1, 1><<<blocks, tw, 0, s>>>(V);
+    kb_emf<1><<<blocks, tw, 0, s>>>(V);
+    kb_ctu_mhd<0><<<blocks, tw, 0, s>>>(V);
+    kb_ctu_mhd<1><<<blocks, tw, 0, s>>>(V);
+    kb_half_ez<<<blocks, tw, 0, s>>>(V);
+    kb_roe_mhd<0, 2><<<blocks, tw, 0, s>>>(V);
+    kb_roe_mhd<1, 2><<<blocks, tw, 0, s>>>(V);
+    kb_emf<2><<<blocks, tw, 0, s>>>(V);
+    kb_final_mhd<<<blocks, tw, 0, s>>>(V);
   } else {
-    kb_dt_reduce<HYDRO><<<blocks, kBlock, 0, s>>>(V);
+    kb_dt_reduce<HYDRO><<<blocks, tw, 0, s>>>(V);
     kb_begin<HYDRO><<<ib, 128, 0, s>>>(V);
-    enqueue_recon_batch<HYDRO>(V, recon, blocks, s);
-    kb_roe_hydro<0><<<blocks, kBlock, 0, s>>>(V);
-    kb_roe_hydro<1><<<blocks, kBlock, 0, s>>>(V);
-    kb_ctu_hydro<0><<<blocks, kBlock, 0, s>>>(V);
-    kb_ctu_hydro<1><<<blocks, kBlock, 0, s>>>(V);
-    kb_roe_hydro<0><<<blocks, kBlock, 0, s>>>(V);
-    kb_roe_hydro<1><<<blocks, kBlock, 0, s>>>(V);
-    kb_final_hydro<<<blocks, kBlock, 0, s>>>(V);
+    enqueue_recon_batch<HYDRO>(V, recon, blocks, tw, s);
+    kb_roe_hydro<0><<<blocks, tw, 0, s>>>(V);
+    kb_roe_hydro<1><<<blocks, tw, 0, s>>>(V);
+    kb_ctu_hydro<0><<<blocks, tw, 0, s>>>(V);
+    kb_ctu_hydro<1><<<blocks, tw, 0, s>>>(V);
+    kb_roe_hydro<0><<<blocks, tw, 0, s>>>(V);
+    kb_roe_hydro<1><<<blocks, tw, 0, s>>>(V);
+    kb_final_hydro<<<blocks, tw, 0, s>>>(V);
   }
   kb_end<<<ib, 128, 0, s>>>(V);
 }

@@ -63,8 +63,10 @@ struct Grid {
   double* emf;                 // (Ny+1)*(Nx+1) corner EMF
   double* nfbx; double* nfby;  // half-step face B
   double* hez;                 // half-step cell Ez
-  double* slopes;              // NV planes over the sweep-extended grid
-  double* eig;                 // eigen words over the sweep-extended grid
+  double* slopes;              // NV planes over the x-sweep-extended grid
+  double* eig;                 // eigen words over the x-sweep-extended grid
+  double* slopes_y;            // the same for the y sweep (separate, so both sweeps
+  double* eig_y;               // can run at once)
   size_t ext_plane;            // plane stride of slopes / eig (max of x/y extended sizes)
   LoopState* loop;             // device
   int* status;                 // device error word (0 = ok)

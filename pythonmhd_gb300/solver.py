@@ -222,8 +222,12 @@ class Batch2D:
                    "mhdb_download")
         return (prim, cons, fbx, fby) if self.mhd else (prim, cons)
 
-    def set_blocks(self, blocks):
-        _lib.check(self.lib.mhdb_set_blocks(self._h, int(blocks)), "mhdb_set_blocks")
+    def configure(self, tile_width=128, fuse=1, blocks=None):
+        """Launch shape of a batched cycle: tile width (32/64/128), fusion depth (1/2), persistent blocks."""
+        if blocks is None:
+            blocks = self.info()["blocks"]
+        _lib.check(self.lib.mhdb_configure(self._h, int(tile_width), int(fuse), int(blocks)), "mhdb_configure")
+        self.launch_shape = (int(tile_width), int(fuse), int(blocks))
 
     def info(self):
         n = ctypes.c_longlong()

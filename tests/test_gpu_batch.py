@@ -92,3 +92,43 @@ def test_batch_of_256_uneven_instances_runs_and_conserves():
         assert abs(c[0].sum() - insts[k]["cons"][0].sum()) <= 1e-12 * insts[k]["cons"][0].sum()
         assert np.array_equal(bx[:, 0], bx[:, -1])
     b.close()
+
+
+@pytest.mark.parametrize("tile_width,fuse", [(32, 1), (64, 2), (128, 2)])
+def test_launch_shape_does_not_change_results(tile_width, fuse):
+    insts = ic.orszag_tang_batch(count=5, seed=9, sizes=(16, 40, 72))
+    outs = []
+    for shape in [(128, 1, 304), (tile_width, fuse, 152)]:
+        b = Batch2D(insts, mhd=True, recon=2, arith="exact")
+        b.configure(*shape)
+        for k, inst in enumerate(insts):
+            b.upload(k, inst["prim"], inst["cons"], inst["fbx"], inst["fby"])
+        b.advance(0.0, 1e30, 0, 4, 0.4)
+        outs.append([b.download(k) for k in range(len(insts))])
+        b.close()
+    for a, w in zip(outs[0], outs[1]):
+        for x, y in zip(a, w):
+            assert np.array_equal(x, y)
+
+
+def test_autotuner_picks_a_shape_and_restores_the_state(tmp_path, monkeypatch):
+    from pythonmhd_gb300 import autotune
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "tune.json"))
+    insts = ic.orszag_tang_batch(count=6, seed=2, sizes=(32, 64, 96))
+    b = Batch2D(insts, mhd=True, recon=1, arith="exact")
+    rec = autotune.tune_batch(b, insts, recon=1, cycles=1)
+    assert rec["tile_width"] in (64, 128) and rec["fuse"] in (1, 2) and len(rec["trials"]) == 8
+    b.advance(0.0, 1e30, 0, 2, 0.4)
+    got = [b.download(k) for k in range(len(insts))]
+    b.close()
+    ref = Batch2D(insts, mhd=True, recon=1, arith="exact")
+    for k, inst in enumerate(insts):
+        ref.upload(k, inst["prim"], inst["cons"], inst["fbx"], inst["fby"])
+    ref.advance(0.0, 1e30, 0, 2, 0.4)
+    for k in range(len(insts)):
+        for x, y in zip(got[k], ref.download(k)):
+            assert np.array_equal(x, y)
+    ref.close()
+    again = Batch2D(insts, mhd=True, recon=1, arith="exact")
+    assert autotune.tune_batch(again, insts, recon=1)["cached"]
+    again.close()
