@@ -149,6 +149,44 @@ int mhdb_info(void* handle, long long* last_launches, size_t* device_bytes, int*
               void** stream);
 void mhdb_destroy(void* handle);
 
+/* ---------------------------------------------------------------------------
+ * Adjoint (reverse mode) of the MHD step, first-order (recon 0) and PLM
+ * (recon 1) reconstruction.  No counterpart in the reference.  States are
+ * "packed" device arrays of mhd2d_adj_info()'s state_words doubles:
+ *   prim (8, ny, nx) | cons (8, ny, nx) | faceBx (ny, nx+1) | faceBy (ny+1, nx);
+ * an adjoint ("bar") array has the same layout.  dt is frozen: the forward
+ * pass records the CFL dt of each cycle and the backward pass treats it as a
+ * constant.  The forward sweep equals the exact-arithmetic step bit for bit.
+ * Every call queues on the handle's own stream and waits for it before
+ * returning.
+ * ------------------------------------------------------------------------- */
+int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma, int recon,
+                     int entropy_fix, double eps, double min_d, double min_p, double min_e, void** handle);
+/* One cycle with the given dt: state_in -> state_out (device, packed). */
+int mhd2d_adj_cycle(void* handle, double dt, const double* state_in, double* state_out);
+/* Vector-Jacobian product of one cycle at state_in: bar_out -> bar_in. */
+int mhd2d_adj_cycle_reverse(void* handle, double dt, const double* state_in, const double* bar_out,
+                            double* bar_in);
+/* `steps` cycles from state_in to state_out with the CFL dt of each cycle (or
+ * the host array fixed_dt when it is not NULL), recorded into the host array
+ * dt_log (may be NULL).  Keeps a state checkpoint every `every` cycles
+ * (0 = ceil(sqrt(steps))) for mhd2d_adj_backward. */
+int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cfl, const double* fixed_dt,
+                      int every, double* state_out, double* dt_log);
+/* Adjoint of the last mhd2d_adj_forward: bar_final -> bar_initial.  Each
+ * checkpoint segment is recomputed once from its checkpoint; when the arrays of
+ * all its cycles fit the segment budget they stay resident for the reverse
+ * sweep, otherwise each cycle is recomputed again right before its reverse. */
+int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initial);
+/* Bytes the backward pass may hold to keep a whole segment resident
+ * (0 = 60% of the free device memory at mhd2d_adj_forward time). */
+int mhd2d_adj_configure(void* handle, size_t segment_bytes);
+/* state_words: length of a packed state; device_bytes: memory held now;
+ * segment_sets: cycles kept resident per segment by the last forward (1 =
+ * recompute mode). */
+int mhd2d_adj_info(void* handle, size_t* state_words, size_t* device_bytes, int* segment_sets);
+void mhd2d_adj_destroy(void* handle);
+
 const char* mhd2d_strerror(int status);
 void mhd2d_destroy(void* handle);
 

@@ -50,6 +50,20 @@ SIGNATURES = {
     "mhdb_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t),
                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]),
     "mhdb_destroy": (None, [ctypes.c_void_p]),
+    "mhd2d_adj_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "mhd2d_adj_cycle": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "mhd2d_adj_cycle_reverse": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]),
+    "mhd2d_adj_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                         c_double_p, ctypes.c_int, ctypes.c_void_p, c_double_p]),
+    "mhd2d_adj_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mhd2d_adj_configure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t]),
+    "mhd2d_adj_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
+                                      ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_int)]),
+    "mhd2d_adj_destroy": (None, [ctypes.c_void_p]),
     "mhd2d_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "mhd2d_destroy": (None, [ctypes.c_void_p]),
 }

@@ -1,0 +1,463 @@
+"""A small straight-line SSA language for the step's pointwise functions, with
+reverse-mode code generation.
+
+A pointwise function (one face's Roe flux, one cell's PLM edge states, ...) is
+written once as a Python function over ``Sym`` values.  Running it on symbolic
+inputs records a list of SSA statements.  Branches are written as ``select``
+on recorded conditions, so every statement executes and a branch decision is a
+plain boolean value, which the reverse code replays.
+
+From one trace the emitters produce:
+
+* ``emit_numpy``: a NumPy function (forward, or forward + reverse sweep) over
+  arrays -- elementwise, so the operation order and rounding of each statement
+  are those of the trace;
+* ``emit_cuda``: ``__device__`` functions ``<name>_fwd`` and ``<name>_rev`` for
+  one item, in the same statement order (built without FMA contraction they
+  round exactly like the NumPy version).
+
+The reverse sweep is the textbook adjoint of each statement, emitted in reverse
+order after a forward recomputation, with adjoints kept only for statements that
+both depend on an input and reach an output.
+"""
+from __future__ import annotations
+
+import math
+
+
+class Trace:
+    def __init__(self, name):
+        self.name = name
+        self.nodes = []          # (op, args, meta)
+        self.inputs = []         # node ids of differentiable inputs
+        self.params = []         # node ids of non-differentiable parameters
+        self.outputs = []        # node ids (or Python floats) of outputs
+        self.consts = {}
+
+    # -- node creation -----------------------------------------------------
+    def _add(self, op, args, meta=None, kind="f"):
+        self.nodes.append((op, tuple(args), meta, kind))
+        return len(self.nodes) - 1
+
+    def const(self, x):
+        x = float(x)
+        key = x.hex()
+        if key not in self.consts:
+            self.consts[key] = self._add("const", (), x)
+        return Sym(self, self.consts[key])
+
+    def input(self, n):
+        out = []
+        for _ in range(n):
+            i = self._add("input", (), len(self.inputs))
+            self.inputs.append(i)
+            out.append(Sym(self, i))
+        return out
+
+    def param(self, n):
+        out = []
+        for _ in range(n):
+            i = self._add("param", (), len(self.params))
+            self.params.append(i)
+            out.append(Sym(self, i))
+        return out
+
+    def set_outputs(self, outs):
+        self.outputs = [self._lift(o).id for o in outs]
+
+    def _lift(self, x):
+        if isinstance(x, Sym):
+            return x
+        return self.const(x)
+
+
+class Sym:
+    __slots__ = ("t", "id")
+
+    def __init__(self, t, i):
+        self.t = t
+        self.id = i
+
+    def _bin(self, op, o, rev=False):
+        o = self.t._lift(o)
+        a, b = (o, self) if rev else (self, o)
+        return Sym(self.t, self.t._add(op, (a.id, b.id)))
+
+    def __add__(self, o): return self._bin("add", o)
+    def __radd__(self, o): return self._bin("add", o, True)
+    def __sub__(self, o): return self._bin("sub", o)
+    def __rsub__(self, o): return self._bin("sub", o, True)
+    def __mul__(self, o): return self._bin("mul", o)
+    def __rmul__(self, o): return self._bin("mul", o, True)
+    def __truediv__(self, o): return self._bin("div", o)
+    def __rtruediv__(self, o): return self._bin("div", o, True)
+    def __neg__(self): return Sym(self.t, self.t._add("neg", (self.id,)))
+
+    def _cmp(self, op, o):
+        o = self.t._lift(o)
+        return Cond(self.t, self.t._add(op, (self.id, o.id), kind="b"))
+
+    def __gt__(self, o): return self._cmp("gt", o)
+    def __ge__(self, o): return self._cmp("ge", o)
+    def __lt__(self, o): return self._cmp("lt", o)
+    def __le__(self, o): return self._cmp("le", o)
+    def eq(self, o): return self._cmp("eq", o)
+
+
+class Cond:
+    __slots__ = ("t", "id")
+
+    def __init__(self, t, i):
+        self.t = t
+        self.id = i
+
+    def __and__(self, o): return Cond(self.t, self.t._add("and", (self.id, o.id), kind="b"))
+    def __or__(self, o): return Cond(self.t, self.t._add("or", (self.id, o.id), kind="b"))
+    def __invert__(self): return Cond(self.t, self.t._add("not", (self.id,), kind="b"))
+
+
+def sqrt(x): return Sym(x.t, x.t._add("sqrt", (x.id,)))
+def fabs(x): return Sym(x.t, x.t._add("abs", (x.id,)))
+
+
+def select(c, a, b):
+    """c ? a : b (both sides are evaluated; the reverse sweep follows c)."""
+    t = c.t
+    a = t._lift(a)
+    b = t._lift(b)
+    return Sym(t, t._add("sel", (c.id, a.id, b.id)))
+
+
+def dmax(a, b):
+    """numpy.maximum on non-NaN data: a > b ? a : b."""
+    t = a.t if isinstance(a, Sym) else b.t
+    a, b = t._lift(a), t._lift(b)
+    return select(a > b, a, b)
+
+
+def dmin(a, b):
+    t = a.t if isinstance(a, Sym) else b.t
+    a, b = t._lift(a), t._lift(b)
+    return select(a < b, a, b)
+
+
+def trace(name, fn, n_in, n_par, **kw):
+    """Record fn(inputs, params, **kw) -> outputs into a Trace."""
+    t = Trace(name)
+    ins = t.input(n_in)
+    pars = t.param(n_par)
+    outs = fn(ins, pars, **kw)
+    t.set_outputs(list(outs))
+    return t
+
+
+# ----------------------------------------------------------------------------
+# analysis
+# ----------------------------------------------------------------------------
+def _active(t):
+    n = len(t.nodes)
+    dep = [False] * n        # depends on a differentiable input
+    for i, (op, args, meta, kind) in enumerate(t.nodes):
+        if op == "input":
+            dep[i] = True
+        elif kind == "f" and op not in ("const", "param"):
+            if op == "sel":
+                dep[i] = dep[args[1]] or dep[args[2]]
+            else:
+                dep[i] = any(dep[a] for a in args)
+    reach = [False] * n      # reaches an output
+    for o in t.outputs:
+        reach[o] = True
+    for i in range(n - 1, -1, -1):
+        if not reach[i]:
+            continue
+        op, args, meta, kind = t.nodes[i]
+        if kind != "f":
+            continue
+        if op == "sel":
+            reach[args[1]] = True
+            reach[args[2]] = True
+        else:
+            for a in args:
+                if t.nodes[a][3] == "f":
+                    reach[a] = True
+    return [dep[i] and reach[i] for i in range(n)]
+
+
+def _live_forward(t, need):
+    """Nodes whose forward value is needed (for outputs and for the reverse sweep)."""
+    n = len(t.nodes)
+    live = [False] * n
+    for i in need:
+        live[i] = True
+    for i in range(n - 1, -1, -1):
+        if live[i]:
+            for a in t.nodes[i][1]:
+                live[a] = True
+    return live
+
+
+def _reverse_needs(t, act):
+    """Forward values the reverse sweep reads."""
+    need = set()
+    for i, (op, args, meta, kind) in enumerate(t.nodes):
+        if not act[i] or kind != "f":
+            continue
+        if op == "mul":
+            need.update(args)
+        elif op == "div":
+            need.update(args)
+            need.add(i)
+        elif op == "sqrt":
+            need.add(i)
+        elif op == "abs":
+            need.add(args[0])
+        elif op == "sel":
+            need.add(args[0])
+    return need
+
+
+# ----------------------------------------------------------------------------
+# emitters
+# ----------------------------------------------------------------------------
+_PY_BIN = {"add": "+", "sub": "-", "mul": "*", "div": "/"}
+_C_RN = {"add": "__dadd_rn", "sub": "__dsub_rn", "mul": "__dmul_rn", "div": "__ddiv_rn"}
+_CMP = {"gt": ">", "ge": ">=", "lt": "<", "le": "<=", "eq": "=="}
+
+
+def _fwd_lines(t, live, lang):
+    L = []
+    for i, (op, args, meta, kind) in enumerate(t.nodes):
+        if not live[i]:
+            continue
+        v = f"v{i}"
+        a = [f"v{x}" for x in args]
+        if op == "const":
+            lit = repr(meta) if lang == "py" else _c_lit(meta)
+            L.append((v, lit, kind))
+        elif op == "input":
+            L.append((v, f"x[{meta}]", kind))
+        elif op == "param":
+            L.append((v, f"p[{meta}]", kind))
+        elif op in _PY_BIN:
+            if lang == "py":
+                L.append((v, f"{a[0]} {_PY_BIN[op]} {a[1]}", kind))
+            else:
+                # round-to-nearest intrinsics are never contracted into an FMA, so
+                # the forward values round exactly like NumPy's even in a unit
+                # compiled with contraction on (the reverse statements use it)
+                L.append((v, f"{_C_RN[op]}({a[0]}, {a[1]})", kind))
+        elif op == "neg":
+            L.append((v, f"-{a[0]}", kind))
+        elif op == "sqrt":
+            L.append((v, f"np.sqrt({a[0]})" if lang == "py" else f"__dsqrt_rn({a[0]})", kind))
+        elif op == "abs":
+            L.append((v, f"np.abs({a[0]})" if lang == "py" else f"fabs({a[0]})", kind))
+        elif op in _CMP:
+            L.append((v, f"{a[0]} {_CMP[op]} {a[1]}", kind))
+        elif op == "and":
+            L.append((v, f"{a[0]} & {a[1]}" if lang == "py" else f"{a[0]} && {a[1]}", kind))
+        elif op == "or":
+            L.append((v, f"{a[0]} | {a[1]}" if lang == "py" else f"{a[0]} || {a[1]}", kind))
+        elif op == "not":
+            L.append((v, f"~{a[0]}" if lang == "py" else f"!{a[0]}", kind))
+        elif op == "sel":
+            L.append((v, f"np.where({a[0]}, {a[1]}, {a[2]})" if lang == "py" else f"{a[0]} ? {a[1]} : {a[2]}", kind))
+        else:
+            raise ValueError(op)
+    return L
+
+
+def _c_lit(x):
+    if math.isinf(x) or math.isnan(x):
+        raise ValueError("non-finite constant")
+    r = repr(float(x))
+    if "e" not in r and "." not in r and "inf" not in r:
+        r += ".0"
+    return r
+
+
+def _rev_lines_c(t, act):
+    """CUDA adjoint statements in reverse order.  b{i} is the adjoint of node i.
+
+    Only a contribution that multiplies the incoming adjoint by a forward value
+    is guarded by ``nz(b)``: a branch not taken may hold a non-finite value
+    (e.g. w/bt with bt == 0) and 0 * inf must not reach the result.  Sums,
+    differences and selects pass the adjoint through unguarded.  A quotient's
+    two contributions share one division.  These statements may contract into
+    FMAs: the adjoint is not required to round like the NumPy reverse sweep.
+    """
+    L = []
+    for i in range(len(t.nodes) - 1, -1, -1):
+        op, args, meta, kind = t.nodes[i]
+        if not act[i] or kind != "f" or op == "input":
+            continue
+        b = f"b{i}"
+        ac = [act[j] for j in args]
+        if op == "add":
+            for j, on in zip(args, ac):
+                if on:
+                    L.append(f"b{j} += {b}")
+        elif op == "sub":
+            if ac[0]:
+                L.append(f"b{args[0]} += {b}")
+            if ac[1]:
+                L.append(f"b{args[1]} -= {b}")
+        elif op == "neg":
+            L.append(f"b{args[0]} -= {b}")
+        elif op == "mul":
+            parts = []
+            if ac[0]:
+                parts.append(f"b{args[0]} += {b} * v{args[1]};")
+            if ac[1]:
+                parts.append(f"b{args[1]} += {b} * v{args[0]};")
+            if parts:
+                L.append(f"if (nz({b})) {{ " + " ".join(parts) + " }")
+        elif op == "div":
+            parts = [f"const double q_ = {b} / v{args[1]};"]
+            if ac[0]:
+                parts.append(f"b{args[0]} += q_;")
+            if ac[1]:
+                parts.append(f"b{args[1]} -= q_ * v{i};")
+            L.append(f"if (nz({b})) {{ " + " ".join(parts) + " }")
+        elif op == "sqrt":
+            L.append(f"if (nz({b}) && v{i} > 0.0) b{args[0]} += (0.5 * {b}) / v{i}")
+        elif op == "abs":
+            L.append(f"b{args[0]} += (v{args[0]} >= 0.0 ? {b} : -{b})")
+        elif op == "sel":
+            if act[args[1]]:
+                L.append(f"b{args[1]} += (v{args[0]} ? {b} : 0.0)")
+            if act[args[2]]:
+                L.append(f"b{args[2]} += (v{args[0]} ? 0.0 : {b})")
+        else:
+            raise ValueError(op)
+    return L
+
+
+def _rev_lines(t, act, lang):
+    """Adjoint statements in reverse order.  b{i} is the adjoint of node i."""
+    L = []
+    where = (lambda c, x: f"np.where({c}, {x}, 0.0)") if lang == "py" else (lambda c, x: f"({c} ? {x} : 0.0)")
+    for i in range(len(t.nodes) - 1, -1, -1):
+        op, args, meta, kind = t.nodes[i]
+        if not act[i] or kind != "f" or op == "input":
+            continue
+        b = f"b{i}"
+
+        # contributions are skipped when the incoming adjoint is exactly zero, so a
+        # non-finite value on a branch not taken (e.g. w/bt with bt == 0) never
+        # turns into 0 * inf
+        def acc(j, expr):
+            if act[j]:
+                if lang == "py":
+                    L.append(f"b{j} = b{j} + np.where({b} != 0.0, {expr}, 0.0)")
+                else:
+                    L.append(f"if (nz({b})) b{j} = b{j} + ({expr})")
+
+        if op == "add":
+            acc(args[0], b)
+            acc(args[1], b)
+        elif op == "sub":
+            acc(args[0], b)
+            acc(args[1], f"-{b}")
+        elif op == "mul":
+            acc(args[0], f"{b} * v{args[1]}")
+            acc(args[1], f"{b} * v{args[0]}")
+        elif op == "div":
+            acc(args[0], f"{b} / v{args[1]}")
+            acc(args[1], f"-({b} * v{i}) / v{args[1]}")
+        elif op == "neg":
+            acc(args[0], f"-{b}")
+        elif op == "sqrt":
+            acc(args[0], where(f"v{i} > 0.0", f"({b} * 0.5) / v{i}"))
+        elif op == "abs":
+            acc(args[0], f"np.where(v{args[0]} >= 0.0, {b}, -{b})" if lang == "py"
+                else f"(v{args[0]} >= 0.0 ? {b} : -{b})")
+        elif op == "sel":
+            acc(args[1], where(f"v{args[0]}", b))
+            nc = f"~v{args[0]}" if lang == "py" else f"!v{args[0]}"
+            acc(args[2], where(nc, b))
+        else:
+            raise ValueError(op)
+    return L
+
+
+def emit_numpy(t, reverse=False):
+    """Python source of ``fwd(x, p) -> outs`` (and ``rev(x, p, ybar) -> xbar``) over NumPy arrays."""
+    act = _active(t)
+    need_out = set(t.outputs)
+    src = [f"def {t.name}_fwd(x, p):", "    with np.errstate(all='ignore'):"]
+    live = _live_forward(t, need_out)
+    for v, e, kind in _fwd_lines(t, live, "py"):
+        src.append(f"        {v} = {e}")
+    src.append("    return [" + ", ".join(f"v{o}" for o in t.outputs) + "]")
+    if reverse:
+        need = need_out | _reverse_needs(t, act)
+        live = _live_forward(t, need)
+        src.append("")
+        src.append(f"def {t.name}_rev(x, p, ybar):")
+        src.append("    with np.errstate(all='ignore'):")
+        for v, e, kind in _fwd_lines(t, live, "py"):
+            src.append(f"        {v} = {e}")
+        for i in range(len(t.nodes)):
+            if act[i] and t.nodes[i][3] == "f":
+                src.append(f"        b{i} = 0.0")
+        for k, o in enumerate(t.outputs):
+            if act[o]:
+                src.append(f"        b{o} = b{o} + ybar[{k}]")
+        for line in _rev_lines(t, act, "py"):
+            src.append("        " + line)
+        xb = []
+        for i in t.inputs:
+            xb.append(f"b{i}" if act[i] else "0.0")
+        src.append("    return [" + ", ".join(xb) + "]")
+    return "\n".join(src) + "\n"
+
+
+def emit_cuda(t, reverse=True):
+    """CUDA source of ``<name>_fwd(x, p, y)`` and ``<name>_rev(x, p, ybar, xbar)`` for one item."""
+    act = _active(t)
+    need_out = set(t.outputs)
+    out = []
+    live = _live_forward(t, need_out)
+    out.append("#ifndef MHD_DSL_NZ\n#define MHD_DSL_NZ\n"
+               "__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }\n"
+               "#endif")
+    out.append(f"__device__ __forceinline__ void {t.name}_fwd(const double* __restrict__ x, "
+               f"const double* __restrict__ p, double* __restrict__ y) {{")
+    for v, e, kind in _fwd_lines(t, live, "c"):
+        ty = "double" if kind == "f" else "bool"
+        out.append(f"  const {ty} {v} = {e};")
+    for k, o in enumerate(t.outputs):
+        out.append(f"  y[{k}] = v{o};")
+    out.append("}")
+    if reverse:
+        need = need_out | _reverse_needs(t, act)
+        live = _live_forward(t, need)
+        out.append(f"__device__ __forceinline__ void {t.name}_rev(const double* __restrict__ x, "
+                   f"const double* __restrict__ p, const double* __restrict__ ybar, double* __restrict__ xbar) {{")
+        for v, e, kind in _fwd_lines(t, live, "c"):
+            ty = "double" if kind == "f" else "bool"
+            out.append(f"  const {ty} {v} = {e};")
+        for i in range(len(t.nodes)):
+            if act[i] and t.nodes[i][3] == "f":
+                out.append(f"  double b{i} = 0.0;")
+        for k, o in enumerate(t.outputs):
+            if act[o]:
+                out.append(f"  b{o} = b{o} + ybar[{k}];")
+        for line in _rev_lines_c(t, act):
+            out.append("  " + line + ("" if line.endswith("}") else ";"))
+        for k, i in enumerate(t.inputs):
+            out.append(f"  xbar[{k}] = {'b%d' % i if act[i] else '0.0'};")
+        out.append("}")
+    return "\n".join(out) + "\n"
+
+
+def compile_numpy(t, reverse=False):
+    """Executable (fwd[, rev]) NumPy functions of a trace."""
+    import numpy as np
+    ns = {"np": np}
+    exec(compile(emit_numpy(t, reverse), f"<dsl:{t.name}>", "exec"), ns)
+    if reverse:
+        return ns[f"{t.name}_fwd"], ns[f"{t.name}_rev"]
+    return ns[f"{t.name}_fwd"]

@@ -1,0 +1,75 @@
+"""Differentiable map from initial fields (rho, vx, vy, p, A_z) to the packed MHD state.
+
+The gradient problem on the step is posed on the fields a user sets up a run
+from -- density, in-plane velocity, pressure and the corner vector potential --
+rather than on the redundant (prim, cons, face B) triple the step consumes.  The
+map is the one the turbulence generator uses (periodic box):
+
+    faceBx = (A_z[j+1, i] - A_z[j, i]) / dy,   faceBy = -(A_z[j, i+1] - A_z[j, i]) / dx
+    Bx, By = face averages,  v_z = B_z = 0,  cons from prim
+
+written in torch so that autograd carries the gradient from the packed state
+back to the fields (a few elementwise ops; the step's own reverse sweep is the
+hand-written one).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .. import initial_conditions as ic
+
+
+def turbulence_fields(n, seed=1, gamma=5.0 / 3.0, kmax_v=16, kmax_a=16, mach=1.0, beta=1.0):
+    """Seeded turbulence fields on an n x n periodic box (the turbulence generator's
+    spectra and normalisation), with A_z scaled to plasma beta ``beta``.
+
+    Returns dict(rho, vx, vy, p, az, dx, dy, gamma) of NumPy arrays.
+    """
+    rng = np.random.default_rng(seed)
+    g = ic._gaussian_field(rng, n, 2.0, 1.0, kmax_v)
+    g /= g.std()
+    vx = ic._gaussian_field(rng, n, 2.0, 1.0, kmax_v)
+    vy = ic._gaussian_field(rng, n, 2.0, 1.0, kmax_v)
+    az = ic._gaussian_field(rng, n, 3.0, 1.0, kmax_a)
+    dx = dy = 1.0 / n
+    rho = np.exp(0.1 * g)
+    p = np.full((n, n), 1.0 / gamma)
+    vscale = mach / np.sqrt(np.mean((vx * vx + vy * vy) / (gamma * p / rho)))
+    vx *= vscale
+    vy *= vscale
+    fbx_u, fby_u = ic.faces_from_potential(az)
+    cbx = (fbx_u[:, :-1] + fbx_u[:, 1:]) / (2.0 * dy)
+    cby = (fby_u[:-1, :] + fby_u[1:, :]) / (2.0 * dx)
+    az = az * np.sqrt(2.0 * (1.0 / gamma) / beta / np.mean(cbx * cbx + cby * cby))
+    return dict(rho=rho, vx=vx, vy=vy, p=p, az=az, dx=dx, dy=dy, gamma=gamma)
+
+
+def perturbed(fields, frac, seed):
+    """The fields with rho, vx, vy, p and A_z each multiplied by (1 + frac N(0,1)) (seeded)."""
+    rng = np.random.default_rng(seed)
+    out = dict(fields)
+    for k in ("rho", "vx", "vy", "p", "az"):
+        out[k] = fields[k] * (1.0 + frac * rng.standard_normal(fields[k].shape))
+    return out
+
+
+def state_from_fields(rho, vx, vy, p, az, gamma, dx, dy):
+    """Packed state ``prim (8) | cons (8) | faceBx | faceBy`` (flattened) from torch fields."""
+    fbx_c = (torch.roll(az, -1, dims=0) - az) / dy           # (ny, nx): face i of row j
+    fby_c = -(torch.roll(az, -1, dims=1) - az) / dx          # (ny, nx): face j of column i
+    fbx = torch.cat([fbx_c, fbx_c[:, :1]], dim=1)
+    fby = torch.cat([fby_c, fby_c[:1, :]], dim=0)
+    bx = (fbx[:, :-1] + fbx[:, 1:]) / 2.0
+    by = (fby[:-1, :] + fby[1:, :]) / 2.0
+    zero = torch.zeros_like(rho)
+    prim = torch.stack([rho, vx, vy, zero, bx, by, zero, p])
+    ke = 0.5 * rho * (vx * vx + vy * vy + zero * zero)
+    etot = p / (gamma - 1.0) + ke + 0.5 * (bx * bx + by * by + zero * zero)
+    cons = torch.stack([rho, rho * vx, rho * vy, rho * zero, bx, by, zero, etot])
+    return torch.cat([prim.reshape(-1), cons.reshape(-1), fbx.reshape(-1), fby.reshape(-1)])
+
+
+def fields_to_torch(fields, device, requires_grad=False):
+    return [torch.tensor(fields[k], dtype=torch.float64, device=device, requires_grad=requires_grad)
+            for k in ("rho", "vx", "vy", "p", "az")]

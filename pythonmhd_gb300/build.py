@@ -1,12 +1,15 @@
 """Build the in-tree CUDA library ``pythonmhd_gb300/libpythonmhd_gb300.so`` for sm_103a.
 
-Three translation units are compiled in parallel with nvcc and linked into one
+The translation units are compiled in parallel with nvcc and linked into one
 shared library with a plain C ABI (``include/pythonmhd_gb300.h``):
 
 * ``csrc/kernels_exact.cu``  -- the step kernels with ``-fmad=false``
 * ``csrc/kernels_fast.cu``   -- the same kernels with FMA contraction
 * ``csrc/capi.cu``           -- handles, copies and the CUDA-graph evolve loop
 * ``csrc/noalloc.cu``        -- the CFL timestep for callers that cannot allocate
+* ``csrc/adjoint.cu``        -- the reverse-mode adjoint of the MHD step; its pointwise
+  stage functions (``csrc/adjoint_gen.cuh``) are generated from ``adjoint/stages.py``
+  first
 """
 from __future__ import annotations
 
@@ -28,7 +31,10 @@ UNITS = [
     ("kernels_fast.cu", ["-fmad=true"]),
     ("capi.cu", []),
     ("noalloc.cu", ["-fmad=false"]),
+    ("adjoint.cu", []),
 ]
+ADJ_GEN = os.path.join(CSRC, "adjoint_gen.cuh")
+ADJ_PY = os.path.join(PKG, "adjoint")
 
 
 def nvcc_path() -> str:
@@ -40,13 +46,20 @@ def nvcc_path() -> str:
 
 def _sources():
     srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f != "fp64_probe.cu"]
+    srcs += [os.path.join(ADJ_PY, f) for f in os.listdir(ADJ_PY) if f.endswith(".py")]
     srcs.append(os.path.join(ROOT, "include", "pythonmhd_gb300.h"))
     srcs.append(os.path.abspath(__file__))
     return srcs
 
 
+def generate_adjoint() -> str:
+    """Write ``csrc/adjoint_gen.cuh`` from the adjoint stage definitions (only if it changed)."""
+    from .adjoint import codegen
+    return codegen.write(ADJ_GEN)
+
+
 def is_stale() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(ADJ_GEN):
         return True
     t = os.path.getmtime(LIB)
     return any(os.path.getmtime(s) > t for s in _sources())
@@ -56,6 +69,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     """Compile and link the library if it is missing or older than its sources."""
     if not force and not is_stale():
         return LIB
+    generate_adjoint()
     nvcc = nvcc_path()
     os.makedirs(BUILD, exist_ok=True)
     common = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -1,0 +1,859 @@
+// Reverse-mode adjoint of the MHD CTU+CT step (first-order and PLM reconstruction).
+//
+// The pointwise stage functions come from adjoint_gen.cuh (generated from
+// pythonmhd_gb300/adjoint/stages.py: <stage>_fwd / <stage>_rev).  This file holds
+// the stencil around them -- which cell, face or corner feeds each input -- in a
+// forward sweep that stores every intermediate array of a cycle and a reverse
+// sweep that runs the stages backwards, scattering input adjoints with atomicAdd.
+// The gathers mirror the forward kernels in godunov2d_kernels.cuh.
+//
+// dt is frozen: the forward pass records the CFL dt of every cycle and the
+// reverse sweep treats it as a constant.  Long runs keep a state checkpoint every
+// K cycles (K ~ sqrt(steps)) and recompute the states inside a segment during the
+// backward pass.  The forward statements use non-contracting round-to-nearest
+// intrinsics, so the forward sweep reproduces the exact-arithmetic step bit for
+// bit although the unit is compiled with FMA contraction for the reverse sweeps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "../../include/pythonmhd_gb300.h"
+#include "adjoint_gen.cuh"
+
+namespace {
+
+constexpr int kT = 128;
+
+struct Arr {
+  double* v = nullptr;   // values
+  double* b = nullptr;   // adjoints
+  size_t ps = 0;         // plane stride
+  __device__ __forceinline__ double* pv(int slot, size_t i) const { return v + (size_t)slot * ps + i; }
+  __device__ __forceinline__ double* pb(int slot, size_t i) const { return b + (size_t)slot * ps + i; }
+};
+
+struct Adj {
+  int nx, ny, bcx, bcy, recon, efix;
+  double dx, dy, gamma, eps, min_d, min_p, min_e;
+  double dt;                       // dt of the cycle being processed
+  Arr P, C, FX, FY;                // input state
+  Arr EX, EY;                      // edge states per cell (lia 7 + ria 7), x and y sweeps
+  Arr XL, XR, YL, YR;              // reconstructed face states
+  Arr F1X, F1Y, EZ, E1, NBX, NBY;  // stage-1 fluxes, cell Ez, corner EMF, half-step faces
+  Arr UXL, UXR, UYL, UYR, WXL, WXR, WYL, WYR;  // CTU-corrected face cons / prim
+  Arr HEZ, F2X, F2Y, E2;           // half-step Ez, stage-2 fluxes and EMF
+  Arr NP, NC, NFX, NFY;            // output state
+  double* red;                     // 2 doubles: CFL maxima (bits)
+};
+
+__device__ __forceinline__ int wrapc(int c, int L, int bc) {
+  if (bc == 1) {
+    int m = c % L;
+    return m < 0 ? m + L : m;
+  }
+  return c < 0 ? 0 : (c >= L ? L - 1 : c);
+}
+
+struct IO {
+  double* v;
+  double* b;
+};
+
+__device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a.pv(slot, i), a.pb(slot, i)}; }
+
+// forward: gather inputs, call fwd, write outputs; reverse: gather inputs, read output
+// adjoints, call rev, scatter input adjoints.
+#define MHD_ADJ_APPLY(NAME, REV, INS, OUTS, PAR)                                  \
+  do {                                                                            \
+    double x_[g_##NAME##_NI];                                                     \
+    _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_) x_[k_] = *INS[k_].v; \
+    if (!(REV)) {                                                                 \
+      double y_[g_##NAME##_NO];                                                   \
+      g_##NAME##_fwd(x_, PAR, y_);                                                \
+      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) *OUTS[k_].v = y_[k_]; \
+    } else {                                                                      \
+      double yb_[g_##NAME##_NO], xb_[g_##NAME##_NI];                              \
+      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) yb_[k_] = *OUTS[k_].b; \
+      g_##NAME##_rev(x_, PAR, yb_, xb_);                                          \
+      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_)               \
+        if (xb_[k_] != 0.0) atomicAdd(INS[k_].b, xb_[k_]);                        \
+    }                                                                             \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// stage kernels (REV = false: forward with stored intermediates; true: reverse)
+// ---------------------------------------------------------------------------
+template <int AX, bool REV>
+__global__ void __launch_bounds__(kT) k_recon(Adj A) {
+  const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
+  if (c0 >= A.nx || t0 >= A.ny) return;
+  const size_t me = (size_t)t0 * A.nx + c0;
+  const Arr& E = AX == 0 ? A.EX : A.EY;
+  const int slots[7] = {0, 1, 2, 3, AX == 0 ? 5 : 6, AX == 0 ? 6 : 4, 7};
+  if (A.recon == 1) {
+    const int bc = AX == 0 ? A.bcx : A.bcy;
+    IO in[22];
+    IO out[14];
+#pragma unroll
+    for (int o = -1; o <= 1; ++o) {
+      const int jj = AX == 0 ? t0 : wrapc(t0 + o, A.ny, bc);
+      const int ii = AX == 0 ? wrapc(c0 + o, A.nx, bc) : c0;
+      const size_t ci = (size_t)jj * A.nx + ii;
+#pragma unroll
+      for (int k = 0; k < 7; ++k) in[(o + 1) * 7 + k] = io(A.P, slots[k], ci);
+    }
+    in[21] = io(A.P, AX == 0 ? 4 : 5, me);
+#pragma unroll
+    for (int k = 0; k < 14; ++k) out[k] = io(E, k, me);
+    const double par[2] = {A.gamma, A.dt / (AX == 0 ? A.dx : A.dy)};
+    if (AX == 0) MHD_ADJ_APPLY(plm0, REV, in, out, par);
+    else MHD_ADJ_APPLY(plm1, REV, in, out, par);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      if (!REV) {
+        *E.pv(k, me) = *A.P.pv(slots[k], me);
+        *E.pv(7 + k, me) = *A.P.pv(slots[k], me);
+      } else {
+        const double g = *E.pb(k, me) + *E.pb(7 + k, me);
+        if (g != 0.0) atomicAdd(A.P.pb(slots[k], me), g);
+      }
+    }
+  }
+}
+
+// face states of one sweep: item = (face, side)
+template <int AX, bool REV>
+__global__ void __launch_bounds__(kT) k_face(Adj A) {
+  const int L = AX == 0 ? A.nx : A.ny;
+  const int Wd = AX == 0 ? A.nx + 1 : A.nx;   // row width of the face array
+  const int H = AX == 0 ? A.ny : A.ny + 1;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y, side = blockIdx.z;
+  if (col >= Wd || row >= H) return;
+  const int f = AX == 0 ? col : row;   // face index along the sweep
+  const int t = AX == 0 ? row : col;   // transverse index
+  const int bc = AX == 0 ? A.bcx : A.bcy;
+  int cell, sd, vc, f1, f2;
+  if (side == 0) {
+    if (bc == 0) {
+      cell = f == 0 ? 0 : f - 1; sd = f == 0 ? 0 : 7;
+      vc = f == 0 ? 0 : f - 1; f1 = f == 0 ? 0 : f - 1; f2 = f == 0 ? 0 : f;
+    } else {
+      cell = f == 0 ? L - 1 : f - 1; sd = 7;
+      vc = cell; f1 = f == 0 ? L - 1 : f - 1; f2 = f;
+    }
+  } else {
+    if (bc == 0) {
+      cell = f == L ? L - 1 : f; sd = f == L ? 7 : 0;
+      vc = cell; f1 = f == L ? L : f; f2 = f == L ? L : f + 1;
+    } else {
+      cell = f == L ? 0 : f; sd = 0;
+      vc = cell; f1 = f == L ? L : f; f2 = f == L ? 1 : f + 1;
+    }
+  }
+  const Arr& E = AX == 0 ? A.EX : A.EY;
+  const Arr& FB = AX == 0 ? A.FX : A.FY;
+  const Arr& OUT = AX == 0 ? (side == 0 ? A.XL : A.XR) : (side == 0 ? A.YL : A.YR);
+  const size_t ci = AX == 0 ? (size_t)t * A.nx + cell : (size_t)cell * A.nx + t;
+  const size_t vi = AX == 0 ? (size_t)t * A.nx + vc : (size_t)vc * A.nx + t;
+  const size_t fi1 = AX == 0 ? (size_t)t * (A.nx + 1) + f1 : (size_t)f1 * A.nx + t;
+  const size_t fi2 = AX == 0 ? (size_t)t * (A.nx + 1) + f2 : (size_t)f2 * A.nx + t;
+  const size_t me = (size_t)row * Wd + col;
+  IO in[10];
+  IO out[7];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) in[k] = io(E, sd + k, ci);
+  in[7] = io(A.P, AX == 0 ? 2 : 1, vi);
+  in[8] = io(FB, 0, fi1);
+  in[9] = io(FB, 0, fi2);
+#pragma unroll
+  for (int k = 0; k < 7; ++k) out[k] = io(OUT, k, me);
+  const double par[4] = {A.min_d, A.min_p, 0.5 * A.dt, 1.0 / (AX == 0 ? A.dx : A.dy)};
+  if (AX == 0) MHD_ADJ_APPLY(face0, REV, in, out, par);
+  else MHD_ADJ_APPLY(face1, REV, in, out, par);
+}
+
+template <int AX, int STAGE, bool REV>
+__global__ void __launch_bounds__(kT) k_roe(Adj A) {
+  const size_t nf = AX == 0 ? (size_t)(A.nx + 1) * A.ny : (size_t)A.nx * (A.ny + 1);
+  const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const Arr& WL = STAGE == 1 ? (AX == 0 ? A.XL : A.YL) : (AX == 0 ? A.WXL : A.WYL);
+  const Arr& WR = STAGE == 1 ? (AX == 0 ? A.XR : A.YR) : (AX == 0 ? A.WXR : A.WYR);
+  const Arr& BN = STAGE == 1 ? (AX == 0 ? A.FX : A.FY) : (AX == 0 ? A.NBX : A.NBY);
+  const Arr& F = STAGE == 1 ? (AX == 0 ? A.F1X : A.F1Y) : (AX == 0 ? A.F2X : A.F2Y);
+  const double par[2] = {A.gamma, A.eps};
+  IO out[7];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) out[k] = io(F, k, f);
+  if (STAGE == 1) {
+    IO in[15];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) { in[k] = io(WL, k, f); in[7 + k] = io(WR, k, f); }
+    in[14] = io(BN, 0, f);
+    if (A.efix) {
+      if (AX == 0) MHD_ADJ_APPLY(roe1_0_efix, REV, in, out, par);
+      else MHD_ADJ_APPLY(roe1_1_efix, REV, in, out, par);
+    } else {
+      if (AX == 0) MHD_ADJ_APPLY(roe1_0, REV, in, out, par);
+      else MHD_ADJ_APPLY(roe1_1, REV, in, out, par);
+    }
+  } else {
+    const Arr& UL = AX == 0 ? A.UXL : A.UYL;
+    const Arr& UR = AX == 0 ? A.UXR : A.UYR;
+    IO in[29];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      in[k] = io(WL, k, f); in[7 + k] = io(WR, k, f);
+      in[14 + k] = io(UL, k, f); in[21 + k] = io(UR, k, f);
+    }
+    in[28] = io(BN, 0, f);
+    if (A.efix) {
+      if (AX == 0) MHD_ADJ_APPLY(roe2_0_efix, REV, in, out, par);
+      else MHD_ADJ_APPLY(roe2_1_efix, REV, in, out, par);
+    } else {
+      if (AX == 0) MHD_ADJ_APPLY(roe2_0, REV, in, out, par);
+      else MHD_ADJ_APPLY(roe2_1, REV, in, out, par);
+    }
+  }
+}
+
+template <bool REV>
+__global__ void __launch_bounds__(kT) k_ez(Adj A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= A.nx || j >= A.ny) return;
+  const size_t me = (size_t)j * A.nx + i;
+  IO in[4] = {io(A.P, 2, me), io(A.P, 4, me), io(A.P, 1, me), io(A.P, 5, me)};
+  IO out[1] = {io(A.EZ, 0, me)};
+  const double* par = nullptr;
+  MHD_ADJ_APPLY(ez, REV, in, out, par);
+}
+
+template <int STAGE, bool REV>
+__global__ void __launch_bounds__(kT) k_emf(Adj A) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y;
+  const int nx = A.nx, ny = A.ny;
+  if (I > nx || J > ny) return;
+  const Arr& FXa = STAGE == 1 ? A.F1X : A.F2X;
+  const Arr& FYa = STAGE == 1 ? A.F1Y : A.F2Y;
+  const Arr& EZa = STAGE == 1 ? A.EZ : A.HEZ;
+  const Arr& OUT = STAGE == 1 ? A.E1 : A.E2;
+  const int ic = wrapc(I, nx, A.bcx), im = wrapc(I - 1, nx, A.bcx);
+  const int jc = wrapc(J, ny, A.bcy), jm = wrapc(J - 1, ny, A.bcy);
+  IO in[12] = {io(FYa, 0, (size_t)J * nx + im), io(FYa, 5, (size_t)J * nx + im),
+               io(FYa, 0, (size_t)J * nx + ic), io(FYa, 5, (size_t)J * nx + ic),
+               io(FXa, 0, (size_t)jc * (nx + 1) + I), io(FXa, 4, (size_t)jc * (nx + 1) + I),
+               io(FXa, 0, (size_t)jm * (nx + 1) + I), io(FXa, 4, (size_t)jm * (nx + 1) + I),
+               io(EZa, 0, (size_t)jc * nx + ic), io(EZa, 0, (size_t)jc * nx + im),
+               io(EZa, 0, (size_t)jm * nx + ic), io(EZa, 0, (size_t)jm * nx + im)};
+  IO out[1] = {io(OUT, 0, (size_t)J * (nx + 1) + I)};
+  const double* par = nullptr;
+  MHD_ADJ_APPLY(emf, REV, in, out, par);
+}
+
+// half-step (FULL=false, from E1 into NBX/NBY) or full-step (FULL=true, from E2 into NFX/NFY) faces
+template <int AX, bool FULL, bool REV>
+__global__ void __launch_bounds__(kT) k_fhalf(Adj A) {
+  const int nx = A.nx, ny = A.ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  const int w = AX == 0 ? nx + 1 : nx, h = AX == 0 ? ny : ny + 1;
+  if (i >= w || j >= h) return;
+  const Arr& E = FULL ? A.E2 : A.E1;
+  const size_t me = (size_t)j * w + i;
+  const size_t cw = nx + 1;
+  if (AX == 0) {
+    IO in[3] = {io(A.FX, 0, me), io(E, 0, (size_t)(j + 1) * cw + i), io(E, 0, (size_t)j * cw + i)};
+    IO out[1] = {io(FULL ? A.NFX : A.NBX, 0, me)};
+    const double par[1] = {FULL ? A.dt / A.dy : 0.5 * (A.dt / A.dy)};
+    MHD_ADJ_APPLY(fhx, REV, in, out, par);
+  } else {
+    IO in[3] = {io(A.FY, 0, me), io(E, 0, (size_t)j * cw + i + 1), io(E, 0, (size_t)j * cw + i)};
+    IO out[1] = {io(FULL ? A.NFY : A.NBY, 0, me)};
+    const double par[1] = {FULL ? A.dt / A.dx : 0.5 * (A.dt / A.dx)};
+    MHD_ADJ_APPLY(fhy, REV, in, out, par);
+  }
+}
+
+template <int AX, bool REV>
+__global__ void __launch_bounds__(kT) k_ctu(Adj A) {
+  const int nx = A.nx, ny = A.ny;
+  const int Wd = AX == 0 ? nx + 1 : nx, H = AX == 0 ? ny : ny + 1;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y, side = blockIdx.z;
+  if (col >= Wd || row >= H) return;
+  const int f = AX == 0 ? col : row, t = AX == 0 ? row : col;
+  const int L = AX == 0 ? nx : ny;
+  const int bc = AX == 0 ? A.bcx : A.bcy;
+  const size_t me = (size_t)row * Wd + col;
+  const int kpad = f + side;
+  int scell, lb, rb;
+  if (AX == 0) {
+    scell = wrapc(kpad - 1, L, bc);
+    if (bc == 0) { lb = kpad - 1 < 0 ? 0 : (kpad - 1 > L ? L : kpad - 1); rb = kpad > L ? L : kpad; }
+    else { lb = kpad == 0 ? L - 1 : kpad - 1; rb = kpad == L + 1 ? 1 : kpad; }
+  } else {
+    if (bc == 0) {
+      scell = kpad == 0 ? 1 : (kpad - 1 > L - 1 ? L - 1 : kpad - 1);
+      lb = kpad == 0 ? 1 : kpad - 1; rb = kpad == L + 1 ? L - 1 : kpad;
+    } else {
+      scell = wrapc(kpad - 1, L, bc);
+      lb = kpad == 0 ? L - 1 : kpad - 1; rb = kpad == L + 1 ? 1 : kpad;
+    }
+  }
+  const int fc = wrapc(f - 1 + side, L, bc);
+  const Arr& W = AX == 0 ? (side == 0 ? A.XL : A.XR) : (side == 0 ? A.YL : A.YR);
+  const Arr& U = AX == 0 ? (side == 0 ? A.UXL : A.UXR) : (side == 0 ? A.UYL : A.UYR);
+  const Arr& W2 = AX == 0 ? (side == 0 ? A.WXL : A.WXR) : (side == 0 ? A.WYL : A.WYR);
+  const Arr& FB = AX == 0 ? A.FX : A.FY;
+  const Arr& NB = AX == 0 ? A.NBX : A.NBY;
+  const Arr& FT = AX == 0 ? A.F1Y : A.F1X;
+  size_t hi, lo, si, lbi, rbi;
+  if (AX == 0) {
+    hi = (size_t)(t + 1) * nx + fc; lo = (size_t)t * nx + fc;
+    si = (size_t)t * nx + scell;
+    lbi = (size_t)t * (nx + 1) + lb; rbi = (size_t)t * (nx + 1) + rb;
+  } else {
+    hi = (size_t)fc * (nx + 1) + t + 1; lo = (size_t)fc * (nx + 1) + t;
+    si = (size_t)scell * nx + t;
+    lbi = (size_t)lb * nx + t; rbi = (size_t)rb * nx + t;
+  }
+  IO in[29];
+  IO out[14];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) in[k] = io(W, k, me);
+  in[7] = io(FB, 0, me);
+#pragma unroll
+  for (int k = 0; k < 7; ++k) { in[8 + k] = io(FT, k, hi); in[15 + k] = io(FT, k, lo); }
+  in[22] = io(A.P, 4, si); in[23] = io(A.P, 5, si); in[24] = io(A.P, 6, si); in[25] = io(A.P, 3, si);
+  in[26] = io(FB, 0, lbi); in[27] = io(FB, 0, rbi);
+  in[28] = io(NB, 0, me);
+#pragma unroll
+  for (int k = 0; k < 7; ++k) { out[k] = io(U, k, me); out[7 + k] = io(W2, k, me); }
+  const double par[6] = {A.gamma, 0.5 * A.dt, 1.0 / (AX == 0 ? A.dx : A.dy),
+                         0.5 * (A.dt / (AX == 0 ? A.dy : A.dx)), A.min_d, A.min_e};
+  if (AX == 0) MHD_ADJ_APPLY(ctu0, REV, in, out, par);
+  else MHD_ADJ_APPLY(ctu1, REV, in, out, par);
+}
+
+template <bool REV>
+__global__ void __launch_bounds__(kT) k_half(Adj A) {
+  const int nx = A.nx;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= nx || j >= A.ny) return;
+  const size_t me = (size_t)j * nx + i;
+  const size_t xl = (size_t)j * (nx + 1) + i, yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
+  IO in[19];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    in[k] = io(A.C, k, me);
+    in[3 + k] = io(A.F1X, k, xl);
+    in[6 + k] = io(A.F1X, k, xl + 1);
+    in[9 + k] = io(A.F1Y, k, yt);
+    in[12 + k] = io(A.F1Y, k, yb);
+  }
+  in[15] = io(A.NBX, 0, xl); in[16] = io(A.NBX, 0, xl + 1);
+  in[17] = io(A.NBY, 0, yt); in[18] = io(A.NBY, 0, yb);
+  IO out[1] = {io(A.HEZ, 0, me)};
+  const double par[2] = {0.5 * (A.dt / A.dx), 0.5 * (A.dt / A.dy)};
+  MHD_ADJ_APPLY(half, REV, in, out, par);
+}
+
+template <bool REV>
+__global__ void __launch_bounds__(kT) k_final(Adj A) {
+  const int nx = A.nx;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= nx || j >= A.ny) return;
+  const size_t me = (size_t)j * nx + i;
+  const size_t xl = (size_t)j * (nx + 1) + i, yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
+  const size_t cw = nx + 1;
+  const int xs[7] = {0, 1, 2, 3, 5, 6, 7};
+  IO in[43];
+  in[0] = io(A.FX, 0, xl); in[1] = io(A.FX, 0, xl + 1);
+  in[2] = io(A.FY, 0, yt); in[3] = io(A.FY, 0, yb);
+  in[4] = io(A.E2, 0, (size_t)j * cw + i); in[5] = io(A.E2, 0, (size_t)(j + 1) * cw + i);
+  in[6] = io(A.E2, 0, (size_t)j * cw + i + 1); in[7] = io(A.E2, 0, (size_t)(j + 1) * cw + i + 1);
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    in[8 + k] = io(A.C, xs[k], me);
+    in[15 + k] = io(A.F2X, k, xl);
+    in[22 + k] = io(A.F2X, k, xl + 1);
+    in[29 + k] = io(A.F2Y, k, yt);
+    in[36 + k] = io(A.F2Y, k, yb);
+  }
+  IO out[16];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { out[k] = io(A.NP, k, me); out[8 + k] = io(A.NC, k, me); }
+  const double par[3] = {A.dt / A.dx, A.dt / A.dy, A.gamma};
+  MHD_ADJ_APPLY(final, REV, in, out, par);
+}
+
+// ---------------------------------------------------------------------------
+// CFL dt of the input state (Source/TimestepCalculations_HelperModule.py:239-289)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dmax2(double a, double b) { return a > b ? a : b; }
+
+__device__ __forceinline__ double M(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double Ad(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double Sb(double a, double b) { return __dsub_rn(a, b); }
+
+// The unit is compiled with FMA contraction (for the reverse sweeps), so the
+// CFL arithmetic spells out its roundings to match the exact-arithmetic step.
+__global__ void __launch_bounds__(256) k_cfl(Adj A) {
+  const int nx = A.nx;
+  const size_t n = (size_t)A.nx * A.ny, plane = n;
+  const double gamma = A.gamma;
+  const double* c = A.C.v;
+  double mx = 0.0, my = 0.0;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const double inv_d = 1.0 / c[idx];
+    const double vx = M(c[plane + idx], inv_d);
+    const double vy = M(c[2 * plane + idx], inv_d);
+    const double vz = M(c[3 * plane + idx], inv_d);
+    const double vsq = Ad(Ad(M(vx, vx), M(vy, vy)), M(vz, vz));
+    const int j = (int)(idx / nx), i = (int)(idx % nx);
+    const double c4 = c[4 * plane + idx], c5 = c[5 * plane + idx];
+    const double bx = Ad(c4, fabs(Sb(A.FX.v[(size_t)j * (nx + 1) + i], c4)));
+    const double by = Ad(c5, fabs(Sb(A.FY.v[(size_t)j * nx + i], c5)));
+    const double bz = c[6 * plane + idx];
+    const double bsq = Ad(Ad(M(bx, bx), M(by, by)), M(bz, bz));
+    const double e_int = Sb(Sb(c[7 * plane + idx], M(M(0.5, c[idx]), vsq)), M(0.5, bsq));
+    const double p = dmax2(M(gamma - 1.0, e_int), 0.000000000001);
+    const double a2 = M(M(gamma, p), inv_d);
+    const double bd = M(bsq, inv_d);
+    const double ssum = Ad(bd, a2);
+    const double sdiff = Sb(bd, a2);
+    const double dd = M(sdiff, sdiff);
+    const double cfx2 = M(0.5, Ad(ssum, __dsqrt_rn(Ad(dd, M(M(M(4.0, a2), Ad(M(by, by), M(bz, bz))), inv_d)))));
+    const double cfy2 = M(0.5, Ad(ssum, __dsqrt_rn(Ad(dd, M(M(M(4.0, a2), Ad(M(bx, bx), M(bz, bz))), inv_d)))));
+    mx = dmax2(mx, Ad(fabs(vx), __dsqrt_rn(cfx2)));
+    my = dmax2(my, Ad(fabs(vy), __dsqrt_rn(cfy2)));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = dmax2(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    my = dmax2(my, __shfl_xor_sync(0xffffffffu, my, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(reinterpret_cast<unsigned long long*>(A.red), (unsigned long long)__double_as_longlong(mx));
+    atomicMax(reinterpret_cast<unsigned long long*>(A.red + 1), (unsigned long long)__double_as_longlong(my));
+  }
+}
+
+__global__ void k_cfl_finish(Adj A, double cfl, double* dt_slot) {
+  const double mx = A.red[0], my = A.red[1];
+  const double inv = dmax2(mx / A.dx, my / A.dy);
+  *dt_slot = cfl / inv;
+  A.red[0] = 0.0;
+  A.red[1] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+// Every array of a cycle, in arena order: inputs first, outputs last (the
+// reverse sweep clears all adjoints below the outputs with one memset).
+struct Slot {
+  Arr Adj::*arr;
+  int planes;
+  int kind;   // 0 cell, 1 x-face, 2 y-face, 3 corner
+};
+const Slot kSlots[] = {
+    {&Adj::P, 8, 0},   {&Adj::C, 8, 0},   {&Adj::FX, 1, 1},  {&Adj::FY, 1, 2},  {&Adj::EX, 14, 0},
+    {&Adj::EY, 14, 0}, {&Adj::XL, 7, 1},  {&Adj::XR, 7, 1},  {&Adj::YL, 7, 2},  {&Adj::YR, 7, 2},
+    {&Adj::F1X, 7, 1}, {&Adj::F1Y, 7, 2}, {&Adj::EZ, 1, 0},  {&Adj::E1, 1, 3},  {&Adj::NBX, 1, 1},
+    {&Adj::NBY, 1, 2}, {&Adj::UXL, 7, 1}, {&Adj::UXR, 7, 1}, {&Adj::UYL, 7, 2}, {&Adj::UYR, 7, 2},
+    {&Adj::WXL, 7, 1}, {&Adj::WXR, 7, 1}, {&Adj::WYL, 7, 2}, {&Adj::WYR, 7, 2}, {&Adj::HEZ, 1, 0},
+    {&Adj::F2X, 7, 1}, {&Adj::F2Y, 7, 2}, {&Adj::E2, 1, 3},  {&Adj::NP, 8, 0},  {&Adj::NC, 8, 0},
+    {&Adj::NFX, 1, 1}, {&Adj::NFY, 1, 2}};
+constexpr int kNumSlots = sizeof(kSlots) / sizeof(kSlots[0]);
+constexpr int kFirstOutput = kNumSlots - 4;
+
+struct Handle {
+  Adj A{};
+  cudaStream_t stream = nullptr;
+  size_t off[kNumSlots] = {};  // word offset of each array in an arena
+  size_t ps[kNumSlots] = {};   // plane stride of each array
+  size_t W = 0;                // words of one arena (all arrays of one cycle)
+  double* bars = nullptr;      // one adjoint arena
+  double* vals = nullptr;      // nsets value arenas
+  int nsets = 0;
+  double* red = nullptr;       // CFL maxima (2) + dt (1)
+  size_t budget = 0;           // bytes the stored-segment mode may use (0: 60% of free memory)
+  // forward record
+  int steps = 0, every = 0;
+  bool stored = false;         // backward keeps every cycle of a segment resident
+  std::vector<double> dts;
+  double* ckpt = nullptr;      // one packed state per segment
+  double* seg = nullptr;       // recompute mode: packed states of the current segment
+  size_t ckpt_bytes = 0, seg_bytes = 0;
+  size_t state_words = 0;
+};
+
+int fail(cudaError_t e) { return e == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; }
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return fail(e_); } while (0)
+
+size_t state_words(const Adj& A) {
+  const size_t cp = (size_t)A.nx * A.ny;
+  return 16 * cp + (size_t)(A.nx + 1) * A.ny + (size_t)A.nx * (A.ny + 1);
+}
+
+// point the Arr views of h->A at value arena k (adjoints always in the one bar arena)
+void select_set(Handle* h, int k) {
+  double* base = h->vals + (size_t)k * h->W;
+  for (int i = 0; i < kNumSlots; ++i) {
+    Arr& a = h->A.*(kSlots[i].arr);
+    a.v = base + h->off[i];
+    a.b = h->bars + h->off[i];
+    a.ps = h->ps[i];
+  }
+}
+
+int alloc_sets(Handle* h, int n) {
+  if (h->nsets == n) return MHD_OK;
+  if (h->vals) { cudaFree(h->vals); h->vals = nullptr; h->nsets = 0; }
+  CK(cudaMalloc(&h->vals, (size_t)n * h->W * sizeof(double)));
+  h->nsets = n;
+  select_set(h, 0);
+  return MHD_OK;
+}
+
+size_t device_bytes(const Handle* h) {
+  return (h->W * (1 + (size_t)h->nsets) + 4) * sizeof(double) + h->ckpt_bytes + h->seg_bytes;
+}
+
+// copy a packed state [prim 8 | cons 8 | fbx | fby] into / out of four arrays
+int pack(Handle* h, double* dst, const Arr& P, const Arr& C, const Arr& FX, const Arr& FY, bool bars) {
+  const Adj& A = h->A;
+  const size_t cp = (size_t)A.nx * A.ny, xp = (size_t)(A.nx + 1) * A.ny, yp = (size_t)A.nx * (A.ny + 1);
+  auto src = [&](const Arr& a) { return bars ? a.b : a.v; };
+  CK(cudaMemcpyAsync(dst, src(P), 8 * cp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(dst + 8 * cp, src(C), 8 * cp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(dst + 16 * cp, src(FX), xp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(dst + 16 * cp + xp, src(FY), yp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  return MHD_OK;
+}
+
+int unpack(Handle* h, const double* src, Arr& P, Arr& C, Arr& FX, Arr& FY, bool bars) {
+  const Adj& A = h->A;
+  const size_t cp = (size_t)A.nx * A.ny, xp = (size_t)(A.nx + 1) * A.ny, yp = (size_t)A.nx * (A.ny + 1);
+  auto dst = [&](Arr& a) { return bars ? a.b : a.v; };
+  CK(cudaMemcpyAsync(dst(P), src, 8 * cp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(dst(C), src + 8 * cp, 8 * cp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(dst(FX), src + 16 * cp, xp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(dst(FY), src + 16 * cp + xp, yp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  return MHD_OK;
+}
+
+dim3 g2(int w, int h, int z = 1) { return dim3((unsigned)((w + kT - 1) / kT), (unsigned)h, (unsigned)z); }
+unsigned g1(size_t n) { return (unsigned)((n + kT - 1) / kT); }
+
+// forward sweep of one cycle from the input arrays (P, C, FX, FY) with A.dt set
+int fwd_cycle(Handle* h) {
+  Adj& A = h->A;
+  cudaStream_t s = h->stream;
+  const int nx = A.nx, ny = A.ny;
+  k_recon<0, false><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_recon<1, false><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_face<0, false><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
+  k_face<1, false><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
+  k_roe<0, 1, false><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_roe<1, 1, false><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_ez<false><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_emf<1, false><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
+  k_fhalf<0, false, false><<<g2(nx + 1, ny), kT, 0, s>>>(A);
+  k_fhalf<1, false, false><<<g2(nx, ny + 1), kT, 0, s>>>(A);
+  k_ctu<0, false><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
+  k_ctu<1, false><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
+  k_half<false><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_roe<0, 2, false><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_roe<1, 2, false><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_emf<2, false><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
+  k_final<false><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_fhalf<0, true, false><<<g2(nx + 1, ny), kT, 0, s>>>(A);
+  k_fhalf<1, true, false><<<g2(nx, ny + 1), kT, 0, s>>>(A);
+  CK(cudaGetLastError());
+  return MHD_OK;
+}
+
+// reverse sweep: output adjoints in NP/NC/NFX/NFY .b -> input adjoints in P/C/FX/FY .b
+int rev_cycle(Handle* h) {
+  Adj& A = h->A;
+  cudaStream_t s = h->stream;
+  const int nx = A.nx, ny = A.ny;
+  // zero every adjoint except the outputs' (they sit at the end of the arena)
+  CK(cudaMemsetAsync(h->bars, 0, h->off[kFirstOutput] * sizeof(double), s));
+  k_fhalf<1, true, true><<<g2(nx, ny + 1), kT, 0, s>>>(A);
+  k_fhalf<0, true, true><<<g2(nx + 1, ny), kT, 0, s>>>(A);
+  k_final<true><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_emf<2, true><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
+  k_roe<1, 2, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_roe<0, 2, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_half<true><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_ctu<1, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
+  k_ctu<0, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
+  k_fhalf<1, false, true><<<g2(nx, ny + 1), kT, 0, s>>>(A);
+  k_fhalf<0, false, true><<<g2(nx + 1, ny), kT, 0, s>>>(A);
+  k_emf<1, true><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
+  k_ez<true><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_roe<1, 1, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_roe<0, 1, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_face<1, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
+  k_face<0, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
+  k_recon<1, true><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_recon<0, true><<<g2(nx, ny), kT, 0, s>>>(A);
+  CK(cudaGetLastError());
+  return MHD_OK;
+}
+
+int cfl_dt(Handle* h, double cfl, double* host_dt) {
+  Adj& A = h->A;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_cfl<<<sms * 4, 256, 0, h->stream>>>(A);
+  k_cfl_finish<<<1, 1, 0, h->stream>>>(A, cfl, h->red + 2);
+  CK(cudaMemcpyAsync(host_dt, h->red + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+// inputs of value arena `to` <- outputs of value arena `from` (the state after that cycle)
+int output_to_input(Handle* h, int from, int to) {
+  const double* src = h->vals + (size_t)from * h->W;
+  double* dst = h->vals + (size_t)to * h->W;
+  for (int i = 0; i < 4; ++i) {
+    const size_t n = (size_t)kSlots[i].planes * h->ps[i];
+    CK(cudaMemcpyAsync(dst + h->off[i], src + h->off[kFirstOutput + i], n * sizeof(double),
+                       cudaMemcpyDeviceToDevice, h->stream));
+  }
+  return MHD_OK;
+}
+
+int bars_in_to_out(Handle* h) {
+  Adj& A = h->A;
+  const size_t cp = (size_t)A.nx * A.ny;
+  CK(cudaMemcpyAsync(A.NP.b, A.P.b, 8 * cp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(A.NC.b, A.C.b, 8 * cp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(A.NFX.b, A.FX.b, A.FX.ps * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(A.NFY.b, A.FY.b, A.FY.ps * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  return MHD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma, int recon,
+                     int entropy_fix, double eps, double min_d, double min_p, double min_e, void** handle) {
+  if (!handle) return MHD_ERR_ARG;
+  *handle = nullptr;
+  if (nx < 2 || ny < 2 || !(dx > 0.0) || !(dy > 0.0) || (recon != 0 && recon != 1)) return MHD_ERR_ARG;
+  if ((bcx != 0 && bcx != 1) || (bcy != 0 && bcy != 1)) return MHD_ERR_ARG;
+  Handle* h = new (std::nothrow) Handle();
+  if (!h) return MHD_ERR_NOMEM;
+  Adj& A = h->A;
+  A.nx = nx; A.ny = ny; A.dx = dx; A.dy = dy; A.bcx = bcx; A.bcy = bcy; A.recon = recon;
+  A.efix = entropy_fix ? 1 : 0; A.gamma = gamma; A.eps = eps; A.min_d = min_d; A.min_p = min_p; A.min_e = min_e;
+  const size_t plane[4] = {(size_t)nx * ny, (size_t)(nx + 1) * ny, (size_t)nx * (ny + 1),
+                           (size_t)(nx + 1) * (ny + 1)};
+  size_t w = 0;
+  for (int i = 0; i < kNumSlots; ++i) {
+    h->off[i] = w;
+    h->ps[i] = plane[kSlots[i].kind];
+    w += (size_t)kSlots[i].planes * h->ps[i];
+    w = (w + 31) & ~(size_t)31;   // 256-byte aligned planes groups
+  }
+  h->W = w;
+  h->state_words = state_words(A);
+  int rc = MHD_OK;
+  cudaError_t e = cudaMalloc(&h->bars, h->W * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->red, 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->red, 0, 4 * sizeof(double), h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) rc = fail(e);
+  if (rc == MHD_OK) rc = alloc_sets(h, 1);
+  A.red = h->red;
+  if (rc != MHD_OK) {
+    cudaFree(h->bars);
+    cudaFree(h->red);
+    cudaFree(h->vals);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return rc;
+  }
+  *handle = h;
+  return MHD_OK;
+}
+
+void mhd2d_adj_destroy(void* handle) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->bars);
+  cudaFree(h->vals);
+  cudaFree(h->red);
+  cudaFree(h->ckpt);
+  cudaFree(h->seg);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int mhd2d_adj_configure(void* handle, size_t segment_bytes) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return MHD_ERR_ARG;
+  h->budget = segment_bytes;
+  return MHD_OK;
+}
+
+int mhd2d_adj_cycle(void* handle, double dt, const double* state_in, double* state_out) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !state_in || !state_out) return MHD_ERR_ARG;
+  Adj& A = h->A;
+  select_set(h, 0);
+  A.dt = dt;
+  int rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false);
+  if (rc) return rc;
+  if ((rc = fwd_cycle(h))) return rc;
+  if ((rc = pack(h, state_out, A.NP, A.NC, A.NFX, A.NFY, false))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd2d_adj_cycle_reverse(void* handle, double dt, const double* state_in, const double* bar_out,
+                            double* bar_in) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !state_in || !bar_out || !bar_in) return MHD_ERR_ARG;
+  Adj& A = h->A;
+  select_set(h, 0);
+  A.dt = dt;
+  int rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false);
+  if (rc) return rc;
+  if ((rc = fwd_cycle(h))) return rc;
+  if ((rc = unpack(h, bar_out, A.NP, A.NC, A.NFX, A.NFY, true))) return rc;
+  if ((rc = rev_cycle(h))) return rc;
+  if ((rc = pack(h, bar_in, A.P, A.C, A.FX, A.FY, true))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cfl, const double* fixed_dt,
+                      int every, double* state_out, double* dt_log) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !state_in || !state_out || steps < 1) return MHD_ERR_ARG;
+  Adj& A = h->A;
+  if (every <= 0) every = (int)std::ceil(std::sqrt((double)steps));
+  every = std::min(every, steps);
+  const int nck = (steps + every - 1) / every;
+  h->steps = 0;
+  cudaFree(h->ckpt);
+  cudaFree(h->seg);
+  h->ckpt = h->seg = nullptr;
+  h->ckpt_bytes = h->seg_bytes = 0;
+  CK(cudaMalloc(&h->ckpt, (size_t)nck * h->state_words * sizeof(double)));
+  h->ckpt_bytes = (size_t)nck * h->state_words * sizeof(double);
+  // backward mode: keep all `every` cycles of a segment resident when they fit
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  // (arenas this handle already holds count as free)
+  const size_t held = ((size_t)h->nsets - 1) * h->W * sizeof(double);
+  const size_t budget = h->budget ? h->budget : (size_t)(0.6 * (double)(free_b + held));
+  const size_t extra = ((size_t)every - 1) * h->W * sizeof(double);
+  h->stored = every > 1 && extra <= budget;
+  int rc;
+  if (h->stored) {
+    if (h->nsets < every && (rc = alloc_sets(h, every))) return rc;
+  } else {
+    if ((rc = alloc_sets(h, 1))) return rc;
+    CK(cudaMalloc(&h->seg, (size_t)every * h->state_words * sizeof(double)));
+    h->seg_bytes = (size_t)every * h->state_words * sizeof(double);
+  }
+  h->every = every;
+  h->dts.assign(steps, 0.0);
+  select_set(h, 0);
+  if ((rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false))) return rc;
+  for (int c = 0; c < steps; ++c) {
+    if (c % every == 0 &&
+        (rc = pack(h, h->ckpt + (size_t)(c / every) * h->state_words, A.P, A.C, A.FX, A.FY, false)))
+      return rc;
+    double dt;
+    if (fixed_dt) dt = fixed_dt[c];
+    else if ((rc = cfl_dt(h, cfl, &dt))) return rc;
+    if (!std::isfinite(dt)) return MHD_ERR_NONFINITE;
+    h->dts[c] = dt;
+    A.dt = dt;
+    if ((rc = fwd_cycle(h))) return rc;
+    if ((rc = output_to_input(h, 0, 0))) return rc;
+  }
+  if ((rc = pack(h, state_out, A.P, A.C, A.FX, A.FY, false))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  h->steps = steps;
+  if (dt_log) std::copy(h->dts.begin(), h->dts.end(), dt_log);
+  return MHD_OK;
+}
+
+int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initial) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !bar_final || !bar_initial) return MHD_ERR_ARG;
+  if (!h->ckpt || h->steps < 1) return MHD_ERR_STATE;
+  Adj& A = h->A;
+  const int every = h->every;
+  const int nck = (h->steps + every - 1) / every;
+  select_set(h, 0);
+  int rc = unpack(h, bar_final, A.NP, A.NC, A.NFX, A.NFY, true);
+  if (rc) return rc;
+  for (int s = nck - 1; s >= 0; --s) {
+    const int c0 = s * every;
+    const int len = std::min(every, h->steps - c0);
+    select_set(h, 0);
+    if ((rc = unpack(h, h->ckpt + (size_t)s * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
+    if (h->stored) {
+      // recompute the segment once, keeping every cycle's arrays, then sweep back
+      for (int k = 0; k < len; ++k) {
+        select_set(h, k);
+        A.dt = h->dts[c0 + k];
+        if ((rc = fwd_cycle(h))) return rc;
+        if (k + 1 < len && (rc = output_to_input(h, k, k + 1))) return rc;
+      }
+      for (int k = len - 1; k >= 0; --k) {
+        select_set(h, k);
+        A.dt = h->dts[c0 + k];
+        if ((rc = rev_cycle(h))) return rc;
+        if ((rc = bars_in_to_out(h))) return rc;
+      }
+    } else {
+      // recompute the segment's states, then each cycle again before its reverse sweep
+      for (int k = 0; k < len; ++k) {
+        if ((rc = pack(h, h->seg + (size_t)k * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
+        if (k + 1 < len) {
+          A.dt = h->dts[c0 + k];
+          if ((rc = fwd_cycle(h))) return rc;
+          if ((rc = output_to_input(h, 0, 0))) return rc;
+        }
+      }
+      for (int k = len - 1; k >= 0; --k) {
+        A.dt = h->dts[c0 + k];
+        if ((rc = unpack(h, h->seg + (size_t)k * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
+        if ((rc = fwd_cycle(h))) return rc;
+        if ((rc = rev_cycle(h))) return rc;
+        if ((rc = bars_in_to_out(h))) return rc;
+      }
+    }
+  }
+  select_set(h, 0);
+  if ((rc = pack(h, bar_initial, A.NP, A.NC, A.NFX, A.NFY, true))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd2d_adj_info(void* handle, size_t* state_words_out, size_t* device_bytes_out, int* segment_sets) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return MHD_ERR_ARG;
+  if (state_words_out) *state_words_out = h->state_words;
+  if (device_bytes_out) *device_bytes_out = device_bytes(h);
+  if (segment_sets) *segment_sets = h->stored ? h->every : 1;
+  return MHD_OK;
+}
+
+}  // extern "C"

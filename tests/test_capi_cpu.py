@@ -69,3 +69,16 @@ def test_null_handle_calls_fail_cleanly(lib):
     c = ctypes.c_longlong()
     assert lib.mhd2d_advance(None, 0.0, 1.0, 0, 1, 0.4, ctypes.byref(t), ctypes.byref(c), ctypes.byref(t)) == 1
     assert lib.mhd2d_download(None, 0, None, None, None, None) == 1
+
+
+def test_adjoint_entry_points_reject_bad_arguments(lib):
+    h = ctypes.c_void_p()
+    # the adjoint covers first order (0) and PLM (1) only
+    rc = lib.mhd2d_adj_create(16, 16, 0.1, 0.1, 1, 1, 1.4, 2, 0, 0.5, 1e-12, 1e-12, 1e-12, ctypes.byref(h))
+    assert rc == 1 and not h.value
+    rc = lib.mhd2d_adj_create(1, 16, 0.1, 0.1, 1, 1, 1.4, 1, 0, 0.5, 1e-12, 1e-12, 1e-12, ctypes.byref(h))
+    assert rc == 1 and not h.value
+    assert lib.mhd2d_adj_cycle(None, 0.1, None, None) == 1
+    assert lib.mhd2d_adj_backward(None, None, None) == 1
+    assert lib.mhd2d_adj_forward(None, None, 1, 0.4, None, 0, None, None) == 1
+    lib.mhd2d_adj_destroy(None)
