@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10,
                     help="cycles of the 256-instance batched workload (0 = skip it)")
     ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--adjoint-steps", type=int, default=400,
+                    help="cycles of the 512^2 PLM adjoint workload (0 = skip it)")
+    ap.add_argument("--adjoint-n", type=int, default=512)
     return ap.parse_args()
 
 
@@ -251,6 +254,69 @@ def run_batch(a, torch):
 
 
 # ----------------------------------------------------------------------------
+# adjoint: gradient of a density-matching loss through many cycles
+# ----------------------------------------------------------------------------
+def run_adjoint(a, torch):
+    """512^2 periodic MHD turbulence (seeded, k <= 16), PLM + Roe + CTU+CT, 400 cycles
+    at CFL 0.4; loss = mean squared difference between the final density and the
+    final density of a run from a smoothly 2%-perturbed initial state; gradient
+    with respect to the initial rho, vx, vy, p, A_z by the hand-written backward
+    pass with sqrt(N) checkpoints.  Timed against the production forward step on
+    the same state (exact arithmetic)."""
+    from pythonmhd_gb300.adjoint import fields
+    from pythonmhd_gb300.adjoint.device import Adjoint2D, evolve
+    from pythonmhd_gb300.solver import Grid2D
+    n, steps = a.adjoint_n, a.adjoint_steps
+    dev = torch.device("cuda", torch.cuda.current_device())
+    fl = fields.turbulence_fields(n, seed=1, kmax_v=16, kmax_a=16)
+    tgt = fields.perturbed(fl, 0.02, seed=2)
+    g0 = fl["gamma"]
+    adj = Adjoint2D(n, n, fl["dx"], fl["dy"], 1, 1, g0, recon=1)
+    st_t = fields.state_from_fields(*fields.fields_to_torch(tgt, dev), g0, fl["dx"], fl["dy"]).contiguous()
+    target = adj.unpack(adj.forward(st_t, steps, cfl=0.4))[0][0].clone()
+    # production forward on the same initial state (the denominator)
+    xs = fields.fields_to_torch(fl, dev)
+    s0 = fields.state_from_fields(*xs, g0, fl["dx"], fl["dy"]).contiguous()
+    prim, cons, fbx, fby = [t.cpu().numpy() for t in adj.unpack(s0)]
+    grid = Grid2D(n, n, fl["dx"], fl["dy"], 1, 1, g0, mhd=True, recon=1, arith="exact")
+    grid.upload(prim, cons, fbx, fby)
+    grid.advance(0.0, 1e30, 0, 3, 0.4)
+    grid.upload(prim, cons, fbx, fby)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grid.advance(0.0, 1e30, 0, steps, 0.4)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    grid.close()
+    # gradient: forward pass (records dt, keeps checkpoints) + backward pass
+    xs = fields.fields_to_torch(fl, dev, requires_grad=True)
+    state = fields.state_from_fields(*xs, g0, fl["dx"], fl["dy"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = evolve(state, adj, steps, cfl=0.4)
+    loss = torch.mean((adj.unpack(out)[0][0] - target) ** 2)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    loss.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    info = adj.info()
+    gnorm = float(sum(float(torch.sum(x.grad * x.grad)) for x in xs)) ** 0.5
+    adj.close()
+    return {"workload": f"{n}x{n} periodic MHD turbulence (seeded, k<=16), PLM+Roe+CTU+CT, {steps} cycles, CFL 0.4; "
+                        "loss = mean((rho_final - rho_target)^2), target from a smoothly 2%-perturbed state; "
+                        "gradient w.r.t. initial rho, vx, vy, p, A_z; dt frozen",
+            "steps": steps, "loss": float(loss.detach()), "grad_norm": gnorm,
+            "forward_ms_per_cycle": 1e3 * t_fwd / steps,
+            "gradient_forward_pass_ms_per_cycle": 1e3 * (t1 - t0) / steps,
+            "backward_ms_per_cycle": 1e3 * (t2 - t1) / steps,
+            "gradient_over_forward": (t2 - t0) / t_fwd, "backward_over_forward": (t2 - t1) / t_fwd,
+            "checkpoint_every": int(np.ceil(np.sqrt(steps))), "segment_cycles_resident": info["segment_sets"],
+            "device_bytes": info["device_bytes"],
+            "timing": "host wall clock around device-synchronised calls; forward = production exact step"}
+
+
+# ----------------------------------------------------------------------------
 # our arm
 # ----------------------------------------------------------------------------
 def run_ours(a):
@@ -370,6 +436,10 @@ def run_ours(a):
     if a.batch_steps > 0:
         g.close()
         batched = run_batch(a, torch)
+    adjoint = None
+    if a.adjoint_steps > 0:
+        g.close()
+        adjoint = run_adjoint(a, torch)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_per, "higher_is_better": True, "scaling": "weak",
@@ -381,7 +451,8 @@ def run_ours(a):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps, "ms_per_step": ms_e2e_per},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
-            "device_bytes": dev_bytes, "final_cycle": cyc, "final_time": t, "batched": batched}
+            "device_bytes": dev_bytes, "final_cycle": cyc, "final_time": t, "batched": batched,
+            "adjoint": adjoint}
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()

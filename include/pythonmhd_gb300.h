@@ -61,6 +61,10 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
 int mhd2d_upload(void* handle, const double* prim, const double* cons,
                  const double* faceBx, const double* faceBy);
 
+/* The same from device memory of the handle's GPU (no host round trip). */
+int mhd2d_upload_device(void* handle, const double* prim, const double* cons,
+                        const double* faceBx, const double* faceBy);
+
 /* Run the evolve loop on the device: while t < t_end and cycle < max_cycles,
  * one CTU(+CT) cycle with the CFL dt clipped to t_end
  * (Source/EvolveFunctions_MHD.py:464-692).  Returns the final time/cycle and the

@@ -22,7 +22,7 @@ OUTFLOW, PERIODIC = 0, 1
 
 
 @functools.lru_cache(maxsize=None)
-def _fn(name, efix=False):
+def _fn(name, efix=False, backend="numpy", device=None):
     spec = {
         "plm0": (stages.plm_cell, 22, 2, dict(axis=0)),
         "plm1": (stages.plm_cell, 22, 2, dict(axis=1)),
@@ -43,6 +43,8 @@ def _fn(name, efix=False):
     }[name]
     fn, nin, npar, kw = spec
     t = dsl.trace(name.replace("-", "_") + ("_efix" if efix else ""), fn, nin, npar, **kw)
+    if backend == "torch":
+        return dsl.compile_torch(t, device), None
     return dsl.compile_numpy(t, reverse=True)
 
 
@@ -51,19 +53,19 @@ def _wrap(i, n, bc):
 
 
 class _Arr:
-    """An array of the cycle with its adjoint accumulator."""
+    """An array of the cycle with its adjoint accumulator (NumPy form only)."""
 
     def __init__(self, data):
         self.v = data
-        self.b = np.zeros_like(data)
+        self.b = np.zeros_like(data) if isinstance(data, np.ndarray) else None
 
 
-def _stage(tape, name, efix, ins, pars, outs_shape=None):
+def _stage(tape, name, efix, ins, pars, backend="numpy", device=None):
     """Run a stage forward on gathered inputs; remember it for the reverse sweep.
 
     ins: list of (arr, slot, idx) -- slot None for a 2D array; idx a tuple of index arrays.
     """
-    fwd, rev = _fn(name, efix)
+    fwd, rev = _fn(name, efix, backend, device)
     x = [a.v[idx] if slot is None else a.v[slot][idx] for (a, slot, idx) in ins]
     y = fwd(x, pars)
     tape.append((rev, ins, pars, x))
@@ -85,12 +87,25 @@ Y_SLOTS = (0, 1, 2, 3, 6, 4, 7)
 
 
 class Cycle:
-    """Forward sweep of one cycle that records what the reverse sweep needs."""
+    """Forward sweep of one cycle that records what the reverse sweep needs.
 
-    def __init__(self, prim, cons, fbx, fby, dt, dx, dy, bcx, bcy, gamma, min_d, min_p, min_e, order, efix, eps):
+    ``backend="torch"`` runs the same stencil on torch float64 tensors with the
+    stage functions emitted as torch code (forward only): a plain PyTorch
+    transcription of the step that torch's own automatic differentiation can
+    differentiate, as an independent check of the hand-written reverse sweeps.
+    """
+
+    def __init__(self, prim, cons, fbx, fby, dt, dx, dy, bcx, bcy, gamma, min_d, min_p, min_e, order, efix, eps,
+                 backend="numpy"):
         assert order in (0, 1)
-        self.P, self.C = _Arr(np.array(prim, dtype=float)), _Arr(np.array(cons, dtype=float))
-        self.FX, self.FY = _Arr(np.array(fbx, dtype=float)), _Arr(np.array(fby, dtype=float))
+        self.backend = backend
+        if backend == "torch":
+            import torch
+            self._torch = torch
+            self.P, self.C, self.FX, self.FY = (_Arr(t) for t in (prim, cons, fbx, fby))
+        else:
+            self.P, self.C = _Arr(np.array(prim, dtype=float)), _Arr(np.array(cons, dtype=float))
+            self.FX, self.FY = _Arr(np.array(fbx, dtype=float)), _Arr(np.array(fby, dtype=float))
         self.dt, self.dx, self.dy = dt, dx, dy
         self.bc = (bcx, bcy)
         self.gamma, self.min_d, self.min_p, self.min_e = gamma, min_d, min_p, min_e
@@ -98,9 +113,18 @@ class Cycle:
         self.tape = []          # (entry, outputs: list of (arr, slot, idx))
         self._run()
 
+    def _zeros(self, shape):
+        if self.backend == "torch":
+            return _Arr(self._torch.zeros(shape, dtype=self._torch.float64, device=self.P.v.device))
+        return _Arr(np.zeros(shape))
+
     # -- helpers -------------------------------------------------------------
     def _rec(self, name, ins, pars, outs):
-        y = _stage(self._t, name, self.efix if name.startswith("roe") else False, ins, pars)
+        if self.backend == "torch":
+            ins = [(a, slot, self._tix(idx)) for (a, slot, idx) in ins]
+            outs = [(a, slot, self._tix(idx)) for (a, slot, idx) in outs]
+        dev = str(self.P.v.device) if self.backend == "torch" else None
+        y = _stage(self._t, name, self.efix if name.startswith("roe") else False, ins, pars, self.backend, dev)
         entry = self._t.pop()
         for (a, slot, idx), val in zip(outs, y):
             tgt = a.v if slot is None else a.v[slot]
@@ -117,14 +141,14 @@ class Cycle:
         dt, dx, dy = self.dt, self.dx, self.dy
         J, I = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
         # ---- reconstruction + face states, x and y
-        self.XL, self.XR = _Arr(np.zeros((7, ny, nx + 1))), _Arr(np.zeros((7, ny, nx + 1)))
-        self.YL, self.YR = _Arr(np.zeros((7, ny + 1, nx))), _Arr(np.zeros((7, ny + 1, nx)))
+        self.XL, self.XR = self._zeros((7, ny, nx + 1)), self._zeros((7, ny, nx + 1))
+        self.YL, self.YR = self._zeros((7, ny + 1, nx)), self._zeros((7, ny + 1, nx))
         for ax in (0, 1):
             slots = X_SLOTS if ax == 0 else Y_SLOTS
             L = nx if ax == 0 else ny
             bc = self.bc[ax]
             dn = dx if ax == 0 else dy
-            E = _Arr(np.zeros((14, ny, nx)))      # lia(7) + ria(7) per cell
+            E = self._zeros((14, ny, nx))      # lia(7) + ria(7) per cell
             if self.order == 1:
                 def cell(off):
                     if ax == 0:
@@ -180,17 +204,17 @@ class Cycle:
                 self._rec(f"face{ax}", ins, [self.min_d, self.min_p, 0.5 * dt, 1.0 / dn],
                           [(out, k, (FJ, FF) if ax == 0 else (FF, FJ)) for k in range(7)])
         # ---- stage-1 Roe
-        self.F1X, self.F1Y = _Arr(np.zeros((7, ny, nx + 1))), _Arr(np.zeros((7, ny + 1, nx)))
+        self.F1X, self.F1Y = self._zeros((7, ny, nx + 1)), self._zeros((7, ny + 1, nx))
         self._roe(1, self.XL, self.XR, None, None, self.FX, self.F1X, 0)
         self._roe(1, self.YL, self.YR, None, None, self.FY, self.F1Y, 1)
         # ---- cell Ez and corner EMF
-        self.EZ = _Arr(np.zeros((ny, nx)))
+        self.EZ = self._zeros((ny, nx))
         self._rec("ez", [(P, 2, (J, I)), (P, 4, (J, I)), (P, 1, (J, I)), (P, 5, (J, I))], [],
                   [(self.EZ, None, (J, I))])
-        self.E1 = _Arr(np.zeros((ny + 1, nx + 1)))
+        self.E1 = self._zeros((ny + 1, nx + 1))
         self._emf(self.F1X, self.F1Y, self.EZ, self.E1)
         # ---- half-step faces
-        self.NBX, self.NBY = _Arr(np.zeros((ny, nx + 1))), _Arr(np.zeros((ny + 1, nx)))
+        self.NBX, self.NBY = self._zeros((ny, nx + 1)), self._zeros((ny + 1, nx))
         hj, hi = np.meshgrid(np.arange(ny), np.arange(nx + 1), indexing="ij")
         self._rec("fhx", [(FX, None, (hj, hi)), (self.E1, None, (hj + 1, hi)), (self.E1, None, (hj, hi))],
                   [0.5 * (dt / dy)], [(self.NBX, None, (hj, hi))])
@@ -198,14 +222,14 @@ class Cycle:
         self._rec("fhy", [(FY, None, (vj, vi)), (self.E1, None, (vj, vi + 1)), (self.E1, None, (vj, vi))],
                   [0.5 * (dt / dx)], [(self.NBY, None, (vj, vi))])
         # ---- CTU
-        self.UXL, self.UXR = _Arr(np.zeros((7, ny, nx + 1))), _Arr(np.zeros((7, ny, nx + 1)))
-        self.UYL, self.UYR = _Arr(np.zeros((7, ny + 1, nx))), _Arr(np.zeros((7, ny + 1, nx)))
-        self.WXL, self.WXR = _Arr(np.zeros((7, ny, nx + 1))), _Arr(np.zeros((7, ny, nx + 1)))
-        self.WYL, self.WYR = _Arr(np.zeros((7, ny + 1, nx))), _Arr(np.zeros((7, ny + 1, nx)))
+        self.UXL, self.UXR = self._zeros((7, ny, nx + 1)), self._zeros((7, ny, nx + 1))
+        self.UYL, self.UYR = self._zeros((7, ny + 1, nx)), self._zeros((7, ny + 1, nx))
+        self.WXL, self.WXR = self._zeros((7, ny, nx + 1)), self._zeros((7, ny, nx + 1))
+        self.WYL, self.WYR = self._zeros((7, ny + 1, nx)), self._zeros((7, ny + 1, nx))
         self._ctu(0)
         self._ctu(1)
         # ---- half-step cell Ez
-        self.HEZ = _Arr(np.zeros((ny, nx)))
+        self.HEZ = self._zeros((ny, nx))
         ins = [(C, k, (J, I)) for k in range(3)]
         ins += [(self.F1X, k, (J, I)) for k in range(3)] + [(self.F1X, k, (J, I + 1)) for k in range(3)]
         ins += [(self.F1Y, k, (J, I)) for k in range(3)] + [(self.F1Y, k, (J + 1, I)) for k in range(3)]
@@ -213,13 +237,13 @@ class Cycle:
                 (self.NBY, None, (J + 1, I))]
         self._rec("half", ins, [0.5 * (dt / dx), 0.5 * (dt / dy)], [(self.HEZ, None, (J, I))])
         # ---- stage-2 Roe and EMF
-        self.F2X, self.F2Y = _Arr(np.zeros((7, ny, nx + 1))), _Arr(np.zeros((7, ny + 1, nx)))
+        self.F2X, self.F2Y = self._zeros((7, ny, nx + 1)), self._zeros((7, ny + 1, nx))
         self._roe(2, self.WXL, self.WXR, self.UXL, self.UXR, self.NBX, self.F2X, 0)
         self._roe(2, self.WYL, self.WYR, self.UYL, self.UYR, self.NBY, self.F2Y, 1)
-        self.E2 = _Arr(np.zeros((ny + 1, nx + 1)))
+        self.E2 = self._zeros((ny + 1, nx + 1))
         self._emf(self.F2X, self.F2Y, self.HEZ, self.E2)
         # ---- final update
-        self.NP, self.NC = _Arr(np.zeros_like(P.v)), _Arr(np.zeros_like(C.v))
+        self.NP, self.NC = self._zeros(tuple(P.v.shape)), self._zeros(tuple(C.v.shape))
         E2 = self.E2
         ins = [(FX, None, (J, I)), (FX, None, (J, I + 1)), (FY, None, (J, I)), (FY, None, (J + 1, I)),
                (E2, None, (J, I)), (E2, None, (J + 1, I)), (E2, None, (J, I + 1)), (E2, None, (J + 1, I + 1))]
@@ -228,11 +252,14 @@ class Cycle:
         ins += [(self.F2Y, k, (J, I)) for k in range(7)] + [(self.F2Y, k, (J + 1, I)) for k in range(7)]
         outs = [(self.NP, k, (J, I)) for k in range(8)] + [(self.NC, k, (J, I)) for k in range(8)]
         self._rec("final", ins, [dt / dx, dt / dy, g], outs)
-        self.NFX, self.NFY = _Arr(np.zeros_like(FX.v)), _Arr(np.zeros_like(FY.v))
+        self.NFX, self.NFY = self._zeros(tuple(FX.v.shape)), self._zeros(tuple(FY.v.shape))
         self._rec("fhx", [(FX, None, (hj, hi)), (E2, None, (hj + 1, hi)), (E2, None, (hj, hi))],
                   [dt / dy], [(self.NFX, None, (hj, hi))])
         self._rec("fhy", [(FY, None, (vj, vi)), (E2, None, (vj, vi + 1)), (E2, None, (vj, vi))],
                   [dt / dx], [(self.NFY, None, (vj, vi))])
+
+    def _tix(self, idx):
+        return tuple(self._torch.as_tensor(np.asarray(i), device=self.P.v.device) for i in idx)
 
     def _rec_copy(self, src, s, dst, k):
         """dst[k] = src[s] (first-order edges), recorded as an identity stage."""

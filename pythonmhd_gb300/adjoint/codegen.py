@@ -46,7 +46,8 @@ def generate() -> str:
     for name, fn, nin, npar, kw in STAGES:
         t = dsl.trace(f"g_{name}", fn, nin, npar, **kw)
         parts.append(f"// ---- {name}: {nin} inputs, {npar} params, {len(t.outputs)} outputs\n")
-        parts.append(f"constexpr int g_{name}_NI = {nin}, g_{name}_NP = {max(npar, 1)}, g_{name}_NO = {len(t.outputs)};\n")
+        parts.append(f"constexpr int g_{name}_NI = {nin}, g_{name}_NP = {max(npar, 1)}, g_{name}_NO = {len(t.outputs)}, "
+                     f"g_{name}_NT = {dsl.tape_words(t)};\n")
         parts.append(dsl.emit_cuda(t))
     return "\n".join(parts)
 

@@ -23,6 +23,7 @@ both depend on an input and reach an output.
 from __future__ import annotations
 
 import math
+import re
 
 
 class Trace:
@@ -277,58 +278,66 @@ def _c_lit(x):
     return r
 
 
-def _rev_lines_c(t, act):
+def _rev_lines_c(t, act, first_of=None):
     """CUDA adjoint statements in reverse order.  b{i} is the adjoint of node i.
 
-    Only a contribution that multiplies the incoming adjoint by a forward value
-    is guarded by ``nz(b)``: a branch not taken may hold a non-finite value
-    (e.g. w/bt with bt == 0) and 0 * inf must not reach the result.  Sums,
-    differences and selects pass the adjoint through unguarded.  A quotient's
-    two contributions share one division.  These statements may contract into
-    FMAs: the adjoint is not required to round like the NumPy reverse sweep.
+    Each adjoint is declared by its first contribution (no zero start, so no
+    extra addition).  Only a contribution that multiplies the incoming adjoint
+    by a forward value is guarded by ``nz(b)``: a branch not taken may hold a
+    non-finite value (e.g. w/bt with bt == 0) and 0 * inf must not reach the
+    result.  Sums, differences and selects pass the adjoint through unguarded.
+    A quotient's two contributions share one division.  These statements may
+    contract into FMAs: the adjoint is not required to round like the NumPy
+    reverse sweep.
     """
     L = []
+    declared = set() if first_of is None else first_of
+
+    def acc(j, expr, guard=None, neg=False):
+        if not act[j]:
+            return
+        if j not in declared:
+            declared.add(j)
+            e = f"-({expr})" if neg else expr
+            L.append(f"double b{j} = {guard} ? {e} : 0.0" if guard else f"double b{j} = {e}")
+        else:
+            op = "-=" if neg else "+="
+            L.append(f"if ({guard}) b{j} {op} {expr}" if guard else f"b{j} {op} {expr}")
+
+    for k, o in enumerate(t.outputs):
+        if act[o]:
+            acc(o, f"ybar[{k}]")
     for i in range(len(t.nodes) - 1, -1, -1):
         op, args, meta, kind = t.nodes[i]
         if not act[i] or kind != "f" or op == "input":
             continue
         b = f"b{i}"
-        ac = [act[j] for j in args]
         if op == "add":
-            for j, on in zip(args, ac):
-                if on:
-                    L.append(f"b{j} += {b}")
+            acc(args[0], b)
+            acc(args[1], b)
         elif op == "sub":
-            if ac[0]:
-                L.append(f"b{args[0]} += {b}")
-            if ac[1]:
-                L.append(f"b{args[1]} -= {b}")
+            acc(args[0], b)
+            acc(args[1], b, neg=True)
         elif op == "neg":
-            L.append(f"b{args[0]} -= {b}")
+            acc(args[0], b, neg=True)
         elif op == "mul":
-            parts = []
-            if ac[0]:
-                parts.append(f"b{args[0]} += {b} * v{args[1]};")
-            if ac[1]:
-                parts.append(f"b{args[1]} += {b} * v{args[0]};")
-            if parts:
-                L.append(f"if (nz({b})) {{ " + " ".join(parts) + " }")
+            if act[args[0]] or act[args[1]]:
+                L.append(f"const bool g{i} = nz({b})")
+            acc(args[0], f"{b} * v{args[1]}", guard=f"g{i}")
+            acc(args[1], f"{b} * v{args[0]}", guard=f"g{i}")
         elif op == "div":
-            parts = [f"const double q_ = {b} / v{args[1]};"]
-            if ac[0]:
-                parts.append(f"b{args[0]} += q_;")
-            if ac[1]:
-                parts.append(f"b{args[1]} -= q_ * v{i};")
-            L.append(f"if (nz({b})) {{ " + " ".join(parts) + " }")
+            # the quotient may be non-finite on a branch not taken: guard its use
+            L.append(f"const bool g{i} = nz({b})")
+            L.append(f"const double q{i} = g{i} ? {b} / v{args[1]} : 0.0")
+            acc(args[0], f"q{i}")
+            acc(args[1], f"q{i} * v{i}", guard=f"g{i}", neg=True)
         elif op == "sqrt":
-            L.append(f"if (nz({b}) && v{i} > 0.0) b{args[0]} += (0.5 * {b}) / v{i}")
+            acc(args[0], f"(0.5 * {b}) / v{i}", guard=f"(nz({b}) && v{i} > 0.0)")
         elif op == "abs":
-            L.append(f"b{args[0]} += (v{args[0]} >= 0.0 ? {b} : -{b})")
+            acc(args[0], f"(v{args[0]} >= 0.0 ? {b} : -{b})")
         elif op == "sel":
-            if act[args[1]]:
-                L.append(f"b{args[1]} += (v{args[0]} ? {b} : 0.0)")
-            if act[args[2]]:
-                L.append(f"b{args[2]} += (v{args[0]} ? 0.0 : {b})")
+            acc(args[1], f"(v{args[0]} ? {b} : 0.0)")
+            acc(args[2], f"(v{args[0]} ? 0.0 : {b})")
         else:
             raise ValueError(op)
     return L
@@ -414,8 +423,55 @@ def emit_numpy(t, reverse=False):
     return "\n".join(src) + "\n"
 
 
+def _reverse_needs_c(t, act):
+    """Forward values the CUDA reverse statements (``_rev_lines_c``) read."""
+    need = set()
+    for i, (op, args, meta, kind) in enumerate(t.nodes):
+        if not act[i] or kind != "f":
+            continue
+        if op == "mul":
+            if act[args[0]]:
+                need.add(args[1])
+            if act[args[1]]:
+                need.add(args[0])
+        elif op == "div":
+            need.add(args[1])
+            if act[args[1]]:
+                need.add(i)
+        elif op == "sqrt":
+            need.add(i)
+        elif op == "abs":
+            need.add(args[0])
+        elif op == "sel":
+            need.add(args[0])
+    return need
+
+
+def tape_layout(t):
+    """(float nodes, bool nodes) the reverse sweep reads that are computed, not inputs,
+    parameters or constants: what a forward sweep stores on the tape."""
+    need = _reverse_needs_c(t, _active(t))
+    fl = sorted(i for i in need if t.nodes[i][3] == "f" and t.nodes[i][0] not in ("input", "param", "const"))
+    bl = sorted(i for i in need if t.nodes[i][3] == "b")
+    return fl, bl
+
+
+def tape_words(t):
+    fl, bl = tape_layout(t)
+    return len(fl) + (len(bl) + 31) // 32
+
+
 def emit_cuda(t, reverse=True):
-    """CUDA source of ``<name>_fwd(x, p, y)`` and ``<name>_rev(x, p, ybar, xbar)`` for one item."""
+    """CUDA source for one item of a traced function:
+
+    * ``<name>_fwd(x, p, y)``: forward;
+    * ``<name>_rev(x, p, ybar, xbar)``: forward recomputation, then the reverse sweep;
+    * ``<name>_fwdt(x, p, y, tape, stride)``: forward that also stores the values
+      the reverse sweep reads (``tape_layout``) at tape[k * stride] (booleans
+      packed 32 to a word);
+    * ``<name>_revt(x, p, ybar, xbar, tape, stride)``: the reverse sweep reading
+      those values back instead of recomputing the forward.
+    """
     act = _active(t)
     need_out = set(t.outputs)
     out = []
@@ -431,26 +487,206 @@ def emit_cuda(t, reverse=True):
     for k, o in enumerate(t.outputs):
         out.append(f"  y[{k}] = v{o};")
     out.append("}")
-    if reverse:
-        need = need_out | _reverse_needs(t, act)
-        live = _live_forward(t, need)
-        out.append(f"__device__ __forceinline__ void {t.name}_rev(const double* __restrict__ x, "
-                   f"const double* __restrict__ p, const double* __restrict__ ybar, double* __restrict__ xbar) {{")
-        for v, e, kind in _fwd_lines(t, live, "c"):
-            ty = "double" if kind == "f" else "bool"
-            out.append(f"  const {ty} {v} = {e};")
-        for i in range(len(t.nodes)):
-            if act[i] and t.nodes[i][3] == "f":
-                out.append(f"  double b{i} = 0.0;")
-        for k, o in enumerate(t.outputs):
-            if act[o]:
-                out.append(f"  b{o} = b{o} + ybar[{k}];")
-        for line in _rev_lines_c(t, act):
-            out.append("  " + line + ("" if line.endswith("}") else ";"))
-        for k, i in enumerate(t.inputs):
-            out.append(f"  xbar[{k}] = {'b%d' % i if act[i] else '0.0'};")
-        out.append("}")
+    if not reverse:
+        return "\n".join(out) + "\n"
+    need = need_out | _reverse_needs_c(t, act)
+    live = _live_forward(t, need)
+    out.append(f"__device__ __forceinline__ void {t.name}_rev(const double* __restrict__ x, "
+               f"const double* __restrict__ p, const double* __restrict__ ybar, double* __restrict__ xbar) {{")
+    for v, e, kind in _fwd_lines(t, live, "c"):
+        ty = "double" if kind == "f" else "bool"
+        out.append(f"  const {ty} {v} = {e};")
+    declared = set()
+    for line in _rev_lines_c(t, act, declared):
+        out.append("  " + line + ";")
+    for k, i in enumerate(t.inputs):
+        out.append(f"  xbar[{k}] = {'b%d' % i if i in declared else '0.0'};")
+    out.append("}")
+    # taped pair
+    fl, bl = tape_layout(t)
+    fslot = {i: k for k, i in enumerate(fl)}
+    bslot = {i: (len(fl) + k // 32, k % 32) for k, i in enumerate(bl)}
+    nbw = (len(bl) + 31) // 32
+    live_out = _live_forward(t, need_out | set(fl) | set(bl))
+    out.append(f"__device__ __forceinline__ void {t.name}_fwdt(const double* __restrict__ x, "
+               f"const double* __restrict__ p, double* __restrict__ y, double* __restrict__ tape, size_t stride) {{")
+    for w in range(nbw):
+        out.append(f"  unsigned int tw{w} = 0u;")
+    for v, e, kind in _fwd_lines(t, live_out, "c"):
+        ty = "double" if kind == "f" else "bool"
+        out.append(f"  const {ty} {v} = {e};")
+        i = int(v[1:])
+        if i in fslot:
+            out.append(f"  tape[{fslot[i]} * stride] = {v};")
+        elif i in bslot:
+            w, bit = bslot[i]
+            out.append(f"  tw{w - len(fl)} |= (unsigned int){v} << {bit};")
+    for w in range(nbw):
+        out.append(f"  tape[{len(fl) + w} * stride] = __hiloint2double(0, (int)tw{w});")
+    for k, o in enumerate(t.outputs):
+        out.append(f"  y[{k}] = v{o};")
+    out.append("}")
+    out.append(f"__device__ __forceinline__ void {t.name}_revt(const double* __restrict__ x, "
+               f"const double* __restrict__ p, const double* __restrict__ ybar, double* __restrict__ xbar, "
+               f"const double* __restrict__ tape, size_t stride) {{")
+    # each forward value is loaded right before the first reverse statement that
+    # reads it, which keeps live ranges (and register pressure) short
+    loaded, words_loaded = set(), set()
+
+    def load(i):
+        op, args, meta, kind = t.nodes[i]
+        if op == "input":
+            return [f"const double v{i} = x[{meta}]"]
+        if op == "param":
+            return [f"const double v{i} = p[{meta}]"]
+        if op == "const":
+            return [f"const double v{i} = {_c_lit(meta)}"]
+        if i in fslot:
+            return [f"const double v{i} = tape[{fslot[i]} * stride]"]
+        w, bit = bslot[i]
+        pre = []
+        if w not in words_loaded:
+            words_loaded.add(w)
+            pre.append(f"const unsigned int tw{w - len(fl)} = (unsigned int)__double2loint(tape[{w} * stride])")
+        return pre + [f"const bool v{i} = (tw{w - len(fl)} >> {bit}) & 1u"]
+
+    declared = set()
+    for line in _rev_lines_c(t, act, declared):
+        for m in re.findall(r"\bv(\d+)\b", line):
+            i = int(m)
+            if i not in loaded:
+                loaded.add(i)
+                for ld in load(i):
+                    out.append("  " + ld + ";")
+        out.append("  " + line + ";")
+    for k, i in enumerate(t.inputs):
+        out.append(f"  xbar[{k}] = {'b%d' % i if i in declared else '0.0'};")
+    out.append("}")
     return "\n".join(out) + "\n"
+
+
+def emit_torch(t):
+    """Python source of ``fwd(x, p) -> outs`` over torch tensors (forward only, for
+    torch's own automatic differentiation)."""
+    live = _live_forward(t, set(t.outputs))
+    src = [f"def {t.name}_fwd(x, p):"]
+    for i, (op, args, meta, kind) in enumerate(t.nodes):
+        if not live[i]:
+            continue
+        a = [f"v{x}" for x in args]
+        if op == "const":
+            e = repr(meta)
+        elif op == "input":
+            e = f"x[{meta}]"
+        elif op == "param":
+            e = f"p[{meta}]"
+        elif op == "div":
+            e = f"_div({a[0]}, {a[1]})"
+        elif op in _PY_BIN:
+            e = f"_t({a[0]}) {_PY_BIN[op]} _t({a[1]})"
+        elif op == "neg":
+            e = f"-{a[0]}"
+        elif op == "sqrt":
+            e = f"_sqrt({a[0]})"
+        elif op == "abs":
+            e = f"_abs({a[0]})"
+        elif op in _CMP:
+            e = f"_t({a[0]}) {_CMP[op]} {a[1]}"
+        elif op == "and":
+            e = f"{a[0]} & {a[1]}"
+        elif op == "or":
+            e = f"{a[0]} | {a[1]}"
+        elif op == "not":
+            e = f"~{a[0]}"
+        elif op == "sel":
+            e = f"_where({a[0]}, {a[1]}, {a[2]})"
+        else:
+            raise ValueError(op)
+        src.append(f"    v{i} = {e}")
+    src.append("    return [" + ", ".join(f"v{o}" for o in t.outputs) + "]")
+    return "\n".join(src) + "\n"
+
+
+_TORCH_SQRT = None
+
+
+def _torch_sqrt():
+    """Correctly rounded float64 square root for torch tensors with its derivative
+    rules (reverse and forward mode).  torch's CPU sqrt is not correctly rounded;
+    the value comes from NumPy on the host, or from torch on a CUDA device, where
+    sqrt is IEEE round-to-nearest."""
+    global _TORCH_SQRT
+    if _TORCH_SQRT is None:
+        import numpy as np
+        import torch
+
+        class Sqrt(torch.autograd.Function):
+            @staticmethod
+            def forward(x):
+                if x.is_cuda:
+                    return torch.sqrt(x)
+                return torch.from_numpy(np.sqrt(x.detach().numpy()))
+
+            @staticmethod
+            def setup_context(ctx, inputs, output):
+                ctx.save_for_backward(output)
+                ctx.save_for_forward(output)
+
+            @staticmethod
+            def backward(ctx, g):
+                (y,) = ctx.saved_tensors
+                return g * (0.5 / y)
+
+            @staticmethod
+            def jvp(ctx, t):
+                (y,) = ctx.saved_tensors
+                return t * (0.5 / y)
+
+        _TORCH_SQRT = Sqrt.apply
+    return _TORCH_SQRT
+
+
+def compile_torch(t, device=None):
+    """Executable torch forward function of a trace on ``device``.
+
+    Constants become tensors on that device: torch computes a tensor divided by a
+    host scalar through the scalar's reciprocal, which rounds differently.
+    Quotients and square roots use the masked ("double where") form, so torch's
+    reverse mode never forms 0 * inf on a branch not taken: the divisor or
+    radicand is replaced by 1 where it is zero (not positive, for the root) and
+    the value by 0 there -- the same convention as the hand-written reverse
+    sweeps, and the same values wherever a result is finite.  |x| is
+    differentiated as +1 at 0, like the hand-written sweeps.
+    """
+    import torch
+
+    dev = torch.device(device) if device is not None else torch.device("cpu")
+
+    def _t(x):
+        return x if isinstance(x, torch.Tensor) else torch.tensor(x, dtype=torch.float64, device=dev)
+
+    def _where(c, a, b):
+        return torch.where(c, _t(a), _t(b))
+
+    sq = _torch_sqrt()
+
+    def _div(a, b):
+        a, b = _t(a), _t(b)
+        z = b == 0.0
+        return torch.where(z, 0.0, a / torch.where(z, 1.0, b))
+
+    def _sqrt(x):
+        x = _t(x)
+        pos = x > 0.0
+        return torch.where(pos, sq(torch.where(pos, x, 1.0)), x * 0.0)
+
+    def _abs(x):
+        x = _t(x)
+        return torch.where(x >= 0.0, x, -x)
+
+    ns = {"_sqrt": _sqrt, "_abs": _abs, "_t": _t, "_where": _where, "_div": _div}
+    exec(compile(emit_torch(t), f"<dsl-torch:{t.name}>", "exec"), ns)
+    return ns[f"{t.name}_fwd"]
 
 
 def compile_numpy(t, reverse=False):

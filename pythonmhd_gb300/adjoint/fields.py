@@ -42,15 +42,20 @@ def turbulence_fields(n, seed=1, gamma=5.0 / 3.0, kmax_v=16, kmax_a=16, mach=1.0
     cbx = (fbx_u[:, :-1] + fbx_u[:, 1:]) / (2.0 * dy)
     cby = (fby_u[:-1, :] + fby_u[1:, :]) / (2.0 * dx)
     az = az * np.sqrt(2.0 * (1.0 / gamma) / beta / np.mean(cbx * cbx + cby * cby))
-    return dict(rho=rho, vx=vx, vy=vy, p=p, az=az, dx=dx, dy=dy, gamma=gamma)
+    return dict(rho=rho, vx=vx, vy=vy, p=p, az=az, dx=dx, dy=dy, gamma=gamma, kmax_v=kmax_v, kmax_a=kmax_a)
 
 
 def perturbed(fields, frac, seed):
-    """The fields with rho, vx, vy, p and A_z each multiplied by (1 + frac N(0,1)) (seeded)."""
+    """The fields with rho, vx, vy, p and A_z each multiplied by (1 + frac g), g a
+    seeded unit-variance Gaussian random field with the generator's spectrum
+    (k^-2 up to kmax_v; k^-3 up to kmax_a for A_z): a smooth perturbation."""
     rng = np.random.default_rng(seed)
+    n = fields["rho"].shape[0]
     out = dict(fields)
     for k in ("rho", "vx", "vy", "p", "az"):
-        out[k] = fields[k] * (1.0 + frac * rng.standard_normal(fields[k].shape))
+        slope, kmax = (3.0, fields["kmax_a"]) if k == "az" else (2.0, fields["kmax_v"])
+        g = ic._gaussian_field(rng, n, slope, 1.0, kmax)
+        out[k] = fields[k] * (1.0 + frac * (g / g.std()))
     return out
 
 

@@ -26,6 +26,10 @@
 namespace {
 
 constexpr int kT = 128;
+static_assert(g_plm0_NT == g_plm1_NT && g_roe1_0_NT == g_roe1_1_NT && g_roe2_0_NT == g_roe2_1_NT &&
+                  g_ctu0_NT == g_ctu1_NT &&
+                  g_roe1_0_efix_NT == g_roe1_1_efix_NT && g_roe2_0_efix_NT == g_roe2_1_efix_NT,
+              "the x and y sweeps of a stage store tapes of the same length");
 
 struct Arr {
   double* v = nullptr;   // values
@@ -47,6 +51,11 @@ struct Adj {
   Arr HEZ, F2X, F2Y, E2;           // half-step Ez, stage-2 fluxes and EMF
   Arr NP, NC, NFX, NFY;            // output state
   double* red;                     // 2 doubles: CFL maxima (bits)
+  // tapes of the heavy stages (values their reverse sweeps read), plane-major:
+  // PLM per cell and sweep, Roe per face, stage and sweep
+  double* tplm[2];
+  double* troe[2][2];              // [stage-1][axis]
+  double* tctu[2];                 // CTU per (face, side) and sweep
 };
 
 __device__ __forceinline__ int wrapc(int c, int L, int bc) {
@@ -70,7 +79,7 @@ __device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a
   do {                                                                            \
     double x_[g_##NAME##_NI];                                                     \
     _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_) x_[k_] = *INS[k_].v; \
-    if (!(REV)) {                                                                 \
+    if constexpr (!(REV)) {                                                       \
       double y_[g_##NAME##_NO];                                                   \
       g_##NAME##_fwd(x_, PAR, y_);                                                \
       _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) *OUTS[k_].v = y_[k_]; \
@@ -83,10 +92,36 @@ __device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a
     }                                                                             \
   } while (0)
 
+// the same with a tape: the forward stores what the reverse reads, the reverse
+// reads it back instead of recomputing the forward
+#define MHD_ADJ_APPLY_T(NAME, REV, INS, OUTS, PAR, TP, ST)                        \
+  do {                                                                            \
+    double x_[g_##NAME##_NI];                                                     \
+    _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_) x_[k_] = *INS[k_].v; \
+    if constexpr (!(REV)) {                                                       \
+      double y_[g_##NAME##_NO];                                                   \
+      g_##NAME##_fwdt(x_, PAR, y_, TP, ST);                                       \
+      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) *OUTS[k_].v = y_[k_]; \
+    } else {                                                                      \
+      double yb_[g_##NAME##_NO], xb_[g_##NAME##_NI];                              \
+      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) yb_[k_] = *OUTS[k_].b; \
+      g_##NAME##_revt(x_, PAR, yb_, xb_, TP, ST);                                 \
+      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_)               \
+        if (xb_[k_] != 0.0) atomicAdd(INS[k_].b, xb_[k_]);                        \
+    }                                                                             \
+  } while (0)
+
+// taped or plain application of a stage
+#define MHD_ADJ_STAGE(NAME, REV, TAPE, INS, OUTS, PAR, TP, ST)                    \
+  do {                                                                            \
+    if constexpr (TAPE) MHD_ADJ_APPLY_T(NAME, REV, INS, OUTS, PAR, TP, ST);       \
+    else MHD_ADJ_APPLY(NAME, REV, INS, OUTS, PAR);                                \
+  } while (0)
+
 // ---------------------------------------------------------------------------
 // stage kernels (REV = false: forward with stored intermediates; true: reverse)
 // ---------------------------------------------------------------------------
-template <int AX, bool REV>
+template <int AX, bool REV, bool TAPE>
 __global__ void __launch_bounds__(kT) k_recon(Adj A) {
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
   if (c0 >= A.nx || t0 >= A.ny) return;
@@ -109,8 +144,10 @@ __global__ void __launch_bounds__(kT) k_recon(Adj A) {
 #pragma unroll
     for (int k = 0; k < 14; ++k) out[k] = io(E, k, me);
     const double par[2] = {A.gamma, A.dt / (AX == 0 ? A.dx : A.dy)};
-    if (AX == 0) MHD_ADJ_APPLY(plm0, REV, in, out, par);
-    else MHD_ADJ_APPLY(plm1, REV, in, out, par);
+    double* tp = A.tplm[AX] + me;
+    const size_t st = (size_t)A.nx * A.ny;
+    if (AX == 0) MHD_ADJ_STAGE(plm0, REV, TAPE, in, out, par, tp, st);
+    else MHD_ADJ_STAGE(plm1, REV, TAPE, in, out, par, tp, st);
   } else {
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
@@ -176,7 +213,7 @@ __global__ void __launch_bounds__(kT) k_face(Adj A) {
   else MHD_ADJ_APPLY(face1, REV, in, out, par);
 }
 
-template <int AX, int STAGE, bool REV>
+template <int AX, int STAGE, bool REV, bool TAPE>
 __global__ void __launch_bounds__(kT) k_roe(Adj A) {
   const size_t nf = AX == 0 ? (size_t)(A.nx + 1) * A.ny : (size_t)A.nx * (A.ny + 1);
   const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -186,6 +223,7 @@ __global__ void __launch_bounds__(kT) k_roe(Adj A) {
   const Arr& BN = STAGE == 1 ? (AX == 0 ? A.FX : A.FY) : (AX == 0 ? A.NBX : A.NBY);
   const Arr& F = STAGE == 1 ? (AX == 0 ? A.F1X : A.F1Y) : (AX == 0 ? A.F2X : A.F2Y);
   const double par[2] = {A.gamma, A.eps};
+  double* tp = A.troe[STAGE - 1][AX] + f;
   IO out[7];
 #pragma unroll
   for (int k = 0; k < 7; ++k) out[k] = io(F, k, f);
@@ -195,11 +233,11 @@ __global__ void __launch_bounds__(kT) k_roe(Adj A) {
     for (int k = 0; k < 7; ++k) { in[k] = io(WL, k, f); in[7 + k] = io(WR, k, f); }
     in[14] = io(BN, 0, f);
     if (A.efix) {
-      if (AX == 0) MHD_ADJ_APPLY(roe1_0_efix, REV, in, out, par);
-      else MHD_ADJ_APPLY(roe1_1_efix, REV, in, out, par);
+      if (AX == 0) MHD_ADJ_STAGE(roe1_0_efix, REV, TAPE, in, out, par, tp, nf);
+      else MHD_ADJ_STAGE(roe1_1_efix, REV, TAPE, in, out, par, tp, nf);
     } else {
-      if (AX == 0) MHD_ADJ_APPLY(roe1_0, REV, in, out, par);
-      else MHD_ADJ_APPLY(roe1_1, REV, in, out, par);
+      if (AX == 0) MHD_ADJ_STAGE(roe1_0, REV, TAPE, in, out, par, tp, nf);
+      else MHD_ADJ_STAGE(roe1_1, REV, TAPE, in, out, par, tp, nf);
     }
   } else {
     const Arr& UL = AX == 0 ? A.UXL : A.UYL;
@@ -212,11 +250,11 @@ __global__ void __launch_bounds__(kT) k_roe(Adj A) {
     }
     in[28] = io(BN, 0, f);
     if (A.efix) {
-      if (AX == 0) MHD_ADJ_APPLY(roe2_0_efix, REV, in, out, par);
-      else MHD_ADJ_APPLY(roe2_1_efix, REV, in, out, par);
+      if (AX == 0) MHD_ADJ_STAGE(roe2_0_efix, REV, TAPE, in, out, par, tp, nf);
+      else MHD_ADJ_STAGE(roe2_1_efix, REV, TAPE, in, out, par, tp, nf);
     } else {
-      if (AX == 0) MHD_ADJ_APPLY(roe2_0, REV, in, out, par);
-      else MHD_ADJ_APPLY(roe2_1, REV, in, out, par);
+      if (AX == 0) MHD_ADJ_STAGE(roe2_0, REV, TAPE, in, out, par, tp, nf);
+      else MHD_ADJ_STAGE(roe2_1, REV, TAPE, in, out, par, tp, nf);
     }
   }
 }
@@ -277,7 +315,7 @@ __global__ void __launch_bounds__(kT) k_fhalf(Adj A) {
   }
 }
 
-template <int AX, bool REV>
+template <int AX, bool REV, bool TAPE>
 __global__ void __launch_bounds__(kT) k_ctu(Adj A) {
   const int nx = A.nx, ny = A.ny;
   const int Wd = AX == 0 ? nx + 1 : nx, H = AX == 0 ? ny : ny + 1;
@@ -333,8 +371,10 @@ __global__ void __launch_bounds__(kT) k_ctu(Adj A) {
   for (int k = 0; k < 7; ++k) { out[k] = io(U, k, me); out[7 + k] = io(W2, k, me); }
   const double par[6] = {A.gamma, 0.5 * A.dt, 1.0 / (AX == 0 ? A.dx : A.dy),
                          0.5 * (A.dt / (AX == 0 ? A.dy : A.dx)), A.min_d, A.min_e};
-  if (AX == 0) MHD_ADJ_APPLY(ctu0, REV, in, out, par);
-  else MHD_ADJ_APPLY(ctu1, REV, in, out, par);
+  const size_t nf = (size_t)H * Wd;
+  double* tp = A.tctu[AX] + side * nf + me;
+  if (AX == 0) MHD_ADJ_STAGE(ctu0, REV, TAPE, in, out, par, tp, 2 * nf);
+  else MHD_ADJ_STAGE(ctu1, REV, TAPE, in, out, par, tp, 2 * nf);
 }
 
 template <bool REV>
@@ -477,6 +517,9 @@ struct Handle {
   size_t W = 0;                // words of one arena (all arrays of one cycle)
   double* bars = nullptr;      // one adjoint arena
   double* vals = nullptr;      // nsets value arenas
+  size_t TW = 0;               // words of one tape arena
+  double* tapes = nullptr;     // nsets tape arenas
+  size_t toff[8] = {};         // tape offsets: plm x, plm y, roe1 x, roe1 y, roe2 x, roe2 y, ctu x, ctu y
   int nsets = 0;
   double* red = nullptr;       // CFL maxima (2) + dt (1)
   size_t budget = 0;           // bytes the stored-segment mode may use (0: 60% of free memory)
@@ -488,6 +531,7 @@ struct Handle {
   double* seg = nullptr;       // recompute mode: packed states of the current segment
   size_t ckpt_bytes = 0, seg_bytes = 0;
   size_t state_words = 0;
+  void* solver = nullptr;      // exact-arithmetic production step: the CFL forward pass
 };
 
 int fail(cudaError_t e) { return e == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; }
@@ -507,19 +551,32 @@ void select_set(Handle* h, int k) {
     a.b = h->bars + h->off[i];
     a.ps = h->ps[i];
   }
+  double* tb = h->tapes + (size_t)k * h->TW;
+  h->A.tplm[0] = tb + h->toff[0];
+  h->A.tplm[1] = tb + h->toff[1];
+  h->A.troe[0][0] = tb + h->toff[2];
+  h->A.troe[0][1] = tb + h->toff[3];
+  h->A.troe[1][0] = tb + h->toff[4];
+  h->A.troe[1][1] = tb + h->toff[5];
+  h->A.tctu[0] = tb + h->toff[6];
+  h->A.tctu[1] = tb + h->toff[7];
 }
 
 int alloc_sets(Handle* h, int n) {
   if (h->nsets == n) return MHD_OK;
-  if (h->vals) { cudaFree(h->vals); h->vals = nullptr; h->nsets = 0; }
+  cudaFree(h->vals);
+  cudaFree(h->tapes);
+  h->vals = h->tapes = nullptr;
+  h->nsets = 0;
   CK(cudaMalloc(&h->vals, (size_t)n * h->W * sizeof(double)));
+  CK(cudaMalloc(&h->tapes, (size_t)n * h->TW * sizeof(double)));
   h->nsets = n;
   select_set(h, 0);
   return MHD_OK;
 }
 
 size_t device_bytes(const Handle* h) {
-  return (h->W * (1 + (size_t)h->nsets) + 4) * sizeof(double) + h->ckpt_bytes + h->seg_bytes;
+  return (h->W + (h->W + h->TW) * (size_t)h->nsets + 4) * sizeof(double) + h->ckpt_bytes + h->seg_bytes;
 }
 
 // copy a packed state [prim 8 | cons 8 | fbx | fby] into / out of four arrays
@@ -548,26 +605,28 @@ int unpack(Handle* h, const double* src, Arr& P, Arr& C, Arr& FX, Arr& FY, bool 
 dim3 g2(int w, int h, int z = 1) { return dim3((unsigned)((w + kT - 1) / kT), (unsigned)h, (unsigned)z); }
 unsigned g1(size_t n) { return (unsigned)((n + kT - 1) / kT); }
 
-// forward sweep of one cycle from the input arrays (P, C, FX, FY) with A.dt set
-int fwd_cycle(Handle* h) {
+// forward sweep of one cycle from the input arrays (P, C, FX, FY) with A.dt set;
+// TAPE: the PLM and Roe stages also write the tapes their reverse sweeps read
+template <bool TAPE>
+int fwd_cycle_t(Handle* h) {
   Adj& A = h->A;
   cudaStream_t s = h->stream;
   const int nx = A.nx, ny = A.ny;
-  k_recon<0, false><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_recon<1, false><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_recon<0, false, TAPE><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_recon<1, false, TAPE><<<g2(nx, ny), kT, 0, s>>>(A);
   k_face<0, false><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
   k_face<1, false><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
-  k_roe<0, 1, false><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
-  k_roe<1, 1, false><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_roe<0, 1, false, TAPE><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_roe<1, 1, false, TAPE><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
   k_ez<false><<<g2(nx, ny), kT, 0, s>>>(A);
   k_emf<1, false><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
   k_fhalf<0, false, false><<<g2(nx + 1, ny), kT, 0, s>>>(A);
   k_fhalf<1, false, false><<<g2(nx, ny + 1), kT, 0, s>>>(A);
-  k_ctu<0, false><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
-  k_ctu<1, false><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
+  k_ctu<0, false, TAPE><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
+  k_ctu<1, false, TAPE><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
   k_half<false><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_roe<0, 2, false><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
-  k_roe<1, 2, false><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_roe<0, 2, false, TAPE><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_roe<1, 2, false, TAPE><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
   k_emf<2, false><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
   k_final<false><<<g2(nx, ny), kT, 0, s>>>(A);
   k_fhalf<0, true, false><<<g2(nx + 1, ny), kT, 0, s>>>(A);
@@ -576,7 +635,10 @@ int fwd_cycle(Handle* h) {
   return MHD_OK;
 }
 
+int fwd_cycle(Handle* h, bool tape) { return tape ? fwd_cycle_t<true>(h) : fwd_cycle_t<false>(h); }
+
 // reverse sweep: output adjoints in NP/NC/NFX/NFY .b -> input adjoints in P/C/FX/FY .b
+// (reads the tapes of the last taped forward sweep of the selected arena)
 int rev_cycle(Handle* h) {
   Adj& A = h->A;
   cudaStream_t s = h->stream;
@@ -587,21 +649,21 @@ int rev_cycle(Handle* h) {
   k_fhalf<0, true, true><<<g2(nx + 1, ny), kT, 0, s>>>(A);
   k_final<true><<<g2(nx, ny), kT, 0, s>>>(A);
   k_emf<2, true><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
-  k_roe<1, 2, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
-  k_roe<0, 2, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_roe<1, 2, true, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_roe<0, 2, true, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
   k_half<true><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_ctu<1, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
-  k_ctu<0, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
+  k_ctu<1, true, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
+  k_ctu<0, true, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
   k_fhalf<1, false, true><<<g2(nx, ny + 1), kT, 0, s>>>(A);
   k_fhalf<0, false, true><<<g2(nx + 1, ny), kT, 0, s>>>(A);
   k_emf<1, true><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
   k_ez<true><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_roe<1, 1, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
-  k_roe<0, 1, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  k_roe<1, 1, true, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  k_roe<0, 1, true, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
   k_face<1, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
   k_face<0, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
-  k_recon<1, true><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_recon<0, true><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_recon<1, true, true><<<g2(nx, ny), kT, 0, s>>>(A);
+  k_recon<0, true, true><<<g2(nx, ny), kT, 0, s>>>(A);
   CK(cudaGetLastError());
   return MHD_OK;
 }
@@ -640,6 +702,42 @@ int bars_in_to_out(Handle* h) {
   return MHD_OK;
 }
 
+// Forward pass with the CFL dt on the production exact-arithmetic step (the same
+// arithmetic as the stage kernels, bit for bit, and faster): one cycle per
+// advance call from t = 0, so the returned time is the cycle's dt exactly.
+int forward_on_solver(Handle* h, const double* state_in, int steps, double cfl, double* state_out) {
+  Adj& A = h->A;
+  const size_t cp = (size_t)A.nx * A.ny, xp = (size_t)(A.nx + 1) * A.ny;
+  if (!h->solver) {
+    int rc = mhd2d_create(A.ny, A.nx, A.dx, A.dy, A.bcx, A.bcy, A.gamma, MHD2D_MHD, A.recon, A.efix, A.eps,
+                          A.min_d, A.min_p, A.min_e, MHD2D_ARITH_EXACT, &h->solver);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  int rc = mhd2d_upload_device(h->solver, state_in, state_in + 8 * cp, state_in + 16 * cp, state_in + 16 * cp + xp);
+  if (rc) return rc;
+  auto save = [&](double* dst) -> int {
+    double *p = nullptr, *c = nullptr, *bx = nullptr, *by = nullptr;
+    int r = mhd2d_state_ptrs(h->solver, 0, &p, &c, &bx, &by);
+    if (r) return r;
+    Arr P, C, FX, FY;
+    P.v = p; C.v = c; FX.v = bx; FY.v = by;
+    return pack(h, dst, P, C, FX, FY, false);
+  };
+  for (int c = 0; c < steps; ++c) {
+    if (c % h->every == 0 && (rc = save(h->ckpt + (size_t)(c / h->every) * h->state_words))) return rc;
+    // the copy above is on this handle's stream; the solver runs on its own
+    CK(cudaStreamSynchronize(h->stream));
+    double t = 0.0;
+    long long cyc = 0;
+    if ((rc = mhd2d_advance(h->solver, 0.0, 1e300, 0, 1, cfl, &t, &cyc, nullptr))) return rc;
+    if (cyc != 1 || !std::isfinite(t)) return MHD_ERR_NONFINITE;
+    h->dts[c] = t;
+  }
+  if ((rc = save(state_out))) return rc;
+  return MHD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -665,6 +763,19 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
     w = (w + 31) & ~(size_t)31;   // 256-byte aligned planes groups
   }
   h->W = w;
+  // tapes: PLM per cell and sweep (first order has no reconstruction stage),
+  // Roe per face, stage and sweep, CTU per face side and sweep
+  const int nt_plm = recon == 1 ? g_plm0_NT : 0;
+  const int nt_roe[2] = {A.efix ? g_roe1_0_efix_NT : g_roe1_0_NT, A.efix ? g_roe2_0_efix_NT : g_roe2_0_NT};
+  const size_t items[8] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2]};
+  const int words[8] = {nt_plm, nt_plm, nt_roe[0], nt_roe[0], nt_roe[1], nt_roe[1], g_ctu0_NT, g_ctu0_NT};
+  size_t tw = 0;
+  for (int i = 0; i < 8; ++i) {
+    h->toff[i] = tw;
+    tw += items[i] * (size_t)words[i];
+    tw = (tw + 31) & ~(size_t)31;
+  }
+  h->TW = tw;
   h->state_words = state_words(A);
   int rc = MHD_OK;
   cudaError_t e = cudaMalloc(&h->bars, h->W * sizeof(double));
@@ -679,6 +790,7 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
     cudaFree(h->bars);
     cudaFree(h->red);
     cudaFree(h->vals);
+    cudaFree(h->tapes);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return rc;
@@ -693,9 +805,11 @@ void mhd2d_adj_destroy(void* handle) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFree(h->bars);
   cudaFree(h->vals);
+  cudaFree(h->tapes);
   cudaFree(h->red);
   cudaFree(h->ckpt);
   cudaFree(h->seg);
+  if (h->solver) mhd2d_destroy(h->solver);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -715,7 +829,7 @@ int mhd2d_adj_cycle(void* handle, double dt, const double* state_in, double* sta
   A.dt = dt;
   int rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false);
   if (rc) return rc;
-  if ((rc = fwd_cycle(h))) return rc;
+  if ((rc = fwd_cycle(h, false))) return rc;
   if ((rc = pack(h, state_out, A.NP, A.NC, A.NFX, A.NFY, false))) return rc;
   CK(cudaStreamSynchronize(h->stream));
   return MHD_OK;
@@ -730,7 +844,7 @@ int mhd2d_adj_cycle_reverse(void* handle, double dt, const double* state_in, con
   A.dt = dt;
   int rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false);
   if (rc) return rc;
-  if ((rc = fwd_cycle(h))) return rc;
+  if ((rc = fwd_cycle(h, true))) return rc;
   if ((rc = unpack(h, bar_out, A.NP, A.NC, A.NFX, A.NFY, true))) return rc;
   if ((rc = rev_cycle(h))) return rc;
   if ((rc = pack(h, bar_in, A.P, A.C, A.FX, A.FY, true))) return rc;
@@ -756,10 +870,10 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
   // backward mode: keep all `every` cycles of a segment resident when they fit
   size_t free_b = 0, total_b = 0;
   CK(cudaMemGetInfo(&free_b, &total_b));
-  // (arenas this handle already holds count as free)
-  const size_t held = ((size_t)h->nsets - 1) * h->W * sizeof(double);
+  const size_t set_bytes = (h->W + h->TW) * sizeof(double);
+  const size_t held = ((size_t)h->nsets - 1) * set_bytes;
   const size_t budget = h->budget ? h->budget : (size_t)(0.6 * (double)(free_b + held));
-  const size_t extra = ((size_t)every - 1) * h->W * sizeof(double);
+  const size_t extra = ((size_t)every - 1) * set_bytes;
   h->stored = every > 1 && extra <= budget;
   int rc;
   if (h->stored) {
@@ -771,22 +885,24 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
   }
   h->every = every;
   h->dts.assign(steps, 0.0);
-  select_set(h, 0);
-  if ((rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false))) return rc;
-  for (int c = 0; c < steps; ++c) {
-    if (c % every == 0 &&
-        (rc = pack(h, h->ckpt + (size_t)(c / every) * h->state_words, A.P, A.C, A.FX, A.FY, false)))
-      return rc;
-    double dt;
-    if (fixed_dt) dt = fixed_dt[c];
-    else if ((rc = cfl_dt(h, cfl, &dt))) return rc;
-    if (!std::isfinite(dt)) return MHD_ERR_NONFINITE;
-    h->dts[c] = dt;
-    A.dt = dt;
-    if ((rc = fwd_cycle(h))) return rc;
-    if ((rc = output_to_input(h, 0, 0))) return rc;
+  if (!fixed_dt) {
+    if ((rc = forward_on_solver(h, state_in, steps, cfl, state_out))) return rc;
+  } else {
+    select_set(h, 0);
+    if ((rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false))) return rc;
+    for (int c = 0; c < steps; ++c) {
+      if (c % every == 0 &&
+          (rc = pack(h, h->ckpt + (size_t)(c / every) * h->state_words, A.P, A.C, A.FX, A.FY, false)))
+        return rc;
+      const double dt = fixed_dt[c];
+      if (!std::isfinite(dt)) return MHD_ERR_NONFINITE;
+      h->dts[c] = dt;
+      A.dt = dt;
+      if ((rc = fwd_cycle(h, false))) return rc;
+      if ((rc = output_to_input(h, 0, 0))) return rc;
+    }
+    if ((rc = pack(h, state_out, A.P, A.C, A.FX, A.FY, false))) return rc;
   }
-  if ((rc = pack(h, state_out, A.P, A.C, A.FX, A.FY, false))) return rc;
   CK(cudaStreamSynchronize(h->stream));
   h->steps = steps;
   if (dt_log) std::copy(h->dts.begin(), h->dts.end(), dt_log);
@@ -813,7 +929,7 @@ int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initia
       for (int k = 0; k < len; ++k) {
         select_set(h, k);
         A.dt = h->dts[c0 + k];
-        if ((rc = fwd_cycle(h))) return rc;
+        if ((rc = fwd_cycle(h, true))) return rc;
         if (k + 1 < len && (rc = output_to_input(h, k, k + 1))) return rc;
       }
       for (int k = len - 1; k >= 0; --k) {
@@ -828,14 +944,14 @@ int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initia
         if ((rc = pack(h, h->seg + (size_t)k * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
         if (k + 1 < len) {
           A.dt = h->dts[c0 + k];
-          if ((rc = fwd_cycle(h))) return rc;
+          if ((rc = fwd_cycle(h, false))) return rc;
           if ((rc = output_to_input(h, 0, 0))) return rc;
         }
       }
       for (int k = len - 1; k >= 0; --k) {
         A.dt = h->dts[c0 + k];
         if ((rc = unpack(h, h->seg + (size_t)k * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
-        if ((rc = fwd_cycle(h))) return rc;
+        if ((rc = fwd_cycle(h, true))) return rc;
         if ((rc = rev_cycle(h))) return rc;
         if ((rc = bars_in_to_out(h))) return rc;
       }
@@ -851,7 +967,11 @@ int mhd2d_adj_info(void* handle, size_t* state_words_out, size_t* device_bytes_o
   Handle* h = static_cast<Handle*>(handle);
   if (!h) return MHD_ERR_ARG;
   if (state_words_out) *state_words_out = h->state_words;
-  if (device_bytes_out) *device_bytes_out = device_bytes(h);
+  if (device_bytes_out) {
+    size_t solver_bytes = 0;
+    if (h->solver) mhd2d_device_bytes(h->solver, &solver_bytes);
+    *device_bytes_out = device_bytes(h) + solver_bytes;
+  }
   if (segment_sets) *segment_sets = h->stored ? h->every : 1;
   return MHD_OK;
 }

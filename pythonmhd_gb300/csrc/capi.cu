@@ -298,24 +298,34 @@ void mhd2d_destroy(void* handle) {
   delete h;
 }
 
-int mhd2d_upload(void* handle, const double* prim, const double* cons, const double* faceBx,
-                 const double* faceBy) {
+static int upload_state(void* handle, const double* prim, const double* cons, const double* faceBx,
+                        const double* faceBy, cudaMemcpyKind kind) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !prim || !cons) return MHD_ERR_ARG;
   const bool mhd = h->g.physics == MHD2D_MHD;
   if (mhd && (!faceBx || !faceBy)) return MHD_ERR_ARG;
   const mhdk::StateBuf& s = h->g.st[h->cur];
   const size_t cb = (size_t)h->nvars * mhdk::cell_plane(h->g) * sizeof(double);
-  CK(cudaMemcpyAsync(s.prim, prim, cb, cudaMemcpyHostToDevice, h->stream));
-  CK(cudaMemcpyAsync(s.cons, cons, cb, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(s.prim, prim, cb, kind, h->stream));
+  CK(cudaMemcpyAsync(s.cons, cons, cb, kind, h->stream));
   if (mhd) {
-    CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(h->g) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(h->g) * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(h->g) * sizeof(double), kind, h->stream));
+    CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(h->g) * sizeof(double), kind, h->stream));
   }
   CK(cudaStreamSynchronize(h->stream));
   h->have_state = 1;
   h->last_cycles_run = 0;
   return MHD_OK;
+}
+
+int mhd2d_upload(void* handle, const double* prim, const double* cons, const double* faceBx,
+                 const double* faceBy) {
+  return upload_state(handle, prim, cons, faceBx, faceBy, cudaMemcpyHostToDevice);
+}
+
+int mhd2d_upload_device(void* handle, const double* prim, const double* cons, const double* faceBx,
+                        const double* faceBy) {
+  return upload_state(handle, prim, cons, faceBx, faceBy, cudaMemcpyDeviceToDevice);
 }
 
 int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,

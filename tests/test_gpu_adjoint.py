@@ -90,6 +90,10 @@ def test_forward_equals_step_and_backward_equals_chained_vjps():
     assert g.last_cycles == steps
     for got, want in zip(_np(a.unpack(out)), g.download()):
         np.testing.assert_array_equal(got, want)
+    # the stage kernels (the fixed-dt forward, and the backward's recomputation)
+    # give the same states
+    for got, want in zip(_np(a.unpack(a.forward(s0, steps, dts=dts))), g.download()):
+        np.testing.assert_array_equal(got, want)
     rng = np.random.default_rng(3)
     bar = torch.tensor(rng.standard_normal(a.state_words), device=s0.device)
     grads = {}
@@ -169,3 +173,31 @@ def test_gradient_matches_finite_differences(n, steps, ndir, p_jitter):
             errs.append(abs(fd - ad) / abs(fd))
         worst = max(worst, min(errs))
     assert worst <= 1e-5, worst
+
+
+def test_backward_matches_torch_autograd_of_transcription():
+    """Several cycles: the GPU backward equals torch's reverse mode through the
+    plain torch transcription of the step (run on the GPU, frozen dts), whose
+    forward equals the GPU forward bit for bit."""
+    n, steps = 48, 6
+    dev = torch.device("cuda", 0)
+    p, c, bx, by, dx, dy = _turb_state(n, 8)
+    a = Adjoint2D(n, n, dx, dy, 1, 1, GAMMA, recon=1)
+    s0 = a.pack(p, c, bx, by)
+    out = a.forward(s0, steps, cfl=0.4, every=2)
+    dts = a.dts.copy()
+    rng = np.random.default_rng(5)
+    bar = torch.tensor(rng.standard_normal(a.state_words), device=dev)
+    got = a.backward(bar)
+    parts = [t.clone().requires_grad_(True) for t in a.unpack(s0)]
+    cur = list(parts)
+    for k in range(steps):
+        cur = list(assembly_np.Cycle(*cur, float(dts[k]), dx, dy, 1, 1, GAMMA, 1e-12, 1e-12, 1e-12, 1, False, 0.5,
+                                     backend="torch").outputs())
+    for t_out, g_out in zip(cur, a.unpack(out)):
+        assert torch.equal(t_out.detach(), g_out)
+    loss = sum(torch.sum(b * o) for b, o in zip(a.unpack(bar), cur))
+    loss.backward()
+    for t_in, g_in in zip(parts, a.unpack(got)):
+        scale = float(t_in.grad.abs().max())
+        assert float((t_in.grad - g_in).abs().max()) <= 1e-11 * scale
