@@ -154,8 +154,8 @@ int mhdb_info(void* handle, long long* last_launches, size_t* device_bytes, int*
 void mhdb_destroy(void* handle);
 
 /* ---------------------------------------------------------------------------
- * Adjoint (reverse mode) of the MHD step, first-order (recon 0) and PLM
- * (recon 1) reconstruction.  No counterpart in the reference.  States are
+ * Adjoint (reverse mode) of the MHD step, first-order (recon 0), PLM (recon 1)
+ * and PPM (recon 2) reconstruction.  No counterpart in the reference.  States are
  * "packed" device arrays of mhd2d_adj_info()'s state_words doubles:
  *   prim (8, ny, nx) | cons (8, ny, nx) | faceBx (ny, nx+1) | faceBy (ny+1, nx);
  * an adjoint ("bar") array has the same layout.  dt is frozen: the forward

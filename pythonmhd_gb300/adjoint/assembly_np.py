@@ -8,7 +8,7 @@ the forward step bit for bit, and its reverse sweep is checked against finite
 differences; the GPU adjoint is then checked against it.
 
 dt is an input of a cycle (frozen): the forward pass records it, the reverse
-sweep does not differentiate it.  Reconstruction: first order (0) and PLM (1).
+sweep does not differentiate it.  Reconstruction: first order (0), PLM (1) and PPM (2).
 """
 from __future__ import annotations
 
@@ -26,6 +26,10 @@ def _fn(name, efix=False, backend="numpy", device=None):
     spec = {
         "plm0": (stages.plm_cell, 22, 2, dict(axis=0)),
         "plm1": (stages.plm_cell, 22, 2, dict(axis=1)),
+        "pslope0": (stages.ppm_slope, 22, 1, dict(axis=0)),
+        "pslope1": (stages.ppm_slope, 22, 1, dict(axis=1)),
+        "ppm0": (stages.ppm_cell, 43, 2, dict(axis=0)),
+        "ppm1": (stages.ppm_cell, 43, 2, dict(axis=1)),
         "face0": (stages.face_state, 10, 4, dict(sb=4)),
         "face1": (stages.face_state, 10, 4, dict(sb=5)),
         "roe1_0": (stages.roe1, 15, 2, dict(axis=0, efix=efix)),
@@ -97,7 +101,7 @@ class Cycle:
 
     def __init__(self, prim, cons, fbx, fby, dt, dx, dy, bcx, bcy, gamma, min_d, min_p, min_e, order, efix, eps,
                  backend="numpy"):
-        assert order in (0, 1)
+        assert order in (0, 1, 2)
         self.backend = backend
         if backend == "torch":
             import torch
@@ -149,14 +153,38 @@ class Cycle:
             bc = self.bc[ax]
             dn = dx if ax == 0 else dy
             E = self._zeros((14, ny, nx))      # lia(7) + ria(7) per cell
+            def cell(off):
+                if ax == 0:
+                    return (J, _wrap(I + off, nx, bc))
+                return (_wrap(J + off, ny, bc), I)
+            bslot = 4 if ax == 0 else 5
             if self.order == 1:
-                def cell(off):
-                    if ax == 0:
-                        return (J, _wrap(I + off, nx, bc))
-                    return (_wrap(J + off, ny, bc), I)
                 ins = [(P, s, cell(off)) for off in (-1, 0, 1) for s in slots]
-                ins.append((P, 4 if ax == 0 else 5, cell(0)))
+                ins.append((P, bslot, cell(0)))
                 self._rec(f"plm{ax}", ins, [g, dt / dn], [(E, k, (J, I)) for k in range(14)])
+            elif self.order == 2:
+                # slopes of the sweep-extended cells -1 .. L (extended index e = cell + 1)
+                if ax == 0:
+                    SJ, SE = np.meshgrid(np.arange(ny), np.arange(nx + 2), indexing="ij")
+                    S = self._zeros((7, ny, nx + 2))
+
+                    def ecell(off):
+                        return (SJ, _wrap(SE - 1 + off, nx, bc))
+                else:
+                    SE, SJ = np.meshgrid(np.arange(ny + 2), np.arange(nx), indexing="ij")
+                    S = self._zeros((7, ny + 2, nx))
+
+                    def ecell(off):
+                        return (_wrap(SE - 1 + off, ny, bc), SJ)
+                ins = [(P, s, ecell(off)) for off in (-1, 0, 1) for s in slots]
+                ins.append((P, bslot, ecell(0)))
+                self._rec(f"pslope{ax}", ins, [g], [(S, k, (SJ, SE) if ax == 0 else (SE, SJ)) for k in range(7)])
+                ins = [(P, s, cell(off)) for off in (-1, 0, 1) for s in slots]
+                for off in (0, 1, 2):
+                    sidx = (J, I + off) if ax == 0 else (J + off, I)
+                    ins += [(S, k, sidx) for k in range(7)]
+                ins.append((P, bslot, cell(0)))
+                self._rec(f"ppm{ax}", ins, [g, dt / dn], [(E, k, (J, I)) for k in range(14)])
             else:
                 for k, s in enumerate(slots):
                     self._rec_copy(P, s, E, k)

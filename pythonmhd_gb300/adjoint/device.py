@@ -28,7 +28,7 @@ def _dptr(t):
 class Adjoint2D:
     """Forward and reverse sweeps of the MHD CTU+CT step on one ny x nx grid.
 
-    ``recon`` 0 (first order) or 1 (PLM).  Parameters mirror
+    ``recon`` 0 (first order), 1 (PLM) or 2 (PPM).  Parameters mirror
     :class:`pythonmhd_gb300.solver.Grid2D` (MHD only).
     """
 

@@ -179,6 +179,73 @@ def plm_cell(ins, pars, axis):
     return lia + ria
 
 
+def ppm_slope(ins, pars, axis):
+    """Characteristic-limited primitive slope of one (sweep-extended) cell (k_ppm_slopes).
+
+    ins = wl(7) + wc(7) + wr(7) + bn ; pars = [gamma] -> s(7)
+    """
+    wl, wc, wr, bn = ins[0:7], ins[7:14], ins[14:21], ins[21]
+    s, _, _, _ = char_slopes(wl, wc, wr, bn, pars[0], axis)
+    return s
+
+
+def ppm_cell(ins, pars, axis):
+    """PPM edge states of one cell with dt/2 characteristic tracing (k_faces MODE 2;
+    oracle.mhd2d.ppm_sweep).
+
+    ins = wl(7) + wc(7) + wr(7) + sl(7) + sc(7) + sr(7) + bn ; pars = [gamma, dtdx]
+    -> lia(7) + ria(7)
+    """
+    wl, wc, wr = ins[0:7], ins[7:14], ins[14:21]
+    sl, sc, sr = ins[21:28], ins[28:35], ins[35:42]
+    bn = ins[42]
+    gamma, dtdx = pars
+    lam, L, R = prim_eig(wc, bn, gamma, axis)
+    order = _order(axis)
+    lia, ria = [], []
+    for k in range(7):
+        a = 0.5 * (wc[k] + wl[k]) - (sc[k] - sl[k]) / 6.0
+        b = 0.5 * (wr[k] + wc[k]) - (sr[k] - sc[k]) / 6.0
+        dprod = (b - wc[k]) * (wc[k] - a)
+        idiff = b - a
+        adiff = 6.0 * (wc[k] - 0.5 * (a + b))
+        nzc = dprod <= 0.0
+        sq = idiff * idiff
+        cl_ = ~nzc & ((idiff * adiff) > sq)
+        cr_ = ~nzc & ~cl_ & ((idiff * adiff) < (-1.0 * sq))
+        a2 = select(nzc, wc[k], select(cl_, (6.0 * wc[k] - 4.0 * b) / 2.0, a))
+        b2 = select(nzc, wc[k], select(cr_, (6.0 * wc[k] - 4.0 * a) / 2.0, b))
+        a2 = dmax(dmin(wc[k], wl[k]), a2)
+        a2 = dmin(dmax(wc[k], wl[k]), a2)
+        b2 = dmax(dmin(wc[k], wr[k]), b2)
+        b2 = dmin(dmax(wc[k], wr[k]), b2)
+        lia.append(a2)
+        ria.append(b2)
+    c1 = [ria[k] - lia[k] for k in range(7)]
+    c2 = [6.0 * (wc[k] - 0.5 * (lia[k] + ria[k])) for k in range(7)]
+    c3 = 0.5 * dmax(lam[6], 0.0) * dtdx
+    c4 = -0.5 * dmin(lam[0], 0.0) * dtdx
+    lia = [lia[k] + c4 * (c1[k] + (1.0 - FOUR_THIRDS * c4) * c2[k]) for k in range(7)]
+    ria = [ria[k] - c3 * (c1[k] - (1.0 - FOUR_THIRDS * c3) * c2[k]) for k in range(7)]
+    for side in (0, 1):
+        edge = lia if side == 0 else ria
+        for i in range(7):
+            active = (lam[i] <= 0.0) if side == 0 else (lam[i] >= 0.0)
+            v1 = 0.5 * dtdx * lam[0 if side == 0 else 6]
+            v2 = 0.5 * dtdx * lam[i]
+            v3 = v1 - v2
+            v4 = FOUR_THIRDS * (v1 * v1 - v2 * v2)
+            if side == 0:
+                terms = [L[i, j] * (v3 * (c1[j] + c2[j]) + v4 * c2[j]) for j in order if (i, j) in L]
+            else:
+                terms = [L[i, j] * (v3 * (c1[j] - c2[j]) + v4 * c2[j]) for j in order if (i, j) in L]
+            fac = _sum_first(terms)
+            for j in range(7):
+                if (j, i) in R:
+                    edge[j] = select(active, edge[j] + fac * R[j, i], edge[j])
+    return lia + ria
+
+
 def face_state(ins, pars, sb):
     """Floors and the transverse-B source of one reconstructed face state (put_face).
 

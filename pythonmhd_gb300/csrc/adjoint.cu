@@ -1,4 +1,4 @@
-// Reverse-mode adjoint of the MHD CTU+CT step (first-order and PLM reconstruction).
+// Reverse-mode adjoint of the MHD CTU+CT step (first-order, PLM and PPM reconstruction).
 //
 // The pointwise stage functions come from adjoint_gen.cuh (generated from
 // pythonmhd_gb300/adjoint/stages.py: <stage>_fwd / <stage>_rev).  This file holds
@@ -27,7 +27,7 @@ namespace {
 
 constexpr int kT = 128;
 static_assert(g_plm0_NT == g_plm1_NT && g_roe1_0_NT == g_roe1_1_NT && g_roe2_0_NT == g_roe2_1_NT &&
-                  g_ctu0_NT == g_ctu1_NT &&
+                  g_ctu0_NT == g_ctu1_NT && g_ppm0_NT == g_ppm1_NT && g_pslope0_NT == g_pslope1_NT &&
                   g_roe1_0_efix_NT == g_roe1_1_efix_NT && g_roe2_0_efix_NT == g_roe2_1_efix_NT,
               "the x and y sweeps of a stage store tapes of the same length");
 
@@ -45,6 +45,7 @@ struct Adj {
   double dt;                       // dt of the cycle being processed
   Arr P, C, FX, FY;                // input state
   Arr EX, EY;                      // edge states per cell (lia 7 + ria 7), x and y sweeps
+  Arr SX, SY;                      // PPM: limited slopes of the sweep-extended cells
   Arr XL, XR, YL, YR;              // reconstructed face states
   Arr F1X, F1Y, EZ, E1, NBX, NBY;  // stage-1 fluxes, cell Ez, corner EMF, half-step faces
   Arr UXL, UXR, UYL, UYR, WXL, WXR, WYL, WYR;  // CTU-corrected face cons / prim
@@ -56,6 +57,7 @@ struct Adj {
   double* tplm[2];
   double* troe[2][2];              // [stage-1][axis]
   double* tctu[2];                 // CTU per (face, side) and sweep
+  double* tslope[2];               // PPM slopes per extended cell and sweep
 };
 
 __device__ __forceinline__ int wrapc(int c, int L, int bc) {
@@ -121,16 +123,51 @@ __device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a
 // ---------------------------------------------------------------------------
 // stage kernels (REV = false: forward with stored intermediates; true: reverse)
 // ---------------------------------------------------------------------------
+// limited slopes of the sweep-extended cells e = 0 .. L+1 (cell e-1), PPM only
 template <int AX, bool REV, bool TAPE>
+__global__ void __launch_bounds__(kT) k_slope(Adj A) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y;
+  const int Wd = AX == 0 ? A.nx + 2 : A.nx, H = AX == 0 ? A.ny : A.ny + 2;
+  if (col >= Wd || row >= H) return;
+  const int e = AX == 0 ? col : row, t = AX == 0 ? row : col;
+  const int L = AX == 0 ? A.nx : A.ny;
+  const int bc = AX == 0 ? A.bcx : A.bcy;
+  const size_t me = (size_t)row * Wd + col;
+  const int slots[7] = {0, 1, 2, 3, AX == 0 ? 5 : 6, AX == 0 ? 6 : 4, 7};
+  IO in[22];
+  IO out[7];
+#pragma unroll
+  for (int o = -1; o <= 1; ++o) {
+    const int c = wrapc(e - 1 + o, L, bc);
+    const size_t ci = AX == 0 ? (size_t)t * A.nx + c : (size_t)c * A.nx + t;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) in[(o + 1) * 7 + k] = io(A.P, slots[k], ci);
+  }
+  {
+    const int c = wrapc(e - 1, L, bc);
+    in[21] = io(A.P, AX == 0 ? 4 : 5, AX == 0 ? (size_t)t * A.nx + c : (size_t)c * A.nx + t);
+  }
+  const Arr& S = AX == 0 ? A.SX : A.SY;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) out[k] = io(S, k, me);
+  const double par[1] = {A.gamma};
+  double* tp = A.tslope[AX] + me;
+  const size_t st = (size_t)Wd * H;
+  if (AX == 0) MHD_ADJ_STAGE(pslope0, REV, TAPE, in, out, par, tp, st);
+  else MHD_ADJ_STAGE(pslope1, REV, TAPE, in, out, par, tp, st);
+}
+
+// edge states of each cell: first order (copies), PLM, or PPM from the slopes
+template <int AX, bool REV, bool TAPE, int RECON>
 __global__ void __launch_bounds__(kT) k_recon(Adj A) {
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
   if (c0 >= A.nx || t0 >= A.ny) return;
   const size_t me = (size_t)t0 * A.nx + c0;
   const Arr& E = AX == 0 ? A.EX : A.EY;
   const int slots[7] = {0, 1, 2, 3, AX == 0 ? 5 : 6, AX == 0 ? 6 : 4, 7};
-  if (A.recon == 1) {
+  if constexpr (RECON >= 1) {
     const int bc = AX == 0 ? A.bcx : A.bcy;
-    IO in[22];
+    IO in[RECON == 1 ? 22 : 43];
     IO out[14];
 #pragma unroll
     for (int o = -1; o <= 1; ++o) {
@@ -140,14 +177,29 @@ __global__ void __launch_bounds__(kT) k_recon(Adj A) {
 #pragma unroll
       for (int k = 0; k < 7; ++k) in[(o + 1) * 7 + k] = io(A.P, slots[k], ci);
     }
-    in[21] = io(A.P, AX == 0 ? 4 : 5, me);
+    if constexpr (RECON == 2) {
+      // slopes of cells c-1, c, c+1 sit at extended indices c, c+1, c+2
+      const Arr& S = AX == 0 ? A.SX : A.SY;
+#pragma unroll
+      for (int o = 0; o < 3; ++o) {
+        const size_t si = AX == 0 ? (size_t)t0 * (A.nx + 2) + c0 + o : (size_t)(t0 + o) * A.nx + c0;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) in[21 + o * 7 + k] = io(S, k, si);
+      }
+    }
+    in[RECON == 1 ? 21 : 42] = io(A.P, AX == 0 ? 4 : 5, me);
 #pragma unroll
     for (int k = 0; k < 14; ++k) out[k] = io(E, k, me);
     const double par[2] = {A.gamma, A.dt / (AX == 0 ? A.dx : A.dy)};
     double* tp = A.tplm[AX] + me;
     const size_t st = (size_t)A.nx * A.ny;
-    if (AX == 0) MHD_ADJ_STAGE(plm0, REV, TAPE, in, out, par, tp, st);
-    else MHD_ADJ_STAGE(plm1, REV, TAPE, in, out, par, tp, st);
+    if constexpr (RECON == 1) {
+      if (AX == 0) MHD_ADJ_STAGE(plm0, REV, TAPE, in, out, par, tp, st);
+      else MHD_ADJ_STAGE(plm1, REV, TAPE, in, out, par, tp, st);
+    } else {
+      if (AX == 0) MHD_ADJ_STAGE(ppm0, REV, TAPE, in, out, par, tp, st);
+      else MHD_ADJ_STAGE(ppm1, REV, TAPE, in, out, par, tp, st);
+    }
   } else {
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
@@ -159,6 +211,37 @@ __global__ void __launch_bounds__(kT) k_recon(Adj A) {
         if (g != 0.0) atomicAdd(A.P.pb(slots[k], me), g);
       }
     }
+  }
+}
+
+// launch the reconstruction of both sweeps (PPM: slopes first)
+template <bool REV, bool TAPE>
+void launch_recon(const Adj& A, cudaStream_t s) {
+  const int nx = A.nx, ny = A.ny;
+  const dim3 gc((unsigned)((nx + kT - 1) / kT), (unsigned)ny);
+  const dim3 gsx((unsigned)((nx + 2 + kT - 1) / kT), (unsigned)ny);
+  const dim3 gsy((unsigned)((nx + kT - 1) / kT), (unsigned)(ny + 2));
+  switch (A.recon) {
+    case 0:
+      k_recon<0, REV, TAPE, 0><<<gc, kT, 0, s>>>(A);
+      k_recon<1, REV, TAPE, 0><<<gc, kT, 0, s>>>(A);
+      break;
+    case 1:
+      k_recon<0, REV, TAPE, 1><<<gc, kT, 0, s>>>(A);
+      k_recon<1, REV, TAPE, 1><<<gc, kT, 0, s>>>(A);
+      break;
+    default:
+      if constexpr (!REV) {
+        k_slope<0, false, TAPE><<<gsx, kT, 0, s>>>(A);
+        k_slope<1, false, TAPE><<<gsy, kT, 0, s>>>(A);
+        k_recon<0, false, TAPE, 2><<<gc, kT, 0, s>>>(A);
+        k_recon<1, false, TAPE, 2><<<gc, kT, 0, s>>>(A);
+      } else {
+        k_recon<1, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
+        k_recon<0, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
+        k_slope<1, true, TAPE><<<gsy, kT, 0, s>>>(A);
+        k_slope<0, true, TAPE><<<gsx, kT, 0, s>>>(A);
+      }
   }
 }
 
@@ -496,11 +579,11 @@ __global__ void k_cfl_finish(Adj A, double cfl, double* dt_slot) {
 struct Slot {
   Arr Adj::*arr;
   int planes;
-  int kind;   // 0 cell, 1 x-face, 2 y-face, 3 corner
+  int kind;   // 0 cell, 1 x-face, 2 y-face, 3 corner, 4 x-extended cell, 5 y-extended cell
 };
 const Slot kSlots[] = {
     {&Adj::P, 8, 0},   {&Adj::C, 8, 0},   {&Adj::FX, 1, 1},  {&Adj::FY, 1, 2},  {&Adj::EX, 14, 0},
-    {&Adj::EY, 14, 0}, {&Adj::XL, 7, 1},  {&Adj::XR, 7, 1},  {&Adj::YL, 7, 2},  {&Adj::YR, 7, 2},
+    {&Adj::EY, 14, 0}, {&Adj::SX, 7, 4},  {&Adj::SY, 7, 5},  {&Adj::XL, 7, 1},  {&Adj::XR, 7, 1},  {&Adj::YL, 7, 2},  {&Adj::YR, 7, 2},
     {&Adj::F1X, 7, 1}, {&Adj::F1Y, 7, 2}, {&Adj::EZ, 1, 0},  {&Adj::E1, 1, 3},  {&Adj::NBX, 1, 1},
     {&Adj::NBY, 1, 2}, {&Adj::UXL, 7, 1}, {&Adj::UXR, 7, 1}, {&Adj::UYL, 7, 2}, {&Adj::UYR, 7, 2},
     {&Adj::WXL, 7, 1}, {&Adj::WXR, 7, 1}, {&Adj::WYL, 7, 2}, {&Adj::WYR, 7, 2}, {&Adj::HEZ, 1, 0},
@@ -519,7 +602,8 @@ struct Handle {
   double* vals = nullptr;      // nsets value arenas
   size_t TW = 0;               // words of one tape arena
   double* tapes = nullptr;     // nsets tape arenas
-  size_t toff[8] = {};         // tape offsets: plm x, plm y, roe1 x, roe1 y, roe2 x, roe2 y, ctu x, ctu y
+  size_t toff[10] = {};        // tape offsets: recon x, recon y, roe1 x, roe1 y, roe2 x, roe2 y, ctu x, ctu y,
+                               // PPM slopes x, y
   int nsets = 0;
   double* red = nullptr;       // CFL maxima (2) + dt (1)
   size_t budget = 0;           // bytes the stored-segment mode may use (0: 60% of free memory)
@@ -560,6 +644,8 @@ void select_set(Handle* h, int k) {
   h->A.troe[1][1] = tb + h->toff[5];
   h->A.tctu[0] = tb + h->toff[6];
   h->A.tctu[1] = tb + h->toff[7];
+  h->A.tslope[0] = tb + h->toff[8];
+  h->A.tslope[1] = tb + h->toff[9];
 }
 
 int alloc_sets(Handle* h, int n) {
@@ -612,8 +698,7 @@ int fwd_cycle_t(Handle* h) {
   Adj& A = h->A;
   cudaStream_t s = h->stream;
   const int nx = A.nx, ny = A.ny;
-  k_recon<0, false, TAPE><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_recon<1, false, TAPE><<<g2(nx, ny), kT, 0, s>>>(A);
+  launch_recon<false, TAPE>(A, s);
   k_face<0, false><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
   k_face<1, false><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
   k_roe<0, 1, false, TAPE><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
@@ -662,8 +747,7 @@ int rev_cycle(Handle* h) {
   k_roe<0, 1, true, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
   k_face<1, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
   k_face<0, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
-  k_recon<1, true, true><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_recon<0, true, true><<<g2(nx, ny), kT, 0, s>>>(A);
+  launch_recon<true, true>(A, s);
   CK(cudaGetLastError());
   return MHD_OK;
 }
@@ -746,15 +830,15 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
                      int entropy_fix, double eps, double min_d, double min_p, double min_e, void** handle) {
   if (!handle) return MHD_ERR_ARG;
   *handle = nullptr;
-  if (nx < 2 || ny < 2 || !(dx > 0.0) || !(dy > 0.0) || (recon != 0 && recon != 1)) return MHD_ERR_ARG;
+  if (nx < 2 || ny < 2 || !(dx > 0.0) || !(dy > 0.0) || recon < 0 || recon > 2) return MHD_ERR_ARG;
   if ((bcx != 0 && bcx != 1) || (bcy != 0 && bcy != 1)) return MHD_ERR_ARG;
   Handle* h = new (std::nothrow) Handle();
   if (!h) return MHD_ERR_NOMEM;
   Adj& A = h->A;
   A.nx = nx; A.ny = ny; A.dx = dx; A.dy = dy; A.bcx = bcx; A.bcy = bcy; A.recon = recon;
   A.efix = entropy_fix ? 1 : 0; A.gamma = gamma; A.eps = eps; A.min_d = min_d; A.min_p = min_p; A.min_e = min_e;
-  const size_t plane[4] = {(size_t)nx * ny, (size_t)(nx + 1) * ny, (size_t)nx * (ny + 1),
-                           (size_t)(nx + 1) * (ny + 1)};
+  const size_t plane[6] = {(size_t)nx * ny, (size_t)(nx + 1) * ny, (size_t)nx * (ny + 1),
+                           (size_t)(nx + 1) * (ny + 1), (size_t)(nx + 2) * ny, (size_t)nx * (ny + 2)};
   size_t w = 0;
   for (int i = 0; i < kNumSlots; ++i) {
     h->off[i] = w;
@@ -763,14 +847,18 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
     w = (w + 31) & ~(size_t)31;   // 256-byte aligned planes groups
   }
   h->W = w;
-  // tapes: PLM per cell and sweep (first order has no reconstruction stage),
+  // tapes: PLM/PPM per cell and sweep (first order has no reconstruction stage), PPM slopes per
+  // extended cell and sweep,
   // Roe per face, stage and sweep, CTU per face side and sweep
-  const int nt_plm = recon == 1 ? g_plm0_NT : 0;
+  const int nt_plm = recon == 1 ? g_plm0_NT : (recon == 2 ? g_ppm0_NT : 0);
+  const int nt_slope = recon == 2 ? g_pslope0_NT : 0;
   const int nt_roe[2] = {A.efix ? g_roe1_0_efix_NT : g_roe1_0_NT, A.efix ? g_roe2_0_efix_NT : g_roe2_0_NT};
-  const size_t items[8] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2]};
-  const int words[8] = {nt_plm, nt_plm, nt_roe[0], nt_roe[0], nt_roe[1], nt_roe[1], g_ctu0_NT, g_ctu0_NT};
+  const size_t items[10] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2],
+                            plane[4], plane[5]};
+  const int words[10] = {nt_plm, nt_plm, nt_roe[0], nt_roe[0], nt_roe[1], nt_roe[1], g_ctu0_NT, g_ctu0_NT,
+                         nt_slope, nt_slope};
   size_t tw = 0;
-  for (int i = 0; i < 8; ++i) {
+  for (int i = 0; i < 10; ++i) {
     h->toff[i] = tw;
     tw += items[i] * (size_t)words[i];
     tw = (tw + 31) & ~(size_t)31;

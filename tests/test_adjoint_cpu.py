@@ -1,8 +1,8 @@
 """CPU checks of the adjoint's building blocks.
 
 * The NumPy assembly of the SSA stage functions (pythonmhd_gb300.adjoint.assembly_np)
-  reproduces the oracle's cycle bit for bit (first order and PLM, periodic and
-  outflow, with and without the entropy fix).
+  reproduces the oracle's cycle bit for bit (first order, PLM and PPM, periodic
+  and outflow, with and without the entropy fix).
 * Its reverse sweep matches central finite differences of the oracle's cycle
   along random directions, on generic states (perturbed away from the exact
   ties -- uniform p, v_z = B_z = 0 -- where the limiters and clamps have kinks).
@@ -21,7 +21,7 @@ GAMMA = 5.0 / 3.0
 
 @pytest.mark.parametrize("name", ["ot_ppm", "rand_outflow_ppm", "rand_px_oy_ppm", "rand_efix_small_eps",
                                   "zero_bx", "floors", "supersonic", "tiny_periodic"])
-@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("order", [0, 1, 2])
 def test_numpy_assembly_forward_is_bitwise(name, order):
     c = cases.build("mhd", name)
     dt = mhd2d.calc_dt(c["cons"], c["fbx"], c["fby"], c["gamma"], c["cfl"], c["dx"], c["dy"])
@@ -50,7 +50,8 @@ def generic_state(kind, bc, seed):
 
 
 @pytest.mark.parametrize("kind,bc,order,efix", [("turb", 1, 1, False), ("ot", 1, 0, False),
-                                                ("ot", 0, 1, True), ("turb", 0, 0, True)])
+                                                ("ot", 0, 1, True), ("turb", 0, 0, True),
+                                                ("turb", 1, 2, False), ("ot", 0, 2, True)])
 def test_numpy_reverse_matches_finite_differences(kind, bc, order, efix):
     p, c, bx, by, dx, dy = generic_state(kind, bc, seed=7)
     dt = mhd2d.calc_dt(c, bx, by, GAMMA, 0.4, dx, dy)
@@ -85,7 +86,9 @@ def test_codegen_emits_every_stage():
         assert f"g_{name}_NI" in src
 
 
-@pytest.mark.parametrize("name,order", [("ot_ppm", 1), ("rand_outflow_ppm", 1), ("rand_efix_small_eps", 1), ("zero_b", 1), ("zero_btran", 1), ("zero_bx", 0),
+@pytest.mark.parametrize("name,order", [("ot_ppm", 1), ("rand_outflow_ppm", 1), ("rand_efix_small_eps", 1),
+                                        ("zero_b", 1), ("zero_btran", 1), ("zero_bx", 0),
+                                        ("ot_ppm", 2), ("rand_outflow_ppm", 2),
                                         ("rand_px_oy_ppm", 0), ("floors", 1)])
 def test_torch_transcription_forward_is_bitwise(name, order):
     torch = pytest.importorskip("torch")
@@ -100,7 +103,8 @@ def test_torch_transcription_forward_is_bitwise(name, order):
         np.testing.assert_array_equal(a.numpy(), b)
 
 
-@pytest.mark.parametrize("kind,bc,order,efix", [("turb", 1, 1, False), ("ot", 0, 1, True), ("ot", 1, 0, False)])
+@pytest.mark.parametrize("kind,bc,order,efix", [("turb", 1, 1, False), ("ot", 0, 1, True), ("ot", 1, 0, False),
+                                                ("turb", 1, 2, False)])
 def test_torch_autograd_matches_numpy_reverse(kind, bc, order, efix):
     """torch's reverse mode and forward mode through the torch transcription agree
     with the hand-written reverse sweep."""

@@ -73,8 +73,8 @@ def test_null_handle_calls_fail_cleanly(lib):
 
 def test_adjoint_entry_points_reject_bad_arguments(lib):
     h = ctypes.c_void_p()
-    # the adjoint covers first order (0) and PLM (1) only
-    rc = lib.mhd2d_adj_create(16, 16, 0.1, 0.1, 1, 1, 1.4, 2, 0, 0.5, 1e-12, 1e-12, 1e-12, ctypes.byref(h))
+    # the adjoint covers first order (0), PLM (1) and PPM (2)
+    rc = lib.mhd2d_adj_create(16, 16, 0.1, 0.1, 1, 1, 1.4, 3, 0, 0.5, 1e-12, 1e-12, 1e-12, ctypes.byref(h))
     assert rc == 1 and not h.value
     rc = lib.mhd2d_adj_create(1, 16, 0.1, 0.1, 1, 1, 1.4, 1, 0, 0.5, 1e-12, 1e-12, 1e-12, ctypes.byref(h))
     assert rc == 1 and not h.value

@@ -1,6 +1,6 @@
 """GPU adjoint of the MHD step (mhd2d_adj_* through pythonmhd_gb300.adjoint.device).
 
-* Its forward cycle equals the oracle's cycle bit for bit (first order and PLM).
+* Its forward cycle equals the oracle's cycle bit for bit (first order, PLM and PPM).
 * Its vector-Jacobian product of one cycle equals the NumPy assembly's reverse
   sweep (itself checked against finite differences on the CPU) to round-off:
   the GPU scatters input adjoints with atomic adds, so the summation order of
@@ -40,7 +40,7 @@ def _np(parts):
 
 
 @pytest.mark.parametrize("name", CASES)
-@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("order", [0, 1, 2])
 def test_cycle_bitwise_vs_oracle(name, order):
     c = cases.build("mhd", name)
     dt = mhd2d.calc_dt(c["cons"], c["fbx"], c["fby"], c["gamma"], c["cfl"], c["dx"], c["dy"])
@@ -53,7 +53,8 @@ def test_cycle_bitwise_vs_oracle(name, order):
 
 
 @pytest.mark.parametrize("kind,bc,order,efix", [("turb", 1, 1, False), ("ot", 1, 0, False),
-                                                ("ot", 0, 1, True), ("turb", 0, 0, True)])
+                                                ("ot", 0, 1, True), ("turb", 0, 0, True),
+                                                ("turb", 1, 2, False), ("ot", 0, 2, True)])
 def test_cycle_vjp_matches_numpy_reverse(kind, bc, order, efix):
     p, c, bx, by, dx, dy = generic_state(kind, bc, seed=7)
     dt = mhd2d.calc_dt(c, bx, by, GAMMA, 0.4, dx, dy)
@@ -77,14 +78,15 @@ def _turb_state(n, seed):
     return p, c, bx, by, dx, dy
 
 
-def test_forward_equals_step_and_backward_equals_chained_vjps():
+@pytest.mark.parametrize("recon", [1, 2])
+def test_forward_equals_step_and_backward_equals_chained_vjps(recon):
     n, steps = 64, 7
     p, c, bx, by, dx, dy = _turb_state(n, 5)
-    a = Adjoint2D(n, n, dx, dy, 1, 1, GAMMA, recon=1)
+    a = Adjoint2D(n, n, dx, dy, 1, 1, GAMMA, recon=recon)
     s0 = a.pack(p, c, bx, by)
     out = a.forward(s0, steps, cfl=0.4, every=3)
     dts = a.dts.copy()
-    g = Grid2D(n, n, dx, dy, 1, 1, GAMMA, mhd=True, recon=1, arith="exact")
+    g = Grid2D(n, n, dx, dy, 1, 1, GAMMA, mhd=True, recon=recon, arith="exact")
     g.upload(p, c, bx, by)
     g.advance(0.0, 1e30, 0, steps, 0.4)
     assert g.last_cycles == steps
@@ -175,14 +177,15 @@ def test_gradient_matches_finite_differences(n, steps, ndir, p_jitter):
     assert worst <= 1e-5, worst
 
 
-def test_backward_matches_torch_autograd_of_transcription():
+@pytest.mark.parametrize("recon", [1, 2])
+def test_backward_matches_torch_autograd_of_transcription(recon):
     """Several cycles: the GPU backward equals torch's reverse mode through the
     plain torch transcription of the step (run on the GPU, frozen dts), whose
     forward equals the GPU forward bit for bit."""
     n, steps = 48, 6
     dev = torch.device("cuda", 0)
     p, c, bx, by, dx, dy = _turb_state(n, 8)
-    a = Adjoint2D(n, n, dx, dy, 1, 1, GAMMA, recon=1)
+    a = Adjoint2D(n, n, dx, dy, 1, 1, GAMMA, recon=recon)
     s0 = a.pack(p, c, bx, by)
     out = a.forward(s0, steps, cfl=0.4, every=2)
     dts = a.dts.copy()
@@ -192,8 +195,8 @@ def test_backward_matches_torch_autograd_of_transcription():
     parts = [t.clone().requires_grad_(True) for t in a.unpack(s0)]
     cur = list(parts)
     for k in range(steps):
-        cur = list(assembly_np.Cycle(*cur, float(dts[k]), dx, dy, 1, 1, GAMMA, 1e-12, 1e-12, 1e-12, 1, False, 0.5,
-                                     backend="torch").outputs())
+        cur = list(assembly_np.Cycle(*cur, float(dts[k]), dx, dy, 1, 1, GAMMA, 1e-12, 1e-12, 1e-12, recon, False,
+                                     0.5, backend="torch").outputs())
     for t_out, g_out in zip(cur, a.unpack(out)):
         assert torch.equal(t_out.detach(), g_out)
     loss = sum(torch.sum(b * o) for b, o in zip(a.unpack(bar), cur))
