@@ -149,6 +149,16 @@ int mhdb_download(void* handle, int instance, int which, double* prim, double* c
  * launches of a stage as one launch, blocks = blocks of each persistent launch
  * (default 2 per SM).  Results do not depend on these. */
 int mhdb_configure(void* handle, int tile_width, int fuse, int blocks);
+/* mhdb_upload from device memory of the handle's GPU. */
+int mhdb_upload_device(void* handle, int inst, const double* prim, const double* cons,
+                       const double* faceBx, const double* faceBy);
+/* Copy instance `inst`'s current MHD state into the packed device layout
+ * prim (8,ny,nx) | cons (8,ny,nx) | faceBx | faceBy (the adjoint's state layout). */
+int mhdb_pack_state(void* handle, int inst, double* dst);
+/* Device pointers of instance `inst`'s current (which = 0) or second-last (1) state;
+ * valid until the next advance or upload. */
+int mhdb_state_ptrs(void* handle, int inst, int which, double** prim, double** cons,
+                    double** faceBx, double** faceBy);
 int mhdb_info(void* handle, long long* last_launches, size_t* device_bytes, int* blocks,
               void** stream);
 void mhdb_destroy(void* handle);
@@ -185,6 +195,20 @@ int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initia
 /* Bytes the backward pass may hold to keep a whole segment resident
  * (0 = 60% of the free device memory at mhd2d_adj_forward time). */
 int mhd2d_adj_configure(void* handle, size_t segment_bytes);
+/* Re-target a handle to another grid with the same reconstruction, entropy fix
+ * and floors (drops its forward record).  Device memory is reused while large
+ * enough, so one handle can run the backward passes of many grids in turn. */
+int mhd2d_adj_reshape(void* handle, int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma);
+/* Device bytes one resident cycle takes in the backward pass (its arrays and
+ * tapes) for an ny x nx grid: a whole checkpoint segment stays resident when
+ * `every` times this fits the segment budget. */
+int mhd2d_adj_cycle_bytes(int ny, int nx, int recon, int entropy_fix, size_t* bytes);
+/* Install a forward record made elsewhere (e.g. by the batched step): `steps`
+ * cycles with the host dts `dt`, and the packed device states at cycles 0,
+ * every, 2*every, ... in `checkpoints` (ceil(steps/every) states, one after the
+ * other; the memory stays the caller's and must outlive the backward pass).
+ * mhd2d_adj_backward then runs from it. */
+int mhd2d_adj_restore(void* handle, const double* checkpoints, int steps, int every, const double* dt);
 /* state_words: length of a packed state; device_bytes: memory held now;
  * segment_sets: cycles kept resident per segment by the last forward (1 =
  * recompute mode). */

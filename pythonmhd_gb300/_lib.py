@@ -48,6 +48,10 @@ SIGNATURES = {
     "mhdb_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p, c_double_p,
                                      c_double_p]),
     "mhdb_configure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "mhdb_upload_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4),
+    "mhdb_pack_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "mhdb_state_ptrs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+                        + [ctypes.POINTER(ctypes.c_void_p)] * 4),
     "mhdb_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t),
                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]),
     "mhdb_destroy": (None, [ctypes.c_void_p]),
@@ -62,6 +66,11 @@ SIGNATURES = {
                                          c_double_p, ctypes.c_int, ctypes.c_void_p, c_double_p]),
     "mhd2d_adj_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mhd2d_adj_configure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t]),
+    "mhd2d_adj_reshape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double]),
+    "mhd2d_adj_cycle_bytes": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_size_t)]),
+    "mhd2d_adj_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_double_p]),
     "mhd2d_adj_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
                                       ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_int)]),
     "mhd2d_adj_destroy": (None, [ctypes.c_void_p]),

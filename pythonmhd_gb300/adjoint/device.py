@@ -56,6 +56,17 @@ class Adjoint2D:
                    "mhd2d_adj_info")
         return dict(state_words=words.value, device_bytes=nbytes.value, segment_sets=sets.value)
 
+    def reshape(self, ny, nx, dx, dy, bcx=PERIODIC, bcy=PERIODIC, gamma=5.0 / 3.0):
+        """Re-target this handle to another grid (same reconstruction and floors),
+        reusing its device memory where it is large enough; drops the forward record."""
+        _lib.check(self.lib.mhd2d_adj_reshape(self._h, int(ny), int(nx), float(dx), float(dy), int(bcx), int(bcy),
+                                              float(gamma)), "mhd2d_adj_reshape")
+        self.ny, self.nx = int(ny), int(nx)
+        self.dx, self.dy = float(dx), float(dy)
+        self.state_words = self.info()["state_words"]
+        self.dts = None
+        self._ckpt_ref = None
+
     def configure(self, segment_bytes=0):
         """Memory the backward pass may use to keep a checkpoint segment resident (0 = automatic)."""
         _lib.check(self.lib.mhd2d_adj_configure(self._h, int(segment_bytes)), "mhd2d_adj_configure")
@@ -132,6 +143,22 @@ class Adjoint2D:
                    "mhd2d_adj_forward")
         self.dts = log
         return out
+
+    def restore(self, checkpoints, steps, every, dts):
+        """Install a forward record made elsewhere: ``checkpoints`` a contiguous device
+        tensor of ceil(steps/every) packed states (at cycles 0, every, ...; kept alive
+        by the caller until the backward pass has run) and the host ``dts``."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        if dts.shape != (int(steps),):
+            raise ValueError("dts must hold one dt per step")
+        nck = -(-int(steps) // int(every))
+        if checkpoints.numel() < nck * self.state_words:
+            raise ValueError("checkpoints hold fewer states than the record needs")
+        self._sync()
+        _lib.check(self.lib.mhd2d_adj_restore(self._h, _dptr(checkpoints), int(steps), int(every),
+                                              dts.ctypes.data_as(_lib.c_double_p)), "mhd2d_adj_restore")
+        self._ckpt_ref = checkpoints
+        self.dts = dts.copy()
 
     def backward(self, bar_final):
         """Adjoint of the last :meth:`forward` with respect to its initial state."""

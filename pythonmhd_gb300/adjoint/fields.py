@@ -20,21 +20,41 @@ import torch
 from .. import initial_conditions as ic
 
 
-def turbulence_fields(n, seed=1, gamma=5.0 / 3.0, kmax_v=16, kmax_a=16, mach=1.0, beta=1.0):
-    """Seeded turbulence fields on an n x n periodic box (the turbulence generator's
-    spectra and normalisation), with A_z scaled to plasma beta ``beta``.
+def _gaussian_field(rng, ny, nx, slope, kmin, kmax):
+    """The generator's Gaussian random field on an ny x nx periodic grid (integer
+    wavevectors of the box; per-mode power |k|^-slope for kmin <= |k| <= kmax)."""
+    if ny == nx:
+        return ic._gaussian_field(rng, nx, slope, kmin, kmax)
+    kx = np.fft.rfftfreq(nx, d=1.0 / nx)
+    ky = np.fft.fftfreq(ny, d=1.0 / ny)
+    KX, KY = np.meshgrid(kx, ky)
+    k = np.sqrt(KX * KX + KY * KY)
+    mask = (k >= kmin) & (k <= kmax)
+    amp = np.zeros_like(k)
+    amp[mask] = k[mask] ** (-slope / 2.0)
+    c = (rng.standard_normal(k.shape) + 1j * rng.standard_normal(k.shape)) * amp
+    f = np.fft.irfft2(c, s=(ny, nx))
+    return f - f.mean()
 
-    Returns dict(rho, vx, vy, p, az, dx, dy, gamma) of NumPy arrays.
+
+def turbulence_fields(n, seed=1, gamma=5.0 / 3.0, kmax_v=16, kmax_a=16, mach=1.0, beta=1.0, ny=None):
+    """Seeded turbulence fields on an ny x n periodic unit box (ny defaults to n;
+    the turbulence generator's spectra and normalisation), with A_z scaled to
+    plasma beta ``beta``.
+
+    Returns dict(rho, vx, vy, p, az, dx, dy, gamma, kmax_v, kmax_a) of NumPy arrays.
     """
+    nx = n
+    ny = n if ny is None else ny
     rng = np.random.default_rng(seed)
-    g = ic._gaussian_field(rng, n, 2.0, 1.0, kmax_v)
+    g = _gaussian_field(rng, ny, nx, 2.0, 1.0, kmax_v)
     g /= g.std()
-    vx = ic._gaussian_field(rng, n, 2.0, 1.0, kmax_v)
-    vy = ic._gaussian_field(rng, n, 2.0, 1.0, kmax_v)
-    az = ic._gaussian_field(rng, n, 3.0, 1.0, kmax_a)
-    dx = dy = 1.0 / n
+    vx = _gaussian_field(rng, ny, nx, 2.0, 1.0, kmax_v)
+    vy = _gaussian_field(rng, ny, nx, 2.0, 1.0, kmax_v)
+    az = _gaussian_field(rng, ny, nx, 3.0, 1.0, kmax_a)
+    dx, dy = 1.0 / nx, 1.0 / ny
     rho = np.exp(0.1 * g)
-    p = np.full((n, n), 1.0 / gamma)
+    p = np.full((ny, nx), 1.0 / gamma)
     vscale = mach / np.sqrt(np.mean((vx * vx + vy * vy) / (gamma * p / rho)))
     vx *= vscale
     vy *= vscale
@@ -45,16 +65,37 @@ def turbulence_fields(n, seed=1, gamma=5.0 / 3.0, kmax_v=16, kmax_a=16, mach=1.0
     return dict(rho=rho, vx=vx, vy=vy, p=p, az=az, dx=dx, dy=dy, gamma=gamma, kmax_v=kmax_v, kmax_a=kmax_a)
 
 
+def turbulence_batch(count=64, seed=0, sizes=tuple(range(128, 1025, 64)), gamma_range=(1.4, 5.0 / 3.0),
+                     kmax=16, mach=1.0, cells_per_wave=None):
+    """Uneven batch of turbulence fields: Nx and Ny drawn independently and uniformly
+    from ``sizes``, gamma uniformly from ``gamma_range``, rms Mach ``mach``, instance k
+    generated with seed ``seed * 100003 + k``.  With ``cells_per_wave`` the spectral
+    cutoff of an instance is min(kmax, min(Nx, Ny) // cells_per_wave), so its
+    shortest wave spans at least that many cells.  Returns a list of field dicts
+    with nx, ny added."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        nx = int(rng.choice(sizes))
+        ny = int(rng.choice(sizes))
+        gamma = float(rng.uniform(*gamma_range))
+        km = kmax if cells_per_wave is None else max(1, min(kmax, min(nx, ny) // cells_per_wave))
+        f = turbulence_fields(nx, seed=seed * 100003 + k, gamma=gamma, kmax_v=km, kmax_a=km, ny=ny, mach=mach)
+        f.update(nx=nx, ny=ny)
+        out.append(f)
+    return out
+
+
 def perturbed(fields, frac, seed):
     """The fields with rho, vx, vy, p and A_z each multiplied by (1 + frac g), g a
     seeded unit-variance Gaussian random field with the generator's spectrum
     (k^-2 up to kmax_v; k^-3 up to kmax_a for A_z): a smooth perturbation."""
     rng = np.random.default_rng(seed)
-    n = fields["rho"].shape[0]
+    ny, nx = fields["rho"].shape
     out = dict(fields)
     for k in ("rho", "vx", "vy", "p", "az"):
         slope, kmax = (3.0, fields["kmax_a"]) if k == "az" else (2.0, fields["kmax_v"])
-        g = ic._gaussian_field(rng, n, slope, 1.0, kmax)
+        g = _gaussian_field(rng, ny, nx, slope, 1.0, kmax)
         out[k] = fields[k] * (1.0 + frac * (g / g.std()))
     return out
 

@@ -599,6 +599,7 @@ struct Handle {
   size_t ps[kNumSlots] = {};   // plane stride of each array
   size_t W = 0;                // words of one arena (all arrays of one cycle)
   double* bars = nullptr;      // one adjoint arena
+  size_t bars_cap = 0, vals_cap = 0, tapes_cap = 0;   // words held
   double* vals = nullptr;      // nsets value arenas
   size_t TW = 0;               // words of one tape arena
   double* tapes = nullptr;     // nsets tape arenas
@@ -612,6 +613,7 @@ struct Handle {
   bool stored = false;         // backward keeps every cycle of a segment resident
   std::vector<double> dts;
   double* ckpt = nullptr;      // one packed state per segment
+  bool ckpt_owned = true;      // false: the caller's memory (mhd2d_adj_restore)
   double* seg = nullptr;       // recompute mode: packed states of the current segment
   size_t ckpt_bytes = 0, seg_bytes = 0;
   size_t state_words = 0;
@@ -648,21 +650,29 @@ void select_set(Handle* h, int k) {
   h->A.tslope[1] = tb + h->toff[9];
 }
 
+// n value+tape arenas of the current layout.  Memory is kept while it is large
+// enough (fewer arenas, or a handle reshaped to a smaller grid, reuse it) and
+// released when the handle is destroyed.
 int alloc_sets(Handle* h, int n) {
-  if (h->nsets == n) return MHD_OK;
-  cudaFree(h->vals);
-  cudaFree(h->tapes);
-  h->vals = h->tapes = nullptr;
-  h->nsets = 0;
-  CK(cudaMalloc(&h->vals, (size_t)n * h->W * sizeof(double)));
-  CK(cudaMalloc(&h->tapes, (size_t)n * h->TW * sizeof(double)));
+  const size_t need_v = (size_t)n * h->W, need_t = (size_t)n * h->TW;
+  if (need_v > h->vals_cap || need_t > h->tapes_cap) {
+    cudaFree(h->vals);
+    cudaFree(h->tapes);
+    h->vals = h->tapes = nullptr;
+    h->vals_cap = h->tapes_cap = 0;
+    h->nsets = 0;
+    CK(cudaMalloc(&h->vals, need_v * sizeof(double)));
+    h->vals_cap = need_v;
+    CK(cudaMalloc(&h->tapes, (need_t ? need_t : 1) * sizeof(double)));
+    h->tapes_cap = need_t;
+  }
   h->nsets = n;
   select_set(h, 0);
   return MHD_OK;
 }
 
 size_t device_bytes(const Handle* h) {
-  return (h->W + (h->W + h->TW) * (size_t)h->nsets + 4) * sizeof(double) + h->ckpt_bytes + h->seg_bytes;
+  return (h->bars_cap + h->vals_cap + h->tapes_cap + 4) * sizeof(double) + h->ckpt_bytes + h->seg_bytes;
 }
 
 // copy a packed state [prim 8 | cons 8 | fbx | fby] into / out of four arrays
@@ -786,6 +796,76 @@ int bars_in_to_out(Handle* h) {
   return MHD_OK;
 }
 
+// Arena layout of one cycle for an nx x ny grid: value/adjoint arena offsets and
+// plane strides (W words), and the tape arena offsets (TW words).
+void layout(int nx, int ny, int recon, int efix, size_t* off, size_t* ps, size_t* W, size_t* toff, size_t* TW) {
+  const size_t plane[6] = {(size_t)nx * ny, (size_t)(nx + 1) * ny, (size_t)nx * (ny + 1),
+                           (size_t)(nx + 1) * (ny + 1), (size_t)(nx + 2) * ny, (size_t)nx * (ny + 2)};
+  size_t w = 0;
+  for (int i = 0; i < kNumSlots; ++i) {
+    off[i] = w;
+    ps[i] = plane[kSlots[i].kind];
+    w += (size_t)kSlots[i].planes * ps[i];
+    w = (w + 31) & ~(size_t)31;   // 256-byte aligned plane groups
+  }
+  *W = w;
+  // tapes: PLM/PPM per cell and sweep (first order has no reconstruction stage), Roe per
+  // face, stage and sweep, CTU per face side and sweep, PPM slopes per extended cell and sweep
+  const int nt_plm = recon == 1 ? g_plm0_NT : (recon == 2 ? g_ppm0_NT : 0);
+  const int nt_slope = recon == 2 ? g_pslope0_NT : 0;
+  const int nt_roe[2] = {efix ? g_roe1_0_efix_NT : g_roe1_0_NT, efix ? g_roe2_0_efix_NT : g_roe2_0_NT};
+  const size_t items[10] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2],
+                            plane[4], plane[5]};
+  const int words[10] = {nt_plm, nt_plm, nt_roe[0], nt_roe[0], nt_roe[1], nt_roe[1], g_ctu0_NT, g_ctu0_NT,
+                         nt_slope, nt_slope};
+  size_t tw = 0;
+  for (int i = 0; i < 10; ++i) {
+    toff[i] = tw;
+    tw += items[i] * (size_t)words[i];
+    tw = (tw + 31) & ~(size_t)31;
+  }
+  *TW = tw;
+}
+
+// Size the record of a run of `steps` cycles: the checkpoint interval, the
+// checkpoint store (owned, or borrowed from the caller), and the backward mode --
+// all `every` cycles of a segment resident when they fit the budget, else one
+// cycle's arrays plus the segment's states.
+int prepare_record(Handle* h, int steps, int& every, bool own_ckpt) {
+  if (every <= 0) every = (int)std::ceil(std::sqrt((double)steps));
+  every = std::min(every, steps);
+  const int nck = (steps + every - 1) / every;
+  h->steps = 0;
+  if (h->ckpt_owned) cudaFree(h->ckpt);
+  cudaFree(h->seg);
+  h->ckpt = h->seg = nullptr;
+  h->ckpt_bytes = h->seg_bytes = 0;
+  h->ckpt_owned = own_ckpt;
+  if (own_ckpt) {
+    CK(cudaMalloc(&h->ckpt, (size_t)nck * h->state_words * sizeof(double)));
+    h->ckpt_bytes = (size_t)nck * h->state_words * sizeof(double);
+  }
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  // (arenas this handle already holds count as free)
+  const size_t set_bytes = (h->W + h->TW) * sizeof(double);
+  const size_t held_all = (h->vals_cap + h->tapes_cap) * sizeof(double);
+  const size_t held = held_all > set_bytes ? held_all - set_bytes : 0;
+  const size_t budget = h->budget ? h->budget : (size_t)(0.6 * (double)(free_b + held));
+  const size_t extra = ((size_t)every - 1) * set_bytes;
+  h->stored = every > 1 && extra <= budget;
+  int rc;
+  if (h->stored) {
+    if (h->nsets < every && (rc = alloc_sets(h, every))) return rc;
+  } else {
+    if ((rc = alloc_sets(h, 1))) return rc;
+    CK(cudaMalloc(&h->seg, (size_t)every * h->state_words * sizeof(double)));
+    h->seg_bytes = (size_t)every * h->state_words * sizeof(double);
+  }
+  h->every = every;
+  return MHD_OK;
+}
+
 // Forward pass with the CFL dt on the production exact-arithmetic step (the same
 // arithmetic as the stage kernels, bit for bit, and faster): one cycle per
 // advance call from t = 0, so the returned time is the cycle's dt exactly.
@@ -837,36 +917,11 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
   Adj& A = h->A;
   A.nx = nx; A.ny = ny; A.dx = dx; A.dy = dy; A.bcx = bcx; A.bcy = bcy; A.recon = recon;
   A.efix = entropy_fix ? 1 : 0; A.gamma = gamma; A.eps = eps; A.min_d = min_d; A.min_p = min_p; A.min_e = min_e;
-  const size_t plane[6] = {(size_t)nx * ny, (size_t)(nx + 1) * ny, (size_t)nx * (ny + 1),
-                           (size_t)(nx + 1) * (ny + 1), (size_t)(nx + 2) * ny, (size_t)nx * (ny + 2)};
-  size_t w = 0;
-  for (int i = 0; i < kNumSlots; ++i) {
-    h->off[i] = w;
-    h->ps[i] = plane[kSlots[i].kind];
-    w += (size_t)kSlots[i].planes * h->ps[i];
-    w = (w + 31) & ~(size_t)31;   // 256-byte aligned planes groups
-  }
-  h->W = w;
-  // tapes: PLM/PPM per cell and sweep (first order has no reconstruction stage), PPM slopes per
-  // extended cell and sweep,
-  // Roe per face, stage and sweep, CTU per face side and sweep
-  const int nt_plm = recon == 1 ? g_plm0_NT : (recon == 2 ? g_ppm0_NT : 0);
-  const int nt_slope = recon == 2 ? g_pslope0_NT : 0;
-  const int nt_roe[2] = {A.efix ? g_roe1_0_efix_NT : g_roe1_0_NT, A.efix ? g_roe2_0_efix_NT : g_roe2_0_NT};
-  const size_t items[10] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2],
-                            plane[4], plane[5]};
-  const int words[10] = {nt_plm, nt_plm, nt_roe[0], nt_roe[0], nt_roe[1], nt_roe[1], g_ctu0_NT, g_ctu0_NT,
-                         nt_slope, nt_slope};
-  size_t tw = 0;
-  for (int i = 0; i < 10; ++i) {
-    h->toff[i] = tw;
-    tw += items[i] * (size_t)words[i];
-    tw = (tw + 31) & ~(size_t)31;
-  }
-  h->TW = tw;
+  layout(nx, ny, recon, A.efix, h->off, h->ps, &h->W, h->toff, &h->TW);
   h->state_words = state_words(A);
   int rc = MHD_OK;
   cudaError_t e = cudaMalloc(&h->bars, h->W * sizeof(double));
+  h->bars_cap = e == cudaSuccess ? h->W : 0;
   if (e == cudaSuccess) e = cudaMalloc(&h->red, 4 * sizeof(double));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->red, 0, 4 * sizeof(double), h->stream);
@@ -895,11 +950,50 @@ void mhd2d_adj_destroy(void* handle) {
   cudaFree(h->vals);
   cudaFree(h->tapes);
   cudaFree(h->red);
-  cudaFree(h->ckpt);
+  if (h->ckpt_owned) cudaFree(h->ckpt);
   cudaFree(h->seg);
   if (h->solver) mhd2d_destroy(h->solver);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+}
+
+int mhd2d_adj_reshape(void* handle, int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || nx < 2 || ny < 2 || !(dx > 0.0) || !(dy > 0.0)) return MHD_ERR_ARG;
+  if ((bcx != 0 && bcx != 1) || (bcy != 0 && bcy != 1)) return MHD_ERR_ARG;
+  CK(cudaStreamSynchronize(h->stream));
+  Adj& A = h->A;
+  A.nx = nx; A.ny = ny; A.dx = dx; A.dy = dy; A.bcx = bcx; A.bcy = bcy; A.gamma = gamma;
+  layout(nx, ny, A.recon, A.efix, h->off, h->ps, &h->W, h->toff, &h->TW);
+  h->state_words = state_words(A);
+  if (h->W > h->bars_cap) {
+    cudaFree(h->bars);
+    h->bars = nullptr;
+    h->bars_cap = 0;
+    CK(cudaMalloc(&h->bars, h->W * sizeof(double)));
+    h->bars_cap = h->W;
+  }
+  // the record, the segment states and the production solver belong to the old grid
+  h->steps = 0;
+  if (h->ckpt_owned) cudaFree(h->ckpt);
+  cudaFree(h->seg);
+  h->ckpt = h->seg = nullptr;
+  h->ckpt_bytes = h->seg_bytes = 0;
+  h->ckpt_owned = true;
+  if (h->solver) {
+    mhd2d_destroy(h->solver);
+    h->solver = nullptr;
+  }
+  h->nsets = 0;
+  return alloc_sets(h, 1);
+}
+
+int mhd2d_adj_cycle_bytes(int ny, int nx, int recon, int entropy_fix, size_t* bytes) {
+  if (!bytes || nx < 2 || ny < 2 || recon < 0 || recon > 2) return MHD_ERR_ARG;
+  size_t off[kNumSlots], ps[kNumSlots], toff[10], W = 0, TW = 0;
+  layout(nx, ny, recon, entropy_fix ? 1 : 0, off, ps, &W, toff, &TW);
+  *bytes = (W + TW) * sizeof(double);
+  return MHD_OK;
 }
 
 int mhd2d_adj_configure(void* handle, size_t segment_bytes) {
@@ -945,33 +1039,9 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !state_in || !state_out || steps < 1) return MHD_ERR_ARG;
   Adj& A = h->A;
-  if (every <= 0) every = (int)std::ceil(std::sqrt((double)steps));
-  every = std::min(every, steps);
-  const int nck = (steps + every - 1) / every;
-  h->steps = 0;
-  cudaFree(h->ckpt);
-  cudaFree(h->seg);
-  h->ckpt = h->seg = nullptr;
-  h->ckpt_bytes = h->seg_bytes = 0;
-  CK(cudaMalloc(&h->ckpt, (size_t)nck * h->state_words * sizeof(double)));
-  h->ckpt_bytes = (size_t)nck * h->state_words * sizeof(double);
-  // backward mode: keep all `every` cycles of a segment resident when they fit
-  size_t free_b = 0, total_b = 0;
-  CK(cudaMemGetInfo(&free_b, &total_b));
-  const size_t set_bytes = (h->W + h->TW) * sizeof(double);
-  const size_t held = ((size_t)h->nsets - 1) * set_bytes;
-  const size_t budget = h->budget ? h->budget : (size_t)(0.6 * (double)(free_b + held));
-  const size_t extra = ((size_t)every - 1) * set_bytes;
-  h->stored = every > 1 && extra <= budget;
-  int rc;
-  if (h->stored) {
-    if (h->nsets < every && (rc = alloc_sets(h, every))) return rc;
-  } else {
-    if ((rc = alloc_sets(h, 1))) return rc;
-    CK(cudaMalloc(&h->seg, (size_t)every * h->state_words * sizeof(double)));
-    h->seg_bytes = (size_t)every * h->state_words * sizeof(double);
-  }
-  h->every = every;
+  int rc = prepare_record(h, steps, every, true);
+  if (rc) return rc;
+  every = h->every;
   h->dts.assign(steps, 0.0);
   if (!fixed_dt) {
     if ((rc = forward_on_solver(h, state_in, steps, cfl, state_out))) return rc;
@@ -994,6 +1064,19 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
   CK(cudaStreamSynchronize(h->stream));
   h->steps = steps;
   if (dt_log) std::copy(h->dts.begin(), h->dts.end(), dt_log);
+  return MHD_OK;
+}
+
+int mhd2d_adj_restore(void* handle, const double* checkpoints, int steps, int every, const double* dt) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !checkpoints || !dt || steps < 1 || every < 1) return MHD_ERR_ARG;
+  int rc = prepare_record(h, steps, every, false);
+  if (rc) return rc;
+  h->ckpt = const_cast<double*>(checkpoints);
+  h->dts.assign(dt, dt + steps);
+  for (int c = 0; c < steps; ++c)
+    if (!std::isfinite(h->dts[c])) return MHD_ERR_NONFINITE;
+  h->steps = steps;
   return MHD_OK;
 }
 

@@ -537,8 +537,8 @@ void mhdb_destroy(void* handle) {
   if (handle) free_batch(static_cast<BatchHandle*>(handle));
 }
 
-int mhdb_upload(void* handle, int inst, const double* prim, const double* cons, const double* faceBx,
-                const double* faceBy) {
+static int batch_upload(void* handle, int inst, const double* prim, const double* cons, const double* faceBx,
+                        const double* faceBy, cudaMemcpyKind kind) {
   BatchHandle* b = static_cast<BatchHandle*>(handle);
   if (!b || inst < 0 || inst >= b->count || !prim || !cons) return MHD_ERR_ARG;
   const Grid& g = b->grids[inst];
@@ -546,15 +546,55 @@ int mhdb_upload(void* handle, int inst, const double* prim, const double* cons, 
   if (mhd && (!faceBx || !faceBy)) return MHD_ERR_ARG;
   const mhdk::StateBuf& s = g.st[b->h_loops[inst].cur];
   const size_t cb = (size_t)b->nvars * mhdk::cell_plane(g) * sizeof(double);
-  CK(cudaMemcpyAsync(s.prim, prim, cb, cudaMemcpyHostToDevice, b->stream));
-  CK(cudaMemcpyAsync(s.cons, cons, cb, cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(s.prim, prim, cb, kind, b->stream));
+  CK(cudaMemcpyAsync(s.cons, cons, cb, kind, b->stream));
   if (mhd) {
-    CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(g) * sizeof(double), cudaMemcpyHostToDevice, b->stream));
-    CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(g) * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(g) * sizeof(double), kind, b->stream));
+    CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(g) * sizeof(double), kind, b->stream));
   }
   CK(cudaStreamSynchronize(b->stream));
   b->uploaded[inst] = 1;
   b->h_loops[inst].cycles_run = 0;
+  return MHD_OK;
+}
+
+int mhdb_upload(void* handle, int inst, const double* prim, const double* cons, const double* faceBx,
+                const double* faceBy) {
+  return batch_upload(handle, inst, prim, cons, faceBx, faceBy, cudaMemcpyHostToDevice);
+}
+
+int mhdb_upload_device(void* handle, int inst, const double* prim, const double* cons, const double* faceBx,
+                       const double* faceBy) {
+  return batch_upload(handle, inst, prim, cons, faceBx, faceBy, cudaMemcpyDeviceToDevice);
+}
+
+int mhdb_pack_state(void* handle, int inst, double* dst) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || inst < 0 || inst >= b->count || !dst || b->physics != MHD2D_MHD) return MHD_ERR_ARG;
+  if (!b->uploaded[inst]) return MHD_ERR_STATE;
+  const Grid& g = b->grids[inst];
+  const mhdk::StateBuf& s = g.st[b->h_loops[inst].cur];
+  const size_t cp = (size_t)b->nvars * mhdk::cell_plane(g), xp = mhdk::xface_plane(g), yp = mhdk::yface_plane(g);
+  CK(cudaMemcpyAsync(dst, s.prim, cp * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  CK(cudaMemcpyAsync(dst + cp, s.cons, cp * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  CK(cudaMemcpyAsync(dst + 2 * cp, s.fbx, xp * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  CK(cudaMemcpyAsync(dst + 2 * cp + xp, s.fby, yp * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return MHD_OK;
+}
+
+int mhdb_state_ptrs(void* handle, int inst, int which, double** prim, double** cons, double** faceBx,
+                    double** faceBy) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || inst < 0 || inst >= b->count || (which != 0 && which != 1)) return MHD_ERR_ARG;
+  if (!b->uploaded[inst]) return MHD_ERR_STATE;
+  int buf = b->h_loops[inst].cur;
+  if (which == 1 && b->h_loops[inst].cycles_run > 0) buf ^= 1;
+  const mhdk::StateBuf& s = b->grids[inst].st[buf];
+  if (prim) *prim = s.prim;
+  if (cons) *cons = s.cons;
+  if (faceBx) *faceBx = s.fbx;
+  if (faceBy) *faceBy = s.fby;
   return MHD_OK;
 }
 
