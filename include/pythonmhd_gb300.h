@@ -39,7 +39,8 @@ enum mhd2d_status {
   MHD_ERR_NOMEM = 3,       /* device or pinned-host allocation failed */
   MHD_ERR_STATE = 4,       /* call out of order (e.g. advance before upload) */
   MHD_ERR_NONFINITE = 5,   /* the time or dt became NaN/Inf during advance */
-  MHD_ERR_TOO_LARGE = 6    /* size above a fixed limit of the entry point */
+  MHD_ERR_TOO_LARGE = 6,   /* size above a fixed limit of the entry point */
+  MHD_ERR_ABORTED = 7      /* mhd2d_run: the stop callback asked to stop */
 };
 
 enum mhd2d_physics { MHD2D_HYDRO = 0, MHD2D_MHD = 1 };
@@ -72,6 +73,22 @@ int mhd2d_upload_device(void* handle, const double* prim, const double* cons,
 int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0,
                   long long max_cycles, double cfl, double* t_out, long long* cycle_out,
                   double* t_second_last);
+
+/* The reference driver's time loop (Source/Simulation.py:290-413) with the state
+ * kept on the device: from t = 0 and cycle 0 it advances to each stop time (the
+ * next save every save_dt and plot every plot_dt, rounded to save_prec /
+ * plot_prec decimals as the driver does, and t_lim), calls on_stop there
+ * (kinds: bit 0 save, bit 1 plot; the callback may mhd2d_download the state;
+ * nonzero return stops the run with MHD_ERR_ABORTED), and -- while the run goes
+ * on -- continues from the state before the short cycle that reached the stop,
+ * keeping that cycle's count, as the driver does.  save_dt / plot_dt <= 0
+ * disable the stop kind.  A save or plot run also calls on_stop for the
+ * initial state (t = 0).  Returns the final time, cycle count and the number of
+ * stops. */
+typedef int (*mhd2d_stop_fn)(void* user, double t, long long cycle, int kinds);
+int mhd2d_run(void* handle, double t_lim, long long max_cycles, double cfl, double save_dt, int save_prec,
+              double plot_dt, int plot_prec, mhd2d_stop_fn on_stop, void* user, double* t_out,
+              long long* cycle_out, long long* stops_out);
 
 /* Copy a state out: which = 0 the current state, 1 the state at the start of
  * the last cycle (the reference's secondLast* arrays).  Any pointer may be

@@ -82,3 +82,23 @@ def test_adjoint_entry_points_reject_bad_arguments(lib):
     assert lib.mhd2d_adj_backward(None, None, None) == 1
     assert lib.mhd2d_adj_forward(None, None, 1, 0.4, None, 0, None, None) == 1
     lib.mhd2d_adj_destroy(None)
+
+
+def test_driver_time_precision_follows_the_reference_rule():
+    from pythonmhd_gb300 import driver
+    assert driver.time_precision(0.01, 0.5) == 2
+    assert driver.time_precision(0.1, 1.0) == 1
+    assert driver.time_precision(0.0075, 0.03) == 4
+    assert driver.time_precision(0.25, 0.125) == 3
+    assert driver.time_precision(1.0 / 3.0, 1.0) == 10
+    h = ctypes.c_void_p()
+    assert lib_run_rejects_null(h)
+
+
+def lib_run_rejects_null(h):
+    from pythonmhd_gb300 import _lib
+    lib = _lib.load()
+    t = ctypes.c_double()
+    c = ctypes.c_longlong()
+    return lib.mhd2d_run(None, 1.0, 10, 0.4, -1.0, 0, -1.0, 0, None, None, ctypes.byref(t), ctypes.byref(c),
+                         ctypes.byref(c)) == 1

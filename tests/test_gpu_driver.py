@@ -1,0 +1,89 @@
+"""The device-resident driver loop (mhd2d_run through pythonmhd_gb300.driver)
+against the oracle's restatement of the reference driver (Source/Simulation.py:
+290-413): the same stops (time, cycle, kind), the same states at every stop and
+at the end, bit for bit in exact arithmetic."""
+import numpy as np
+import pytest
+
+from oracle import driver as odriver
+from pythonmhd_gb300 import driver
+from pythonmhd_gb300 import initial_conditions as ic
+from pythonmhd_gb300.solver import Grid2D
+
+pytestmark = pytest.mark.gpu
+
+
+def _mhd_case():
+    prim, cons, fbx, fby, dx, dy = ic.orszag_tang(32, 28, gamma=5.0 / 3.0)
+    return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=dx, dy=dy, bcx=1, bcy=1, gamma=5.0 / 3.0)
+
+
+def _hydro_case():
+    prim = np.zeros((5, 24, 30))
+    prim[0] = 1.0
+    prim[4] = 0.1
+    prim[4, 10:14, 13:17] = 10.0
+    return dict(prim=prim, cons=ic.prim_to_cons_hydro(prim, 1.4), fbx=None, fby=None, dx=1 / 30, dy=1 / 24,
+                bcx=0, bcy=0, gamma=1.4)
+
+
+@pytest.mark.parametrize("physics,t_lim,max_cycles,save_dt,plot_dt,order", [
+    ("mhd", 0.05, 1000, 0.01, -1.0, 2),
+    ("mhd", 0.04, 1000, 0.01, 0.015, 1),
+    ("mhd", 0.05, 9, 0.01, -1.0, 2),
+    ("hydro", 0.03, 1000, 0.005, 0.0075, 2),
+    ("hydro", 0.02, 1000, -1.0, -1.0, 0),
+])
+def test_driver_matches_oracle_driver(physics, t_lim, max_cycles, save_dt, plot_dt, order):
+    c = _mhd_case() if physics == "mhd" else _hydro_case()
+    mhd = physics == "mhd"
+    sp = driver.time_precision(save_dt, t_lim) if save_dt > 0 else 0
+    pp = driver.time_precision(plot_dt, t_lim) if plot_dt > 0 else 0
+    args = (c["dx"], c["dy"], c["bcx"], c["bcy"], t_lim, max_cycles, c["gamma"], 0.4, 1e-12, 1e-12, 1e-12, order,
+            False, 0.5)
+    t_w, cyc_w, stops_w, final_w = odriver.run(c["prim"], c["cons"], c["fbx"], c["fby"], *args,
+                                               save_dt=save_dt, save_prec=sp, plot_dt=plot_dt, plot_prec=pp)
+    got = []
+
+    def on_stop(t, cycle, kinds, grid):
+        got.append((t, cycle, kinds, grid.download()))
+
+    ny, nx = c["prim"].shape[1:]
+    g = Grid2D(ny, nx, c["dx"], c["dy"], c["bcx"], c["bcy"], c["gamma"], mhd=mhd, recon=order, arith="exact")
+    g.upload(c["prim"], c["cons"], c["fbx"], c["fby"])
+    t, cyc, n = driver.run(g, t_lim, max_cycles, 0.4, save_dt=save_dt, plot_dt=plot_dt, on_stop=on_stop)
+    final = g.download()
+    g.close()
+    assert (t, cyc) == (t_w, cyc_w)
+    assert len(got) == len(stops_w) and n == len([s for s in stops_w if s[0] > 0.0 or s[1] > 0])
+    for (tg, cg, kg, sg), (tw, cw, kw, sw) in zip(got, stops_w):
+        assert (tg, cg, kg) == (tw, cw, kw)
+        for a, b in zip(sg, sw):
+            if b is not None:
+                np.testing.assert_array_equal(a, b)
+    for a, b in zip(final, final_w):
+        if b is not None:
+            np.testing.assert_array_equal(a, b)
+
+
+def test_driver_stop_callback_can_end_the_run(tmp_path):
+    c = _mhd_case()
+    g = Grid2D(28, 32, c["dx"], c["dy"], 1, 1, c["gamma"], mhd=True, recon=2, arith="exact")
+    g.upload(c["prim"], c["cons"], c["fbx"], c["fby"])
+    seen = []
+
+    def on_stop(t, cycle, kinds, grid):
+        p, u, bx, by = grid.download()
+        driver.save_mat(str(tmp_path / f"snap_{len(seen)}.mat"), p, u, bx, by)
+        seen.append(t)
+        return len(seen) == 3
+
+    with pytest.raises(Exception) as e:
+        driver.run(g, 0.05, 1000, 0.4, save_dt=0.01, on_stop=on_stop)
+    assert "stop callback" in str(e.value)
+    g.close()
+    assert seen[0] == 0.0 and len(seen) == 3
+    import scipy.io
+    d = scipy.io.loadmat(str(tmp_path / "snap_0.mat"))
+    np.testing.assert_array_equal(d["faceBx"], c["fbx"])
+    np.testing.assert_array_equal(d["density"], c["prim"][0])
