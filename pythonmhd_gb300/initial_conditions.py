@@ -207,3 +207,65 @@ def orszag_tang_batch(count=256, seed=0, sizes=tuple(range(64, 513, 32)), gamma_
         out.append(dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=dx, dy=dy, nx=nx, ny=ny, gamma=gamma,
                         bcx=PERIODIC, bcy=PERIODIC))
     return out
+
+
+# ---------------------------------------------------------------------------
+# the same generator with the transforms and field algebra on the GPU
+# ---------------------------------------------------------------------------
+def _gaussian_field_device(rng, n, slope, kmin, kmax, device):
+    """``_gaussian_field`` with the inverse FFT on the device (cuFFT through torch).
+
+    The random coefficients come from the same NumPy generator in the same order,
+    so the field equals the host one up to the transform's rounding."""
+    import torch
+    kx = np.fft.rfftfreq(n, d=1.0 / n)
+    ky = np.fft.fftfreq(n, d=1.0 / n)
+    KX, KY = np.meshgrid(kx, ky)
+    k = np.sqrt(KX * KX + KY * KY)
+    mask = (k >= kmin) & (k <= kmax)
+    amp = np.zeros_like(k)
+    amp[mask] = k[mask] ** (-slope / 2.0)
+    re = rng.standard_normal(k.shape)
+    im = rng.standard_normal(k.shape)
+    c = torch.complex(torch.from_numpy(re * amp), torch.from_numpy(im * amp)).to(device)
+    f = torch.fft.irfft2(c, s=(n, n))
+    return f - f.mean()
+
+
+def turbulence_device(n, seed=1, gamma=5.0 / 3.0, kmax_v=32, kmax_a=16, mach=1.0, beta=1.0, device="cuda"):
+    """``turbulence`` generated on the GPU: returns (prim, cons, faceBx, faceBy) as
+    float64 torch tensors on ``device`` plus dx, dy, ready for
+    ``mhd2d_upload_device`` -- no n^2 transform or field array on the host.  The
+    state equals ``turbulence``'s to rounding (the transforms and reductions are
+    evaluated differently)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    g = _gaussian_field_device(rng, n, 2.0, 1.0, kmax_v, device)
+    g = g / g.std(unbiased=False)
+    vx = _gaussian_field_device(rng, n, 2.0, 1.0, kmax_v, device)
+    vy = _gaussian_field_device(rng, n, 2.0, 1.0, kmax_v, device)
+    az = _gaussian_field_device(rng, n, 3.0, 1.0, kmax_a, device)
+    dx = dy = 1.0 / n
+    rho = torch.exp(0.1 * g)
+    p = torch.full((n, n), 1.0 / gamma, dtype=torch.float64, device=device)
+    cs2 = gamma * p / rho
+    vscale = mach / torch.sqrt(torch.mean((vx * vx + vy * vy) / cs2))
+    vx = vx * vscale
+    vy = vy * vscale
+    bxf = torch.roll(az, -1, dims=0) - az
+    byf = -(torch.roll(az, -1, dims=1) - az)
+    fbx = torch.cat([bxf, bxf[:, :1]], dim=1) / dy
+    fby = torch.cat([byf, byf[:1, :]], dim=0) / dx
+    cbx = (fbx[:, :-1] + fbx[:, 1:]) / 2.0
+    cby = (fby[:-1, :] + fby[1:, :]) / 2.0
+    bscale = torch.sqrt(2.0 * (1.0 / gamma) / beta / torch.mean(cbx * cbx + cby * cby))
+    fbx = fbx * bscale
+    fby = fby * bscale
+    cbx = (fbx[:, :-1] + fbx[:, 1:]) / 2.0
+    cby = (fby[:-1, :] + fby[1:, :]) / 2.0
+    zero = torch.zeros_like(rho)
+    prim = torch.stack([rho, vx, vy, zero, cbx, cby, zero, p])
+    e = p / (gamma - 1.0) + 0.5 * rho * (vx * vx + vy * vy + zero * zero)
+    e = e + 0.5 * (cbx * cbx + cby * cby + zero * zero)
+    cons = torch.stack([rho, rho * vx, rho * vy, rho * zero, cbx, cby, zero, e])
+    return prim.contiguous(), cons.contiguous(), fbx.contiguous(), fby.contiguous(), dx, dy

@@ -90,6 +90,20 @@ class Grid2D:
         _lib.check(self.lib.mhd2d_upload(self._h, _ptr(prim), _ptr(cons), _ptr(fbx), _ptr(fby)),
                    "mhd2d_upload")
 
+    def upload_device(self, prim, cons, fbx=None, fby=None):
+        """Upload from contiguous float64 CUDA tensors of the handle's device (no host copy)."""
+        import torch
+
+        def ptr(t):
+            if t is None:
+                return None
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError("upload_device expects contiguous float64 CUDA tensors")
+            return ctypes.c_void_p(t.data_ptr())
+        torch.cuda.current_stream(prim.device).synchronize()
+        _lib.check(self.lib.mhd2d_upload_device(self._h, ptr(prim), ptr(cons), ptr(fbx), ptr(fby)),
+                   "mhd2d_upload_device")
+
     def download(self, which=0, prim=None, cons=None, fbx=None, fby=None):
         """Copy the current (which=0) or second-last (which=1) state into new or given arrays."""
         prim = np.empty(self.cell_shape()) if prim is None else prim
