@@ -56,6 +56,16 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
                  int physics, int recon, int entropy_fix, double eps, double min_d,
                  double min_p, double min_e, int arith, void** handle);
 
+/* A 1D grid of n cells: the reference's evolve_1D_mhd / evolve_1D_hydro
+ * (Source/EvolveFunctions_MHD.py:195-340, Source/EvolveFunctions_Hydro.py:232-305):
+ * x-sweep reconstruction (recon 2 PPM, 0 first order; 1 PLM as an addition) and
+ * Roe fluxes, then cons -= dt/dx (F_right - F_left); MHD keeps B_x uniform at
+ * the uploaded prim[4][0] and has no face B or CT.  States are (nvars, n); the
+ * handle is then used with mhd2d_advance / mhd2d_download (NULL face arrays). */
+int mhd1d_create(int n, double dx, int bcx, double gamma, int physics, int recon, int entropy_fix,
+                 double eps, double min_d, double min_p, double min_e, int arith, void** handle);
+int mhd1d_upload(void* handle, const double* prim, const double* cons);
+
 /* Copy a host state in (becomes the current state).  The reference reads
  * grid.primVars, grid.consVars, grid.faceBx, grid.faceBy at the start of an
  * evolve call (Source/EvolveFunctions_MHD.py:396-444). */

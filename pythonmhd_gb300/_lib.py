@@ -25,6 +25,10 @@ SIGNATURES = {
                                     ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p)]),
     "mhd2d_upload": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p]),
+    "mhd1d_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "mhd1d_upload": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "mhd2d_upload_device": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 4),
     "mhd2d_advance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_longlong,
                                      ctypes.c_longlong, ctypes.c_double, ctypes.POINTER(ctypes.c_double),

@@ -232,12 +232,12 @@ const char* mhd2d_strerror(int status) {
   }
 }
 
-int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma, int physics,
-                 int recon, int entropy_fix, double eps, double min_d, double min_p, double min_e,
-                 int arith, void** handle) {
+static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma, int physics,
+                       int recon, int entropy_fix, double eps, double min_d, double min_p, double min_e,
+                       int arith, int one_d, void** handle) {
   if (!handle) return MHD_ERR_ARG;
   *handle = nullptr;
-  if (nx < 2 || ny < 2 || !(dx > 0.0) || !(dy > 0.0)) return MHD_ERR_ARG;
+  if (nx < 2 || ny < (one_d ? 1 : 2) || !(dx > 0.0) || !(dy > 0.0)) return MHD_ERR_ARG;
   if ((bcx != 0 && bcx != 1) || (bcy != 0 && bcy != 1)) return MHD_ERR_ARG;
   if (physics != MHD2D_HYDRO && physics != MHD2D_MHD) return MHD_ERR_ARG;
   if (recon != 0 && recon != 1 && recon != 2) return MHD_ERR_ARG;
@@ -250,6 +250,8 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
   g.nx = nx; g.ny = ny; g.dx = dx; g.dy = dy; g.bcx = bcx; g.bcy = bcy;
   g.physics = physics; g.recon = recon; g.efix = entropy_fix ? 1 : 0;
   g.gamma = gamma; g.eps = eps; g.min_d = min_d; g.min_p = min_p; g.min_e = min_e;
+  g.one_d = one_d;
+  g.bx1d = 0.0;
   h->arith = arith;
   h->nvars = physics == MHD2D_MHD ? 8 : 5;
 
@@ -284,6 +286,46 @@ int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double 
     return cuda_fail(e);
   }
   *handle = h;
+  return MHD_OK;
+}
+
+int mhd2d_create(int ny, int nx, double dx, double dy, int bcx, int bcy, double gamma, int physics,
+                 int recon, int entropy_fix, double eps, double min_d, double min_p, double min_e,
+                 int arith, void** handle) {
+  return create_grid(ny, nx, dx, dy, bcx, bcy, gamma, physics, recon, entropy_fix, eps, min_d, min_p, min_e,
+                     arith, 0, handle);
+}
+
+int mhd1d_create(int n, double dx, int bcx, double gamma, int physics, int recon, int entropy_fix, double eps,
+                 double min_d, double min_p, double min_e, int arith, void** handle) {
+  return create_grid(1, n, dx, 1.0, bcx, 1, gamma, physics, recon, entropy_fix, eps, min_d, min_p, min_e, arith,
+                     1, handle);
+}
+
+static int upload_state(void* handle, const double* prim, const double* cons, const double* faceBx,
+                        const double* faceBy, cudaMemcpyKind kind);
+
+int mhd1d_upload(void* handle, const double* prim, const double* cons) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !prim || !cons) return MHD_ERR_ARG;
+  if (!h->g.one_d) return MHD_ERR_STATE;
+  const int n = h->g.nx;
+  if (h->g.physics == MHD2D_HYDRO) return upload_state(handle, prim, cons, nullptr, nullptr, cudaMemcpyHostToDevice);
+  // B_x is the first cell's value everywhere (Source/EvolveFunctions_MHD.py:201-205); the
+  // face array of both state buffers holds it for the Roe solver's normal B
+  const double bx = prim[4 * (size_t)n];
+  std::vector<double> fbx((size_t)n + 1, bx), fby(2 * (size_t)n, 0.0);
+  int rc = upload_state(handle, prim, cons, fbx.data(), fby.data(), cudaMemcpyHostToDevice);
+  if (rc) return rc;
+  const mhdk::StateBuf& other = h->g.st[h->cur ^ 1];
+  CK(cudaMemcpyAsync(other.fbx, fbx.data(), fbx.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (h->g.bx1d != bx) {
+    // the kernels take the grid by value: rebuild the cycle graphs with the new B_x
+    h->g.bx1d = bx;
+    for (auto& ge : h->graph)
+      if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+  }
   return MHD_OK;
 }
 

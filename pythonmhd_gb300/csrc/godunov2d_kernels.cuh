@@ -175,7 +175,9 @@ __device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, 
   load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
   load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
   double bn = 0.0;
-  if (S::BN >= 0) bn = __ldg(in.prim + (size_t)(S::BN >= 0 ? S::BN : 0) * plane + cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx));
+  if (S::BN >= 0)
+    bn = G.one_d ? G.bx1d
+                 : __ldg(in.prim + (size_t)(S::BN >= 0 ? S::BN : 0) * plane + cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx));
   typename S::Eig e;
   S::eig(wc, bn, G.gamma, e);
 
@@ -225,14 +227,14 @@ __device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, 
 // then the transverse-B source term (Source/EvolveFunctions_MHD.py:524-535).
 template <class S>
 __device__ __forceinline__ void put_face(double* buf, size_t fplane, size_t fidx, const double* v,
-                                         double min_d, double min_p, double bsrc) {
+                                         double min_d, double min_p, double bsrc, bool add_src = true) {
   constexpr int NV = S::NV;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
     double x = v[k];
     if (k == 0 && x < min_d) x = min_d;
     if (k == NV - 1 && x < min_p) x = min_p;
-    if (k == S::SB) x = x + bsrc;
+    if (k == S::SB && add_src) x = x + bsrc;
     buf[k * fplane + fidx] = x;
   }
 }
@@ -441,7 +443,8 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
   const size_t fplane = AX == 0 ? xface_plane(G) : yface_plane(G);
   const int Ls = g.Ls;
   double s_mid = 0.0, s_lo = 0.0, s_hi = 0.0;
-  if (S::SB >= 0) {
+  const bool src = S::SB >= 0 && !G.one_d;   // 1D MHD has no B source terms
+  if (src) {
     const double* fb = AX == 0 ? in.fbx : in.fby;
     const double half_dt = 0.5 * dt;
     const double inv_dn = 1.0 / dn;
@@ -455,15 +458,15 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
       else s_lo = bsource<AX>(in.prim, fb, plane, Ls - 1, Ls - 1, 0, t, g.nx, half_dt, inv_dn);
     }
   }
-  put_face<S>(outR, fplane, face_index<AX>(c, t, g.nx), lia, G.min_d, G.min_p, s_mid);
-  put_face<S>(outL, fplane, face_index<AX>(c + 1, t, g.nx), ria, G.min_d, G.min_p, s_mid);
+  put_face<S>(outR, fplane, face_index<AX>(c, t, g.nx), lia, G.min_d, G.min_p, s_mid, src);
+  put_face<S>(outL, fplane, face_index<AX>(c + 1, t, g.nx), ria, G.min_d, G.min_p, s_mid, src);
   if (c == 0) {
-    if (g.bc == OUTFLOW) put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), lia, G.min_d, G.min_p, s_lo);
-    else put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), lia, G.min_d, G.min_p, s_hi);
+    if (g.bc == OUTFLOW) put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), lia, G.min_d, G.min_p, s_lo, src);
+    else put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), lia, G.min_d, G.min_p, s_hi, src);
   }
   if (c == Ls - 1) {
-    if (g.bc == OUTFLOW) put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), ria, G.min_d, G.min_p, s_hi);
-    else put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), ria, G.min_d, G.min_p, s_lo);
+    if (g.bc == OUTFLOW) put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), ria, G.min_d, G.min_p, s_hi, src);
+    else put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), ria, G.min_d, G.min_p, s_lo, src);
   }
 }
 
@@ -1005,6 +1008,83 @@ __global__ void __launch_bounds__(kBlock) k_final_hydro(Grid G, StateBuf in, Sta
 }
 
 // ----------------------------------------------------------------------------
+// 1D grids (ny = 1): the reference's evolve_1D_mhd / evolve_1D_hydro
+// (Source/EvolveFunctions_MHD.py:195-340, Source/EvolveFunctions_Hydro.py:232-305):
+// x-sweep reconstruction and Roe fluxes, then cons -= dt/dx (F_right - F_left).
+// ----------------------------------------------------------------------------
+// largest x signal speed of cell i (Source/TimestepCalculations_HelperModule.py:24-56,
+// :183-225: B from the cell's conserved B, no face B)
+template <int PHYS>
+__device__ __forceinline__ void b_dt_cell_1d(const Grid& G, const StateBuf& in, size_t i, double& mx) {
+  const size_t plane = cell_plane(G);
+  const double gamma = G.gamma;
+  const double* c = in.cons;
+  const double inv_d = 1.0 / c[i];
+  const double vx = c[plane + i] * inv_d;
+  const double vy = c[2 * plane + i] * inv_d;
+  const double vz = c[3 * plane + i] * inv_d;
+  const double vsq = vx * vx + vy * vy + vz * vz;
+  if (PHYS == MHD) {
+    const double bx = c[4 * plane + i], by = c[5 * plane + i], bz = c[6 * plane + i];
+    const double bsq = bx * bx + by * by + bz * bz;
+    const double p = dmax((gamma - 1.0) * (c[7 * plane + i] - 0.5 * c[i] * vsq - 0.5 * bsq), SMALL_VALUE);
+    const double a2 = gamma * p * inv_d;
+    const double ssum = bsq * inv_d + a2;
+    const double sdiff = bsq * inv_d - a2;
+    const double cf2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (by * by + bz * bz) * inv_d));
+    mx = dmax(mx, fabs(vx) + sqrt(cf2));
+  } else {
+    const double p = dmax((gamma - 1.0) * (c[4 * plane + i] - 0.5 * c[i] * vsq), SMALL_VALUE);
+    mx = dmax(mx, fabs(vx) + sqrt(gamma * p * inv_d));
+  }
+}
+
+template <int PHYS>
+__global__ void __launch_bounds__(256) k_dt_reduce_1d(Grid G, StateBuf in) {
+  if (!loop_running(G.loop)) return;
+  double mx = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)G.nx; i += (size_t)gridDim.x * blockDim.x)
+    b_dt_cell_1d<PHYS>(G, in, i, mx);
+  // the y maximum stays 0, so the 2D dt rule reduces to cfl / (max_x / dx)
+  block_max_to_loop(mx, 0.0, G.loop);
+}
+
+template <int PHYS>
+__global__ void __launch_bounds__(kBlock) k_update_1d(Grid G, StateBuf in, StateBuf out) {
+  if (!G.loop->active) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= G.nx) return;
+  const double dtdx = G.loop->dt / G.dx;
+  const size_t plane = cell_plane(G), fp = xface_plane(G);
+  if (PHYS == MHD) {
+    constexpr int src[7] = {0, 1, 2, 3, 5, 6, 7};
+    double u[7], w[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+      u[k] = __ldg(in.cons + src[k] * plane + i) - dtdx * (G.fx[k * fp + i + 1] - G.fx[k * fp + i]);
+    cons_to_prim7(u, G.bx1d, G.gamma, w);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      out.prim[src[k] * plane + i] = w[k];
+      out.cons[src[k] * plane + i] = u[k];
+    }
+    out.prim[4 * plane + i] = G.bx1d;
+    out.cons[4 * plane + i] = G.bx1d;
+  } else {
+    double u[5], w[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+      u[k] = __ldg(in.cons + k * plane + i) - dtdx * (G.fx[k * fp + i + 1] - G.fx[k * fp + i]);
+    hcons_to_prim<false>(u, G.gamma, w);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      out.prim[k * plane + i] = w[k];
+      out.cons[k * plane + i] = u[k];
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
 // Host-side enqueue of one cycle reading state buffer `parity`.
 // ----------------------------------------------------------------------------
 inline dim3 row_grid(int n, int rows) { return dim3((unsigned)((n + kBlock - 1) / kBlock), (unsigned)rows); }
@@ -1030,9 +1110,29 @@ void enqueue_recon(const Grid& g, const StateBuf& in, cudaStream_t s) {
   }
 }
 
+template <int PHYS>
+void enqueue_cycle_1d(const Grid& g, const StateBuf& in, const StateBuf& out, int dt_blocks, cudaStream_t s) {
+  using SX = typename std::conditional<PHYS == MHD, MhdSweep<0>, HydroSweep<0>>::type;
+  k_dt_reduce_1d<PHYS><<<dt_blocks, 256, 0, s>>>(g, in);
+  k_begin<PHYS><<<1, 1, 0, s>>>(g);
+  if (g.recon >= 1) k_ppm_slopes<SX, 0><<<row_grid(g.nx + 2, 1), kBlock, 0, s>>>(g, in);
+  if (g.recon == 2) k_faces<SX, 0, 2><<<row_grid(g.nx, 1), kBlock, 0, s>>>(g, in);
+  else if (g.recon == 1) k_faces<SX, 0, 1><<<row_grid(g.nx, 1), kBlock, 0, s>>>(g, in);
+  else k_faces<SX, 0, 0><<<row_grid(g.nx, 1), kBlock, 0, s>>>(g, in);
+  if (PHYS == MHD) k_roe_mhd<0, 1><<<lin_grid(xface_plane(g)), kBlock, 0, s>>>(g, in);
+  else k_roe_hydro<0><<<lin_grid(xface_plane(g)), kBlock, 0, s>>>(g);
+  k_update_1d<PHYS><<<lin_grid(g.nx), kBlock, 0, s>>>(g, in, out);
+  k_end<<<1, 1, 0, s>>>(g);
+}
+
 void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s) {
   const StateBuf in = g.st[parity];
   const StateBuf out = g.st[parity ^ 1];
+  if (g.one_d) {
+    if (g.physics == MHD) enqueue_cycle_1d<MHD>(g, in, out, dt_blocks, s);
+    else enqueue_cycle_1d<HYDRO>(g, in, out, dt_blocks, s);
+    return;
+  }
   const size_t nxf = xface_plane(g), nyf = yface_plane(g);
   if (g.physics == MHD) {
     k_dt_reduce<MHD><<<dt_blocks, 256, 0, s>>>(g, in);

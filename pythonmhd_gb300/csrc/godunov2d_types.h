@@ -70,6 +70,10 @@ struct Grid {
   size_t ext_plane;            // plane stride of slopes / eig (max of x/y extended sizes)
   LoopState* loop;             // device
   int* status;                 // device error word (0 = ok)
+  // 1D grids (ny = 1): the x sweep only, no transverse or CT stages; MHD keeps
+  // B_x uniform at bx1d (the reference's evolve_1D_mhd)
+  int one_d;
+  double bx1d;
 };
 
 // index spaces of the batched work lists

@@ -2,7 +2,8 @@
 
 The reference driver picks its evolve function from module attributes at run
 time (Source/Simulation.py:312-324: ``evolveMHD.evolve_2D_mhd`` /
-``evolveHydro.evolve_2D_hydro``) and calls it at Source/Simulation.py:349-377.
+``evolveHydro.evolve_2D_hydro``, and the 1D ones) and calls it at
+Source/Simulation.py:349-377.
 Assigning those attributes swaps in the GPU step; initialization files and the
 ``Simulation`` driver stay unchanged:
 
@@ -21,13 +22,15 @@ from . import evolve
 TARGETS = (
     ("Source.EvolveFunctions_MHD", "evolve_2D_mhd", evolve.evolve_2D_mhd),
     ("Source.EvolveFunctions_Hydro", "evolve_2D_hydro", evolve.evolve_2D_hydro),
+    ("Source.EvolveFunctions_MHD", "evolve_1D_mhd", evolve.evolve_1D_mhd),
+    ("Source.EvolveFunctions_Hydro", "evolve_1D_hydro", evolve.evolve_1D_hydro),
 )
 
 _saved: dict = {}
 
 
 def install(arith: str | None = None):
-    """Replace the reference's 2D evolve functions; returns the patched modules.
+    """Replace the reference's 1D and 2D evolve functions; returns the patched modules.
 
     ``arith`` ("exact" or "fast") overrides PYTHONMHD_GB300_ARITH for these calls.
     """

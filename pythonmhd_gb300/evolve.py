@@ -1,4 +1,4 @@
-"""Drop-in replacements for the reference's 2D evolve functions.
+"""Drop-in replacements for the reference's 1D and 2D evolve functions.
 
 ``evolve_2D_mhd`` and ``evolve_2D_hydro`` keep the reference signatures, the
 preconditions they assert, their return tuples and their aliasing:
@@ -14,6 +14,11 @@ preconditions they assert, their return tuples and their aliasing:
   -> (prim, cons, time, cycle, secondLastPrim, secondLastCons, secondLastTime);
   the grid's primVars/consVars are updated in place and returned.
 
+``evolve_1D_mhd`` / ``evolve_1D_hydro`` (Source/EvolveFunctions_MHD.py:195-340,
+Source/EvolveFunctions_Hydro.py:232-305) keep theirs too: the 1D MHD function
+returns new arrays with B_x made uniform; the 1D hydro function updates the
+grid's arrays in place and returns them.
+
 The cycles run on the GPU (``Grid2D.advance``); the host uploads the grid once
 per call and downloads the result.  Handles are cached per grid geometry and
 parameters, so the driver's repeated calls reuse device memory and CUDA graphs.
@@ -22,10 +27,21 @@ from __future__ import annotations
 
 import numpy as np
 
-from .solver import Grid2D, default_arith
+from .solver import Grid1D, Grid2D, default_arith
 
 OUTFLOW = 0
 PERIODIC = 1
+# reconstructOrder value that selects PLM, an addition: the reference runs PPM for
+# reconstructOrder == 2 and first order for every other value (its PLM branches are
+# commented out, Source/EvolveFunctions_MHD.py:487-488, Source/EvolveFunctions_Hydro.py:
+# 410-412), so an integer other than 2 keeps the reference's first-order behaviour.
+PLM = "plm"
+
+
+def _order(reconstructOrder):
+    if reconstructOrder == PLM:
+        return 1
+    return 2 if reconstructOrder == 2 else 0
 
 _cache: dict = {}
 _CACHE_MAX = 4
@@ -67,7 +83,7 @@ def evolve_2D_mhd(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cf
     assert (tStart <= tEnd)
     assert (startCycle >= 0)
     ny, nx = prim.shape[1:]
-    order = reconstructOrder if reconstructOrder in (1, 2) else 0
+    order = _order(reconstructOrder)
     mode = arith or default_arith()
     key = ("mhd", ny, nx, float(dx), float(dy), bcx, bcy, float(gamma), order, bool(entropyFix),
            float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)
@@ -106,7 +122,7 @@ def evolve_2D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, 
     assert (bcy == OUTFLOW or bcy == PERIODIC)
     assert (tStart <= tEnd)
     assert (startCycle >= 0 and maxCycles > 0)
-    order = reconstructOrder if reconstructOrder in (1, 2) else 0
+    order = _order(reconstructOrder)
     mode = arith or default_arith()
     key = ("hydro", ny, nx, float(dx), float(dy), bcx, bcy, float(gamma), order, bool(entropyFix),
            float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)
@@ -122,3 +138,77 @@ def evolve_2D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, 
     np.copyto(prim, new_prim)
     np.copyto(cons, new_cons)
     return prim, cons, t, cyc, sl_prim, sl_cons, t_sl
+
+
+# ---------------------------------------------------------------------------
+# 1D (Source/EvolveFunctions_MHD.py:195-340, Source/EvolveFunctions_Hydro.py:232-305)
+# ---------------------------------------------------------------------------
+def evolve_1D_mhd(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cfl, minDens, minPres,
+                  minEnergy, reconstructOrder=0, entropyFix=False, epsilon=0.5, arith=None):
+    """evolve_1D_mhd: returns (prim, cons, time, cycle, secondLastPrim, secondLastCons,
+    secondLastTime) as new arrays (the grid's arrays are not modified); B_x is the
+    first cell's value everywhere, as in the reference."""
+    prim = simulationGrid.primVars
+    assert (len(prim.shape) == 2)
+    assert (prim.shape[0] == 8)
+    assert (prim.shape[1] > 0)
+    cons = simulationGrid.consVars
+    assert (prim.shape == cons.shape)
+    dx = simulationGrid.dx
+    assert (dx > 0)
+    bcx = simulationGrid.BcX
+    assert (bcx == OUTFLOW or bcx == PERIODIC)
+    assert (tStart <= tEnd)
+    assert (startCycle >= 0)
+    n = prim.shape[1]
+    order = _order(reconstructOrder)
+    mode = arith or default_arith()
+    key = ("mhd1d", n, float(dx), bcx, float(gamma), order, bool(entropyFix), float(epsilon), float(minDens),
+           float(minPres), float(minEnergy), mode)
+    g = _handle(key, lambda: Grid1D(n, dx, bcx, gamma, mhd=True, recon=order, entropy_fix=entropyFix,
+                                    eps=epsilon, min_d=minDens, min_p=minPres, min_e=minEnergy, arith=mode))
+    g.upload(prim, cons)
+    t, cycle, t_sl = g.advance(tStart, tEnd, startCycle, maxCycles, cfl)
+    new_prim, new_cons = g.download(0)
+    if g.last_cycles > 0:
+        sl_prim, sl_cons = g.download(1)
+    else:
+        sl_prim, sl_cons = np.copy(prim), np.copy(cons)
+        # with no cycle the reference still returns B_x made uniform
+        new_prim = np.array(prim, dtype=np.float64)
+        new_cons = np.array(cons, dtype=np.float64)
+        new_prim[4] = prim[4][0]
+        new_cons[4] = prim[4][0]
+    return new_prim, new_cons, t, cycle, sl_prim, sl_cons, t_sl
+
+
+def evolve_1D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cfl, minDens, minPres,
+                    minEnergy, reconstructOrder=0, entropyFix=False, epsilon=0.5, arith=None):
+    """evolve_1D_hydro: updates the grid's primVars/consVars in place and returns them,
+    as the reference does: (prim, cons, time, cycle, secondLastPrim, secondLastCons,
+    secondLastTime)."""
+    prim = simulationGrid.primVars
+    assert (len(prim.shape) == 2)
+    cons = simulationGrid.consVars
+    assert (prim.shape == cons.shape)
+    dx = simulationGrid.dx
+    assert (dx > 0)
+    bcx = simulationGrid.BcX
+    assert (bcx == OUTFLOW or bcx == PERIODIC)
+    assert (tEnd >= tStart)
+    assert (startCycle >= 0 and maxCycles > 0)
+    n = prim.shape[1]
+    order = _order(reconstructOrder)
+    mode = arith or default_arith()
+    key = ("hydro1d", n, float(dx), bcx, float(gamma), order, bool(entropyFix), float(epsilon),
+           float(minDens), float(minPres), float(minEnergy), mode)
+    g = _handle(key, lambda: Grid1D(n, dx, bcx, gamma, mhd=False, recon=order, entropy_fix=entropyFix,
+                                    eps=epsilon, min_d=minDens, min_p=minPres, min_e=minEnergy, arith=mode))
+    g.upload(prim, cons)
+    t, cycle, t_sl = g.advance(tStart, tEnd, startCycle, maxCycles, cfl)
+    if g.last_cycles > 0:
+        sl_prim, sl_cons = g.download(1)
+        g.download(0, prim, cons)
+    else:
+        sl_prim, sl_cons = np.copy(prim), np.copy(cons)
+    return prim, cons, t, cycle, sl_prim, sl_cons, t_sl

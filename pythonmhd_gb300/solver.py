@@ -161,6 +161,49 @@ class Grid2D:
         return s.value
 
 
+class Grid1D(Grid2D):
+    """One 1D grid of n cells (the reference's evolve_1D_mhd / evolve_1D_hydro step).
+
+    States are (nvars, n); ``advance``/``download`` are Grid2D's (no face arrays).
+    MHD keeps B_x uniform at the uploaded prim[4][0], as the reference does.
+    """
+
+    def __init__(self, n, dx, bcx, gamma, mhd=True, recon=2, entropy_fix=False, eps=0.5, min_d=1e-12,
+                 min_p=1e-12, min_e=1e-12, arith=None):
+        self.lib = _lib.load()
+        self.ny, self.nx = 1, int(n)
+        self.mhd = bool(mhd)
+        self.nvars = 8 if self.mhd else 5
+        self.arith = arith or default_arith()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.mhd1d_create(self.nx, float(dx), int(bcx), float(gamma), 1 if self.mhd else 0,
+                                         int(recon), 1 if entropy_fix else 0, float(eps), float(min_d),
+                                         float(min_p), float(min_e), ARITH[self.arith], ctypes.byref(h)),
+                   "mhd1d_create")
+        self._h = h
+        self.last_cycles = 0
+
+    def upload(self, prim, cons, fbx=None, fby=None):
+        prim, cons = _as_f64c(prim), _as_f64c(cons)
+        if prim.shape != (self.nvars, self.nx) or cons.shape != prim.shape:
+            raise ValueError(f"prim/cons must be {(self.nvars, self.nx)}")
+        _lib.check(self.lib.mhd1d_upload(self._h, _ptr(prim), _ptr(cons)), "mhd1d_upload")
+
+    def download(self, which=0, prim=None, cons=None, fbx=None, fby=None):
+        """(prim, cons) of the current (0) or second-last (1) state, as (nvars, n) arrays."""
+        p = np.empty((self.nvars, 1, self.nx))
+        c = np.empty((self.nvars, 1, self.nx))
+        _lib.check(self.lib.mhd2d_download(self._h, int(which), _ptr(p), _ptr(c), None, None), "mhd2d_download")
+        p, c = p[:, 0, :], c[:, 0, :]
+        if prim is not None:
+            prim[...] = p
+            p = prim
+        if cons is not None:
+            cons[...] = c
+            c = cons
+        return p, c
+
+
 class Batch2D:
     """Many independent grids advanced together (one persistent launch per stage).
 

@@ -204,3 +204,113 @@ def build(physics, name):
 
 def names(physics):
     return [n for n, _ in (mhd_cases() if physics == "mhd" else hydro_cases())]
+
+
+# ---------------------------------------------------------------------------
+# 1D cases (evolve_1D_mhd / evolve_1D_hydro): state arrays (nvars, N)
+# ---------------------------------------------------------------------------
+def _p1(**kw):
+    p = dict(t_start=0.0, t_end=10.0, start_cycle=0, max_cycles=6, gamma=G53, cfl=0.4,
+             min_d=1e-12, min_p=1e-12, min_e=1e-12, order=2, efix=False, eps=0.5, bcx=ic.OUTFLOW)
+    p.update(kw)
+    return p
+
+
+def _brio_wu(n, gamma=2.0):
+    prim = np.zeros((8, n))
+    left = np.arange(n) < n // 2
+    prim[0] = np.where(left, 1.0, 0.125)
+    prim[4] = 0.75
+    prim[5] = np.where(left, 1.0, -1.0)
+    prim[7] = np.where(left, 1.0, 0.1)
+    return prim, ic.prim_to_cons_mhd(prim, gamma)
+
+
+def _random_mhd_1d(n, seed, gamma=G53):
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + 0.5) / n
+    prim = np.zeros((8, n))
+    prim[0] = 1.0 + 0.3 * np.sin(2 * math.pi * x) + 0.05 * rng.standard_normal(n)
+    prim[1] = 0.4 * np.cos(2 * math.pi * x) + 0.05 * rng.standard_normal(n)
+    prim[2] = 0.2 * np.sin(4 * math.pi * x)
+    prim[3] = 0.1 * np.cos(6 * math.pi * x)
+    prim[4] = 0.6
+    prim[5] = 0.5 * np.sin(2 * math.pi * x + 0.3)
+    prim[6] = 0.3 * np.cos(2 * math.pi * x + 0.1)
+    prim[7] = 0.8 + 0.2 * np.cos(2 * math.pi * x) + 0.02 * rng.standard_normal(n)
+    return prim, ic.prim_to_cons_mhd(prim, gamma)
+
+
+def mhd1d_cases():
+    def brio_wu(order, **kw):
+        def f():
+            prim, cons = _brio_wu(64)
+            return dict(prim=prim, cons=cons, dx=1.0 / 64, **_p1(gamma=2.0, order=order, max_cycles=12, **kw))
+        return f
+
+    def random(order, bc, **kw):
+        def f():
+            prim, cons = _random_mhd_1d(48, 3)
+            return dict(prim=prim, cons=cons, dx=1.0 / 48, **_p1(order=order, bcx=bc, **kw))
+        return f
+
+    def tend_clip():
+        prim, cons = _brio_wu(40)
+        return dict(prim=prim, cons=cons, dx=1.0 / 40, **_p1(gamma=2.0, t_end=0.011, max_cycles=50))
+
+    def floors():
+        prim, cons = _random_mhd_1d(32, 5)
+        return dict(prim=prim, cons=cons, dx=1.0 / 32, **_p1(min_d=0.9, min_p=0.75, bcx=ic.PERIODIC))
+
+    return [("brio_wu_ppm", brio_wu(2)), ("brio_wu_order0", brio_wu(0)),
+            ("brio_wu_efix", brio_wu(2, efix=True, eps=0.3)),
+            ("random_periodic_ppm", random(2, ic.PERIODIC)), ("random_outflow_ppm", random(2, ic.OUTFLOW)),
+            ("random_periodic_order0", random(0, ic.PERIODIC)), ("tend_clip", tend_clip), ("floors", floors)]
+
+
+def _sod(n, gamma=1.4):
+    prim = np.zeros((5, n))
+    left = np.arange(n) < n // 2
+    prim[0] = np.where(left, 1.0, 0.125)
+    prim[4] = np.where(left, 1.0, 0.1)
+    return prim, ic.prim_to_cons_hydro(prim, gamma)
+
+
+def hydro1d_cases():
+    def sod(order, **kw):
+        def f():
+            prim, cons = _sod(64)
+            p = dict(gamma=1.4, order=order, max_cycles=12)
+            p.update(kw)
+            return dict(prim=prim, cons=cons, dx=1.0 / 64, **_p1(**p))
+        return f
+
+    def random(order, bc, **kw):
+        def f():
+            rng = np.random.default_rng(7)
+            n = 40
+            x = (np.arange(n) + 0.5) / n
+            prim = np.zeros((5, n))
+            prim[0] = 1.0 + 0.3 * np.sin(2 * math.pi * x) + 0.05 * rng.standard_normal(n)
+            prim[1] = 0.5 * np.cos(2 * math.pi * x)
+            prim[2] = 0.2 * np.sin(2 * math.pi * x)
+            prim[3] = 0.1 * np.cos(4 * math.pi * x)
+            prim[4] = 0.7 + 0.1 * np.cos(2 * math.pi * x)
+            return dict(prim=prim, cons=ic.prim_to_cons_hydro(prim, 1.4), dx=1.0 / n,
+                        **_p1(gamma=1.4, order=order, bcx=bc, **kw))
+        return f
+
+    # (the reference's 1D hydro PPM with periodic boundaries raises in np.append,
+    # Source/Reconstruction_PPM_Hydro_HelperModule.py:355, so no periodic PPM case)
+    return [("sod_ppm", sod(2)), ("sod_order0", sod(0)), ("sod_efix", sod(2, efix=True, eps=0.4)),
+            ("random_outflow_ppm", random(2, ic.OUTFLOW)), ("random_periodic_order0", random(0, ic.PERIODIC)),
+            ("random_outflow_order0", random(0, ic.OUTFLOW)), ("tend_clip", sod(2, t_end=0.013, max_cycles=50))]
+
+
+def build1d(physics, name):
+    table = dict(mhd1d_cases() if physics == "mhd" else hydro1d_cases())
+    return table[name]()
+
+
+def names1d(physics):
+    return [n for n, _ in (mhd1d_cases() if physics == "mhd" else hydro1d_cases())]

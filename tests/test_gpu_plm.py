@@ -38,7 +38,8 @@ def test_plm_mhd_bitwise_vs_oracle(name):
     c["order"] = 1
     args = (c["t_start"], c["t_end"], c["start_cycle"], c["max_cycles"], c["gamma"], c["cfl"], c["min_d"],
             c["min_p"], c["min_e"], 1, c["efix"], c["eps"])
-    got = evolve.evolve_2D_mhd(_grid(c, True), *args, arith="exact")
+    dargs = args[:9] + (evolve.PLM,) + args[10:]
+    got = evolve.evolve_2D_mhd(_grid(c, True), *dargs, arith="exact")
     want = mhd2d.evolve(c["prim"], c["cons"], c["fbx"], c["fby"], c["dx"], c["dy"], c["bcx"], c["bcy"], *args)
     for a, b in zip(got, want):
         assert np.array_equal(np.asarray(a), np.asarray(b))
@@ -49,7 +50,8 @@ def test_plm_hydro_bitwise_vs_oracle(name):
     c = cases.build("hydro", name)
     args = (c["t_start"], c["t_end"], c["start_cycle"], c["max_cycles"], c["gamma"], c["cfl"], c["min_d"],
             c["min_p"], c["min_e"], 1, c["efix"], c["eps"])
-    got = evolve.evolve_2D_hydro(_grid(c, False), *args, arith="exact")
+    dargs = args[:9] + (evolve.PLM,) + args[10:]
+    got = evolve.evolve_2D_hydro(_grid(c, False), *dargs, arith="exact")
     want = hydro2d.evolve(c["prim"], c["cons"], c["dx"], c["dy"], c["bcx"], c["bcy"], *args)
     for a, b in zip(got, want):
         assert np.array_equal(np.asarray(a), np.asarray(b))
@@ -60,7 +62,7 @@ def test_plm_ot_128_bitwise_vs_oracle():
     args = (0.0, 1e30, 0, 4, 5 / 3, 0.4, 1e-12, 1e-12, 1e-12, 1, False, 0.5)
     g = SimpleNamespace(primVars=prim.copy(), consVars=cons.copy(), faceBx=fbx.copy(), faceBy=fby.copy(),
                         dx=dx, dy=dy, BcX=1, BcY=1)
-    got = evolve.evolve_2D_mhd(g, *args, arith="exact")
+    got = evolve.evolve_2D_mhd(g, *(args[:9] + (evolve.PLM,) + args[10:]), arith="exact")
     want = mhd2d.evolve(prim, cons, fbx, fby, dx, dy, 1, 1, *args)
     for a, b in zip(got, want):
         assert np.array_equal(np.asarray(a), np.asarray(b))
@@ -122,3 +124,22 @@ def test_second_order_convergence_on_a_smooth_wave(recon):
     e1 = _advected_wave_error(32, recon)
     e2 = _advected_wave_error(64, recon)
     assert e1 / e2 > 3.0, (e1, e2)
+
+
+@pytest.mark.parametrize("physics", ["mhd", "hydro"])
+def test_dropin_reconstruct_order_1_is_first_order_as_in_the_reference(physics):
+    """The reference runs first order for every reconstructOrder other than 2 (its PLM
+    branches are commented out); the drop-in keeps that, PLM needs evolve.PLM."""
+    name = "ot_ppm" if physics == "mhd" else "blast_ppm"
+    c = cases.build(physics, name)
+    args = (c["t_start"], c["t_end"], c["start_cycle"], c["max_cycles"], c["gamma"], c["cfl"], c["min_d"],
+            c["min_p"], c["min_e"], 1, c["efix"], c["eps"])
+    fn = evolve.evolve_2D_mhd if physics == "mhd" else evolve.evolve_2D_hydro
+    got = fn(_grid(c, physics == "mhd"), *args, arith="exact")
+    o0 = args[:9] + (0,) + args[10:]
+    if physics == "mhd":
+        want = mhd2d.evolve(c["prim"], c["cons"], c["fbx"], c["fby"], c["dx"], c["dy"], c["bcx"], c["bcy"], *o0)
+    else:
+        want = hydro2d.evolve(c["prim"], c["cons"], c["dx"], c["dy"], c["bcx"], c["bcy"], *o0)
+    for a, b in zip(got, want):
+        assert np.array_equal(np.asarray(a), np.asarray(b))

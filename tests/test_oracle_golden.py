@@ -35,3 +35,22 @@ def test_oracle_hydro_matches_reference_bitwise(path):
 def test_golden_set_is_complete():
     assert len(golden_files("mhd")) >= 18
     assert len(golden_files("hydro")) >= 8
+
+
+@pytest.mark.parametrize("path", golden_files("mhd1d") + golden_files("hydro1d"), ids=case_id)
+def test_oracle_1d_matches_reference_bitwise(path):
+    """The 1D restatement (oracle/evolve1d.py) against evolve_1D_mhd / evolve_1D_hydro
+    (Source/EvolveFunctions_MHD.py:195, Source/EvolveFunctions_Hydro.py:232)."""
+    from oracle import evolve1d
+    p, i, o = load(path)
+    fn = evolve1d.evolve_mhd if case_id(path).startswith("mhd1d") else evolve1d.evolve_hydro
+    res = fn(i["prim"], i["cons"], p["dx"], p["bcx"], p["t_start"], p["t_end"], p["start_cycle"],
+             p["max_cycles"], p["gamma"], p["cfl"], p["min_d"], p["min_p"], p["min_e"], p["order"], p["efix"],
+             p["eps"])
+    for k, v in zip(HYDRO_KEYS, res):
+        assert np.array_equal(np.asarray(v), o[k]), k
+
+
+def test_golden_1d_set_is_complete():
+    assert len(golden_files("mhd1d")) >= 8
+    assert len(golden_files("hydro1d")) >= 7
