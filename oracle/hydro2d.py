@@ -1,9 +1,10 @@
 """CPU oracle: one 2D CTU cycle of adiabatic hydrodynamics, restated in NumPy.
 
 TEST INFRASTRUCTURE ONLY (see ``oracle/common.py``). State vectors are
-[rho, vx, vy, vz, p] / [rho, mx, my, mz, E] in both sweeps; the y-direction
-routines differ from the x ones in the order of a few sums and in the order
-of their waves, which is kept here through the ``yaxis`` flag.
+[rho, vx, vy, vz, p] / [rho, mx, my, mz, E] in every sweep; the y- and
+z-direction routines differ from the x ones in the order of a few sums and in
+the order of their waves, which is kept here through the ``yaxis`` argument:
+False / 0 is x, True / 1 is y and 2 is z (the z forms serve ``oracle/hydro3d.py``).
 """
 from __future__ import annotations
 
@@ -14,13 +15,15 @@ from .common import (FOUR_THIRDS, OUTFLOW, SMALL_VALUE, apply_floors_inplace,
 
 
 def prim_to_cons(w, gamma, yaxis=False):
-    """primToCons_hydro_x / _y (Source/PrimCons_HelperModule.py:46-83)."""
+    """primToCons_hydro_x / _y / _z (Source/PrimCons_HelperModule.py:46-114)."""
     u = np.empty_like(w)
     u[0] = w[0]
     u[1] = w[0] * w[1]
     u[2] = w[0] * w[2]
     u[3] = w[0] * w[3]
-    if yaxis:
+    if yaxis == 2:
+        ke = np.square(w[3]) + np.square(w[1]) + np.square(w[2])
+    elif yaxis:
         ke = np.square(w[2]) + np.square(w[3]) + np.square(w[1])
     else:
         ke = np.square(w[1]) + np.square(w[2]) + np.square(w[3])
@@ -29,14 +32,16 @@ def prim_to_cons(w, gamma, yaxis=False):
 
 
 def cons_to_prim(u, gamma, yaxis=False):
-    """consToPrim_hydro_x / _y (Source/PrimCons_HelperModule.py:135-171)."""
+    """consToPrim_hydro_x / _y / _z (Source/PrimCons_HelperModule.py:135-196)."""
     w = np.empty_like(u)
     w[0] = u[0]
     inv_d = 1.0 / w[0]
     w[1] = u[1] * inv_d
     w[2] = u[2] * inv_d
     w[3] = u[3] * inv_d
-    if yaxis:
+    if yaxis == 2:
+        m2 = np.square(u[3]) + np.square(u[1]) + np.square(u[2])
+    elif yaxis:
         m2 = np.square(u[2]) + np.square(u[3]) + np.square(u[1])
     else:
         m2 = np.square(u[1]) + np.square(u[2]) + np.square(u[3])
@@ -63,15 +68,14 @@ def calc_dt(cons, gamma, cfl, dx, dy):
 
 
 def prim_eigensystem(w, gamma, yaxis=False):
-    """getEigenmatricesX/Y_hydro (Source/ReconstructionEigenmatrices_Hydro_HelperModule.py:25-151).
+    """getEigenmatricesX/Y/Z_hydro (Source/ReconstructionEigenmatrices_Hydro_HelperModule.py:25-151, :230-282).
 
     Wave order: x = (acoustic-, entropy, vy, vz, acoustic+),
-                y = (acoustic-, vx, entropy, vz, acoustic+).
+                y = (acoustic-, vx, entropy, vz, acoustic+),
+                z = (acoustic-, vx, vy, entropy, acoustic+).
     """
-    n = 2 if yaxis else 1
-    ent = 2 if yaxis else 1
-    sh1 = 1 if yaxis else 2       # wave carrying the first shear component
-    sh1v = 1 if yaxis else 2      # its velocity slot
+    n = 3 if yaxis == 2 else (2 if yaxis else 1)
+    ent = n                       # the entropy wave sits at the normal velocity's index
     a2 = gamma * w[4] / w[0]
     a = np.sqrt(a2)
     vn = w[n]
@@ -81,8 +85,9 @@ def prim_eigensystem(w, gamma, yaxis=False):
     R[n, 0] = -a / w[0]
     R[4, 0] = a2
     R[0, ent] = np.ones_like(a)
-    R[sh1v, sh1] = np.ones_like(a)
-    R[3, 3] = np.ones_like(a)
+    for k in (1, 2, 3):           # shear waves: wave k carries velocity slot k
+        if k != ent:
+            R[k, k] = np.ones_like(a)
     R[0, 4] = np.ones_like(a)
     R[n, 4] = -R[n, 0]
     R[4, 4] = a2
@@ -91,8 +96,9 @@ def prim_eigensystem(w, gamma, yaxis=False):
     L[0, 4] = 0.5 / a2
     L[ent, 0] = np.ones_like(a)
     L[ent, 4] = -1.0 / a2
-    L[sh1, sh1v] = np.ones_like(a)
-    L[3, 3] = np.ones_like(a)
+    for k in (1, 2, 3):
+        if k != ent:
+            L[k, k] = np.ones_like(a)
     L[4, n] = -L[0, n]
     L[4, 4] = L[0, 4]
     return lam, L, R
@@ -226,15 +232,18 @@ def faces_from_cells(lia, ria, bc):
 
 
 def roe_flux(wl, wr, gamma, efix, eps, yaxis):
-    """riemannSolverX/Y_hydro_roe (Source/RiemannSolvers_Hydro_Roe_HelperModule.py:68-328, :342-596)."""
+    """riemannSolverX/Y/Z_hydro_roe (Source/RiemannSolvers_Hydro_Roe_HelperModule.py:68-328, :342-596,
+    :614-869)."""
     ul = prim_to_cons(wl, gamma, yaxis)
     ur = prim_to_cons(wr, gamma, yaxis)
-    n = 2 if yaxis else 1
+    n = 3 if yaxis == 2 else (2 if yaxis else 1)
     sl = np.sqrt(wl[0])
     sr = np.sqrt(wr[0])
     isum = 1.0 / (sl + sr)
     v = {k: (sl * wl[k] + sr * wr[k]) * isum for k in (1, 2, 3)}
-    if yaxis:
+    if yaxis == 2:
+        vsq = v[3] * v[3] + v[1] * v[1] + v[2] * v[2]
+    elif yaxis:
         vsq = v[2] * v[2] + v[3] * v[3] + v[1] * v[1]
     else:
         vsq = v[1] * v[1] + v[2] * v[2] + v[3] * v[3]
@@ -251,7 +260,47 @@ def roe_flux(wl, wr, gamma, efix, eps, yaxis):
     nf = 0.5 / a2
     g1 = gamma - 1.0
     gn = g1 / a2
-    if not yaxis:
+    if yaxis == 2:
+        # wave order (acoustic-, vy, entropy, vx, acoustic+) (:720-783)
+        R[0, 0] = one
+        R[1, 0] = v[1]
+        R[2, 0] = v[2]
+        R[3, 0] = v[3] - a
+        R[4, 0] = H - v[3] * a
+        R[2, 1] = one
+        R[4, 1] = v[2]
+        R[0, 2] = one
+        R[1, 2] = v[1]
+        R[2, 2] = v[2]
+        R[3, 2] = v[3]
+        R[4, 2] = 0.5 * vsq
+        R[1, 3] = one
+        R[4, 3] = v[1]
+        R[0, 4] = one
+        R[1, 4] = v[1]
+        R[2, 4] = v[2]
+        R[3, 4] = v[3] + a
+        R[4, 4] = H + v[3] * a
+        L[0, 0] = nf * (0.5 * g1 * vsq + v[3] * a)
+        L[0, 1] = -nf * g1 * v[1]
+        L[0, 2] = -nf * g1 * v[2]
+        L[0, 3] = -nf * (g1 * v[3] + a)
+        L[0, 4] = nf * g1
+        L[1, 0] = -v[2]
+        L[1, 2] = one
+        L[2, 0] = 1.0 - nf * g1 * vsq
+        L[2, 1] = gn * v[1]
+        L[2, 2] = gn * v[2]
+        L[2, 3] = gn * v[3]
+        L[2, 4] = -gn
+        L[3, 0] = -v[1]
+        L[3, 1] = one
+        L[4, 0] = nf * (0.5 * g1 * vsq - v[3] * a)
+        L[4, 1] = L[0, 1]
+        L[4, 2] = L[0, 2]
+        L[4, 3] = -nf * (g1 * v[3] - a)
+        L[4, 4] = L[0, 4]
+    elif not yaxis:
         R[0, 0] = one
         R[1, 0] = v[1] - a
         R[2, 0] = v[2]
@@ -331,10 +380,9 @@ def roe_flux(wl, wr, gamma, efix, eps, yaxis):
         L[4, 4] = L[0, 4]
 
     def cell_flux(w, u):
-        return np.array([u[n],
-                         u[n] * w[1] + (w[4] if n == 1 else 0.0),
-                         u[n] * w[2] + (w[4] if n == 2 else 0.0),
-                         u[n] * w[3],
+        def mom(k):  # the normal momentum flux carries the pressure
+            return u[n] * w[k] + w[4] if k == n else u[n] * w[k]
+        return np.array([u[n], mom(1), mom(2), mom(3),
                          (u[4] + w[4]) * w[n]])
 
     fl = cell_flux(wl, ul)

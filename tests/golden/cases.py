@@ -314,3 +314,103 @@ def build1d(physics, name):
 
 def names1d(physics):
     return [n for n, _ in (mhd1d_cases() if physics == "mhd" else hydro1d_cases())]
+
+
+# ----------------------------------------------------------------------------
+# 3D hydro (evolve_3D_hydro): arrays (nvars, ny, nx, nz).  The reference's 3D
+# step raises with an outflow x boundary (Source/EvolveFunctions_Hydro.py:700-703
+# reshape a z-flux slab to a y-flux shape), so every 3D case has a periodic x.
+# ----------------------------------------------------------------------------
+def _p3(**kw):
+    p = dict(t_start=0.0, t_end=10.0, start_cycle=0, max_cycles=3, gamma=1.4, cfl=0.4, min_d=1e-12,
+             min_p=1e-12, min_e=1e-12, order=2, efix=False, eps=0.5, bcx=ic.PERIODIC, bcy=ic.PERIODIC,
+             bcz=ic.PERIODIC)
+    p.update(kw)
+    return p
+
+
+def _random_hydro_3d(ny, nx, nz, seed, gamma=1.4, mach=0.5):
+    """Smooth random fields (a few 3D Fourier modes) plus a little cell noise."""
+    rng = np.random.default_rng(seed)
+    y, x, z = np.meshgrid((np.arange(ny) + 0.5) / ny, (np.arange(nx) + 0.5) / nx, (np.arange(nz) + 0.5) / nz,
+                          indexing="ij")
+
+    def field():
+        f = np.zeros((ny, nx, nz))
+        for _ in range(3):
+            k = rng.integers(1, 3, size=3)
+            ph = rng.uniform(0, 2 * math.pi, size=3)
+            f += (rng.standard_normal() * np.sin(2 * math.pi * k[0] * x + ph[0]) * np.cos(2 * math.pi * k[1] * y + ph[1])
+                  * np.cos(2 * math.pi * k[2] * z + ph[2]))
+        return f / 3.0 + 0.02 * rng.standard_normal((ny, nx, nz))
+
+    prim = np.zeros((5, ny, nx, nz))
+    prim[0] = 1.0 + 0.3 * field()
+    prim[0] = np.maximum(prim[0], 0.3)
+    prim[1] = mach * field()
+    prim[2] = mach * field()
+    prim[3] = mach * field()
+    prim[4] = 1.0 / gamma + 0.2 * field()
+    prim[4] = np.maximum(prim[4], 0.1)
+    return prim, ic.prim_to_cons_hydro(prim, gamma)
+
+
+def _blast_3d(ny, nx, nz, gamma=1.4):
+    prim = np.zeros((5, ny, nx, nz))
+    prim[0] = 1.0
+    prim[4] = 0.1
+    prim[4, ny // 2 - 1:ny // 2 + 1, nx // 2 - 1:nx // 2 + 1, nz // 2 - 1:nz // 2 + 1] = 10.0
+    return prim, ic.prim_to_cons_hydro(prim, gamma)
+
+
+def hydro3d_cases():
+    def rnd(shape=(6, 8, 5), seed=11, mach=0.5, **kw):
+        def f():
+            ny, nx, nz = shape
+            prim, cons = _random_hydro_3d(ny, nx, nz, seed, mach=mach)
+            return dict(prim=prim, cons=cons, dx=1.0 / nx, dy=1.0 / ny, dz=1.0 / nz, **_p3(**kw))
+        return f
+
+    def blast(**kw):
+        def f():
+            prim, cons = _blast_3d(8, 8, 8)
+            return dict(prim=prim, cons=cons, dx=1.0 / 8, dy=1.0 / 8, dz=1.0 / 8, **_p3(**kw))
+        return f
+
+    def floors(order):
+        # one interior cell below both floors: the reference's 3D floor routine raises
+        # while it formats its message once three or more values of one array are
+        # floored (Source/PrimCons_HelperModule.py:537-548 index with the message
+        # loop's counter), so only that cell's own face states are floored
+        def f():
+            prim, _ = _random_hydro_3d(6, 8, 5, 15, mach=0.3)
+            prim[0, 3, 4, 2] = 0.2
+            prim[4, 3, 4, 2] = 0.05
+            return dict(prim=prim, cons=ic.prim_to_cons_hydro(prim, 1.4), dx=1.0 / 8, dy=1.0 / 6, dz=1.0 / 5,
+                        **_p3(min_d=0.25, min_p=0.06, order=order, max_cycles=1))
+        return f
+
+    def uniform():
+        prim = np.zeros((5, 4, 5, 6))
+        prim[0] = 1.0
+        prim[4] = 0.6
+        return dict(prim=prim, cons=ic.prim_to_cons_hydro(prim, 1.4), dx=0.2, dy=0.25, dz=1.0 / 6, **_p3())
+
+    O, P = ic.OUTFLOW, ic.PERIODIC
+    return [("random_ppm", rnd()), ("random_ppm_ybc_outflow", rnd(bcy=O)),
+            ("random_ppm_zbc_outflow", rnd(bcz=O)), ("random_ppm_yzbc_outflow", rnd(bcy=O, bcz=O, seed=12)),
+            ("random_order0", rnd(order=0)), ("random_order0_yzbc_outflow", rnd(order=0, bcy=O, bcz=O)),
+            ("random_efix", rnd(efix=True, eps=0.4)), ("supersonic", rnd(mach=2.5, seed=13)),
+            ("supersonic_order0_efix", rnd(mach=2.5, seed=14, order=0, efix=True, eps=0.3)),
+            ("floors_ppm", floors(2)), ("floors_order0", floors(0)), ("blast_ppm", blast(max_cycles=4)),
+            ("blast_tend_clip", blast(t_end=0.011, max_cycles=50)), ("uniform_static", uniform),
+            ("no_cycle", rnd(start_cycle=4, max_cycles=4)), ("cube_4", rnd(shape=(4, 4, 4), seed=16))]
+
+
+def build3d(physics, name):
+    assert physics == "hydro"
+    return dict(hydro3d_cases())[name]()
+
+
+def names3d(physics):
+    return [n for n, _ in hydro3d_cases()] if physics == "hydro" else []

@@ -5,8 +5,8 @@ so the tests do not need the reference):
 
     python -B tests/golden/make_golden.py /root/reference/PythonMHD
 
-For every case in ``tests/golden/cases.py`` (2D; and the 1D cases with
-``evolve_1D_mhd`` / ``evolve_1D_hydro``) this imports the reference's own
+For every case in ``tests/golden/cases.py`` (2D; the 1D cases with
+``evolve_1D_mhd`` / ``evolve_1D_hydro``; the 3D cases with ``evolve_3D_hydro``) this imports the reference's own
 ``Source.EvolveFunctions_MHD.evolve_2D_mhd`` / ``Source.EvolveFunctions_Hydro.evolve_2D_hydro``
 (which depend only on NumPy), calls it on a minimal grid object carrying the
 attributes the reference reads (Source/EvolveFunctions_MHD.py:396-444,
@@ -93,6 +93,41 @@ def main_1d(ref_root):
             print(f"{path}: cycles={int(outs['out_cycle'])} t={float(outs['out_t']):.6g}")
 
 
+SCALARS_3D = ("t_start", "t_end", "start_cycle", "max_cycles", "gamma", "cfl", "min_d", "min_p",
+              "min_e", "order", "efix", "eps", "bcx", "bcy", "bcz", "dx", "dy", "dz")
+
+
+def run_reference_3d(ref_root, physics, case):
+    """evolve_3D_hydro (Source/EvolveFunctions_Hydro.py:559-806) on a grid object with the
+    attributes it reads."""
+    sys.path.insert(0, ref_root)
+    import Source.EvolveFunctions_Hydro as ref_hydro  # noqa: E402
+    ny, nx, nz = case["prim"].shape[1:]
+    grid = SimpleNamespace(primVars=case["prim"].copy(), consVars=case["cons"].copy(), dx=case["dx"],
+                           dy=case["dy"], dz=case["dz"], BcX=case["bcx"], BcY=case["bcy"], BcZ=case["bcz"],
+                           numXCells=nx, numYCells=ny, numZCells=nz)
+    args = (grid, case["t_start"], case["t_end"], case["start_cycle"], case["max_cycles"], case["gamma"],
+            case["cfl"], case["min_d"], case["min_p"], case["min_e"], case["order"], case["efix"], case["eps"])
+    with contextlib.redirect_stdout(io.StringIO()):
+        res = ref_hydro.evolve_3D_hydro(*args)
+    keys = ("prim", "cons", "t", "cycle", "sl_prim", "sl_cons", "sl_t")
+    return {"out_" + k: np.asarray(v) for k, v in zip(keys, res)}
+
+
+def main_3d(ref_root):
+    for physics in ("hydro",):
+        for name in cases.names3d(physics):
+            case = cases.build3d(physics, name)
+            outs = run_reference_3d(ref_root, physics, case)
+            arrays = {"in_prim": case["prim"], "in_cons": case["cons"]}
+            for k in SCALARS_3D:
+                arrays["p_" + k] = np.asarray(case[k])
+            arrays.update(outs)
+            path = os.path.join(HERE, f"{physics}3d_{name}.npz")
+            np.savez_compressed(path, **arrays)
+            print(f"{path}: cycles={int(outs['out_cycle'])} t={float(outs['out_t']):.6g}")
+
+
 def main(ref_root):
     for physics in ("mhd", "hydro"):
         for name in cases.names(physics):
@@ -110,10 +145,12 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    # make_golden.py [reference root] [2d|1d|all]
+    # make_golden.py [reference root] [2d|1d|3d|all]
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/PythonMHD"
     which = sys.argv[2] if len(sys.argv) > 2 else "all"
     if which in ("2d", "all"):
         main(root)
     if which in ("1d", "all"):
         main_1d(root)
+    if which in ("3d", "all"):
+        main_3d(root)
