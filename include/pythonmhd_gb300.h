@@ -242,6 +242,33 @@ int mhd2d_adj_restore(void* handle, const double* checkpoints, int steps, int ev
 int mhd2d_adj_info(void* handle, size_t* state_words, size_t* device_bytes, int* segment_sets);
 void mhd2d_adj_destroy(void* handle);
 
+/* ---------------------------------------------------------------------------
+ * 3D step (hydro): replaces the reference's
+ *   Source/EvolveFunctions_Hydro.py:559-560  evolve_3D_hydro(simulationGrid, tStart, tEnd,
+ *                                            startCycle, maxCycles, gamma, cfl, minDens,
+ *                                            minPres, minEnergy, reconstructOrder,
+ *                                            entropyFix, epsilon)
+ * States are (5, ny, nx, nz), z fastest (the reference's layout, also the device
+ * layout).  bcx/bcy/bcz: 0 outflow, 1 periodic; recon: 2 PPM, 0 first order, 1
+ * PLM (an addition).  physics must be MHD2D_HYDRO (the 3D MHD step is not built).
+ * The evolve loop, second-last state and download semantics are mhd2d_advance's /
+ * mhd2d_download's.  nx, ny, nz >= 2; (nx+2)(ny+2)(nz+2) below 2^32.
+ * ------------------------------------------------------------------------- */
+int mhd3d_create(int ny, int nx, int nz, double dx, double dy, double dz, int bcx, int bcy, int bcz,
+                 double gamma, int physics, int recon, int entropy_fix, double eps, double min_d, double min_p,
+                 double min_e, int arith, void** handle);
+int mhd3d_upload(void* handle, const double* prim, const double* cons);
+/* as mhd3d_upload, from device pointers */
+int mhd3d_upload_device(void* handle, const double* prim, const double* cons);
+int mhd3d_advance(void* handle, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
+                  double* t_out, long long* cycle_out, double* t_second_last);
+int mhd3d_download(void* handle, int which, double* prim, double* cons);
+/* device pointers of the current (which = 0) or second-last (1) state */
+int mhd3d_state_ptrs(void* handle, int which, double** prim, double** cons);
+/* kernel launches of the last advance, device bytes held, the handle's cudaStream_t */
+int mhd3d_info(void* handle, long long* last_launches, size_t* device_bytes, void** stream);
+void mhd3d_destroy(void* handle);
+
 const char* mhd2d_strerror(int status);
 void mhd2d_destroy(void* handle);
 

@@ -6,6 +6,8 @@ shared library with a plain C ABI (``include/pythonmhd_gb300.h``):
 * ``csrc/kernels_exact.cu``  -- the step kernels with ``-fmad=false``
 * ``csrc/kernels_fast.cu``   -- the same kernels with FMA contraction
 * ``csrc/capi.cu``           -- handles, copies and the CUDA-graph evolve loop
+* ``csrc/kernels3d_exact.cu`` / ``csrc/kernels3d_fast.cu`` -- the 3D hydro step kernels
+* ``csrc/capi3d.cu``         -- the 3D handle and its evolve loop
 * ``csrc/noalloc.cu``        -- the CFL timestep for callers that cannot allocate
 * ``csrc/adjoint.cu``        -- the reverse-mode adjoint of the MHD step; its pointwise
   stage functions (``csrc/adjoint_gen.cuh``) are generated from ``adjoint/stages.py``
@@ -30,6 +32,9 @@ UNITS = [
     ("kernels_exact.cu", ["-fmad=false"]),
     ("kernels_fast.cu", ["-fmad=true"]),
     ("capi.cu", []),
+    ("kernels3d_exact.cu", ["-fmad=false"]),
+    ("kernels3d_fast.cu", ["-fmad=true"]),
+    ("capi3d.cu", []),
     ("noalloc.cu", ["-fmad=false"]),
     ("adjoint.cu", []),
 ]

@@ -83,17 +83,16 @@ template <int AX>
 struct HydroSweep {
   static constexpr int NV = 5;
   static constexpr int NW = 10;
-  static constexpr bool Y = AX == 1;
   static constexpr int BN = -1;
   static constexpr int SB = -1;
   __device__ static constexpr int src(int k) { return k; }
   __device__ static constexpr int ord(int k) { return k; }
   using Eig = HPrimEig;
-  __device__ static void eig(const double* w, double, double gamma, Eig& e) { hprim_eigensystem<Y>(w, gamma, e); }
-  __device__ static bool Lnz(int i, int j) { return hprim_L_nz<Y>(i, j); }
-  __device__ static bool Rnz(int i, int j) { return hprim_R_nz<Y>(i, j); }
-  __device__ static double L(const Eig& e, int i, int j) { return hprim_L<Y>(e, i, j); }
-  __device__ static double R(const Eig& e, int i, int j) { return hprim_R<Y>(e, i, j); }
+  __device__ static void eig(const double* w, double, double gamma, Eig& e) { hprim_eigensystem<AX>(w, gamma, e); }
+  __device__ static bool Lnz(int i, int j) { return hprim_L_nz<AX>(i, j); }
+  __device__ static bool Rnz(int i, int j) { return hprim_R_nz<AX>(i, j); }
+  __device__ static double L(const Eig& e, int i, int j) { return hprim_L<AX>(e, i, j); }
+  __device__ static double R(const Eig& e, int i, int j) { return hprim_R<AX>(e, i, j); }
   __device__ static double* lam(Eig& e) { return e.lam; }
   __device__ static void store(const Eig& e, double* p, size_t stride) {
     const double* s = reinterpret_cast<const double*>(&e);
@@ -151,6 +150,53 @@ __device__ __forceinline__ void load_sweep_cell(const double* prim, size_t plane
   for (int k = 0; k < S::NV; ++k) w[k] = __ldg(prim + S::src(k) * plane + idx);
 }
 
+// Characteristic-limited slope of one cell from its two neighbours, in primitive
+// variables: the differences projected on the left eigenvectors, limited (van Leer
+// weight, 2x one-sided and centred bounds), and mapped back with the right
+// eigenvectors (Source/Reconstruction_PPM_MHD_HelperModule.py:317-389, Hydro :86-200).
+template <class S>
+__device__ __forceinline__ void limited_slopes(const double* wl, const double* wc, const double* wr,
+                                               const typename S::Eig& e, double* out) {
+  constexpr int NV = S::NV;
+  double dc[NV], dl[NV], dr[NV], wt[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    dc[k] = wr[k] - wl[k];
+    dl[k] = wc[k] - wl[k];
+    dr[k] = wr[k] - wc[k];
+    wt[k] = (dl[k] * dr[k] > 0.0) ? (2.0 * dl[k] * dr[k]) / (dl[k] + dr[k]) : 0.0;
+  }
+  double sc[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const double cc = project<S>(e, i, dc);
+    const double cl = project<S>(e, i, dl);
+    const double cr = project<S>(e, i, dr);
+    const double cw = project<S>(e, i, wt);
+    double s = 0.0;
+    if (cl * cr > 0.0) {
+      const double lim1 = dmin(fabs(cl), fabs(cr));
+      const double lim2 = dmin(0.5 * fabs(cc), fabs(cw));
+      s = signed_mag(cc, dmin(2.0 * lim1, lim2));
+    }
+    sc[i] = s;
+  }
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double acc = 0.0;
+    bool first = true;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      if (S::Rnz(i, j)) {
+        const double tt = sc[j] * S::R(e, i, j);
+        acc = first ? tt : acc + tt;
+        first = false;
+      }
+    }
+    out[i] = acc;
+  }
+}
+
 // ----------------------------------------------------------------------------
 // PPM phase A: eigensystem + monotonised characteristic slopes for cells -1..Ls
 // (Source/Reconstruction_PPM_MHD_HelperModule.py:317-389, Hydro :86-200)
@@ -180,46 +226,12 @@ __device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, 
                  : __ldg(in.prim + (size_t)(S::BN >= 0 ? S::BN : 0) * plane + cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx));
   typename S::Eig e;
   S::eig(wc, bn, G.gamma, e);
-
-  double dc[NV], dl[NV], dr[NV], wt[NV];
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    dc[k] = wr[k] - wl[k];
-    dl[k] = wc[k] - wl[k];
-    dr[k] = wr[k] - wc[k];
-    wt[k] = (dl[k] * dr[k] > 0.0) ? (2.0 * dl[k] * dr[k]) / (dl[k] + dr[k]) : 0.0;
-  }
-  double sc[NV];
-#pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    const double cc = project<S>(e, i, dc);
-    const double cl = project<S>(e, i, dl);
-    const double cr = project<S>(e, i, dr);
-    const double cw = project<S>(e, i, wt);
-    double s = 0.0;
-    if (cl * cr > 0.0) {
-      const double lim1 = dmin(fabs(cl), fabs(cr));
-      const double lim2 = dmin(0.5 * fabs(cc), fabs(cw));
-      s = signed_mag(cc, dmin(2.0 * lim1, lim2));
-    }
-    sc[i] = s;
-  }
+  double ps[NV];
+  limited_slopes<S>(wl, wc, wr, e, ps);
   const size_t xi = ext_index<AX>(c, t, g.nx);
   const size_t es = G.ext_plane;
 #pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    double acc = 0.0;
-    bool first = true;
-#pragma unroll
-    for (int j = 0; j < NV; ++j) {
-      if (S::Rnz(i, j)) {
-        const double tt = sc[j] * S::R(e, i, j);
-        acc = first ? tt : acc + tt;
-        first = false;
-      }
-    }
-    (AX == 0 ? G.slopes : G.slopes_y)[i * es + xi] = acc;
-  }
+  for (int i = 0; i < NV; ++i) (AX == 0 ? G.slopes : G.slopes_y)[i * es + xi] = ps[i];
   S::store(e, (AX == 0 ? G.eig : G.eig_y) + xi, es);
 }
 
@@ -251,43 +263,25 @@ __device__ __forceinline__ double bsource(const double* prim, const double* fb, 
   return half_dt * vt * ((b2 - b1) * inv_dn);
 }
 
-// ----------------------------------------------------------------------------
-// Reconstruction phase B: edge values, monotonicity, characteristic tracing and
-// face states.  MODE 2 = PPM (Source/Reconstruction_PPM_MHD_HelperModule.py:391-548),
-// MODE 1 = PLM (no reference counterpart: the reference's limited slope taken as a
-// linear profile W -/+ s/2, clamped to the neighbours, traced with the reference's
-// own tracing with the parabolic coefficient zero -- Stone et al. 2008 eqs. 38-42),
-// MODE 0 = first order (cell values copied to both faces, :489-511).
-// ----------------------------------------------------------------------------
-// work item (x, y) of the cell space nx x ny
-template <class S, int AX, int MODE>
-__device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x, int y) {
-  if (!G.loop->active) return;
-  SweepGeom g;
-  g.nx = G.nx;
-  g.Ls = AX == 0 ? G.nx : G.ny;
-  g.Lt = AX == 0 ? G.ny : G.nx;
-  g.bc = AX == 0 ? G.bcx : G.bcy;
-  int c, t;
-  if (AX == 0) { c = x; t = y; }
-  else { t = x; c = y; }
-  if (c >= g.Ls || t >= g.Lt) return;
-  const size_t plane = cell_plane(G);
+// Edge states of one cell along a sweep from the cell, its two neighbours and
+// (PLM/PPM) the limited slopes: MODE 2 = PPM interfaces, monotonicity and
+// characteristic tracing (Source/Reconstruction_PPM_MHD_HelperModule.py:391-548,
+// Hydro :202-371), MODE 1 = PLM (no reference counterpart: the reference's limited
+// slope taken as a linear profile W -/+ s/2, clamped to the neighbours, traced with
+// the reference's own tracing with the parabolic coefficient zero -- Stone et al.
+// 2008 eqs. 38-42), MODE 0 = first order (the cell value on both sides).
+// slope_at(k, d) returns slot k's slope at cell offset d in {-1, 0, 1}; eig_at(e)
+// loads the cell's stored eigensystem.  lia / ria: the states at the cell's minus /
+// plus interface.
+template <class S, int MODE, class SlopeAt, class EigAt>
+__device__ __forceinline__ void edge_states(const double* wl, const double* wc, const double* wr,
+                                            SlopeAt slope_at, EigAt eig_at, double dt, double dn, double* lia,
+                                            double* ria) {
   constexpr int NV = S::NV;
-  const double dt = G.loop->dt;
-  const double dn = AX == 0 ? G.dx : G.dy;
-  double lia[NV], ria[NV];
-  double wc[NV];
-  load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
   if (MODE == 1) {
-    double wl[NV], wr[NV];
-    load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
-    load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
-    const size_t es = G.ext_plane;
-    const size_t xc = ext_index<AX>(c, t, g.nx);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const double s_c = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xc];
+      const double s_c = slope_at(k, 0);
       double a = wc[k] - 0.5 * s_c;
       double b = wc[k] + 0.5 * s_c;
       a = dmax(dmin(wc[k], wl[k]), a);
@@ -298,7 +292,7 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
       ria[k] = b;
     }
     typename S::Eig e;
-    S::load(e, (AX == 0 ? G.eig : G.eig_y) + xc, es);
+    eig_at(e);
     const double* lam = S::lam(e);
     const double dtdx = dt / dn;
     double c1[NV];
@@ -336,18 +330,11 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
       }
     }
   } else if (MODE == 2) {
-    double wl[NV], wr[NV];
-    load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
-    load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
-    const size_t es = G.ext_plane;
-    const size_t xl = ext_index<AX>(c - 1, t, g.nx);
-    const size_t xc = ext_index<AX>(c, t, g.nx);
-    const size_t xr = ext_index<AX>(c + 1, t, g.nx);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const double s_l = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xl];
-      const double s_c = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xc];
-      const double s_r = (AX == 0 ? G.slopes : G.slopes_y)[k * es + xr];
+      const double s_l = slope_at(k, -1);
+      const double s_c = slope_at(k, 0);
+      const double s_r = slope_at(k, 1);
       double a = 0.5 * (wc[k] + wl[k]) - (s_c - s_l) / 6.0;
       double b = 0.5 * (wr[k] + wc[k]) - (s_r - s_c) / 6.0;
       const double dprod = (b - wc[k]) * (wc[k] - a);
@@ -369,7 +356,7 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
       ria[k] = b;
     }
     typename S::Eig e;
-    S::load(e, (AX == 0 ? G.eig : G.eig_y) + xc, es);
+    eig_at(e);
     const double* lam = S::lam(e);
     const double dtdx = dt / dn;
     double c1[NV], c2[NV];
@@ -434,6 +421,51 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
   } else {
 #pragma unroll
     for (int k = 0; k < NV; ++k) { lia[k] = wc[k]; ria[k] = wc[k]; }
+  }
+
+}
+
+// ----------------------------------------------------------------------------
+// Reconstruction phase B: edge values, monotonicity, characteristic tracing and
+// face states.  MODE 2 = PPM (Source/Reconstruction_PPM_MHD_HelperModule.py:391-548),
+// MODE 1 = PLM (no reference counterpart: the reference's limited slope taken as a
+// linear profile W -/+ s/2, clamped to the neighbours, traced with the reference's
+// own tracing with the parabolic coefficient zero -- Stone et al. 2008 eqs. 38-42),
+// MODE 0 = first order (cell values copied to both faces, :489-511).
+// ----------------------------------------------------------------------------
+// work item (x, y) of the cell space nx x ny
+template <class S, int AX, int MODE>
+__device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x, int y) {
+  if (!G.loop->active) return;
+  SweepGeom g;
+  g.nx = G.nx;
+  g.Ls = AX == 0 ? G.nx : G.ny;
+  g.Lt = AX == 0 ? G.ny : G.nx;
+  g.bc = AX == 0 ? G.bcx : G.bcy;
+  int c, t;
+  if (AX == 0) { c = x; t = y; }
+  else { t = x; c = y; }
+  if (c >= g.Ls || t >= g.Lt) return;
+  const size_t plane = cell_plane(G);
+  constexpr int NV = S::NV;
+  const double dt = G.loop->dt;
+  const double dn = AX == 0 ? G.dx : G.dy;
+  double lia[NV], ria[NV];
+  double wc[NV], wl[NV], wr[NV];
+  load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
+  if (MODE != 0) {
+    load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
+    load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
+  }
+  {
+    const size_t es = G.ext_plane;
+    const size_t xc = ext_index<AX>(c, t, g.nx);
+    const double* sl = AX == 0 ? G.slopes : G.slopes_y;
+    const double* eg = AX == 0 ? G.eig : G.eig_y;
+    const size_t step = AX == 0 ? 1 : (size_t)g.nx;
+    edge_states<S, MODE>(
+        wl, wc, wr, [&](int k, int d) { return sl[k * es + xc + (ptrdiff_t)d * (ptrdiff_t)step]; },
+        [&](typename S::Eig& e) { S::load(e, eg + xc, es); }, dt, dn, lia, ria);
   }
 
   // Face writes: cell c gives the right state of face c and the left state of face c+1;
@@ -516,7 +548,7 @@ __device__ __forceinline__ void b_roe_hydro(const Grid& G, size_t f) {
   double wl[5], wr[5], flux[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) { wl[k] = WL[k * nf + f]; wr[k] = WR[k * nf + f]; }
-  hroe_flux<AX == 1>(wl, wr, G.gamma, G.efix != 0, G.eps, flux);
+  hroe_flux<AX>(wl, wr, G.gamma, G.efix != 0, G.eps, flux);
   double* F = AX == 0 ? G.fx : G.fy;
 #pragma unroll
   for (int k = 0; k < 5; ++k) F[k * nf + f] = flux[k];
@@ -721,14 +753,14 @@ __device__ __forceinline__ void b_ctu_hydro(const Grid& G, size_t fl) {
     double w[5], u[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) w[k] = Wout[side][k * nf + fl];
-    hprim_to_cons<AX == 1>(w, G.gamma, u);
+    hprim_to_cons<AX>(w, G.gamma, u);
     const int fc = wrapc(f - 1 + side, Ls, bc);
     size_t i_lo, i_hi;
     if (AX == 0) { i_lo = (size_t)t * nx + fc; i_hi = (size_t)(t + 1) * nx + fc; }
     else { i_lo = (size_t)fc * (nx + 1) + t; i_hi = (size_t)fc * (nx + 1) + t + 1; }
 #pragma unroll
     for (int k = 0; k < 5; ++k) u[k] = u[k] - half_dtdt * (F[k * tfp + i_hi] - F[k * tfp + i_lo]);
-    hcons_to_prim<AX == 1>(u, G.gamma, w);
+    hcons_to_prim<AX>(u, G.gamma, w);
 #pragma unroll
     for (int k = 0; k < 5; ++k) Wout[side][k * nf + fl] = w[k];
   }
@@ -836,7 +868,7 @@ __device__ __forceinline__ void b_final_hydro(const Grid& G, const StateBuf& in,
     v = v - dtdy * (G.fy[k * yfp + yb] - G.fy[k * yfp + yt]);
     u[k] = v;
   }
-  hcons_to_prim<false>(u, G.gamma, w);
+  hcons_to_prim<0>(u, G.gamma, w);
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     out.prim[k * plane + idx] = w[k];
@@ -953,6 +985,9 @@ __device__ __forceinline__ void b_end(const Grid& G) {
   L->active = 0;
 }
 
+// MHD_BODIES_ONLY: a translation unit that wants the sweep policies and the
+// per-item bodies above without these kernels (the 3D step) defines it.
+#ifndef MHD_BODIES_ONLY
 // ============================================================================
 // Plain kernels: one grid per launch, work item from the block/thread index.
 // ============================================================================
@@ -1075,7 +1110,7 @@ __global__ void __launch_bounds__(kBlock) k_update_1d(Grid G, StateBuf in, State
 #pragma unroll
     for (int k = 0; k < 5; ++k)
       u[k] = __ldg(in.cons + k * plane + i) - dtdx * (G.fx[k * fp + i + 1] - G.fx[k * fp + i]);
-    hcons_to_prim<false>(u, G.gamma, w);
+    hcons_to_prim<0>(u, G.gamma, w);
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       out.prim[k * plane + i] = w[k];
@@ -1438,6 +1473,8 @@ void enqueue_cycle_batch(const BatchView& V, int physics, int recon, unsigned bl
   }
   kb_end<<<ib, 128, 0, s>>>(V);
 }
+
+#endif  // MHD_BODIES_ONLY
 
 }  // namespace MHD_NS
 }  // namespace mhdk

@@ -33,6 +33,7 @@ struct LoopState {
   int active;           // 1 while the cycle in flight is a real cycle
   int cur;              // state buffer (0/1) holding the current state
   int pad[2];
+  unsigned long long max_sz;  // 3D grids: bits of max(|vz| + c) over cells
 };
 
 // One state buffer: SoA planes, row-major (x fastest).

@@ -515,34 +515,42 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
 }
 
 // ---------------------------------------------------------------------------
-// Hydro (5 slots: [rho, vx, vy, vz, p] in both sweeps)
-// Source/PrimCons_HelperModule.py:46-83, :135-171 ; the y forms sum the kinetic
-// terms in the order (vy, vz, vx).
+// Hydro (5 slots: [rho, vx, vy, vz, p] in every sweep); template argument A is
+// the sweep direction (0 x, 1 y, 2 z).
+// Source/PrimCons_HelperModule.py:46-114, :135-196 ; the y forms sum the kinetic
+// terms in the order (vy, vz, vx), the z forms in the order (vz, vx, vy).
 // ---------------------------------------------------------------------------
-template <bool Y>
+template <int A>
+__device__ __forceinline__ double hkin(double a1, double a2, double a3) {
+  return A == 2 ? (sq(a3) + sq(a1) + sq(a2)) : A == 1 ? (sq(a2) + sq(a3) + sq(a1)) : (sq(a1) + sq(a2) + sq(a3));
+}
+
+template <int A>
 __device__ __forceinline__ void hprim_to_cons(const double w[5], double gamma, double u[5]) {
   u[0] = w[0];
   u[1] = w[0] * w[1];
   u[2] = w[0] * w[2];
   u[3] = w[0] * w[3];
-  const double ke = Y ? (sq(w[2]) + sq(w[3]) + sq(w[1])) : (sq(w[1]) + sq(w[2]) + sq(w[3]));
+  const double ke = hkin<A>(w[1], w[2], w[3]);
   u[4] = (w[4] / (gamma - 1.0)) + 0.5 * w[0] * ke;
 }
 
-template <bool Y>
+template <int A>
 __device__ __forceinline__ void hcons_to_prim(const double u[5], double gamma, double w[5]) {
   w[0] = u[0];
   const double inv_d = 1.0 / w[0];
   w[1] = u[1] * inv_d;
   w[2] = u[2] * inv_d;
   w[3] = u[3] * inv_d;
-  const double m2 = Y ? (sq(u[2]) + sq(u[3]) + sq(u[1])) : (sq(u[1]) + sq(u[2]) + sq(u[3]));
+  const double m2 = hkin<A>(u[1], u[2], u[3]);
   const double p = u[4] - 0.5 * m2 * inv_d;
   w[4] = p * (gamma - 1.0);
 }
 
-// Hydro primitive eigensystem (Source/ReconstructionEigenmatrices_Hydro_HelperModule.py:25-151).
-// Wave order x = (a-, entropy, vy, vz, a+), y = (a-, vx, entropy, vz, a+).
+// Hydro primitive eigensystem (Source/ReconstructionEigenmatrices_Hydro_HelperModule.py:25-151,
+// :230-282).  Wave order x = (a-, entropy, vy, vz, a+), y = (a-, vx, entropy, vz, a+),
+// z = (a-, vx, vy, entropy, a+): the entropy wave sits at the normal velocity's slot
+// n = A + 1 and shear wave k carries velocity slot k.
 struct HPrimEig {
   double lam[5];
   double rn0;   // R[n][0] = -a/rho ; R[n][4] = -rn0
@@ -552,30 +560,22 @@ struct HPrimEig {
   double le4;   // L[ent][4] = -1/a2
 };
 
-template <bool Y>
+template <int A>
 __host__ __device__ constexpr bool hprim_L_nz(int i, int j) {
-  // n = 1 (x) / 2 (y); ent = 1 / 2; shear1 row/col = 2,2 (x) / 1,1 (y)
-  return (i == 0 || i == 4) ? (j == (Y ? 2 : 1) || j == 4)
-       : (i == (Y ? 2 : 1)) ? (j == 0 || j == 4)
-       : (i == 3) ? (j == 3)
-       : (j == (Y ? 1 : 2));
+  return (i == 0 || i == 4) ? (j == A + 1 || j == 4) : (i == A + 1) ? (j == 0 || j == 4) : (j == i);
 }
-template <bool Y>
+template <int A>
 __host__ __device__ constexpr bool hprim_R_nz(int i, int j) {
-  // columns: wave 0: rows 0, n, 4 ; ent: row 0 ; shear1: row (Y?1:2) ; 3: row 3 ; 4: rows 0, n, 4
-  return (j == 0 || j == 4) ? (i == 0 || i == (Y ? 2 : 1) || i == 4)
-       : (j == (Y ? 2 : 1)) ? (i == 0)
-       : (j == 3) ? (i == 3)
-       : (i == (Y ? 1 : 2));
+  return (j == 0 || j == 4) ? (i == 0 || i == A + 1 || i == 4) : (j == A + 1) ? (i == 0) : (i == j);
 }
-template <bool Y>
+template <int A>
 __device__ __forceinline__ double hprim_L(const HPrimEig& e, int i, int j) {
   if (i == 0) return j == 4 ? e.l04 : e.l0n;
   if (i == 4) return j == 4 ? e.l04 : -e.l0n;
-  if (i == (Y ? 2 : 1)) return j == 0 ? 1.0 : e.le4;
+  if (i == A + 1) return j == 0 ? 1.0 : e.le4;
   return 1.0;
 }
-template <bool Y>
+template <int A>
 __device__ __forceinline__ double hprim_R(const HPrimEig& e, int i, int j) {
   if (j == 0 || j == 4) {
     if (i == 0) return 1.0;
@@ -584,9 +584,9 @@ __device__ __forceinline__ double hprim_R(const HPrimEig& e, int i, int j) {
   }
   return 1.0;
 }
-template <bool Y>
+template <int A>
 __device__ __forceinline__ void hprim_eigensystem(const double w[5], double gamma, HPrimEig& e) {
-  const int n = Y ? 2 : 1;
+  const int n = A + 1;
   const double gp = gamma * w[4];
   const double a2 = gp / w[0];
   const double a = sqrt(a2);
@@ -598,14 +598,14 @@ __device__ __forceinline__ void hprim_eigensystem(const double w[5], double gamm
   e.l04 = 0.5 / a2;
   e.le4 = -1.0 / a2;
 }
-template <bool Y>
+template <int A>
 __device__ __forceinline__ double hprim_project(const HPrimEig& e, int i, const double v[5]) {
   double acc = 0.0;
   bool first = true;
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
-    if (hprim_L_nz<Y>(i, j)) {
-      const double t = hprim_L<Y>(e, i, j) * v[j];
+    if (hprim_L_nz<A>(i, j)) {
+      const double t = hprim_L<A>(e, i, j) * v[j];
       acc = first ? t : acc + t;
       first = false;
     }
@@ -613,21 +613,25 @@ __device__ __forceinline__ double hprim_project(const HPrimEig& e, int i, const 
   return acc;
 }
 
-// Hydro Roe flux (Source/RiemannSolvers_Hydro_Roe_HelperModule.py:68-328, :342-596).
-template <bool Y>
+// Hydro Roe flux (Source/RiemannSolvers_Hydro_Roe_HelperModule.py:68-328, :342-596, :614-869).
+// Wave order x = (a-, vy, vz, entropy, a+), y = (a-, entropy, vz, vx, a+),
+// z = (a-, vy, entropy, vx, a+).
+template <int A>
 __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5], double gamma, bool efix,
                                           double eps, double flux[5]) {
-  constexpr int n = Y ? 2 : 1;
+  constexpr int n = A + 1;
   double ul[5], ur[5];
-  hprim_to_cons<Y>(wl, gamma, ul);
-  hprim_to_cons<Y>(wr, gamma, ur);
+  hprim_to_cons<A>(wl, gamma, ul);
+  hprim_to_cons<A>(wr, gamma, ur);
   const double sl = sqrt(wl[0]);
   const double sr = sqrt(wr[0]);
   const double isum = 1.0 / (sl + sr);
   double v[4];
 #pragma unroll
   for (int k = 1; k <= 3; ++k) v[k] = (sl * wl[k] + sr * wr[k]) * isum;
-  const double vsq = Y ? (v[2] * v[2] + v[3] * v[3] + v[1] * v[1]) : (v[1] * v[1] + v[2] * v[2] + v[3] * v[3]);
+  const double vsq = A == 2 ? (v[3] * v[3] + v[1] * v[1] + v[2] * v[2])
+                   : A == 1 ? (v[2] * v[2] + v[3] * v[3] + v[1] * v[1])
+                            : (v[1] * v[1] + v[2] * v[2] + v[3] * v[3]);
   const double H = ((ul[4] + wl[4]) / sl + (ur[4] + wr[4]) / sr) * isum;
   const double a2 = (gamma - 1.0) * dmax(H - 0.5 * vsq, SMALL_VALUE);
   const double a = sqrt(a2);
@@ -647,8 +651,8 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
   fl[0] = ul[n]; fr[0] = ur[n];
   fl[1] = ul[n] * wl[1]; fr[1] = ur[n] * wr[1];
   fl[2] = ul[n] * wl[2]; fr[2] = ur[n] * wr[2];
-  fl[n] = fl[n] + wl[4]; fr[n] = fr[n] + wr[4];
   fl[3] = ul[n] * wl[3]; fr[3] = ur[n] * wr[3];
+  fl[n] = fl[n] + wl[4]; fr[n] = fr[n] + wr[4];
   fl[4] = (ul[4] + wl[4]) * wl[n]; fr[4] = (ur[4] + wr[4]) * wr[n];
   if (lam[4] <= 0.0) {
 #pragma unroll
@@ -667,7 +671,7 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
 #pragma unroll
   for (int i = 0; i < 5; ++i) du[i] = ur[i] - ul[i];
   double c[5];  // L . du in the reference order j = 0..4 (structural zeros skipped)
-  if (!Y) {
+  if (A == 0) {
     const double l00 = nf * (0.5 * g1 * vsq + v[1] * a);
     const double l01 = -nf * (g1 * v[1] + a);
     const double l02 = -nf * g1 * v[2];
@@ -680,7 +684,7 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
     const double l40 = nf * (0.5 * g1 * vsq - v[1] * a);
     const double l41 = -nf * (g1 * v[1] - a);
     c[4] = l40 * du[0] + l41 * du[1] + l02 * du[2] + l03 * du[3] + l04 * du[4];
-  } else {
+  } else if (A == 1) {
     const double l00 = nf * (0.5 * g1 * vsq + v[2] * a);
     const double l01 = -nf * g1 * v[1];
     const double l02 = -nf * (g1 * v[2] + a);
@@ -693,32 +697,52 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
     const double l40 = nf * (0.5 * g1 * vsq - v[2] * a);
     const double l42 = -nf * (g1 * v[2] - a);
     c[4] = l40 * du[0] + l01 * du[1] + l42 * du[2] + l03 * du[3] + l04 * du[4];
+  } else {
+    const double l00 = nf * (0.5 * g1 * vsq + v[3] * a);
+    const double l01 = -nf * g1 * v[1];
+    const double l02 = -nf * g1 * v[2];
+    const double l03 = -nf * (g1 * v[3] + a);
+    const double l04 = nf * g1;
+    c[0] = l00 * du[0] + l01 * du[1] + l02 * du[2] + l03 * du[3] + l04 * du[4];
+    c[1] = -v[2] * du[0] + 1.0 * du[2];
+    c[2] = (1.0 - nf * g1 * vsq) * du[0] + gn * v[1] * du[1] + gn * v[2] * du[2] + gn * v[3] * du[3] + -gn * du[4];
+    c[3] = -v[1] * du[0] + 1.0 * du[1];
+    const double l40 = nf * (0.5 * g1 * vsq - v[3] * a);
+    const double l43 = -nf * (g1 * v[3] - a);
+    c[4] = l40 * du[0] + l01 * du[1] + l02 * du[2] + l43 * du[3] + l04 * du[4];
   }
   double amps[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) amps[k] = 0.5 * fabs(lam[k]) * c[k];
   double R[5][5];
   // non-zero entries only; R[i][j] for wave j
-  if (!Y) {
+  if (A == 0) {
     R[0][0] = 1.0; R[1][0] = v[1] - a; R[2][0] = v[2]; R[3][0] = v[3]; R[4][0] = H - v[1] * a;
     R[2][1] = 1.0; R[4][1] = v[2];
     R[3][2] = 1.0; R[4][2] = v[3];
     R[0][3] = 1.0; R[1][3] = v[1]; R[2][3] = v[2]; R[3][3] = v[3]; R[4][3] = 0.5 * vsq;
     R[0][4] = 1.0; R[1][4] = v[1] + a; R[2][4] = v[2]; R[3][4] = v[3]; R[4][4] = H + v[1] * a;
-  } else {
+  } else if (A == 1) {
     R[0][0] = 1.0; R[1][0] = v[1]; R[2][0] = v[2] - a; R[3][0] = v[3]; R[4][0] = H - v[2] * a;
     R[0][1] = 1.0; R[1][1] = v[1]; R[2][1] = v[2]; R[3][1] = v[3]; R[4][1] = 0.5 * vsq;
     R[3][2] = 1.0; R[4][2] = v[3];
     R[1][3] = 1.0; R[4][3] = v[1];
     R[0][4] = 1.0; R[1][4] = v[1]; R[2][4] = v[2] + a; R[3][4] = v[3]; R[4][4] = H + v[2] * a;
+  } else {
+    R[0][0] = 1.0; R[1][0] = v[1]; R[2][0] = v[2]; R[3][0] = v[3] - a; R[4][0] = H - v[3] * a;
+    R[2][1] = 1.0; R[4][1] = v[2];
+    R[0][2] = 1.0; R[1][2] = v[1]; R[2][2] = v[2]; R[3][2] = v[3]; R[4][2] = 0.5 * vsq;
+    R[1][3] = 1.0; R[4][3] = v[1];
+    R[0][4] = 1.0; R[1][4] = v[1]; R[2][4] = v[2]; R[3][4] = v[3] + a; R[4][4] = H + v[3] * a;
   }
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
     double acc = 0.5 * (fl[i] + fr[i]);
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-      const bool nz = !Y ? ((j == 0 || j == 3 || j == 4) || (j == 1 && (i == 2 || i == 4)) || (j == 2 && (i == 3 || i == 4)))
-                         : ((j == 0 || j == 1 || j == 4) || (j == 2 && (i == 3 || i == 4)) || (j == 3 && (i == 1 || i == 4)));
+      const bool nz = A == 0 ? ((j == 0 || j == 3 || j == 4) || (j == 1 && (i == 2 || i == 4)) || (j == 2 && (i == 3 || i == 4)))
+                    : A == 1 ? ((j == 0 || j == 1 || j == 4) || (j == 2 && (i == 3 || i == 4)) || (j == 3 && (i == 1 || i == 4)))
+                             : ((j == 0 || j == 2 || j == 4) || (j == 1 && (i == 2 || i == 4)) || (j == 3 && (i == 1 || i == 4)));
       if (nz) acc = acc - amps[j] * R[i][j];
     }
     flux[i] = acc;

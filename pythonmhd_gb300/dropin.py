@@ -24,13 +24,15 @@ TARGETS = (
     ("Source.EvolveFunctions_Hydro", "evolve_2D_hydro", evolve.evolve_2D_hydro),
     ("Source.EvolveFunctions_MHD", "evolve_1D_mhd", evolve.evolve_1D_mhd),
     ("Source.EvolveFunctions_Hydro", "evolve_1D_hydro", evolve.evolve_1D_hydro),
+    ("Source.EvolveFunctions_Hydro", "evolve_3D_hydro", evolve.evolve_3D_hydro),
 )
 
 _saved: dict = {}
 
 
 def install(arith: str | None = None):
-    """Replace the reference's 1D and 2D evolve functions; returns the patched modules.
+    """Replace the reference's 1D and 2D evolve functions and its 3D hydro evolve
+    function; returns the patched modules.
 
     ``arith`` ("exact" or "fast") overrides PYTHONMHD_GB300_ARITH for these calls.
     """

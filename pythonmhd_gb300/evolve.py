@@ -17,7 +17,9 @@ preconditions they assert, their return tuples and their aliasing:
 ``evolve_1D_mhd`` / ``evolve_1D_hydro`` (Source/EvolveFunctions_MHD.py:195-340,
 Source/EvolveFunctions_Hydro.py:232-305) keep theirs too: the 1D MHD function
 returns new arrays with B_x made uniform; the 1D hydro function updates the
-grid's arrays in place and returns them.
+grid's arrays in place and returns them.  ``evolve_3D_hydro``
+(Source/EvolveFunctions_Hydro.py:559-806) updates the grid's (5, ny, nx, nz)
+arrays in place and returns them, as the reference does.
 
 The cycles run on the GPU (``Grid2D.advance``); the host uploads the grid once
 per call and downloads the result.  Handles are cached per grid geometry and
@@ -27,7 +29,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .solver import Grid1D, Grid2D, default_arith
+from .solver import Grid1D, Grid2D, Grid3D, default_arith
 
 OUTFLOW = 0
 PERIODIC = 1
@@ -212,3 +214,54 @@ def evolve_1D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, 
     else:
         sl_prim, sl_cons = np.copy(prim), np.copy(cons)
     return prim, cons, t, cycle, sl_prim, sl_cons, t_sl
+
+
+# ---------------------------------------------------------------------------
+# 3D hydro (Source/EvolveFunctions_Hydro.py:559-806)
+# ---------------------------------------------------------------------------
+def evolve_3D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cfl, minDens, minPres,
+                    minEnergy, reconstructOrder=0, entropyFix=False, epsilon=0.5, arith=None):
+    """evolve_3D_hydro: updates the grid's primVars/consVars, (5, ny, nx, nz), in place
+    and returns them: (prim, cons, time, cycle, secondLastPrim, secondLastCons,
+    secondLastTime).  reconstructOrder 2 is PPM, :data:`PLM` is PLM, anything else
+    first order, as in 2D."""
+    prim = simulationGrid.primVars
+    assert (len(prim.shape) - 1 == 3)
+    cons = simulationGrid.consVars
+    assert (prim.shape == cons.shape)
+    nx = simulationGrid.numXCells
+    assert (nx > 1)
+    ny = simulationGrid.numYCells
+    assert (ny > 1)
+    nz = simulationGrid.numZCells
+    assert (nz > 1)
+    dx = simulationGrid.dx
+    assert (dx > 0)
+    dy = simulationGrid.dy
+    assert (dy > 0)
+    dz = simulationGrid.dz
+    assert (dz > 0)
+    bcx = simulationGrid.BcX
+    assert (bcx == OUTFLOW or bcx == PERIODIC)
+    bcy = simulationGrid.BcY
+    assert (bcy == OUTFLOW or bcy == PERIODIC)
+    bcz = simulationGrid.BcZ
+    assert (bcz == OUTFLOW or bcz == PERIODIC)
+    assert (tStart <= tEnd)
+    assert (startCycle >= 0 and maxCycles > 0)
+    order = _order(reconstructOrder)
+    mode = arith or default_arith()
+    key = ("hydro3d", ny, nx, nz, float(dx), float(dy), float(dz), bcx, bcy, bcz, float(gamma), order,
+           bool(entropyFix), float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)
+    g = _handle(key, lambda: Grid3D(ny, nx, nz, dx, dy, dz, bcx, bcy, bcz, gamma, recon=order,
+                                    entropy_fix=entropyFix, eps=epsilon, min_d=minDens, min_p=minPres,
+                                    min_e=minEnergy, arith=mode))
+    g.upload(prim, cons)
+    t, cyc, t_sl = g.advance(tStart, tEnd, startCycle, maxCycles, cfl)
+    if g.last_cycles == 0:
+        return prim, cons, tStart, startCycle, np.copy(prim), np.copy(cons), tStart
+    sl_prim, sl_cons = g.download(1)
+    new_prim, new_cons = g.download(0)
+    np.copyto(prim, new_prim)
+    np.copyto(cons, new_cons)
+    return prim, cons, t, cyc, sl_prim, sl_cons, t_sl

@@ -1,4 +1,4 @@
-"""Host-side initial states for the 2D step (inputs, not part of the hot path).
+"""Initial states for the 2D and 3D steps (inputs, not part of the hot path).
 
 * ``orszag_tang``: the Orszag-Tang vortex of the reference's sample script
   (InitializationFiles/SampleSimulations/2D_MHD/OrszagTang_InitializationFile.py:117-194),
@@ -8,6 +8,8 @@
   (Source/SimulationGrid.py:147-156).
 * ``turbulence``: the seeded driven-free turbulence state (Gaussian random
   density, velocity and vector-potential fields with power-law spectra).
+* ``turbulence_hydro_3d``: seeded 3D hydro turbulence for the 3D step, generated
+  with torch (on the GPU for the large boxes).
 * ``prim_to_cons_mhd`` / ``prim_to_cons_hydro``: the conserved variables the
   reference's grid derives at construction
   (Source/PrimCons_HelperModule.py:23-35 and :314-340).
@@ -269,3 +271,47 @@ def turbulence_device(n, seed=1, gamma=5.0 / 3.0, kmax_v=32, kmax_a=16, mach=1.0
     e = e + 0.5 * (cbx * cbx + cby * cby + zero * zero)
     cons = torch.stack([rho, rho * vx, rho * vy, rho * zero, cbx, cby, zero, e])
     return prim.contiguous(), cons.contiguous(), fbx.contiguous(), fby.contiguous(), dx, dy
+
+
+# ---------------------------------------------------------------------------
+# 3D hydro turbulence (inputs of the 3D step; arrays (5, ny, nx, nz), z fastest)
+# ---------------------------------------------------------------------------
+def _gaussian_field_3d(rng, n, slope, kmin, kmax, device):
+    """A 3D Gaussian random field on an n^3 periodic box with the 2D generator's
+    convention: ``irfftn`` of (N(0,1) + i N(0,1)) |k|^(-slope/2) on the integer
+    wavevectors with kmin <= |k| <= kmax (axes y, x, z; z is the half axis), zero
+    mean.  The transform runs in torch on ``device``."""
+    import torch
+    k1 = np.fft.fftfreq(n, d=1.0 / n)
+    kz = np.fft.rfftfreq(n, d=1.0 / n)
+    KY, KX, KZ = np.meshgrid(k1, k1, kz, indexing="ij")
+    k = np.sqrt(KX * KX + KY * KY + KZ * KZ)
+    mask = (k >= kmin) & (k <= kmax)
+    amp = np.zeros_like(k)
+    amp[mask] = k[mask] ** (-slope / 2.0)
+    re = rng.standard_normal(k.shape)
+    im = rng.standard_normal(k.shape)
+    c = torch.complex(torch.from_numpy(re * amp), torch.from_numpy(im * amp)).to(device)
+    f = torch.fft.irfftn(c, s=(n, n, n))
+    return f - f.mean()
+
+
+def turbulence_hydro_3d(n, seed=1, gamma=1.4, kmax=16, mach=1.0, device="cuda"):
+    """Seeded 3D hydro turbulence on the unit n^3 periodic box: density exp(0.1 g),
+    velocities with power ~ k^-2 up to ``kmax`` scaled to rms Mach ``mach``, uniform
+    pressure 1/gamma.  Returns (prim, cons) float64 torch tensors of shape
+    (5, n, n, n) on ``device`` and the cell size."""
+    import torch
+    rng = np.random.default_rng(seed)
+    g = _gaussian_field_3d(rng, n, 2.0, 1.0, kmax, device)
+    g = g / g.std(unbiased=False)
+    v = [_gaussian_field_3d(rng, n, 2.0, 1.0, kmax, device) for _ in range(3)]
+    rho = torch.exp(0.1 * g)
+    p = torch.full_like(rho, 1.0 / gamma)
+    vsq = v[0] * v[0] + v[1] * v[1] + v[2] * v[2]
+    scale = mach / torch.sqrt(torch.mean(vsq / (gamma * p / rho)))
+    v = [c * scale for c in v]
+    prim = torch.stack([rho, v[0], v[1], v[2], p])
+    e = p / (gamma - 1.0) + 0.5 * rho * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    cons = torch.stack([rho, rho * v[0], rho * v[1], rho * v[2], e])
+    return prim.contiguous(), cons.contiguous(), 1.0 / n

@@ -204,6 +204,102 @@ class Grid1D(Grid2D):
         return p, c
 
 
+class Grid3D:
+    """One ny x nx x nz hydro grid (the reference's evolve_3D_hydro step) on the GPU.
+
+    States are (5, ny, nx, nz) with z fastest, the reference's layout.  The evolve
+    loop and the second-last state behave as in :class:`Grid2D`.
+    """
+
+    def __init__(self, ny, nx, nz, dx, dy, dz, bcx, bcy, bcz, gamma, recon=2, entropy_fix=False, eps=0.5,
+                 min_d=1e-12, min_p=1e-12, min_e=1e-12, arith=None):
+        self.lib = _lib.load()
+        self.ny, self.nx, self.nz = int(ny), int(nx), int(nz)
+        self.mhd = False
+        self.nvars = 5
+        self.arith = arith or default_arith()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.mhd3d_create(self.ny, self.nx, self.nz, float(dx), float(dy), float(dz), int(bcx),
+                                         int(bcy), int(bcz), float(gamma), 0, int(recon), 1 if entropy_fix else 0,
+                                         float(eps), float(min_d), float(min_p), float(min_e), ARITH[self.arith],
+                                         ctypes.byref(h)), "mhd3d_create")
+        self._h = h
+        self.last_cycles = 0
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.lib.mhd3d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def cell_shape(self):
+        return (self.nvars, self.ny, self.nx, self.nz)
+
+    def upload(self, prim, cons):
+        prim, cons = _as_f64c(prim), _as_f64c(cons)
+        if prim.shape != self.cell_shape() or cons.shape != self.cell_shape():
+            raise ValueError(f"prim/cons must have shape {self.cell_shape()}, got {prim.shape}, {cons.shape}")
+        _lib.check(self.lib.mhd3d_upload(self._h, _ptr(prim), _ptr(cons)), "mhd3d_upload")
+
+    def upload_device(self, prim, cons):
+        """Upload from contiguous float64 CUDA tensors of the handle's device (no host copy)."""
+        import torch
+        for t in (prim, cons):
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()
+                    and tuple(t.shape) == self.cell_shape()):
+                raise ValueError(f"upload_device expects contiguous float64 CUDA tensors of shape {self.cell_shape()}")
+        torch.cuda.current_stream(prim.device).synchronize()
+        _lib.check(self.lib.mhd3d_upload_device(self._h, ctypes.c_void_p(prim.data_ptr()),
+                                                ctypes.c_void_p(cons.data_ptr())), "mhd3d_upload_device")
+
+    def download(self, which=0, prim=None, cons=None):
+        """(prim, cons) of the current (which=0) or second-last (which=1) state."""
+        prim = np.empty(self.cell_shape()) if prim is None else prim
+        cons = np.empty(self.cell_shape()) if cons is None else cons
+        for a in (prim, cons):
+            if not (a.dtype == np.float64 and a.flags.c_contiguous and a.shape == self.cell_shape()):
+                raise ValueError("download targets must be C-contiguous float64 of the cell shape")
+        _lib.check(self.lib.mhd3d_download(self._h, int(which), _ptr(prim), _ptr(cons)), "mhd3d_download")
+        return prim, cons
+
+    def advance(self, t0, t_end, cycle0, max_cycles, cfl):
+        t = ctypes.c_double()
+        c = ctypes.c_longlong()
+        tsl = ctypes.c_double()
+        _lib.check(self.lib.mhd3d_advance(self._h, float(t0), float(t_end), int(cycle0), int(max_cycles),
+                                          float(cfl), ctypes.byref(t), ctypes.byref(c), ctypes.byref(tsl)),
+                   "mhd3d_advance")
+        self.last_cycles = c.value - int(cycle0)
+        return t.value, c.value, tsl.value
+
+    def _info(self):
+        n = ctypes.c_longlong()
+        b = ctypes.c_size_t()
+        s = ctypes.c_void_p()
+        _lib.check(self.lib.mhd3d_info(self._h, ctypes.byref(n), ctypes.byref(b), ctypes.byref(s)), "mhd3d_info")
+        return n.value, b.value, s.value
+
+    def last_launches(self):
+        return self._info()[0]
+
+    def device_bytes(self):
+        return self._info()[1]
+
+    def stream(self):
+        return self._info()[2]
+
+    def state_ptrs(self, which=0):
+        ptrs = [ctypes.c_void_p() for _ in range(2)]
+        _lib.check(self.lib.mhd3d_state_ptrs(self._h, int(which), *[ctypes.byref(p) for p in ptrs]),
+                   "mhd3d_state_ptrs")
+        return [p.value for p in ptrs]
+
+
 class Batch2D:
     """Many independent grids advanced together (one persistent launch per stage).
 

@@ -16,7 +16,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(mhd2d_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mhd(?:1d|2d|3d|b)_\w+)\s*\(", text)))
 
 
 @pytest.fixture(scope="module")
@@ -28,7 +28,7 @@ def lib():
 def test_header_declares_the_entry_points():
     names = declared_functions()
     for n in ("mhd2d_create", "mhd2d_upload", "mhd2d_advance", "mhd2d_download", "mhd2d_destroy",
-              "mhd2d_strerror"):
+              "mhd2d_strerror", "mhd1d_create", "mhdb_create", "mhd3d_create", "mhd3d_advance"):
         assert n in names
 
 
@@ -102,3 +102,22 @@ def lib_run_rejects_null(h):
     c = ctypes.c_longlong()
     return lib.mhd2d_run(None, 1.0, 10, 0.4, -1.0, 0, -1.0, 0, None, None, ctypes.byref(t), ctypes.byref(c),
                          ctypes.byref(c)) == 1
+
+
+def test_3d_entry_points_reject_bad_arguments(lib):
+    h = ctypes.c_void_p()
+    ok = [8, 8, 8, 0.1, 0.1, 0.1, 1, 1, 1, 1.4, 0, 2, 0, 0.5, 1e-12, 1e-12, 1e-12, 0]
+    bad = {0: 1, 2: 1, 5: 0.0, 8: 2, 10: 1, 11: 3, 17: 2}   # nz < 2, ny < 2, dz <= 0, BC, MHD, recon, arith
+    for i, v in bad.items():
+        args = list(ok)
+        args[i] = v
+        assert lib.mhd3d_create(*args, ctypes.byref(h)) == 1 and not h.value, i
+    big = list(ok)
+    big[0] = big[1] = big[2] = 2000   # (n+2)^3 above the 32-bit work-item range
+    assert lib.mhd3d_create(*big, ctypes.byref(h)) == 6 and not h.value
+    t = ctypes.c_double()
+    c = ctypes.c_longlong()
+    assert lib.mhd3d_advance(None, 0.0, 1.0, 0, 1, 0.4, ctypes.byref(t), ctypes.byref(c), ctypes.byref(t)) == 1
+    assert lib.mhd3d_upload(None, None, None) == 1
+    assert lib.mhd3d_download(None, 0, None, None) == 1
+    lib.mhd3d_destroy(None)

@@ -16,6 +16,7 @@ def _fake_source(monkeypatch):
     hyd.evolve_2D_hydro = lambda *a, **k: "reference-hydro"
     mhd.evolve_1D_mhd = lambda *a, **k: "reference-mhd-1d"
     hyd.evolve_1D_hydro = lambda *a, **k: "reference-hydro-1d"
+    hyd.evolve_3D_hydro = lambda *a, **k: "reference-hydro-3d"
     monkeypatch.setitem(sys.modules, "Source", pkg)
     monkeypatch.setitem(sys.modules, "Source.EvolveFunctions_MHD", mhd)
     monkeypatch.setitem(sys.modules, "Source.EvolveFunctions_Hydro", hyd)
@@ -30,9 +31,11 @@ def test_install_and_uninstall(monkeypatch):
     assert hyd.evolve_2D_hydro is evolve.evolve_2D_hydro
     assert mhd.evolve_1D_mhd is evolve.evolve_1D_mhd
     assert hyd.evolve_1D_hydro is evolve.evolve_1D_hydro
+    assert hyd.evolve_3D_hydro is evolve.evolve_3D_hydro
     dropin.uninstall()
     assert mhd.evolve_2D_mhd is orig_m and hyd.evolve_2D_hydro is orig_h
     assert mhd.evolve_1D_mhd() == "reference-mhd-1d"
+    assert hyd.evolve_3D_hydro() == "reference-hydro-3d"
 
 
 def test_install_with_arith_binds_the_mode(monkeypatch):
@@ -47,7 +50,8 @@ def test_evolve_keeps_reference_signature():
     import inspect
     ref = ["simulationGrid", "tStart", "tEnd", "startCycle", "maxCycles", "gamma", "cfl", "minDens",
            "minPres", "minEnergy", "reconstructOrder", "entropyFix", "epsilon"]
-    for fn in (evolve.evolve_2D_mhd, evolve.evolve_2D_hydro, evolve.evolve_1D_mhd, evolve.evolve_1D_hydro):
+    for fn in (evolve.evolve_2D_mhd, evolve.evolve_2D_hydro, evolve.evolve_1D_mhd, evolve.evolve_1D_hydro,
+               evolve.evolve_3D_hydro):
         params = list(inspect.signature(fn).parameters)
         assert params[:len(ref)] == ref
         sig = inspect.signature(fn).parameters
