@@ -100,6 +100,13 @@ int mhd2d_run(void* handle, double t_lim, long long max_cycles, double cfl, doub
               double plot_dt, int plot_prec, mhd2d_stop_fn on_stop, void* user, double* t_out,
               long long* cycle_out, long long* stops_out);
 
+/* Log each cycle's dt on the device: the cycle numbered c (the loop's cycle counter,
+ * cycle0 + cycles run) writes its dt to dt_log[c] when c < capacity.  dt_log is a
+ * device pointer of the handle's GPU that must stay valid while the log is set;
+ * capacity 0 (dt_log NULL) switches the log off.  Used by the adjoint's forward
+ * pass to record the CFL dts of many cycles in one advance call. */
+int mhd2d_set_dt_log(void* handle, double* dt_log, long long capacity);
+
 /* Copy a state out: which = 0 the current state, 1 the state at the start of
  * the last cycle (the reference's secondLast* arrays).  Any pointer may be
  * NULL to skip that array. */
@@ -240,6 +247,14 @@ int mhd2d_adj_restore(void* handle, const double* checkpoints, int steps, int ev
  * segment_sets: cycles kept resident per segment by the last forward (1 =
  * recompute mode). */
 int mhd2d_adj_info(void* handle, size_t* state_words, size_t* device_bytes, int* segment_sets);
+/* Tail of the forward record: when the backward pass can keep segments resident,
+ * mhd2d_adj_forward runs the last cycles of the run (as many as the segment budget
+ * holds, at least the checkpoint interval) with the taped kernels and leaves their
+ * arrays resident, so the first mhd2d_adj_backward reverses them without
+ * recomputing them.  max_cycles: -1 (default) as many as fit, 0 no tail, n at most n. */
+int mhd2d_adj_set_tail(void* handle, int max_cycles);
+/* The last record: its cycles, checkpoint interval and tail length (0: none). */
+int mhd2d_adj_record(void* handle, int* steps, int* every, int* tail);
 void mhd2d_adj_destroy(void* handle);
 
 /* ---------------------------------------------------------------------------

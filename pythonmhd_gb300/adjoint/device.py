@@ -67,9 +67,19 @@ class Adjoint2D:
         self.dts = None
         self._ckpt_ref = None
 
-    def configure(self, segment_bytes=0):
-        """Memory the backward pass may use to keep a checkpoint segment resident (0 = automatic)."""
+    def configure(self, segment_bytes=0, tail=None):
+        """Memory the backward pass may use to keep a checkpoint segment resident (0 =
+        automatic); ``tail``: cycles at the end of a forward pass run with tapes and left
+        resident for the backward pass (-1 as many as fit, 0 none; None leaves it)."""
         _lib.check(self.lib.mhd2d_adj_configure(self._h, int(segment_bytes)), "mhd2d_adj_configure")
+        if tail is not None:
+            _lib.check(self.lib.mhd2d_adj_set_tail(self._h, int(tail)), "mhd2d_adj_set_tail")
+
+    def record(self):
+        """The last forward record: steps, checkpoint interval and tail cycles."""
+        v = [ctypes.c_int() for _ in range(3)]
+        _lib.check(self.lib.mhd2d_adj_record(self._h, *[ctypes.byref(x) for x in v]), "mhd2d_adj_record")
+        return dict(steps=v[0].value, every=v[1].value, tail=v[2].value)
 
     # -- lifetime ---------------------------------------------------------
     def close(self):

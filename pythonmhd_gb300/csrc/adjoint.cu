@@ -608,8 +608,15 @@ struct Handle {
   int nsets = 0;
   double* red = nullptr;       // CFL maxima (2) + dt (1)
   size_t budget = 0;           // bytes the stored-segment mode may use (0: 60% of free memory)
-  // forward record
+  // forward record: uniform segments of `every` cycles over the first steps - tail
+  // cycles, then (stored mode) a tail segment whose cycles the forward pass runs with
+  // the taped kernels and leaves resident, so the backward pass reverses them at once
   int steps = 0, every = 0;
+  int tail = 0;                // cycles of the tail segment (0: none)
+  int tail_max = -1;           // -1: as many as the segment budget holds; 0: no tail
+  bool tail_resident = false;  // the tail's arrays and tapes are still in the arenas
+  double* dtlog = nullptr;     // device log of the production solver's dts
+  size_t dtlog_cap = 0;
   bool stored = false;         // backward keeps every cycle of a segment resident
   std::vector<double> dts;
   double* ckpt = nullptr;      // one packed state per segment
@@ -672,7 +679,23 @@ int alloc_sets(Handle* h, int n) {
 }
 
 size_t device_bytes(const Handle* h) {
-  return (h->bars_cap + h->vals_cap + h->tapes_cap + 4) * sizeof(double) + h->ckpt_bytes + h->seg_bytes;
+  return (h->bars_cap + h->vals_cap + h->tapes_cap + 4 + h->dtlog_cap) * sizeof(double) + h->ckpt_bytes +
+         h->seg_bytes;
+}
+
+// segments of a record: ceil(head / every) uniform segments over the first
+// head = steps - tail cycles, then the tail segment when tail > 0
+int head_segments(const Handle* h) { return (h->steps - h->tail + h->every - 1) / h->every; }
+int num_segments(const Handle* h) { return head_segments(h) + (h->tail > 0 ? 1 : 0); }
+void segment(const Handle* h, int s, int* c0, int* len) {
+  const int head = h->steps - h->tail;
+  if (s < head_segments(h)) {
+    *c0 = s * h->every;
+    *len = std::min(h->every, head - *c0);
+  } else {
+    *c0 = head;
+    *len = h->tail;
+  }
 }
 
 // copy a packed state [prim 8 | cons 8 | fbx | fby] into / out of four arrays
@@ -830,18 +853,22 @@ void layout(int nx, int ny, int recon, int efix, size_t* off, size_t* ps, size_t
 // Size the record of a run of `steps` cycles: the checkpoint interval, the
 // checkpoint store (owned, or borrowed from the caller), and the backward mode --
 // all `every` cycles of a segment resident when they fit the budget, else one
-// cycle's arrays plus the segment's states.
-int prepare_record(Handle* h, int steps, int& every, bool own_ckpt) {
+// cycle's arrays plus the segment's states.  In stored mode with `allow_tail`, the
+// last segment is a tail of as many cycles as the budget holds (at most tail_max).
+int prepare_record(Handle* h, int steps, int& every, bool own_ckpt, bool allow_tail) {
   if (every <= 0) every = (int)std::ceil(std::sqrt((double)steps));
   every = std::min(every, steps);
-  const int nck = (steps + every - 1) / every;
   h->steps = 0;
+  h->tail = 0;
+  h->tail_resident = false;
   if (h->ckpt_owned) cudaFree(h->ckpt);
   cudaFree(h->seg);
   h->ckpt = h->seg = nullptr;
   h->ckpt_bytes = h->seg_bytes = 0;
   h->ckpt_owned = own_ckpt;
   if (own_ckpt) {
+    // one state per segment: at most ceil(steps / every) + 1 with a tail
+    const int nck = (steps + every - 1) / every + (allow_tail ? 1 : 0);
     CK(cudaMalloc(&h->ckpt, (size_t)nck * h->state_words * sizeof(double)));
     h->ckpt_bytes = (size_t)nck * h->state_words * sizeof(double);
   }
@@ -854,21 +881,53 @@ int prepare_record(Handle* h, int steps, int& every, bool own_ckpt) {
   const size_t budget = h->budget ? h->budget : (size_t)(0.6 * (double)(free_b + held));
   const size_t extra = ((size_t)every - 1) * set_bytes;
   h->stored = every > 1 && extra <= budget;
+  int tail = 0;
+  if (allow_tail && h->stored && h->tail_max != 0) {
+    const size_t fit = 1 + budget / set_bytes;
+    tail = (int)std::min<size_t>(fit, (size_t)steps);
+    if (h->tail_max > 0) tail = std::min(tail, h->tail_max);
+    if (tail < every) tail = 0;   // no longer than a plain segment: keep the uniform record
+  }
   int rc;
   if (h->stored) {
-    if (h->nsets < every && (rc = alloc_sets(h, every))) return rc;
+    const int sets = std::max(every, tail);
+    if (h->nsets < sets && (rc = alloc_sets(h, sets))) return rc;
   } else {
     if ((rc = alloc_sets(h, 1))) return rc;
     CK(cudaMalloc(&h->seg, (size_t)every * h->state_words * sizeof(double)));
     h->seg_bytes = (size_t)every * h->state_words * sizeof(double);
   }
   h->every = every;
+  h->tail = tail;
+  return MHD_OK;
+}
+
+// Run the tail segment from the state in value arena 0's inputs: per cycle the CFL
+// dt (the production step's arithmetic, bit for bit), then the taped forward sweep
+// into arena k, whose outputs become arena k+1's inputs.  The arrays and tapes stay
+// resident for the backward pass.
+int run_tail(Handle* h, int c0, double cfl, const double* fixed_dt) {
+  Adj& A = h->A;
+  int rc;
+  for (int k = 0; k < h->tail; ++k) {
+    select_set(h, k);
+    double dt = 0.0;
+    if (fixed_dt) dt = fixed_dt[c0 + k];
+    else if ((rc = cfl_dt(h, cfl, &dt))) return rc;
+    if (!std::isfinite(dt)) return MHD_ERR_NONFINITE;
+    h->dts[c0 + k] = dt;
+    A.dt = dt;
+    if ((rc = fwd_cycle(h, true))) return rc;
+    if (k + 1 < h->tail && (rc = output_to_input(h, k, k + 1))) return rc;
+  }
+  h->tail_resident = true;
   return MHD_OK;
 }
 
 // Forward pass with the CFL dt on the production exact-arithmetic step (the same
-// arithmetic as the stage kernels, bit for bit, and faster): one cycle per
-// advance call from t = 0, so the returned time is the cycle's dt exactly.
+// arithmetic as the stage kernels, bit for bit, and faster): one advance call per
+// segment, each cycle's dt logged on the device; then the tail, if any, on the
+// taped stage kernels.
 int forward_on_solver(Handle* h, const double* state_in, int steps, double cfl, double* state_out) {
   Adj& A = h->A;
   const size_t cp = (size_t)A.nx * A.ny, xp = (size_t)(A.nx + 1) * A.ny;
@@ -877,8 +936,17 @@ int forward_on_solver(Handle* h, const double* state_in, int steps, double cfl, 
                           A.min_d, A.min_p, A.min_e, MHD2D_ARITH_EXACT, &h->solver);
     if (rc) return rc;
   }
+  if (h->dtlog_cap < (size_t)steps) {
+    cudaFree(h->dtlog);
+    h->dtlog = nullptr;
+    h->dtlog_cap = 0;
+    CK(cudaMalloc(&h->dtlog, (size_t)steps * sizeof(double)));
+    h->dtlog_cap = steps;
+  }
+  int rc = mhd2d_set_dt_log(h->solver, h->dtlog, (long long)h->dtlog_cap);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(h->stream));
-  int rc = mhd2d_upload_device(h->solver, state_in, state_in + 8 * cp, state_in + 16 * cp, state_in + 16 * cp + xp);
+  rc = mhd2d_upload_device(h->solver, state_in, state_in + 8 * cp, state_in + 16 * cp, state_in + 16 * cp + xp);
   if (rc) return rc;
   auto save = [&](double* dst) -> int {
     double *p = nullptr, *c = nullptr, *bx = nullptr, *by = nullptr;
@@ -888,18 +956,36 @@ int forward_on_solver(Handle* h, const double* state_in, int steps, double cfl, 
     P.v = p; C.v = c; FX.v = bx; FY.v = by;
     return pack(h, dst, P, C, FX, FY, false);
   };
-  for (int c = 0; c < steps; ++c) {
-    if (c % h->every == 0 && (rc = save(h->ckpt + (size_t)(c / h->every) * h->state_words))) return rc;
+  const int nh = head_segments(h);
+  const int head = steps - h->tail;
+  for (int s = 0; s < nh; ++s) {
+    int c0 = 0, len = 0;
+    segment(h, s, &c0, &len);
+    if ((rc = save(h->ckpt + (size_t)s * h->state_words))) return rc;
     // the copy above is on this handle's stream; the solver runs on its own
     CK(cudaStreamSynchronize(h->stream));
     double t = 0.0;
     long long cyc = 0;
-    if ((rc = mhd2d_advance(h->solver, 0.0, 1e300, 0, 1, cfl, &t, &cyc, nullptr))) return rc;
-    if (cyc != 1 || !std::isfinite(t)) return MHD_ERR_NONFINITE;
-    h->dts[c] = t;
+    if ((rc = mhd2d_advance(h->solver, 0.0, 1e300, c0, c0 + len, cfl, &t, &cyc, nullptr))) return rc;
+    if (cyc != c0 + len || !std::isfinite(t)) return MHD_ERR_NONFINITE;
   }
-  if ((rc = save(state_out))) return rc;
-  return MHD_OK;
+  if (head > 0) {
+    CK(cudaMemcpy(h->dts.data(), h->dtlog, (size_t)head * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < head; ++c)
+      if (!std::isfinite(h->dts[c])) return MHD_ERR_NONFINITE;
+  }
+  if (h->tail > 0) {
+    double* ck = h->ckpt + (size_t)nh * h->state_words;
+    if ((rc = save(ck))) return rc;
+    select_set(h, 0);
+    if ((rc = unpack(h, ck, A.P, A.C, A.FX, A.FY, false))) return rc;
+    if ((rc = run_tail(h, head, cfl, nullptr))) return rc;
+    select_set(h, h->tail - 1);
+    rc = pack(h, state_out, A.NP, A.NC, A.NFX, A.NFY, false);
+    select_set(h, 0);
+    return rc;
+  }
+  return save(state_out);
 }
 
 }  // namespace
@@ -950,6 +1036,7 @@ void mhd2d_adj_destroy(void* handle) {
   cudaFree(h->vals);
   cudaFree(h->tapes);
   cudaFree(h->red);
+  cudaFree(h->dtlog);
   if (h->ckpt_owned) cudaFree(h->ckpt);
   cudaFree(h->seg);
   if (h->solver) mhd2d_destroy(h->solver);
@@ -975,6 +1062,8 @@ int mhd2d_adj_reshape(void* handle, int ny, int nx, double dx, double dy, int bc
   }
   // the record, the segment states and the production solver belong to the old grid
   h->steps = 0;
+  h->tail = 0;
+  h->tail_resident = false;
   if (h->ckpt_owned) cudaFree(h->ckpt);
   cudaFree(h->seg);
   h->ckpt = h->seg = nullptr;
@@ -1007,6 +1096,7 @@ int mhd2d_adj_cycle(void* handle, double dt, const double* state_in, double* sta
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !state_in || !state_out) return MHD_ERR_ARG;
   Adj& A = h->A;
+  h->tail_resident = false;   // arena 0 is overwritten
   select_set(h, 0);
   A.dt = dt;
   int rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false);
@@ -1022,6 +1112,7 @@ int mhd2d_adj_cycle_reverse(void* handle, double dt, const double* state_in, con
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !state_in || !bar_out || !bar_in) return MHD_ERR_ARG;
   Adj& A = h->A;
+  h->tail_resident = false;   // arena 0 is overwritten
   select_set(h, 0);
   A.dt = dt;
   int rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false);
@@ -1039,7 +1130,7 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !state_in || !state_out || steps < 1) return MHD_ERR_ARG;
   Adj& A = h->A;
-  int rc = prepare_record(h, steps, every, true);
+  int rc = prepare_record(h, steps, every, true, true);
   if (rc) return rc;
   every = h->every;
   h->dts.assign(steps, 0.0);
@@ -1048,18 +1139,29 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
   } else {
     select_set(h, 0);
     if ((rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false))) return rc;
-    for (int c = 0; c < steps; ++c) {
-      if (c % every == 0 &&
-          (rc = pack(h, h->ckpt + (size_t)(c / every) * h->state_words, A.P, A.C, A.FX, A.FY, false)))
-        return rc;
-      const double dt = fixed_dt[c];
-      if (!std::isfinite(dt)) return MHD_ERR_NONFINITE;
-      h->dts[c] = dt;
-      A.dt = dt;
-      if ((rc = fwd_cycle(h, false))) return rc;
-      if ((rc = output_to_input(h, 0, 0))) return rc;
+    const int nh = head_segments(h);
+    for (int s = 0; s < nh; ++s) {
+      int c0 = 0, len = 0;
+      segment(h, s, &c0, &len);
+      if ((rc = pack(h, h->ckpt + (size_t)s * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
+      for (int c = c0; c < c0 + len; ++c) {
+        const double dt = fixed_dt[c];
+        if (!std::isfinite(dt)) return MHD_ERR_NONFINITE;
+        h->dts[c] = dt;
+        A.dt = dt;
+        if ((rc = fwd_cycle(h, false))) return rc;
+        if ((rc = output_to_input(h, 0, 0))) return rc;
+      }
     }
-    if ((rc = pack(h, state_out, A.P, A.C, A.FX, A.FY, false))) return rc;
+    if (h->tail > 0) {
+      if ((rc = pack(h, h->ckpt + (size_t)nh * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
+      if ((rc = run_tail(h, steps - h->tail, cfl, fixed_dt))) return rc;
+      select_set(h, h->tail - 1);
+      if ((rc = pack(h, state_out, A.NP, A.NC, A.NFX, A.NFY, false))) return rc;
+      select_set(h, 0);
+    } else if ((rc = pack(h, state_out, A.P, A.C, A.FX, A.FY, false))) {
+      return rc;
+    }
   }
   CK(cudaStreamSynchronize(h->stream));
   h->steps = steps;
@@ -1070,7 +1172,7 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
 int mhd2d_adj_restore(void* handle, const double* checkpoints, int steps, int every, const double* dt) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !checkpoints || !dt || steps < 1 || every < 1) return MHD_ERR_ARG;
-  int rc = prepare_record(h, steps, every, false);
+  int rc = prepare_record(h, steps, every, false, false);
   if (rc) return rc;
   h->ckpt = const_cast<double*>(checkpoints);
   h->dts.assign(dt, dt + steps);
@@ -1085,24 +1187,28 @@ int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initia
   if (!h || !bar_final || !bar_initial) return MHD_ERR_ARG;
   if (!h->ckpt || h->steps < 1) return MHD_ERR_STATE;
   Adj& A = h->A;
-  const int every = h->every;
-  const int nck = (h->steps + every - 1) / every;
+  const int nseg = num_segments(h);
   select_set(h, 0);
   int rc = unpack(h, bar_final, A.NP, A.NC, A.NFX, A.NFY, true);
   if (rc) return rc;
-  for (int s = nck - 1; s >= 0; --s) {
-    const int c0 = s * every;
-    const int len = std::min(every, h->steps - c0);
-    select_set(h, 0);
-    if ((rc = unpack(h, h->ckpt + (size_t)s * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
+  for (int s = nseg - 1; s >= 0; --s) {
+    int c0 = 0, len = 0;
+    segment(h, s, &c0, &len);
+    const bool resident = h->tail > 0 && s == nseg - 1 && h->tail_resident;
     if (h->stored) {
       // recompute the segment once, keeping every cycle's arrays, then sweep back
-      for (int k = 0; k < len; ++k) {
-        select_set(h, k);
-        A.dt = h->dts[c0 + k];
-        if ((rc = fwd_cycle(h, true))) return rc;
-        if (k + 1 < len && (rc = output_to_input(h, k, k + 1))) return rc;
+      // (the tail left resident by the forward pass needs no recomputation)
+      if (!resident) {
+        select_set(h, 0);
+        if ((rc = unpack(h, h->ckpt + (size_t)s * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
+        for (int k = 0; k < len; ++k) {
+          select_set(h, k);
+          A.dt = h->dts[c0 + k];
+          if ((rc = fwd_cycle(h, true))) return rc;
+          if (k + 1 < len && (rc = output_to_input(h, k, k + 1))) return rc;
+        }
       }
+      h->tail_resident = false;   // the arenas now hold this segment
       for (int k = len - 1; k >= 0; --k) {
         select_set(h, k);
         A.dt = h->dts[c0 + k];
@@ -1111,6 +1217,8 @@ int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initia
       }
     } else {
       // recompute the segment's states, then each cycle again before its reverse sweep
+      select_set(h, 0);
+      if ((rc = unpack(h, h->ckpt + (size_t)s * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
       for (int k = 0; k < len; ++k) {
         if ((rc = pack(h, h->seg + (size_t)k * h->state_words, A.P, A.C, A.FX, A.FY, false))) return rc;
         if (k + 1 < len) {
@@ -1131,6 +1239,22 @@ int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initia
   select_set(h, 0);
   if ((rc = pack(h, bar_initial, A.NP, A.NC, A.NFX, A.NFY, true))) return rc;
   CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd2d_adj_set_tail(void* handle, int max_cycles) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || max_cycles < -1) return MHD_ERR_ARG;
+  h->tail_max = max_cycles;
+  return MHD_OK;
+}
+
+int mhd2d_adj_record(void* handle, int* steps, int* every, int* tail) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return MHD_ERR_ARG;
+  if (steps) *steps = h->steps;
+  if (every) *every = h->every;
+  if (tail) *tail = h->tail;
   return MHD_OK;
 }
 

@@ -482,6 +482,19 @@ int mhd2d_run(void* handle, double t_lim, long long max_cycles, double cfl, doub
   return MHD_OK;
 }
 
+int mhd2d_set_dt_log(void* handle, double* dt_log, long long capacity) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || capacity < 0 || (capacity > 0 && !dt_log)) return MHD_ERR_ARG;
+  if (h->g.dt_log == dt_log && h->g.dt_log_cap == capacity) return MHD_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  h->g.dt_log = capacity > 0 ? dt_log : nullptr;
+  h->g.dt_log_cap = capacity;
+  // the kernels take the grid by value: rebuild the cycle graphs with the new log
+  for (auto& ge : h->graph)
+    if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+  return MHD_OK;
+}
+
 int mhd2d_download(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || (which != 0 && which != 1)) return MHD_ERR_ARG;

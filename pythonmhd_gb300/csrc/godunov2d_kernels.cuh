@@ -977,6 +977,7 @@ __device__ __forceinline__ void b_begin(const Grid& G) {
 __device__ __forceinline__ void b_end(const Grid& G) {
   LoopState* L = G.loop;
   if (!L->active) return;
+  if (G.dt_log && L->cycle >= 0 && L->cycle < G.dt_log_cap) G.dt_log[L->cycle] = L->dt;
   L->t_prev = L->t;
   L->t = L->t + L->dt;
   L->cycle = L->cycle + 1;

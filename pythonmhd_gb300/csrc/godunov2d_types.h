@@ -75,6 +75,10 @@ struct Grid {
   // B_x uniform at bx1d (the reference's evolve_1D_mhd)
   int one_d;
   double bx1d;
+  // optional device log of each cycle's dt, indexed by the loop's cycle counter
+  // (cycles at or past dt_log_cap are not logged)
+  double* dt_log;
+  long long dt_log_cap;
 };
 
 // index spaces of the batched work lists

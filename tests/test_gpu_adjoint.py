@@ -100,13 +100,27 @@ def test_forward_equals_step_and_backward_equals_chained_vjps(recon):
     bar = torch.tensor(rng.standard_normal(a.state_words), device=s0.device)
     grads = {}
     # stored mode (a segment's cycles stay resident) and recompute mode (a budget
-    # too small to hold them) for several checkpoint intervals
-    for every, budget, sets in ((3, 0, 3), (3, 1, 1), (1, 0, 1), (0, 0, 3), (7, 0, 7)):
-        a.configure(budget)
-        a.forward(s0, steps, cfl=0.4, every=every)
+    # too small to hold them) for several checkpoint intervals, without a tail; then
+    # with the forward pass's resident tail (the whole run, or the last 4 cycles after
+    # segments of 2), whose dts come from the stage kernels' CFL reduction and must
+    # equal the production step's bit for bit
+    for every, budget, sets, tail, want_tail in ((3, 0, 3, 0, 0), (3, 1, 1, 0, 0), (1, 0, 1, 0, 0),
+                                                 (0, 0, 3, 0, 0), (7, 0, 7, 0, 0), (3, 0, 3, -1, 7),
+                                                 (2, 0, 2, 4, 4), (3, 1, 1, -1, 0)):
+        a.configure(budget, tail=tail)
+        out_t = a.forward(s0, steps, cfl=0.4, every=every)
         assert a.info()["segment_sets"] == sets
+        assert a.record() == dict(steps=steps, every=every or 3, tail=want_tail)
         np.testing.assert_array_equal(a.dts, dts)
-        grads[(every, budget)] = a.backward(bar).cpu().numpy()
+        assert torch.equal(out_t, out)
+        grads[(every, budget, tail)] = a.backward(bar).cpu().numpy()
+        if want_tail:
+            # a second backward pass recomputes the tail from its checkpoint
+            again = a.backward(bar).cpu().numpy()
+            assert np.max(np.abs(again - grads[(every, budget, tail)])) <= 1e-12 * np.max(np.abs(again))
+        # the fixed-dt forward (stage kernels, tail included) gives the same state
+        assert torch.equal(a.forward(s0, steps, dts=dts, every=every), out)
+    a.configure(0, tail=-1)
     states = [s0]
     for k in range(steps - 1):
         states.append(a.cycle(states[-1], dts[k]))
