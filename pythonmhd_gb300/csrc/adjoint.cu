@@ -899,6 +899,7 @@ int prepare_record(Handle* h, int steps, int& every, bool own_ckpt, bool allow_t
   }
   h->every = every;
   h->tail = tail;
+  h->steps = steps;   // the segment helpers read it; callers reset it if the record fails
   return MHD_OK;
 }
 
@@ -987,6 +988,9 @@ int forward_on_solver(Handle* h, const double* state_in, int steps, double cfl, 
   }
   return save(state_out);
 }
+
+int forward_record(Handle* h, Adj& A, const double* state_in, int steps, double cfl, const double* fixed_dt,
+                   double* state_out);
 
 }  // namespace
 
@@ -1131,9 +1135,28 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
   if (!h || !state_in || !state_out || steps < 1) return MHD_ERR_ARG;
   Adj& A = h->A;
   int rc = prepare_record(h, steps, every, true, true);
-  if (rc) return rc;
-  every = h->every;
+  if (rc) {
+    h->steps = 0;
+    return rc;
+  }
   h->dts.assign(steps, 0.0);
+  rc = forward_record(h, A, state_in, steps, cfl, fixed_dt, state_out);
+  if (rc) {
+    h->steps = 0;
+    h->tail_resident = false;
+    return rc;
+  }
+  if (dt_log) std::copy(h->dts.begin(), h->dts.end(), dt_log);
+  return MHD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// the body of mhd2d_adj_forward once the record is sized
+int forward_record(Handle* h, Adj& A, const double* state_in, int steps, double cfl, const double* fixed_dt,
+                   double* state_out) {
+  int rc;
   if (!fixed_dt) {
     if ((rc = forward_on_solver(h, state_in, steps, cfl, state_out))) return rc;
   } else {
@@ -1164,21 +1187,27 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
     }
   }
   CK(cudaStreamSynchronize(h->stream));
-  h->steps = steps;
-  if (dt_log) std::copy(h->dts.begin(), h->dts.end(), dt_log);
   return MHD_OK;
 }
+}  // namespace
+
+extern "C" {
 
 int mhd2d_adj_restore(void* handle, const double* checkpoints, int steps, int every, const double* dt) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !checkpoints || !dt || steps < 1 || every < 1) return MHD_ERR_ARG;
   int rc = prepare_record(h, steps, every, false, false);
-  if (rc) return rc;
+  if (rc) {
+    h->steps = 0;
+    return rc;
+  }
   h->ckpt = const_cast<double*>(checkpoints);
   h->dts.assign(dt, dt + steps);
   for (int c = 0; c < steps; ++c)
-    if (!std::isfinite(h->dts[c])) return MHD_ERR_NONFINITE;
-  h->steps = steps;
+    if (!std::isfinite(h->dts[c])) {
+      h->steps = 0;
+      return MHD_ERR_NONFINITE;
+    }
   return MHD_OK;
 }
 
