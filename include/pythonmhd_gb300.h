@@ -277,6 +277,10 @@ int mhd3d_upload(void* handle, const double* prim, const double* cons);
 int mhd3d_upload_device(void* handle, const double* prim, const double* cons);
 int mhd3d_advance(void* handle, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
                   double* t_out, long long* cycle_out, double* t_second_last);
+/* mhd2d_run's driver loop (Source/Simulation.py:290-413) on a 3D handle */
+int mhd3d_run(void* handle, double t_lim, long long max_cycles, double cfl, double save_dt, int save_prec,
+              double plot_dt, int plot_prec, mhd2d_stop_fn on_stop, void* user, double* t_out,
+              long long* cycle_out, long long* stops_out);
 int mhd3d_download(void* handle, int which, double* prim, double* cons);
 /* device pointers of the current (which = 0) or second-last (1) state */
 int mhd3d_state_ptrs(void* handle, int which, double** prim, double** cons);

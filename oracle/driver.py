@@ -12,21 +12,17 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import hydro2d, mhd2d
+from . import hydro2d, hydro3d, mhd2d
 
 
-def run(prim, cons, fbx, fby, dx, dy, bcx, bcy, t_lim, max_cycles, gamma, cfl, min_d, min_p, min_e, order,
-        efix, eps, save_dt=-1.0, save_prec=0, plot_dt=-1.0, plot_prec=0):
-    """Returns (t, cycle, stops, final_state); stops = [(t, cycle, kinds, state), ...]."""
-    mhd = prim.shape[0] == 8
+def _drive(state, evolve, t_lim, max_cycles, save_dt, save_prec, plot_dt, plot_prec):
+    """The loop itself.  ``evolve(state, t0, t_end, cycle0)`` returns (state, t, cycle,
+    second_last_state, second_last_t); a state is a tuple of arrays."""
     save, plot = save_dt > 0, plot_dt > 0
-    prim, cons = prim.copy(), cons.copy()
-    fbx = fbx.copy() if mhd else None
-    fby = fby.copy() if mhd else None
     stops = []
 
     def snap():
-        return tuple(a.copy() for a in ((prim, cons, fbx, fby) if mhd else (prim, cons)))
+        return tuple(a.copy() for a in state)
 
     if save or plot:
         stops.append((0.0, 0, (1 if save else 0) | (2 if plot else 0), snap()))
@@ -39,18 +35,7 @@ def run(prim, cons, fbx, fby, dx, dy, bcx, bcy, t_lim, max_cycles, gamma, cfl, m
         next_save = np.minimum(next_save, save_dt)
     next_stop = np.minimum(next_plot, next_save)
     while sim_t < t_lim and cycles < max_cycles:
-        if mhd:
-            (p2, c2, bx2, by2, t2, cyc2, psl, csl, bxsl, bysl, tsl) = mhd2d.evolve(
-                prim, cons, fbx, fby, dx, dy, bcx, bcy, sim_t, next_stop, cycles, max_cycles, gamma, cfl,
-                min_d, min_p, min_e, order, efix, eps)
-        else:
-            (p2, c2, t2, cyc2, psl, csl, tsl) = hydro2d.evolve(
-                prim, cons, dx, dy, bcx, bcy, sim_t, next_stop, cycles, max_cycles, gamma, cfl, min_d, min_p,
-                min_e, order, efix, eps)
-        prim, cons = p2, c2
-        if mhd:
-            fbx, fby = bx2, by2
-        sim_t, cycles = t2, cyc2
+        state, sim_t, cycles, sl_state, tsl = evolve(state, sim_t, next_stop, cycles)
         kinds = 0
         if save and next_stop == next_save:
             last_save = sim_t
@@ -67,7 +52,36 @@ def run(prim, cons, fbx, fby, dx, dy, bcx, bcy, t_lim, max_cycles, gamma, cfl, m
             next_save = np.round(np.minimum(next_save, last_save + save_dt), save_prec)
         next_stop = np.minimum(next_plot, next_save)
         if sim_t < t_lim and cycles < max_cycles:
-            prim, cons, sim_t = psl, csl, tsl
-            if mhd:
-                fbx, fby = bxsl, bysl
+            state, sim_t = sl_state, tsl
     return sim_t, cycles, stops, snap()
+
+
+def run(prim, cons, fbx, fby, dx, dy, bcx, bcy, t_lim, max_cycles, gamma, cfl, min_d, min_p, min_e, order,
+        efix, eps, save_dt=-1.0, save_prec=0, plot_dt=-1.0, plot_prec=0):
+    """2D driver run.  Returns (t, cycle, stops, final_state); stops = [(t, cycle, kinds, state), ...]."""
+    mhd = prim.shape[0] == 8
+
+    def evolve(st, t0, t_end, cyc0):
+        if mhd:
+            (p2, c2, bx2, by2, t2, cyc2, psl, csl, bxsl, bysl, tsl) = mhd2d.evolve(
+                *st, dx, dy, bcx, bcy, t0, t_end, cyc0, max_cycles, gamma, cfl, min_d, min_p, min_e, order, efix,
+                eps)
+            return (p2, c2, bx2, by2), t2, cyc2, (psl, csl, bxsl, bysl), tsl
+        (p2, c2, t2, cyc2, psl, csl, tsl) = hydro2d.evolve(
+            *st, dx, dy, bcx, bcy, t0, t_end, cyc0, max_cycles, gamma, cfl, min_d, min_p, min_e, order, efix, eps)
+        return (p2, c2), t2, cyc2, (psl, csl), tsl
+
+    state = (prim.copy(), cons.copy(), fbx.copy(), fby.copy()) if mhd else (prim.copy(), cons.copy())
+    return _drive(state, evolve, t_lim, max_cycles, save_dt, save_prec, plot_dt, plot_prec)
+
+
+def run3d(prim, cons, dx, dy, dz, bcx, bcy, bcz, t_lim, max_cycles, gamma, cfl, min_d, min_p, min_e, order, efix,
+          eps, save_dt=-1.0, save_prec=0, plot_dt=-1.0, plot_prec=0):
+    """The same loop around the 3D hydro evolve function (oracle/hydro3d.py)."""
+    def evolve(st, t0, t_end, cyc0):
+        (p2, c2, t2, cyc2, psl, csl, tsl) = hydro3d.evolve(
+            *st, dx, dy, dz, bcx, bcy, bcz, t0, t_end, cyc0, max_cycles, gamma, cfl, min_d, min_p, min_e, order,
+            efix, eps)
+        return (p2, c2), t2, cyc2, (psl, csl), tsl
+
+    return _drive((prim.copy(), cons.copy()), evolve, t_lim, max_cycles, save_dt, save_prec, plot_dt, plot_prec)

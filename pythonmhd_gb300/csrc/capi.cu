@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/pythonmhd_gb300.h"
+#include "driver_loop.h"
 #include "godunov2d_types.h"
 
 namespace mhdk {
@@ -424,62 +425,24 @@ int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0, long 
   return MHD_OK;
 }
 
-// numpy.round(x, decimals) for decimals >= 0: rint(x * 10**decimals) / 10**decimals
-static double round_decimals(double x, int decimals) {
-  const double p = std::pow(10.0, (double)decimals);
-  return std::nearbyint(x * p) / p;
-}
-
 int mhd2d_run(void* handle, double t_lim, long long max_cycles, double cfl, double save_dt, int save_prec,
               double plot_dt, int plot_prec, mhd2d_stop_fn on_stop, void* user, double* t_out,
               long long* cycle_out, long long* stops_out) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h) return MHD_ERR_ARG;
   if (!h->have_state) return MHD_ERR_STATE;
-  if (!(t_lim > 0.0) || max_cycles < 0 || save_prec < 0 || plot_prec < 0 || save_prec > 15 || plot_prec > 15)
-    return MHD_ERR_ARG;
-  const bool save = save_dt > 0.0, plot = plot_dt > 0.0;
-  double sim_t = 0.0;
-  long long cycles = 0, stops = 0;
-  // the initial state is saved / shown before the first cycle
-  if ((save || plot) && on_stop) {
-    const int r = on_stop(user, 0.0, 0, (save ? 1 : 0) | (plot ? 2 : 0));
-    if (r) return MHD_ERR_ABORTED;
-  }
-  double next_plot = t_lim, next_save = t_lim, last_plot = 0.0, last_save = 0.0;
-  if (plot) next_plot = std::min(next_plot, plot_dt);
-  if (save) next_save = std::min(next_save, save_dt);
-  double next_stop = std::min(next_plot, next_save);
-  while (sim_t < t_lim && cycles < max_cycles) {
-    double t_new = 0.0, t_sl = 0.0;
-    long long c_new = 0;
-    int rc = mhd2d_advance(handle, sim_t, next_stop, cycles, max_cycles, cfl, &t_new, &c_new, &t_sl);
-    if (rc) return rc;
-    sim_t = t_new;
-    cycles = c_new;
-    int kinds = 0;
-    if (save && next_stop == next_save) { last_save = sim_t; kinds |= 1; }
-    if (plot && next_stop == next_plot) { last_plot = sim_t; kinds |= 2; }
-    if (kinds) {
-      ++stops;
-      if (on_stop && on_stop(user, sim_t, cycles, kinds)) return MHD_ERR_ABORTED;
-    }
-    next_plot = t_lim;
-    next_save = t_lim;
-    if (plot) next_plot = round_decimals(std::min(next_plot, last_plot + plot_dt), plot_prec);
-    if (save) next_save = round_decimals(std::min(next_save, last_save + save_dt), save_prec);
-    next_stop = std::min(next_plot, next_save);
-    // still running: continue from the state before the short cycle that reached the stop
-    if (sim_t < t_lim && cycles < max_cycles && h->last_cycles_run > 0) {
-      h->cur ^= 1;
-      h->last_cycles_run = 0;
-      sim_t = t_sl;
-    }
-  }
-  if (t_out) *t_out = sim_t;
-  if (cycle_out) *cycle_out = cycles;
-  if (stops_out) *stops_out = stops;
-  return MHD_OK;
+  auto advance = [&](double t0, double t_end, long long c0, long long cmax, double* t, long long* c, double* tsl,
+                     long long* ran) {
+    int rc = mhd2d_advance(handle, t0, t_end, c0, cmax, cfl, t, c, tsl);
+    *ran = h->last_cycles_run;
+    return rc;
+  };
+  auto revert = [&]() {
+    h->cur ^= 1;
+    h->last_cycles_run = 0;
+  };
+  return mhdk::driver_loop(t_lim, max_cycles, save_dt, save_prec, plot_dt, plot_prec, on_stop, user, advance, revert,
+                           t_out, cycle_out, stops_out);
 }
 
 int mhd2d_set_dt_log(void* handle, double* dt_log, long long capacity) {

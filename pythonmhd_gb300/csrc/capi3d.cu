@@ -9,6 +9,7 @@
 #include <new>
 
 #include "../../include/pythonmhd_gb300.h"
+#include "driver_loop.h"
 #include "godunov3d_types.h"
 
 namespace mhdk {
@@ -247,6 +248,26 @@ int mhd3d_advance(void* handle, double t0, double t_end, long long cycle0, long 
   if (cycle_out) *cycle_out = st.cycle;
   if (t_second_last) *t_second_last = st.cycles_run > 0 ? st.t_prev : t0;
   return MHD_OK;
+}
+
+int mhd3d_run(void* handle, double t_lim, long long max_cycles, double cfl, double save_dt, int save_prec,
+              double plot_dt, int plot_prec, mhd2d_stop_fn on_stop, void* user, double* t_out,
+              long long* cycle_out, long long* stops_out) {
+  Handle3* h = static_cast<Handle3*>(handle);
+  if (!h) return MHD_ERR_ARG;
+  if (!h->have_state) return MHD_ERR_STATE;
+  auto advance = [&](double t0, double t_end, long long c0, long long cmax, double* t, long long* c, double* tsl,
+                     long long* ran) {
+    int rc = mhd3d_advance(handle, t0, t_end, c0, cmax, cfl, t, c, tsl);
+    *ran = h->last_cycles_run;
+    return rc;
+  };
+  auto revert = [&]() {
+    h->cur ^= 1;
+    h->last_cycles_run = 0;
+  };
+  return mhdk::driver_loop(t_lim, max_cycles, save_dt, save_prec, plot_dt, plot_prec, on_stop, user, advance, revert,
+                           t_out, cycle_out, stops_out);
 }
 
 int mhd3d_download(void* handle, int which, double* prim, double* cons) {

@@ -17,7 +17,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .solver import Grid2D, default_arith
+from .solver import Grid2D, Grid3D, default_arith
 
 STOP_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong, ctypes.c_int)
 SAVE, PLOT = 1, 2
@@ -38,9 +38,10 @@ def time_precision(dt, t_lim):
     return max(_decimals(t_lim), _decimals(dt))
 
 
-def run(grid: Grid2D, t_lim, max_cycles, cfl, save_dt=-1.0, save_prec=None, plot_dt=-1.0, plot_prec=None,
+def run(grid, t_lim, max_cycles, cfl, save_dt=-1.0, save_prec=None, plot_dt=-1.0, plot_prec=None,
         on_stop=None):
-    """Run the driver loop on an uploaded ``Grid2D``.
+    """Run the driver loop on an uploaded ``Grid2D`` or ``Grid3D`` (``mhd2d_run`` /
+    ``mhd3d_run``).
 
     ``on_stop(t, cycle, kinds, grid)`` is called at t = 0 and at every save/plot
     stop (``kinds`` bit 0 save, bit 1 plot) with the stop's state on the device
@@ -67,11 +68,14 @@ def run(grid: Grid2D, t_lim, max_cycles, cfl, save_dt=-1.0, save_prec=None, plot
     t = ctypes.c_double()
     c = ctypes.c_longlong()
     n = ctypes.c_longlong()
-    rc = lib.mhd2d_run(grid.handle, float(t_lim), int(max_cycles), float(cfl), float(save_dt), int(save_prec),
-                       float(plot_dt), int(plot_prec), fn, None, ctypes.byref(t), ctypes.byref(c), ctypes.byref(n))
+    three_d = isinstance(grid, Grid3D)
+    entry = lib.mhd3d_run if three_d else lib.mhd2d_run
+    rc = entry(grid._h if three_d else grid.handle, float(t_lim), int(max_cycles), float(cfl), float(save_dt),
+               int(save_prec), float(plot_dt), int(plot_prec), fn, None, ctypes.byref(t), ctypes.byref(c),
+               ctypes.byref(n))
     if err:
         raise err[0]
-    _lib.check(rc, "mhd2d_run")
+    _lib.check(rc, "mhd3d_run" if three_d else "mhd2d_run")
     return t.value, c.value, n.value
 
 

@@ -87,3 +87,35 @@ def test_driver_stop_callback_can_end_the_run(tmp_path):
     d = scipy.io.loadmat(str(tmp_path / "snap_0.mat"))
     np.testing.assert_array_equal(d["faceBx"], c["fbx"])
     np.testing.assert_array_equal(d["density"], c["prim"][0])
+
+
+@pytest.mark.parametrize("t_lim,save_dt,plot_dt,order", [(0.03, 0.01, 0.0075, 2), (0.02, -1.0, 0.005, 0)])
+def test_3d_driver_matches_oracle_driver(t_lim, save_dt, plot_dt, order):
+    """mhd3d_run on a 3D hydro blast against the oracle's driver around its 3D step."""
+    from pythonmhd_gb300.solver import Grid3D
+    ny, nx, nz = 10, 12, 8
+    prim = np.zeros((5, ny, nx, nz))
+    prim[0] = 1.0
+    prim[4] = 0.1
+    prim[4, 4:6, 5:7, 3:5] = 10.0
+    cons = ic.prim_to_cons_hydro(prim, 1.4)
+    sp = driver.time_precision(save_dt, t_lim) if save_dt > 0 else 0
+    pp = driver.time_precision(plot_dt, t_lim) if plot_dt > 0 else 0
+    args = (1 / nx, 1 / ny, 1 / nz, 1, 0, 1, t_lim, 1000, 1.4, 0.4, 1e-12, 1e-12, 1e-12, order, False, 0.5)
+    t_w, cyc_w, stops_w, final_w = odriver.run3d(prim, cons, *args, save_dt=save_dt, save_prec=sp,
+                                                 plot_dt=plot_dt, plot_prec=pp)
+    got = []
+    g = Grid3D(ny, nx, nz, 1 / nx, 1 / ny, 1 / nz, 1, 0, 1, 1.4, recon=order, arith="exact")
+    g.upload(prim, cons)
+    t, cyc, n = driver.run(g, t_lim, 1000, 0.4, save_dt=save_dt, plot_dt=plot_dt,
+                           on_stop=lambda t, c, k, grid: got.append((t, c, k, grid.download())))
+    final = g.download()
+    g.close()
+    assert (t, cyc) == (t_w, cyc_w) and cyc > 5
+    assert len(got) == len(stops_w) and n == len(stops_w) - 1
+    for (tg, cg, kg, sg), (tw, cw, kw, sw) in zip(got, stops_w):
+        assert (tg, cg, kg) == (tw, cw, kw)
+        for a, b in zip(sg, sw):
+            assert np.array_equal(a, b)
+    for a, b in zip(final, final_w):
+        assert np.array_equal(a, b)
