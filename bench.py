@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=400,
                     help="cycles of the 512^2 PLM adjoint workload (0 = skip it)")
     ap.add_argument("--adjoint-n", type=int, default=512)
+    ap.add_argument("--adjoint-tail", type=int, default=-1,
+                    help="cycles the adjoint's forward pass leaves resident (-1 as many as fit, 0 none)")
     ap.add_argument("--hydro3d-steps", type=int, default=10,
                     help="cycles of the 3D hydro turbulence workload (0 = skip it)")
     ap.add_argument("--hydro3d-n", type=int, default=256)
@@ -332,6 +334,7 @@ def run_adjoint(a, torch):
     tgt = fields.perturbed(fl, 0.02, seed=2)
     g0 = fl["gamma"]
     adj = Adjoint2D(n, n, fl["dx"], fl["dy"], 1, 1, g0, recon=1)
+    adj.configure(0, tail=a.adjoint_tail)
     st_t = fields.state_from_fields(*fields.fields_to_torch(tgt, dev), g0, fl["dx"], fl["dy"]).contiguous()
     target = adj.unpack(adj.forward(st_t, steps, cfl=0.4))[0][0].clone()
     # production forward on the same initial state (the denominator)
@@ -351,7 +354,7 @@ def run_adjoint(a, torch):
     # warm-up (untimed): one short gradient through the same handle (first launches of
     # the reverse kernels, the autograd path)
     xw = fields.fields_to_torch(fl, dev, requires_grad=True)
-    ow = evolve(fields.state_from_fields(*xw, g0, fl["dx"], fl["dy"]), adj, 8, cfl=0.4)
+    ow = evolve(fields.state_from_fields(*xw, g0, fl["dx"], fl["dy"]), adj, min(8, steps), cfl=0.4)
     torch.mean((adj.unpack(ow)[0][0] - target) ** 2).backward()
     torch.cuda.synchronize()
     # gradient: forward pass (records dt, keeps checkpoints) + backward pass
@@ -381,7 +384,7 @@ def run_adjoint(a, torch):
             "checkpoint_every": rec["every"], "segment_cycles_resident": info["segment_sets"],
             "tail_cycles_resident_from_forward": rec["tail"],
             "device_bytes": info["device_bytes"],
-            "timing": "host wall clock around device-synchronised calls, after an untimed 8-cycle gradient; "
+            "timing": "host wall clock around device-synchronised calls, after an untimed gradient of min(8, steps) cycles; "
                       "forward = production exact step"}
 
 
