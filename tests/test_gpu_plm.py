@@ -1,5 +1,5 @@
-"""PLM reconstruction (recon = 1), the reconstruction BASELINE's configs [0], [2]
-and [3] ask for.  The reference has no PLM (its branches are commented out,
+"""PLM reconstruction (recon = 1), the reconstruction of the 128^2 Orszag-Tang,
+batched Orszag-Tang and 512^2 adjoint workloads.  The reference has no PLM (its branches are commented out,
 Source/EvolveFunctions_MHD.py:487-488), so parity against the reference is
 unpinned; the GPU path is checked bit for bit against the oracle's restatement
 (oracle.mhd2d.plm_edges) and through properties PLM must have: a uniform state
