@@ -26,6 +26,12 @@
 namespace {
 
 constexpr int kT = 128;
+// resident blocks per SM the heavy reverse kernels are compiled for (1: up to 255
+// registers a thread; more blocks cap the registers and trade spills for occupancy)
+#ifndef MHD_ADJ_REV_MIN_BLOCKS
+#define MHD_ADJ_REV_MIN_BLOCKS 1
+#endif
+constexpr int kRevMinBlocks = MHD_ADJ_REV_MIN_BLOCKS;
 static_assert(g_plm0_NT == g_plm1_NT && g_roe1_0_NT == g_roe1_1_NT && g_roe2_0_NT == g_roe2_1_NT &&
                   g_ctu0_NT == g_ctu1_NT && g_ppm0_NT == g_ppm1_NT && g_pslope0_NT == g_pslope1_NT &&
                   g_roe1_0_efix_NT == g_roe1_1_efix_NT && g_roe2_0_efix_NT == g_roe2_1_efix_NT,
@@ -125,7 +131,7 @@ __device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a
 // ---------------------------------------------------------------------------
 // limited slopes of the sweep-extended cells e = 0 .. L+1 (cell e-1), PPM only
 template <int AX, bool REV, bool TAPE>
-__global__ void __launch_bounds__(kT) k_slope(Adj A) {
+__global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_slope(Adj A) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y;
   const int Wd = AX == 0 ? A.nx + 2 : A.nx, H = AX == 0 ? A.ny : A.ny + 2;
   if (col >= Wd || row >= H) return;
@@ -159,7 +165,7 @@ __global__ void __launch_bounds__(kT) k_slope(Adj A) {
 
 // edge states of each cell: first order (copies), PLM, or PPM from the slopes
 template <int AX, bool REV, bool TAPE, int RECON>
-__global__ void __launch_bounds__(kT) k_recon(Adj A) {
+__global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
   if (c0 >= A.nx || t0 >= A.ny) return;
   const size_t me = (size_t)t0 * A.nx + c0;
@@ -297,7 +303,7 @@ __global__ void __launch_bounds__(kT) k_face(Adj A) {
 }
 
 template <int AX, int STAGE, bool REV, bool TAPE>
-__global__ void __launch_bounds__(kT) k_roe(Adj A) {
+__global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_roe(Adj A) {
   const size_t nf = AX == 0 ? (size_t)(A.nx + 1) * A.ny : (size_t)A.nx * (A.ny + 1);
   const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
