@@ -408,9 +408,82 @@ def hydro3d_cases():
 
 
 def build3d(physics, name):
-    assert physics == "hydro"
-    return dict(hydro3d_cases())[name]()
+    return dict(hydro3d_cases() if physics == "hydro" else mhd3d_cases())[name]()
 
 
 def names3d(physics):
-    return [n for n, _ in hydro3d_cases()] if physics == "hydro" else []
+    return [n for n, _ in (hydro3d_cases() if physics == "hydro" else mhd3d_cases())]
+
+
+# ----------------------------------------------------------------------------
+# 3D MHD (evolve_3D_mhd): prim/cons (8, ny, nx, nz), faceBx (ny, nx+1, nz),
+# faceBy (ny+1, nx, nz), faceBz (ny, nx, nz+1).  The reference runs PPM on cubes
+# for every boundary combination and on other boxes when y and z are periodic;
+# its first-order path needs a periodic y (Source/EvolveFunctions_MHD.py:857-866
+# reshape an outflow y slab to 3 dimensions).
+# ----------------------------------------------------------------------------
+def _random_mhd_3d(ny, nx, nz, seed, gamma=G53, mach=0.6, b0=0.5):
+    """Smooth random fields; face B from a smooth random edge vector potential, so the
+    discrete divergence of B is zero."""
+    rng = np.random.default_rng(seed)
+
+    def smooth(y, x, z):
+        f = np.zeros(np.broadcast(y, x, z).shape)
+        for _ in range(3):
+            k = rng.integers(1, 3, size=3)
+            ph = rng.uniform(0, 2 * math.pi, size=3)
+            f = f + rng.standard_normal() * (np.sin(2 * math.pi * k[0] * x + ph[0]) * np.cos(2 * math.pi * k[1] * y + ph[1])
+                                             * np.cos(2 * math.pi * k[2] * z + ph[2]))
+        return f / 3.0
+
+    dx, dy, dz = 1.0 / nx, 1.0 / ny, 1.0 / nz
+    yc, xc, zc = (np.arange(ny) + 0.5) * dy, (np.arange(nx) + 0.5) * dx, (np.arange(nz) + 0.5) * dz
+    yf, xf, zf = np.arange(ny + 1) * dy, np.arange(nx + 1) * dx, np.arange(nz + 1) * dz
+    Y, X, Z = np.meshgrid(yc, xc, zc, indexing="ij")
+    ax = b0 * smooth(*np.meshgrid(yf, xc, zf, indexing="ij")) * dy
+    ay = b0 * smooth(*np.meshgrid(yc, xf, zf, indexing="ij")) * dx
+    az = b0 * smooth(*np.meshgrid(yf, xf, zc, indexing="ij")) * dx
+    fbx = (az[1:, :, :] - az[:-1, :, :]) / dy - (ay[:, :, 1:] - ay[:, :, :-1]) / dz
+    fby = (ax[:, :, 1:] - ax[:, :, :-1]) / dz - (az[:, 1:, :] - az[:, :-1, :]) / dx
+    fbz = (ay[:, 1:, :] - ay[:, :-1, :]) / dx - (ax[1:, :, :] - ax[:-1, :, :]) / dy
+    prim = np.zeros((8, ny, nx, nz))
+    prim[0] = 1.0 + 0.25 * smooth(Y, X, Z) + 0.01 * rng.standard_normal((ny, nx, nz))
+    prim[1] = mach * smooth(Y, X, Z)
+    prim[2] = mach * smooth(Y, X, Z)
+    prim[3] = mach * smooth(Y, X, Z)
+    prim[4] = 0.5 * (fbx[:, :-1] + fbx[:, 1:])
+    prim[5] = 0.5 * (fby[:-1] + fby[1:])
+    prim[6] = 0.5 * (fbz[:, :, :-1] + fbz[:, :, 1:])
+    prim[7] = 0.6 + 0.1 * smooth(Y, X, Z)
+    return prim, ic.prim_to_cons_mhd(prim, gamma), fbx, fby, fbz, dx, dy, dz
+
+
+def mhd3d_cases():
+    def rnd(shape=(6, 6, 6), seed=31, **kw):
+        def f():
+            prim, cons, fbx, fby, fbz, dx, dy, dz = _random_mhd_3d(*shape, seed)
+            p = dict(_p3(gamma=G53, efix=True, max_cycles=2), **kw)
+            return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, fbz=fbz, dx=dx, dy=dy, dz=dz, **p)
+        return f
+
+    O, P = ic.OUTFLOW, ic.PERIODIC
+
+    def floors():
+        prim, cons, fbx, fby, fbz, dx, dy, dz = _random_mhd_3d(6, 6, 6, 37)
+        prim[0, 3, 2, 3] = 0.3
+        prim[7, 3, 2, 3] = 0.05
+        cons = ic.prim_to_cons_mhd(prim, G53)
+        return dict(prim=prim, cons=cons, fbx=fbx, fby=fby, fbz=fbz, dx=dx, dy=dy, dz=dz,
+                    **_p3(gamma=G53, efix=True, max_cycles=1, min_d=0.35, min_p=0.06))
+
+    return [("ppm_periodic", rnd()), ("ppm_periodic_noncubic", rnd(shape=(4, 5, 6), seed=32)),
+            ("ppm_outflow", rnd(bcx=O, bcy=O, bcz=O)), ("ppm_x_outflow", rnd(bcx=O, seed=33)),
+            ("ppm_y_outflow", rnd(bcy=O, seed=34)), ("ppm_z_outflow", rnd(bcz=O, seed=35)),
+            ("ppm_xz_outflow_no_efix", rnd(bcx=O, bcz=O, efix=False)), ("ppm_xy_outflow", rnd(bcx=O, bcy=O, seed=36)),
+            ("order0_periodic", rnd(order=0)), ("order0_xz_outflow", rnd(order=0, bcx=O, bcz=O, seed=38)),
+            ("order0_noncubic_periodic", rnd(shape=(4, 5, 6), order=0, seed=39)),
+            ("ppm_8cube_4cycles", rnd(shape=(8, 8, 8), seed=40, max_cycles=4)),
+            ("tend_clip", rnd(t_end=0.011, max_cycles=50)), ("no_cycle", rnd(start_cycle=3, max_cycles=3)),
+            ("floors", floors)]
+
+

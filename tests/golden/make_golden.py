@@ -98,10 +98,11 @@ SCALARS_3D = ("t_start", "t_end", "start_cycle", "max_cycles", "gamma", "cfl", "
 
 
 def run_reference_3d(ref_root, physics, case):
-    """evolve_3D_hydro (Source/EvolveFunctions_Hydro.py:559-806) on a grid object with the
-    attributes it reads."""
+    """evolve_3D_hydro / evolve_3D_mhd (Source/EvolveFunctions_Hydro.py:559-806,
+    Source/EvolveFunctions_MHD.py:750-1157) on a grid object with the attributes they read."""
     sys.path.insert(0, ref_root)
     import Source.EvolveFunctions_Hydro as ref_hydro  # noqa: E402
+    import Source.EvolveFunctions_MHD as ref_mhd  # noqa: E402
     ny, nx, nz = case["prim"].shape[1:]
     grid = SimpleNamespace(primVars=case["prim"].copy(), consVars=case["cons"].copy(), dx=case["dx"],
                            dy=case["dy"], dz=case["dz"], BcX=case["bcx"], BcY=case["bcy"], BcZ=case["bcz"],
@@ -109,17 +110,25 @@ def run_reference_3d(ref_root, physics, case):
     args = (grid, case["t_start"], case["t_end"], case["start_cycle"], case["max_cycles"], case["gamma"],
             case["cfl"], case["min_d"], case["min_p"], case["min_e"], case["order"], case["efix"], case["eps"])
     with contextlib.redirect_stdout(io.StringIO()):
-        res = ref_hydro.evolve_3D_hydro(*args)
-    keys = ("prim", "cons", "t", "cycle", "sl_prim", "sl_cons", "sl_t")
+        if physics == "mhd":
+            grid.faceBx, grid.faceBy, grid.faceBz = case["fbx"].copy(), case["fby"].copy(), case["fbz"].copy()
+            res = ref_mhd.evolve_3D_mhd(*args)
+            keys = ("prim", "cons", "fbx", "fby", "fbz", "t", "cycle", "sl_prim", "sl_cons", "sl_fbx", "sl_fby",
+                    "sl_fbz", "sl_t")
+        else:
+            res = ref_hydro.evolve_3D_hydro(*args)
+            keys = ("prim", "cons", "t", "cycle", "sl_prim", "sl_cons", "sl_t")
     return {"out_" + k: np.asarray(v) for k, v in zip(keys, res)}
 
 
 def main_3d(ref_root):
-    for physics in ("hydro",):
+    for physics in ("hydro", "mhd"):
         for name in cases.names3d(physics):
             case = cases.build3d(physics, name)
             outs = run_reference_3d(ref_root, physics, case)
             arrays = {"in_prim": case["prim"], "in_cons": case["cons"]}
+            if physics == "mhd":
+                arrays.update(in_fbx=case["fbx"], in_fby=case["fby"], in_fbz=case["fbz"])
             for k in SCALARS_3D:
                 arrays["p_" + k] = np.asarray(case[k])
             arrays.update(outs)

@@ -82,3 +82,33 @@ def test_3d_floor_cases_apply_floors():
                              p["t_start"], p["t_end"], p["start_cycle"], p["max_cycles"], p["gamma"], p["cfl"],
                              1e-12, 1e-12, 1e-12, p["order"], p["efix"], p["eps"])
         assert not np.array_equal(res[1], o["cons"])
+
+
+MHD3D_KEYS = ("prim", "cons", "fbx", "fby", "fbz", "t", "cycle", "sl_prim", "sl_cons", "sl_fbx", "sl_fby", "sl_fbz",
+              "sl_t")
+
+
+@pytest.mark.parametrize("path", golden_files("mhd3d"), ids=case_id)
+def test_oracle_3d_mhd_matches_reference_bitwise(path):
+    """The 3D MHD restatement (oracle/mhd3d.py) against evolve_3D_mhd
+    (Source/EvolveFunctions_MHD.py:750).  The reference's x predictor computes its y
+    terms in np.longdouble (80-bit on the x86 host that made these fixtures), and so
+    does the oracle; on a host whose long double differs the last bits can too."""
+    import platform
+
+    from oracle import mhd3d
+    p, i, o = load(path)
+    res = mhd3d.evolve(i["prim"], i["cons"], i["fbx"], i["fby"], i["fbz"], p["dx"], p["dy"], p["dz"], p["bcx"],
+                       p["bcy"], p["bcz"], p["t_start"], p["t_end"], p["start_cycle"], p["max_cycles"], p["gamma"],
+                       p["cfl"], p["min_d"], p["min_p"], p["min_e"], p["order"], p["efix"], p["eps"])
+    exact = platform.machine() in ("x86_64", "AMD64")
+    for k, v in zip(MHD3D_KEYS, res):
+        v = np.asarray(v)
+        if exact:
+            assert np.array_equal(v, o[k]), k
+        else:
+            assert np.allclose(v, o[k], rtol=1e-12, atol=1e-12 * max(1.0, float(np.max(np.abs(o[k]))))), k
+
+
+def test_golden_3d_mhd_set_is_complete():
+    assert len(golden_files("mhd3d")) >= 15
