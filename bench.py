@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--hydro3d-steps", type=int, default=10,
                     help="cycles of the 3D hydro turbulence workload (0 = skip it)")
     ap.add_argument("--hydro3d-n", type=int, default=256)
+    ap.add_argument("--mhd3d-steps", type=int, default=5,
+                    help="cycles of the 3D MHD turbulence workload (0 = skip it)")
+    ap.add_argument("--mhd3d-n", type=int, default=192)
     return ap.parse_args()
 
 
@@ -314,6 +317,60 @@ def run_hydro3d(a, torch):
             "timing": "CUDA events on the handle's stream; state 0.67 GB per buffer >> 129 MB L2"}
 
 
+def run_mhd3d(a, torch):
+    """3D MHD turbulence, n^3 periodic, PPM + Roe + CTU+CT with three EMF components,
+    FP64: device-resident zone-updates/s of the 3D MHD step (CUDA events on the
+    handle's stream); the oracle's 3D restatement on one host core on a 24^3 sample."""
+    from oracle import mhd3d
+    from pythonmhd_gb300 import initial_conditions as ic
+    from pythonmhd_gb300.solver import Grid3D
+    n = a.mhd3d_n
+    dev = torch.device("cuda", torch.cuda.current_device())
+    st = ic.turbulence_mhd_3d(n, seed=a.seed, gamma=5.0 / 3.0, kmax=16, mach=1.0, device=dev)
+    d = st[5]
+    g = Grid3D(n, n, n, d, d, d, 1, 1, 1, 5.0 / 3.0, recon=2, entropy_fix=True, arith=a.arith, mhd=True)
+    g.upload_device(*st[:5])
+    del st
+    torch.cuda.empty_cache()
+    stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+    t, cyc, _ = g.advance(0.0, 1e30, 0, 2, 0.4)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    t, cyc, _ = g.advance(t, 1e30, cyc, cyc + a.mhd3d_steps, 0.4)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / a.mhd3d_steps
+    launches = g.last_launches()
+    dev_bytes = g.device_bytes()
+    out = g.download(0)
+    g.close()
+    if not np.isfinite(out[1]).all():
+        raise RuntimeError("non-finite 3D MHD state after the timed cycles")
+    zones = n ** 3
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    achieved = 176.0 * zones / (ms * 1e-3) / 1e9
+    m = 24
+    sc = ic.turbulence_mhd_3d(m, seed=a.seed, gamma=5.0 / 3.0, kmax=4, mach=1.0, device="cpu")
+    arrs = [x.numpy() for x in sc[:5]]
+    t0 = time.perf_counter()
+    mhd3d.evolve(*arrs, sc[5], sc[5], sc[5], 1, 1, 1, 0.0, 1e30, 0, 2, 5.0 / 3.0, 0.4, 1e-12, 1e-12, 1e-12, 2, True,
+                 0.5)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"3D ideal-MHD turbulence {n}^3 periodic, gamma=5/3, rms Mach 1, beta 1, k<=16, "
+                        f"PPM+Roe+CTU+CT (three edge EMFs), entropy fix, CFL 0.4, FP64, seeded (seed {a.seed})",
+            "zone_updates_per_s": zones / (ms * 1e-3), "ms_per_cycle": ms, "steps": a.mhd3d_steps,
+            "gpu_launches": launches, "device_bytes": dev_bytes,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "kernel": "one full 3D MHD cycle (29 kernels, CUDA graphs), 176 algorithmic B/zone "
+                                   "(8 conserved and 3 face-B words in and out)", "compute_bound": "fp64"},
+            "cpu_baseline": {"value": m ** 3 * 2 / cpu_s, "unit": "zone-updates/s", "cores": 1, "kind": "port",
+                             "sample": f"oracle/mhd3d.py, {m}^3 periodic turbulence, 2 PPM cycles"},
+            "timing": "CUDA events on the handle's stream; state 1.3 GB per buffer >> 129 MB L2"}
+
+
 # ----------------------------------------------------------------------------
 # adjoint: gradient of a density-matching loss through many cycles
 # ----------------------------------------------------------------------------
@@ -519,6 +576,10 @@ def run_ours(a):
     if a.hydro3d_steps > 0:
         g.close()
         hydro_3d = run_hydro3d(a, torch)
+    mhd_3d = None
+    if a.mhd3d_steps > 0:
+        g.close()
+        mhd_3d = run_mhd3d(a, torch)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_per, "higher_is_better": True, "scaling": "weak",
@@ -531,7 +592,7 @@ def run_ours(a):
                     "steps": e2e_steps, "ms_per_step": ms_e2e_per},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "device_bytes": dev_bytes, "final_cycle": cyc, "final_time": t, "batched": batched,
-            "adjoint": adjoint, "hydro3d": hydro_3d}
+            "adjoint": adjoint, "hydro3d": hydro_3d, "mhd3d": mhd_3d}
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()

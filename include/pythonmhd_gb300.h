@@ -258,32 +258,40 @@ int mhd2d_adj_record(void* handle, int* steps, int* every, int* tail);
 void mhd2d_adj_destroy(void* handle);
 
 /* ---------------------------------------------------------------------------
- * 3D step (hydro): replaces the reference's
+ * 3D step: replaces the reference's
  *   Source/EvolveFunctions_Hydro.py:559-560  evolve_3D_hydro(simulationGrid, tStart, tEnd,
  *                                            startCycle, maxCycles, gamma, cfl, minDens,
  *                                            minPres, minEnergy, reconstructOrder,
  *                                            entropyFix, epsilon)
- * States are (5, ny, nx, nz), z fastest (the reference's layout, also the device
- * layout).  bcx/bcy/bcz: 0 outflow, 1 periodic; recon: 2 PPM, 0 first order, 1
- * PLM (an addition).  physics must be MHD2D_HYDRO (the 3D MHD step is not built).
- * The evolve loop, second-last state and download semantics are mhd2d_advance's /
- * mhd2d_download's.  nx, ny, nz >= 2; (nx+2)(ny+2)(nz+2) below 2^32.
+ *   Source/EvolveFunctions_MHD.py:750-751    evolve_3D_mhd(...)  (same arguments)
+ * States are (nvars, ny, nx, nz), z fastest (the reference's layout, also the device
+ * layout); MHD adds faceBx (ny, nx+1, nz), faceBy (ny+1, nx, nz), faceBz (ny, nx, nz+1)
+ * (NULL for hydro).  bcx/bcy/bcz: 0 outflow, 1 periodic; recon: 2 PPM, 0 first
+ * order, 1 PLM (an addition).  The evolve loop, second-last state and download
+ * semantics are mhd2d_advance's / mhd2d_download's.  nx, ny, nz >= 2;
+ * (nx+2)(ny+2)(nz+2) below 2^32.  The MHD x predictor's y terms, which the reference
+ * computes in long double (Source/CTU_HelperModule.py:455), are FP64 here: results
+ * match the reference to rounding, not bit for bit.
  * ------------------------------------------------------------------------- */
 int mhd3d_create(int ny, int nx, int nz, double dx, double dy, double dz, int bcx, int bcy, int bcz,
                  double gamma, int physics, int recon, int entropy_fix, double eps, double min_d, double min_p,
                  double min_e, int arith, void** handle);
-int mhd3d_upload(void* handle, const double* prim, const double* cons);
+int mhd3d_upload(void* handle, const double* prim, const double* cons, const double* faceBx, const double* faceBy,
+                 const double* faceBz);
 /* as mhd3d_upload, from device pointers */
-int mhd3d_upload_device(void* handle, const double* prim, const double* cons);
+int mhd3d_upload_device(void* handle, const double* prim, const double* cons, const double* faceBx,
+                        const double* faceBy, const double* faceBz);
 int mhd3d_advance(void* handle, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
                   double* t_out, long long* cycle_out, double* t_second_last);
 /* mhd2d_run's driver loop (Source/Simulation.py:290-413) on a 3D handle */
 int mhd3d_run(void* handle, double t_lim, long long max_cycles, double cfl, double save_dt, int save_prec,
               double plot_dt, int plot_prec, mhd2d_stop_fn on_stop, void* user, double* t_out,
               long long* cycle_out, long long* stops_out);
-int mhd3d_download(void* handle, int which, double* prim, double* cons);
+int mhd3d_download(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy,
+                   double* faceBz);
 /* device pointers of the current (which = 0) or second-last (1) state */
-int mhd3d_state_ptrs(void* handle, int which, double** prim, double** cons);
+int mhd3d_state_ptrs(void* handle, int which, double** prim, double** cons, double** faceBx, double** faceBy,
+                     double** faceBz);
 /* kernel launches of the last advance, device bytes held, the handle's cudaStream_t */
 int mhd3d_info(void* handle, long long* last_launches, size_t* device_bytes, void** stream);
 void mhd3d_destroy(void* handle);

@@ -276,12 +276,13 @@ def _minmod(nch, tch):
 STEPS = {0: ((1, 5, 1.0), (2, 4, -1.0)), 1: ((0, 4, -1.0), (2, 5, 1.0)), 2: ((0, 5, 1.0), (1, 4, -1.0))}
 
 
-def transverse(d, u_sides, prim, fluxes, fb, emf, dt, dn, bc):
+def transverse(d, u_sides, prim, fluxes, fb, emf, dt, dn, bc, long_double=True):
     """getXTransverseUpdates_3D / Y / Z (Source/CTU_HelperModule.py:451-1078): the
     face states of direction d (conserved, [minus, plus]) take, per transverse
     direction, the half-dt flux difference at their cell (B slots zeroed) and the
     EMF term of the edge EMF parallel to d, then the source vector of their
-    (sweep-extended) cell.  Returns new [minus, plus]."""
+    (sweep-extended) cell.  Returns new [minus, plus].  ``long_double=False`` computes
+    the x predictor's y terms in float64, as the CUDA step does."""
     n = {0: prim.shape[2], 1: prim.shape[1], 2: prim.shape[3]}
     L = n[d]
     ax = FAX[d]
@@ -304,7 +305,7 @@ def transverse(d, u_sides, prim, fluxes, fb, emf, dt, dn, bc):
                 a = np.take(ed, np.arange(eh, ne + eh), axis=FAX[e])
                 return np.take(a, np.arange(oh, no + oh), axis=FAX[o])
             delta = ((at(1, 0) - at(0, 0)) + at(1, 1)) - at(0, 1)
-            if d == 0 and e == 1:
+            if d == 0 and e == 1 and long_double:
                 half_ld = 0.5 * (np.longdouble(dt) / np.longdouble(dn[e]))
                 u = (u.astype(np.longdouble) - half_ld * diff).astype(np.float64)
                 upd = (half_ld * 0.5) * delta
@@ -352,7 +353,8 @@ def _normal_ghost_div(fb, d, n, bc, h, hi_face):
     return (_take(e, ax, np.arange(1, n + 3)) - _take(e, ax, np.arange(0, n + 2))) / h
 
 
-def cycle(prim, cons, fbx, fby, fbz, dt, dx, dy, dz, bcx, bcy, bcz, gamma, min_d, min_p, min_e, order, efix, eps):
+def cycle(prim, cons, fbx, fby, fbz, dt, dx, dy, dz, bcx, bcy, bcz, gamma, min_d, min_p, min_e, order, efix, eps,
+          long_double=True):
     """One cycle of evolve_3D_mhd (Source/EvolveFunctions_MHD.py:819-1152).
     Returns new (prim, cons, faceBx, faceBy, faceBz); the inputs are not modified."""
     ny, nx, nz = prim.shape[1:]
@@ -379,7 +381,7 @@ def cycle(prim, cons, fbx, fby, fbz, dt, dx, dy, dz, bcx, bcy, bcz, gamma, min_d
     f1 = [mhd2d.roe_flux(wf[d][0], wf[d][1], uf[d][0], uf[d][1], fb[d], gamma, efix, eps, FRAMES[d]) for d in range(3)]
     e1 = corner_emfs(f1[0], f1[1], f1[2], ex, ey, ez, (nx, ny, nz), bcs)
     for d in range(3):
-        uf[d] = transverse(d, uf[d], prim, f1, fb, e1[d], dt, dn, bcs[d])
+        uf[d] = transverse(d, uf[d], prim, f1, fb, e1[d], dt, dn, bcs[d], long_double)
     h = [0.5 * (dt / v) for v in dn]
     nfb = _ct(fb, e1, h, ny, nx, nz)
     wf = {d: [cons_to_prim_dir(s, nfb[d], gamma, FRAMES[d]) for s in uf[d]] for d in range(3)}
@@ -426,10 +428,11 @@ def _ct(fb, emf, h, ny, nx, nz):
 
 
 def evolve(prim, cons, fbx, fby, fbz, dx, dy, dz, bcx, bcy, bcz, t_start, t_end, start_cycle, max_cycles, gamma,
-           cfl, min_d, min_p, min_e, order=0, efix=True, eps=0.5, dt_log=None):
+           cfl, min_d, min_p, min_e, order=0, efix=True, eps=0.5, dt_log=None, long_double=True):
     """The evolve_3D_mhd loop (Source/EvolveFunctions_MHD.py:750-1157); returns the
     reference's 13-tuple (prim, cons, faceBx, faceBy, faceBz, time, cycle and the
-    second-last prim, cons, faceBx, faceBy, faceBz and time)."""
+    second-last prim, cons, faceBx, faceBy, faceBz and time).  ``long_double=False``
+    gives the FP64 predictor of the CUDA step (see ``transverse``)."""
     st = [np.array(a, dtype=np.float64) for a in (prim, cons, fbx, fby, fbz)]
     t = t_start
     cyc = start_cycle
@@ -441,7 +444,8 @@ def evolve(prim, cons, fbx, fby, fbz, dx, dy, dz, bcx, bcy, bcz, t_start, t_end,
             dt = t_end - t
         if dt_log is not None:
             dt_log.append(dt)
-        st = list(cycle(*st, dt, dx, dy, dz, bcx, bcy, bcz, gamma, min_d, min_p, min_e, order, efix, eps))
+        st = list(cycle(*st, dt, dx, dy, dz, bcx, bcy, bcz, gamma, min_d, min_p, min_e, order, efix, eps,
+                        long_double))
         t += dt
         cyc += 1
     return tuple(st) + (t, cyc) + sl

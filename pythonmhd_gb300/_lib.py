@@ -34,13 +34,13 @@ SIGNATURES = {
                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_void_p)]),
-    "mhd3d_upload": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
-    "mhd3d_upload_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mhd3d_upload": (ctypes.c_int, [ctypes.c_void_p] + [c_double_p] * 5),
+    "mhd3d_upload_device": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 5),
     "mhd3d_advance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_longlong,
                                      ctypes.c_longlong, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                      ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)]),
-    "mhd3d_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, c_double_p]),
-    "mhd3d_state_ptrs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_void_p)] * 2),
+    "mhd3d_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [c_double_p] * 5),
+    "mhd3d_state_ptrs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_void_p)] * 5),
     "mhd3d_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t),
                                   ctypes.POINTER(ctypes.c_void_p)]),
     "mhd3d_destroy": (None, [ctypes.c_void_p]),

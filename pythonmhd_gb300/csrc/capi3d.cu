@@ -1,4 +1,4 @@
-// C ABI of the 3D Godunov step (hydro): handle lifetime, host<->device copies and
+// C ABI of the 3D Godunov step (hydro and MHD): handle lifetime, host<->device copies and
 // the device-resident evolve loop, CUDA graphs of two cycles replayed in chunks as
 // in 2D.  State arrays cross the boundary in the reference's 3D layout
 // (nvars, ny, nx, nz), z fastest, which is also the device layout.
@@ -55,7 +55,8 @@ size_t al256(size_t n) { return (n + 255) & ~size_t(255); }
 
 // Lay out every buffer from `base` (256-byte aligned pieces); returns the bytes used.
 size_t carve3(Grid3& g, int nvars, char* base) {
-  const int nv = 5, nw = 10;
+  const bool mhd = g.physics == MHD2D_MHD;
+  const int nv = mhd ? 7 : 5, nw = mhd ? 42 : 10;
   const size_t cp = mhdk::cells3(g);
   g.ext_plane = std::max(mhdk::plane3(g, 0, 2), std::max(mhdk::plane3(g, 1, 2), mhdk::plane3(g, 2, 2)));
   size_t off = 0;
@@ -66,13 +67,25 @@ size_t carve3(Grid3& g, int nvars, char* base) {
   for (int b = 0; b < 2; ++b) {
     take(&g.st[b].prim, (size_t)nvars * cp);
     take(&g.st[b].cons, (size_t)nvars * cp);
-    for (auto& p : g.st[b].fb) p = nullptr;
+    for (int d = 0; d < 3; ++d) {
+      if (mhd) take(&g.st[b].fb[d], mhdk::plane3(g, d, 1));
+      else g.st[b].fb[d] = nullptr;
+    }
   }
   for (int d = 0; d < 3; ++d) {
     const size_t fp = mhdk::plane3(g, d, 1);
     take(&g.wl[d], nv * fp);
     take(&g.wr[d], nv * fp);
     take(&g.f[d], nv * fp);
+    if (mhd) {
+      take(&g.ul[d], nv * fp);
+      take(&g.ur[d], nv * fp);
+      take(&g.emf[d], mhdk::edges3(g));
+      take(&g.nfb[d], fp);
+      take(&g.ce[d], cp);
+    } else {
+      g.ul[d] = g.ur[d] = g.emf[d] = g.nfb[d] = g.ce[d] = nullptr;
+    }
   }
   if (g.recon >= 1) {
     take(&g.slopes, nv * g.ext_plane);
@@ -105,12 +118,17 @@ int build_graph3(Handle3* h, int parity) {
   return e == cudaSuccess ? MHD_OK : fail(e);
 }
 
-int upload3(Handle3* h, const double* prim, const double* cons, cudaMemcpyKind kind) {
+int upload3(Handle3* h, const double* prim, const double* cons, const double* const* fb, cudaMemcpyKind kind) {
   if (!h || !prim || !cons) return MHD_ERR_ARG;
+  const bool mhd = h->g.physics == MHD2D_MHD;
+  if (mhd && (!fb[0] || !fb[1] || !fb[2])) return MHD_ERR_ARG;
   const mhdk::StateBuf3& s = h->g.st[h->cur];
   const size_t cb = (size_t)h->nvars * mhdk::cells3(h->g) * sizeof(double);
   CK3(cudaMemcpyAsync(s.prim, prim, cb, kind, h->stream));
   CK3(cudaMemcpyAsync(s.cons, cons, cb, kind, h->stream));
+  if (mhd)
+    for (int d = 0; d < 3; ++d)
+      CK3(cudaMemcpyAsync(s.fb[d], fb[d], mhdk::plane3(h->g, d, 1) * sizeof(double), kind, h->stream));
   CK3(cudaStreamSynchronize(h->stream));
   h->have_state = 1;
   h->last_cycles_run = 0;
@@ -129,7 +147,7 @@ int mhd3d_create(int ny, int nx, int nz, double dx, double dy, double dz, int bc
   if (nx < 2 || ny < 2 || nz < 2 || !(dx > 0.0) || !(dy > 0.0) || !(dz > 0.0)) return MHD_ERR_ARG;
   for (int bc : {bcx, bcy, bcz})
     if (bc != 0 && bc != 1) return MHD_ERR_ARG;
-  if (physics != MHD2D_HYDRO) return MHD_ERR_ARG;  // the 3D step is built for hydro only
+  if (physics != MHD2D_HYDRO && physics != MHD2D_MHD) return MHD_ERR_ARG;
   if (recon != 0 && recon != 1 && recon != 2) return MHD_ERR_ARG;
   if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST) return MHD_ERR_ARG;
   // work items are 32-bit linear indices of the largest (sweep-extended) array
@@ -145,7 +163,7 @@ int mhd3d_create(int ny, int nx, int nz, double dx, double dy, double dz, int bc
   g.physics = physics; g.recon = recon; g.efix = entropy_fix ? 1 : 0;
   g.gamma = gamma; g.eps = eps; g.min_d = min_d; g.min_p = min_p; g.min_e = min_e;
   h->arith = arith;
-  h->nvars = 5;
+  h->nvars = physics == MHD2D_MHD ? 8 : 5;
 
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
@@ -194,12 +212,16 @@ void mhd3d_destroy(void* handle) {
   delete h;
 }
 
-int mhd3d_upload(void* handle, const double* prim, const double* cons) {
-  return upload3(static_cast<Handle3*>(handle), prim, cons, cudaMemcpyHostToDevice);
+int mhd3d_upload(void* handle, const double* prim, const double* cons, const double* faceBx, const double* faceBy,
+                 const double* faceBz) {
+  const double* fb[3] = {faceBx, faceBy, faceBz};
+  return upload3(static_cast<Handle3*>(handle), prim, cons, fb, cudaMemcpyHostToDevice);
 }
 
-int mhd3d_upload_device(void* handle, const double* prim, const double* cons) {
-  return upload3(static_cast<Handle3*>(handle), prim, cons, cudaMemcpyDeviceToDevice);
+int mhd3d_upload_device(void* handle, const double* prim, const double* cons, const double* faceBx,
+                        const double* faceBy, const double* faceBz) {
+  const double* fb[3] = {faceBx, faceBy, faceBz};
+  return upload3(static_cast<Handle3*>(handle), prim, cons, fb, cudaMemcpyDeviceToDevice);
 }
 
 int mhd3d_advance(void* handle, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
@@ -270,7 +292,8 @@ int mhd3d_run(void* handle, double t_lim, long long max_cycles, double cfl, doub
                            t_out, cycle_out, stops_out);
 }
 
-int mhd3d_download(void* handle, int which, double* prim, double* cons) {
+int mhd3d_download(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy,
+                   double* faceBz) {
   Handle3* h = static_cast<Handle3*>(handle);
   if (!h || (which != 0 && which != 1)) return MHD_ERR_ARG;
   if (!h->have_state) return MHD_ERR_STATE;
@@ -280,17 +303,28 @@ int mhd3d_download(void* handle, int which, double* prim, double* cons) {
   const size_t cb = (size_t)h->nvars * mhdk::cells3(h->g) * sizeof(double);
   if (prim) CK3(cudaMemcpyAsync(prim, s.prim, cb, cudaMemcpyDeviceToHost, h->stream));
   if (cons) CK3(cudaMemcpyAsync(cons, s.cons, cb, cudaMemcpyDeviceToHost, h->stream));
+  double* fb[3] = {faceBx, faceBy, faceBz};
+  if (h->g.physics == MHD2D_MHD)
+    for (int d = 0; d < 3; ++d)
+      if (fb[d])
+        CK3(cudaMemcpyAsync(fb[d], s.fb[d], mhdk::plane3(h->g, d, 1) * sizeof(double), cudaMemcpyDeviceToHost,
+                            h->stream));
   CK3(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
 
-int mhd3d_state_ptrs(void* handle, int which, double** prim, double** cons) {
+int mhd3d_state_ptrs(void* handle, int which, double** prim, double** cons, double** faceBx, double** faceBy,
+                     double** faceBz) {
   Handle3* h = static_cast<Handle3*>(handle);
   if (!h || (which != 0 && which != 1)) return MHD_ERR_ARG;
   int b = h->cur;
   if (which == 1 && h->last_cycles_run > 0) b ^= 1;
-  if (prim) *prim = h->g.st[b].prim;
-  if (cons) *cons = h->g.st[b].cons;
+  const mhdk::StateBuf3& s = h->g.st[b];
+  if (prim) *prim = s.prim;
+  if (cons) *cons = s.cons;
+  if (faceBx) *faceBx = s.fb[0];
+  if (faceBy) *faceBy = s.fb[1];
+  if (faceBz) *faceBz = s.fb[2];
   return MHD_OK;
 }
 

@@ -42,18 +42,20 @@ __device__ __forceinline__ int wrapc(int c, int L, int bc) {
 // ----------------------------------------------------------------------------
 // Sweep policies
 // ----------------------------------------------------------------------------
+// Sweep vectors [rho, v, B_t1, B_t2, p] in the frame (n, t1, t2): x (vx, vy, vz) with
+// (By, Bz), y (vy, vz, vx) with (Bz, Bx), z (vz, vx, vy) with (Bx, By) -- the z frame
+// serves the 3D step.
 template <int AX>
 struct MhdSweep {
   static constexpr int NV = 7;
   static constexpr int NW = kPrimEigWords;
-  static constexpr int N = AX == 0 ? 1 : 2;
-  static constexpr int T1 = AX == 0 ? 2 : 3;
-  static constexpr int T2 = AX == 0 ? 3 : 1;
-  static constexpr int BN = AX == 0 ? 4 : 5;   // prim8 slot of the cell normal B
-  static constexpr int SB = AX == 0 ? 4 : 5;   // sweep slot that gets the B source term
+  static constexpr int N = AX + 1;
+  static constexpr int T1 = AX == 0 ? 2 : (AX == 1 ? 3 : 1);
+  static constexpr int T2 = AX == 0 ? 3 : (AX == 1 ? 1 : 2);
+  static constexpr int BN = 4 + AX;            // prim8 slot of the cell normal B
+  static constexpr int SB = AX == 0 ? 4 : 5;   // 2D: sweep slot that gets the B source term
   __device__ static constexpr int src(int k) {
-    return AX == 0 ? (k < 4 ? k : (k == 4 ? 5 : (k == 5 ? 6 : 7)))
-                   : (k < 4 ? k : (k == 4 ? 6 : (k == 5 ? 4 : 7)));
+    return k < 4 ? k : (k == 6 ? 7 : 3 + (k == 4 ? T1 : T2));
   }
   __device__ static constexpr int ord(int k) {
     return k == 0 ? 0 : k == 1 ? N : k == 2 ? T1 : k == 3 ? T2 : k == 4 ? 6 : k == 5 ? 4 : 5;

@@ -46,19 +46,23 @@ template <class S, int D>
 struct Line3 {
   size_t base, cs, plane;
   int L, bc;
-  __device__ Line3(const Grid3& G, const int* c) {
+  __device__ Line3(const Grid3& G, const int* c, int bc_line = -1) {
     int c0[3] = {c[0], c[1], c[2]};
     c0[D] = 0;
     base = lin3<D, 0>(G, c0);
     cs = stride3<D, 0, D>(G);
     plane = cells3(G);
     L = G.n[D];
-    bc = G.bc[D];
+    bc = bc_line >= 0 ? bc_line : G.bc[D];
   }
   __device__ void load(const double* prim, int cell, double* w) const {
     const size_t idx = base + (size_t)wrapc(cell, L, bc) * cs;
 #pragma unroll
     for (int k = 0; k < S::NV; ++k) w[k] = __ldg(prim + S::src(k) * plane + idx);
+  }
+  // one plane's value at cell `cell` of the line
+  __device__ double at(const double* a, int slot, int cell) const {
+    return __ldg(a + (size_t)slot * plane + base + (size_t)wrapc(cell, L, bc) * cs);
   }
 };
 
@@ -80,8 +84,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k3_slopes(Grid3 G, StateBu
   ln.load(in.prim, cc - 1, wl);
   ln.load(in.prim, cc, wc);
   ln.load(in.prim, cc + 1, wr);
+  double bn = 0.0;
+  if (S::BN >= 0) bn = ln.at(in.prim, S::BN >= 0 ? S::BN : 0, cc);
   typename S::Eig e;
-  S::eig(wc, 0.0, G.gamma, e);
+  S::eig(wc, bn, G.gamma, e);
   double ps[NV];
   limited_slopes<S>(wl, wc, wr, e, ps);
   const size_t es = G.ext_plane;
@@ -333,7 +339,13 @@ void enqueue_recon3(const Grid3& g, const StateBuf3& in, cudaStream_t s) {
   else k3_faces<S, D, 0><<<grid3(cells3(g)), kBlock, 0, s>>>(g, in);
 }
 
+void enqueue_cycle3_mhd(const Grid3& g, int parity, int dt_blocks, cudaStream_t s);
+
 void enqueue_cycle3(const Grid3& g, int parity, int dt_blocks, cudaStream_t s) {
+  if (g.physics == MHD) {
+    enqueue_cycle3_mhd(g, parity, dt_blocks, s);
+    return;
+  }
   const StateBuf3 in = g.st[parity];
   const StateBuf3 out = g.st[parity ^ 1];
   k3_dt_reduce_hydro<<<dt_blocks, 256, 0, s>>>(g, in);

@@ -23,7 +23,7 @@ struct Grid3 {
   int n[3];          // cells along x, y, z
   double d[3];       // dx, dy, dz
   int bc[3];         // OUTFLOW / PERIODIC per direction
-  int physics;       // HYDRO (MHD is not built in 3D)
+  int physics;       // HYDRO / MHD
   int recon;         // 0 first order, 1 PLM, 2 PPM
   int efix;
   double gamma, eps, min_d, min_p, min_e;
@@ -37,11 +37,18 @@ struct Grid3 {
   size_t ext_plane;  // plane stride of slopes / eig (largest extended grid)
   LoopState* loop;
   int* status;
+  // MHD only
+  double* ul[3];     // 7 planes of face cons states per direction, minus side
+  double* ur[3];     // plus side
+  double* emf[3];    // edge EMF components (x, y, z) on the (ny+1)(nx+1)(nz+1) edge grid
+  double* nfb[3];    // half-step face B
+  double* ce[3];     // cell E field: stage 1, then the half step
 };
 
 // extent of an array along direction a (0 x, 1 y, 2 z) that is `add` cells larger along `dir`
 MHD_HD inline int ext_n(const Grid3& g, int a, int dir, int add) { return g.n[a] + (a == dir ? add : 0); }
 MHD_HD inline size_t cells3(const Grid3& g) { return (size_t)g.n[0] * g.n[1] * g.n[2]; }
+MHD_HD inline size_t edges3(const Grid3& g) { return (size_t)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1); }
 MHD_HD inline size_t plane3(const Grid3& g, int dir, int add) {
   return (size_t)ext_n(g, 0, dir, add) * ext_n(g, 1, dir, add) * ext_n(g, 2, dir, add);
 }

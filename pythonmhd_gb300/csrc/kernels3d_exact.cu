@@ -4,3 +4,4 @@
 #define MHD_BODIES_ONLY
 #include "godunov2d_kernels.cuh"
 #include "godunov3d_kernels.cuh"
+#include "godunov3d_mhd.cuh"

@@ -25,14 +25,14 @@ TARGETS = (
     ("Source.EvolveFunctions_MHD", "evolve_1D_mhd", evolve.evolve_1D_mhd),
     ("Source.EvolveFunctions_Hydro", "evolve_1D_hydro", evolve.evolve_1D_hydro),
     ("Source.EvolveFunctions_Hydro", "evolve_3D_hydro", evolve.evolve_3D_hydro),
+    ("Source.EvolveFunctions_MHD", "evolve_3D_mhd", evolve.evolve_3D_mhd),
 )
 
 _saved: dict = {}
 
 
 def install(arith: str | None = None):
-    """Replace the reference's 1D and 2D evolve functions and its 3D hydro evolve
-    function; returns the patched modules.
+    """Replace the reference's 1D, 2D and 3D evolve functions; returns the patched modules.
 
     ``arith`` ("exact" or "fast") overrides PYTHONMHD_GB300_ARITH for these calls.
     """

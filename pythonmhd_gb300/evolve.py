@@ -19,7 +19,9 @@ Source/EvolveFunctions_Hydro.py:232-305) keep theirs too: the 1D MHD function
 returns new arrays with B_x made uniform; the 1D hydro function updates the
 grid's arrays in place and returns them.  ``evolve_3D_hydro``
 (Source/EvolveFunctions_Hydro.py:559-806) updates the grid's (5, ny, nx, nz)
-arrays in place and returns them, as the reference does.
+arrays in place and returns them, and ``evolve_3D_mhd``
+(Source/EvolveFunctions_MHD.py:750-1157) returns new prim/cons arrays and updates
+the three face-B arrays in place, as the reference does.
 
 The cycles run on the GPU (``Grid2D.advance``); the host uploads the grid once
 per call and downloads the result.  Handles are cached per grid geometry and
@@ -265,3 +267,57 @@ def evolve_3D_hydro(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, 
     np.copyto(prim, new_prim)
     np.copyto(cons, new_cons)
     return prim, cons, t, cyc, sl_prim, sl_cons, t_sl
+
+
+# ---------------------------------------------------------------------------
+# 3D MHD (Source/EvolveFunctions_MHD.py:750-1157)
+# ---------------------------------------------------------------------------
+def evolve_3D_mhd(simulationGrid, tStart, tEnd, startCycle, maxCycles, gamma, cfl, minDens, minPres,
+                  minEnergy, reconstructOrder=0, entropyFix=True, epsilon=0.5, arith=None):
+    """evolve_3D_mhd: returns (prim, cons, faceBx, faceBy, faceBz, time, cycle,
+    secondLastPrim, secondLastCons, secondLastFaceBx, secondLastFaceBy,
+    secondLastFaceBz, secondLastTime); the face arrays are the grid's own, updated in
+    place, and prim/cons are new arrays (the grid's own when no cycle runs), as in
+    the reference.  Its entropy fix defaults to on, as the reference's does."""
+    prim = simulationGrid.primVars
+    bcx = simulationGrid.BcX
+    assert (bcx == OUTFLOW or bcx == PERIODIC)
+    bcy = simulationGrid.BcY
+    assert (bcy == OUTFLOW or bcy == PERIODIC)
+    bcz = simulationGrid.BcZ
+    assert (bcz == OUTFLOW or bcz == PERIODIC)
+    assert (len(prim.shape) == 4)
+    assert (prim.shape[0] == 8)
+    assert (prim.shape[1] > 0)
+    fbx = simulationGrid.faceBx
+    fby = simulationGrid.faceBy
+    fbz = simulationGrid.faceBz
+    cons = simulationGrid.consVars
+    assert (prim.shape == cons.shape)
+    dx = simulationGrid.dx
+    assert (dx > 0)
+    dy = simulationGrid.dy
+    assert (dy > 0)
+    dz = simulationGrid.dz
+    assert (dz > 0)
+    assert (tStart <= tEnd)
+    assert (startCycle >= 0)
+    ny, nx, nz = prim.shape[1:]
+    order = _order(reconstructOrder)
+    mode = arith or default_arith()
+    key = ("mhd3d", ny, nx, nz, float(dx), float(dy), float(dz), bcx, bcy, bcz, float(gamma), order,
+           bool(entropyFix), float(epsilon), float(minDens), float(minPres), float(minEnergy), mode)
+    g = _handle(key, lambda: Grid3D(ny, nx, nz, dx, dy, dz, bcx, bcy, bcz, gamma, recon=order,
+                                    entropy_fix=entropyFix, eps=epsilon, min_d=minDens, min_p=minPres,
+                                    min_e=minEnergy, arith=mode, mhd=True))
+    g.upload(prim, cons, fbx, fby, fbz)
+    t, cyc, t_sl = g.advance(tStart, tEnd, startCycle, maxCycles, cfl)
+    if g.last_cycles == 0:
+        return (prim, cons, fbx, fby, fbz, tStart, startCycle, np.copy(prim), np.copy(cons), np.copy(fbx),
+                np.copy(fby), np.copy(fbz), tStart)
+    new_prim, new_cons, nbx, nby, nbz = g.download(0)
+    sl = g.download(1)
+    np.copyto(fbx, nbx)
+    np.copyto(fby, nby)
+    np.copyto(fbz, nbz)
+    return (new_prim, new_cons, fbx, fby, fbz, t, cyc) + tuple(sl) + (t_sl,)

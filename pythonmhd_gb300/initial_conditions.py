@@ -315,3 +315,48 @@ def turbulence_hydro_3d(n, seed=1, gamma=1.4, kmax=16, mach=1.0, device="cuda"):
     e = p / (gamma - 1.0) + 0.5 * rho * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
     cons = torch.stack([rho, rho * v[0], rho * v[1], rho * v[2], e])
     return prim.contiguous(), cons.contiguous(), 1.0 / n
+
+
+def turbulence_mhd_3d(n, seed=1, gamma=5.0 / 3.0, kmax=16, mach=1.0, beta=1.0, device="cuda"):
+    """Seeded 3D MHD turbulence on the unit n^3 periodic box: density exp(0.1 g),
+    velocities with power ~ k^-2 up to ``kmax`` scaled to rms Mach ``mach``, uniform
+    pressure 1/gamma, and face B from the edge-centred vector potential of three
+    fields with power ~ k^-3 (div B = 0 to round-off), scaled to plasma beta ``beta``.
+    Returns (prim, cons, faceBx, faceBy, faceBz) float64 torch tensors on ``device``
+    in the reference's 3D layout, and the cell size."""
+    import torch
+    rng = np.random.default_rng(seed)
+    g = _gaussian_field_3d(rng, n, 2.0, 1.0, kmax, device)
+    g = g / g.std(unbiased=False)
+    v = [_gaussian_field_3d(rng, n, 2.0, 1.0, kmax, device) for _ in range(3)]
+    a = [_gaussian_field_3d(rng, n, 3.0, 1.0, kmax, device) for _ in range(3)]   # A_x, A_y, A_z on edges
+    d = 1.0 / n
+    rho = torch.exp(0.1 * g)
+    p = torch.full_like(rho, 1.0 / gamma)
+    vsq = v[0] * v[0] + v[1] * v[1] + v[2] * v[2]
+    scale = mach / torch.sqrt(torch.mean(vsq / (gamma * p / rho)))
+    v = [c * scale for c in v]
+
+    def up(t, dim):   # t[i+1] - t[i] along dim, periodic
+        return torch.roll(t, -1, dims=dim) - t
+
+    # arrays are (y, x, z): dims 0 y, 1 x, 2 z
+    bx = up(a[2], 0) / d - up(a[1], 2) / d
+    by = up(a[0], 2) / d - up(a[2], 1) / d
+    bz = up(a[1], 1) / d - up(a[0], 0) / d
+    cbx = 0.5 * (bx + torch.roll(bx, -1, dims=1))
+    cby = 0.5 * (by + torch.roll(by, -1, dims=0))
+    cbz = 0.5 * (bz + torch.roll(bz, -1, dims=2))
+    bscale = torch.sqrt(2.0 * (1.0 / gamma) / beta / torch.mean(cbx * cbx + cby * cby + cbz * cbz))
+    bx, by, bz = bx * bscale, by * bscale, bz * bscale
+    fbx = torch.cat([bx, bx[:, :1, :]], dim=1)
+    fby = torch.cat([by, by[:1, :, :]], dim=0)
+    fbz = torch.cat([bz, bz[:, :, :1]], dim=2)
+    cbx = 0.5 * (fbx[:, :-1, :] + fbx[:, 1:, :])
+    cby = 0.5 * (fby[:-1, :, :] + fby[1:, :, :])
+    cbz = 0.5 * (fbz[:, :, :-1] + fbz[:, :, 1:])
+    prim = torch.stack([rho, v[0], v[1], v[2], cbx, cby, cbz, p])
+    e = p / (gamma - 1.0) + 0.5 * rho * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    e = e + 0.5 * (cbx * cbx + cby * cby + cbz * cbz)
+    cons = torch.stack([rho, rho * v[0], rho * v[1], rho * v[2], cbx, cby, cbz, e])
+    return (prim.contiguous(), cons.contiguous(), fbx.contiguous(), fby.contiguous(), fbz.contiguous(), d)

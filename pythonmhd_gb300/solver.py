@@ -205,24 +205,25 @@ class Grid1D(Grid2D):
 
 
 class Grid3D:
-    """One ny x nx x nz hydro grid (the reference's evolve_3D_hydro step) on the GPU.
+    """One ny x nx x nz grid (the reference's evolve_3D_hydro / evolve_3D_mhd step) on the GPU.
 
-    States are (5, ny, nx, nz) with z fastest, the reference's layout.  The evolve
-    loop and the second-last state behave as in :class:`Grid2D`.
+    States are (nvars, ny, nx, nz) with z fastest, the reference's layout; MHD grids
+    also carry faceBx (ny, nx+1, nz), faceBy (ny+1, nx, nz) and faceBz (ny, nx, nz+1).
+    The evolve loop and the second-last state behave as in :class:`Grid2D`.
     """
 
     def __init__(self, ny, nx, nz, dx, dy, dz, bcx, bcy, bcz, gamma, recon=2, entropy_fix=False, eps=0.5,
-                 min_d=1e-12, min_p=1e-12, min_e=1e-12, arith=None):
+                 min_d=1e-12, min_p=1e-12, min_e=1e-12, arith=None, mhd=False):
         self.lib = _lib.load()
         self.ny, self.nx, self.nz = int(ny), int(nx), int(nz)
-        self.mhd = False
-        self.nvars = 5
+        self.mhd = bool(mhd)
+        self.nvars = 8 if self.mhd else 5
         self.arith = arith or default_arith()
         h = ctypes.c_void_p()
         _lib.check(self.lib.mhd3d_create(self.ny, self.nx, self.nz, float(dx), float(dy), float(dz), int(bcx),
-                                         int(bcy), int(bcz), float(gamma), 0, int(recon), 1 if entropy_fix else 0,
-                                         float(eps), float(min_d), float(min_p), float(min_e), ARITH[self.arith],
-                                         ctypes.byref(h)), "mhd3d_create")
+                                         int(bcy), int(bcz), float(gamma), 1 if self.mhd else 0, int(recon),
+                                         1 if entropy_fix else 0, float(eps), float(min_d), float(min_p),
+                                         float(min_e), ARITH[self.arith], ctypes.byref(h)), "mhd3d_create")
         self._h = h
         self.last_cycles = 0
 
@@ -240,32 +241,57 @@ class Grid3D:
     def cell_shape(self):
         return (self.nvars, self.ny, self.nx, self.nz)
 
-    def upload(self, prim, cons):
+    def face_shapes(self):
+        return ((self.ny, self.nx + 1, self.nz), (self.ny + 1, self.nx, self.nz), (self.ny, self.nx, self.nz + 1))
+
+    def _check_faces(self, fb, kind):
+        if not self.mhd:
+            return [None, None, None]
+        if fb is None or len(fb) != 3 or any(f is None for f in fb):
+            raise ValueError("MHD grids need faceBx, faceBy and faceBz")
+        for f, shape in zip(fb, self.face_shapes()):
+            if tuple(f.shape) != shape:
+                raise ValueError(f"face B arrays must have shapes {self.face_shapes()}")
+        return list(fb)
+
+    def upload(self, prim, cons, fbx=None, fby=None, fbz=None):
         prim, cons = _as_f64c(prim), _as_f64c(cons)
         if prim.shape != self.cell_shape() or cons.shape != self.cell_shape():
             raise ValueError(f"prim/cons must have shape {self.cell_shape()}, got {prim.shape}, {cons.shape}")
-        _lib.check(self.lib.mhd3d_upload(self._h, _ptr(prim), _ptr(cons)), "mhd3d_upload")
+        fb = self._check_faces(None if fbx is None else (fbx, fby, fbz), "host")
+        fb = [_as_f64c(f) if f is not None else None for f in fb]
+        _lib.check(self.lib.mhd3d_upload(self._h, _ptr(prim), _ptr(cons), *[_ptr(f) for f in fb]), "mhd3d_upload")
 
-    def upload_device(self, prim, cons):
+    def upload_device(self, prim, cons, fbx=None, fby=None, fbz=None):
         """Upload from contiguous float64 CUDA tensors of the handle's device (no host copy)."""
         import torch
+        fb = self._check_faces(None if fbx is None else (fbx, fby, fbz), "device")
+        for t in [prim, cons] + [f for f in fb if f is not None]:
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError("upload_device expects contiguous float64 CUDA tensors")
         for t in (prim, cons):
-            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()
-                    and tuple(t.shape) == self.cell_shape()):
-                raise ValueError(f"upload_device expects contiguous float64 CUDA tensors of shape {self.cell_shape()}")
+            if tuple(t.shape) != self.cell_shape():
+                raise ValueError(f"prim/cons must have shape {self.cell_shape()}")
         torch.cuda.current_stream(prim.device).synchronize()
-        _lib.check(self.lib.mhd3d_upload_device(self._h, ctypes.c_void_p(prim.data_ptr()),
-                                                ctypes.c_void_p(cons.data_ptr())), "mhd3d_upload_device")
+        ptrs = [ctypes.c_void_p(t.data_ptr()) if t is not None else None for t in [prim, cons] + fb]
+        _lib.check(self.lib.mhd3d_upload_device(self._h, *ptrs), "mhd3d_upload_device")
 
-    def download(self, which=0, prim=None, cons=None):
-        """(prim, cons) of the current (which=0) or second-last (which=1) state."""
+    def download(self, which=0, prim=None, cons=None, fbx=None, fby=None, fbz=None):
+        """(prim, cons) -- plus (faceBx, faceBy, faceBz) for MHD -- of the current
+        (which=0) or second-last (which=1) state."""
         prim = np.empty(self.cell_shape()) if prim is None else prim
         cons = np.empty(self.cell_shape()) if cons is None else cons
-        for a in (prim, cons):
-            if not (a.dtype == np.float64 and a.flags.c_contiguous and a.shape == self.cell_shape()):
-                raise ValueError("download targets must be C-contiguous float64 of the cell shape")
-        _lib.check(self.lib.mhd3d_download(self._h, int(which), _ptr(prim), _ptr(cons)), "mhd3d_download")
-        return prim, cons
+        fb = [fbx, fby, fbz]
+        if self.mhd:
+            fb = [np.empty(sh) if f is None else f for f, sh in zip(fb, self.face_shapes())]
+        for a in [prim, cons] + [f for f in fb if f is not None]:
+            if not (a.dtype == np.float64 and a.flags.c_contiguous):
+                raise ValueError("download targets must be C-contiguous float64")
+        if prim.shape != self.cell_shape() or cons.shape != self.cell_shape():
+            raise ValueError("download targets must have the cell shape")
+        _lib.check(self.lib.mhd3d_download(self._h, int(which), _ptr(prim), _ptr(cons), *[_ptr(f) for f in fb]),
+                   "mhd3d_download")
+        return (prim, cons, fb[0], fb[1], fb[2]) if self.mhd else (prim, cons)
 
     def advance(self, t0, t_end, cycle0, max_cycles, cfl):
         t = ctypes.c_double()
@@ -294,10 +320,10 @@ class Grid3D:
         return self._info()[2]
 
     def state_ptrs(self, which=0):
-        ptrs = [ctypes.c_void_p() for _ in range(2)]
+        ptrs = [ctypes.c_void_p() for _ in range(5)]
         _lib.check(self.lib.mhd3d_state_ptrs(self._h, int(which), *[ctypes.byref(p) for p in ptrs]),
                    "mhd3d_state_ptrs")
-        return [p.value for p in ptrs]
+        return [p.value for p in ptrs[:5 if self.mhd else 2]]
 
 
 class Batch2D:

@@ -107,7 +107,7 @@ def lib_run_rejects_null(h):
 def test_3d_entry_points_reject_bad_arguments(lib):
     h = ctypes.c_void_p()
     ok = [8, 8, 8, 0.1, 0.1, 0.1, 1, 1, 1, 1.4, 0, 2, 0, 0.5, 1e-12, 1e-12, 1e-12, 0]
-    bad = {0: 1, 2: 1, 5: 0.0, 8: 2, 10: 1, 11: 3, 17: 2}   # nz < 2, ny < 2, dz <= 0, BC, MHD, recon, arith
+    bad = {0: 1, 2: 1, 5: 0.0, 8: 2, 10: 2, 11: 3, 17: 2}   # ny < 2, nz < 2, dz <= 0, BC, physics, recon, arith
     for i, v in bad.items():
         args = list(ok)
         args[i] = v
@@ -118,6 +118,6 @@ def test_3d_entry_points_reject_bad_arguments(lib):
     t = ctypes.c_double()
     c = ctypes.c_longlong()
     assert lib.mhd3d_advance(None, 0.0, 1.0, 0, 1, 0.4, ctypes.byref(t), ctypes.byref(c), ctypes.byref(t)) == 1
-    assert lib.mhd3d_upload(None, None, None) == 1
-    assert lib.mhd3d_download(None, 0, None, None) == 1
+    assert lib.mhd3d_upload(None, None, None, None, None, None) == 1
+    assert lib.mhd3d_download(None, 0, None, None, None, None, None) == 1
     lib.mhd3d_destroy(None)

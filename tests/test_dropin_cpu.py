@@ -17,6 +17,7 @@ def _fake_source(monkeypatch):
     mhd.evolve_1D_mhd = lambda *a, **k: "reference-mhd-1d"
     hyd.evolve_1D_hydro = lambda *a, **k: "reference-hydro-1d"
     hyd.evolve_3D_hydro = lambda *a, **k: "reference-hydro-3d"
+    mhd.evolve_3D_mhd = lambda *a, **k: "reference-mhd-3d"
     monkeypatch.setitem(sys.modules, "Source", pkg)
     monkeypatch.setitem(sys.modules, "Source.EvolveFunctions_MHD", mhd)
     monkeypatch.setitem(sys.modules, "Source.EvolveFunctions_Hydro", hyd)
@@ -32,6 +33,7 @@ def test_install_and_uninstall(monkeypatch):
     assert mhd.evolve_1D_mhd is evolve.evolve_1D_mhd
     assert hyd.evolve_1D_hydro is evolve.evolve_1D_hydro
     assert hyd.evolve_3D_hydro is evolve.evolve_3D_hydro
+    assert mhd.evolve_3D_mhd is evolve.evolve_3D_mhd
     dropin.uninstall()
     assert mhd.evolve_2D_mhd is orig_m and hyd.evolve_2D_hydro is orig_h
     assert mhd.evolve_1D_mhd() == "reference-mhd-1d"
@@ -58,3 +60,7 @@ def test_evolve_keeps_reference_signature():
         assert sig["reconstructOrder"].default == 0
         assert sig["entropyFix"].default is False
         assert sig["epsilon"].default == 0.5
+    # the reference's evolve_3D_mhd turns its entropy fix on by default
+    params = list(inspect.signature(evolve.evolve_3D_mhd).parameters)
+    assert params[:len(ref)] == ref
+    assert inspect.signature(evolve.evolve_3D_mhd).parameters["entropyFix"].default is True

@@ -1,0 +1,125 @@
+"""The 3D MHD step (mhd3d_* with MHD2D_MHD, evolve.evolve_3D_mhd).
+
+* against the reference's own outputs (tests/golden/mhd3d_*.npz, made by running
+  evolve_3D_mhd) to 1e-12 relative per field: the reference computes the x
+  predictor's y terms in long double, the CUDA step in FP64;
+* bit for bit against the oracle's restatement with the FP64 predictor, on the
+  fixtures' inputs and on larger runs, for every boundary combination (also those
+  where the reference raises);
+* at full size through properties: div B stays at round-off, mass and energy are
+  conserved on a periodic box.
+"""
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from oracle import mhd3d
+from pythonmhd_gb300 import evolve
+from pythonmhd_gb300.solver import Grid3D
+from tests.golden import cases
+from tests.golden_io import case_id, golden_files, load
+
+pytestmark = pytest.mark.gpu
+KEYS = ("prim", "cons", "fbx", "fby", "fbz", "t", "cycle", "sl_prim", "sl_cons", "sl_fbx", "sl_fby", "sl_fbz", "sl_t")
+
+
+def _grid(i, p):
+    ny, nx, nz = i["prim"].shape[1:]
+    return SimpleNamespace(primVars=i["prim"].copy(), consVars=i["cons"].copy(), faceBx=i["fbx"].copy(),
+                           faceBy=i["fby"].copy(), faceBz=i["fbz"].copy(), dx=p["dx"], dy=p["dy"], dz=p["dz"],
+                           BcX=p["bcx"], BcY=p["bcy"], BcZ=p["bcz"], numXCells=nx, numYCells=ny, numZCells=nz)
+
+
+def _args(p):
+    return (p["t_start"], p["t_end"], p["start_cycle"], p["max_cycles"], p["gamma"], p["cfl"], p["min_d"],
+            p["min_p"], p["min_e"], p["order"], p["efix"], p["eps"])
+
+
+def _close(a, b, rel):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    if a.ndim == 0:
+        return abs(float(a) - float(b)) <= rel * max(abs(float(b)), 1e-300)
+    fields = a.reshape(a.shape[0], -1) if a.ndim == 4 else a.reshape(1, -1)
+    want = b.reshape(fields.shape)
+    for f, w in zip(fields, want):
+        if float(np.max(np.abs(f - w))) > rel * max(float(np.max(np.abs(w))), 1e-300):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("path", golden_files("mhd3d"), ids=case_id)
+def test_3d_mhd_vs_reference(path):
+    p, i, o = load(path)
+    grid = _grid(i, p)
+    got = evolve.evolve_3D_mhd(grid, *_args(p), arith="exact")
+    for k, v in zip(KEYS, got):
+        if k == "cycle":
+            assert v == o[k]
+        else:
+            assert _close(v, o[k], 1e-12), k
+    # the reference's aliasing: the grid's face arrays are updated and returned
+    assert got[2] is grid.faceBx and got[3] is grid.faceBy and got[4] is grid.faceBz
+
+
+@pytest.mark.parametrize("path", golden_files("mhd3d"), ids=case_id)
+def test_3d_mhd_bitwise_vs_oracle_fp64_predictor(path):
+    p, i, o = load(path)
+    got = evolve.evolve_3D_mhd(_grid(i, p), *_args(p), arith="exact")
+    want = mhd3d.evolve(i["prim"], i["cons"], i["fbx"], i["fby"], i["fbz"], p["dx"], p["dy"], p["dz"], p["bcx"],
+                        p["bcy"], p["bcz"], *_args(p), long_double=False)
+    for k, a, b in zip(KEYS, got, want):
+        assert np.array_equal(np.asarray(a), np.asarray(b)), k
+
+
+@pytest.mark.parametrize("shape,bcs,order,efix", [((10, 12, 8), (1, 1, 1), 2, True), ((9, 9, 9), (0, 0, 0), 2, False),
+                                                  ((8, 10, 12), (0, 1, 0), 2, True), ((8, 8, 8), (1, 0, 1), 0, True),
+                                                  ((7, 9, 6), (0, 0, 1), 0, False), ((8, 8, 8), (1, 1, 1), 1, True)])
+def test_3d_mhd_runs_bitwise_vs_oracle(shape, bcs, order, efix):
+    """Several cycles on boxes the reference cannot run (non-cubic with outflow, PLM)."""
+    prim, cons, fbx, fby, fbz, dx, dy, dz = cases._random_mhd_3d(*shape, seed=41)
+    args = (0.0, 10.0, 0, 5, 5.0 / 3.0, 0.4, 1e-12, 1e-12, 1e-12, order, efix, 0.5)
+    grid = SimpleNamespace(primVars=prim.copy(), consVars=cons.copy(), faceBx=fbx.copy(), faceBy=fby.copy(),
+                           faceBz=fbz.copy(), dx=dx, dy=dy, dz=dz, BcX=bcs[0], BcY=bcs[1], BcZ=bcs[2])
+    oargs = args[:9] + ((evolve.PLM if order == 1 else order),) + args[10:]
+    got = evolve.evolve_3D_mhd(grid, *oargs, arith="exact")
+    want = mhd3d.evolve(prim, cons, fbx, fby, fbz, dx, dy, dz, *bcs, *args, long_double=False)
+    assert got[6] == 5
+    for k, a, b in zip(KEYS, got, want):
+        assert np.array_equal(np.asarray(a), np.asarray(b)), k
+
+
+def test_3d_mhd_fast_arith_close_to_reference():
+    for path in golden_files("mhd3d"):
+        p, i, o = load(path)
+        got = evolve.evolve_3D_mhd(_grid(i, p), *_args(p), arith="fast")
+        for k in ("prim", "cons", "fbx", "fby", "fbz"):
+            assert _close(got[KEYS.index(k)], o[k], 1e-11), (case_id(path), k)
+
+
+def _div_b(fbx, fby, fbz, dx, dy, dz):
+    return ((fbx[:, 1:, :] - fbx[:, :-1, :]) / dx + (fby[1:, :, :] - fby[:-1, :, :]) / dy
+            + (fbz[:, :, 1:] - fbz[:, :, :-1]) / dz)
+
+
+def test_3d_mhd_div_b_and_conservation_at_size():
+    n = 64
+    prim, cons, fbx, fby, fbz, dx, dy, dz = cases._random_mhd_3d(n, n, n, seed=42)
+    g = Grid3D(n, n, n, dx, dy, dz, 1, 1, 1, 5.0 / 3.0, recon=2, entropy_fix=True, arith="exact", mhd=True)
+    # periodic faces: the last face of each direction equals the first
+    fbx[:, -1, :] = fbx[:, 0, :]
+    fby[-1, :, :] = fby[0, :, :]
+    fbz[:, :, -1] = fbz[:, :, 0]
+    div0 = _div_b(fbx, fby, fbz, dx, dy, dz)
+    bscale = max(float(np.max(np.abs(a))) for a in (fbx, fby, fbz)) / dx
+    g.upload(prim, cons, fbx, fby, fbz)
+    g.advance(0.0, 10.0, 0, 20, 0.4)
+    assert g.last_cycles == 20
+    p2, c2, bx2, by2, bz2 = g.download(0)
+    g.close()
+    assert np.isfinite(c2).all()
+    div1 = _div_b(bx2, by2, bz2, dx, dy, dz)
+    assert float(np.max(np.abs(div1 - div0))) <= 1e-12 * bscale
+    for k in (0, 7):
+        scale = float(np.sum(np.abs(cons[k])))
+        assert abs(float(np.sum(c2[k])) - float(np.sum(cons[k]))) <= 1e-12 * scale, k
