@@ -85,3 +85,18 @@ def run3d(prim, cons, dx, dy, dz, bcx, bcy, bcz, t_lim, max_cycles, gamma, cfl, 
         return (p2, c2), t2, cyc2, (psl, csl), tsl
 
     return _drive((prim.copy(), cons.copy()), evolve, t_lim, max_cycles, save_dt, save_prec, plot_dt, plot_prec)
+
+
+def run3d_mhd(prim, cons, fbx, fby, fbz, dx, dy, dz, bcx, bcy, bcz, t_lim, max_cycles, gamma, cfl, min_d, min_p,
+              min_e, order, efix, eps, save_dt=-1.0, save_prec=0, plot_dt=-1.0, plot_prec=0, long_double=True):
+    """The same loop around the 3D MHD evolve function (oracle/mhd3d.py); ``long_double``
+    is passed through to its transverse predictor."""
+    from . import mhd3d
+
+    def evolve(st, t0, t_end, cyc0):
+        r = mhd3d.evolve(*st, dx, dy, dz, bcx, bcy, bcz, t0, t_end, cyc0, max_cycles, gamma, cfl, min_d, min_p,
+                         min_e, order, efix, eps, long_double=long_double)
+        return tuple(r[:5]), r[5], r[6], tuple(r[7:12]), r[12]
+
+    state = tuple(a.copy() for a in (prim, cons, fbx, fby, fbz))
+    return _drive(state, evolve, t_lim, max_cycles, save_dt, save_prec, plot_dt, plot_prec)

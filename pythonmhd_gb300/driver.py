@@ -79,12 +79,15 @@ def run(grid, t_lim, max_cycles, cfl, save_dt=-1.0, save_prec=None, plot_dt=-1.0
     return t.value, c.value, n.value
 
 
-def save_mat(path, prim, cons, fbx=None, fby=None):
-    """A stop's state in the reference's .mat layout, plus faceBx/faceBy for MHD."""
+def save_mat(path, prim, cons, fbx=None, fby=None, fbz=None):
+    """A stop's state in the reference's .mat layout, plus faceBx/faceBy (and faceBz
+    for a 3D grid) for MHD."""
     import scipy.io
     if prim.shape[0] == 8:
         d = {"density": prim[0], "vx": prim[1], "vy": prim[2], "vz": prim[3], "Bx": prim[4], "By": prim[5],
              "Bz": prim[6], "pressure": prim[7], "energy": cons[7], "faceBx": fbx, "faceBy": fby}
+        if fbz is not None:
+            d["faceBz"] = fbz
     else:
         d = {"density": prim[0], "vx": prim[1], "vy": prim[2], "vz": prim[3], "pressure": prim[4],
              "energy": cons[4]}

@@ -119,3 +119,34 @@ def test_3d_driver_matches_oracle_driver(t_lim, save_dt, plot_dt, order):
             assert np.array_equal(a, b)
     for a, b in zip(final, final_w):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("t_lim,save_dt,plot_dt,order", [(0.04, 0.01, 0.0075, 2), (0.03, -1.0, 0.005, 1)])
+def test_3d_mhd_driver_matches_oracle_driver(t_lim, save_dt, plot_dt, order):
+    """mhd3d_run on a 3D MHD grid against the oracle's driver around its 3D MHD step
+    (FP64 predictor, as the CUDA step computes it)."""
+    from pythonmhd_gb300.solver import Grid3D
+    from tests.golden import cases
+    ny, nx, nz = 8, 10, 6
+    prim, cons, fbx, fby, fbz, dx, dy, dz = cases._random_mhd_3d(ny, nx, nz, seed=7)
+    sp = driver.time_precision(save_dt, t_lim) if save_dt > 0 else 0
+    pp = driver.time_precision(plot_dt, t_lim) if plot_dt > 0 else 0
+    args = (dx, dy, dz, 1, 0, 1, t_lim, 1000, 5.0 / 3.0, 0.4, 1e-12, 1e-12, 1e-12, order, True, 0.5)
+    t_w, cyc_w, stops_w, final_w = odriver.run3d_mhd(prim, cons, fbx, fby, fbz, *args, save_dt=save_dt,
+                                                     save_prec=sp, plot_dt=plot_dt, plot_prec=pp,
+                                                     long_double=False)
+    got = []
+    g = Grid3D(ny, nx, nz, dx, dy, dz, 1, 0, 1, 5.0 / 3.0, recon=order, entropy_fix=True, arith="exact", mhd=True)
+    g.upload(prim, cons, fbx, fby, fbz)
+    t, cyc, n = driver.run(g, t_lim, 1000, 0.4, save_dt=save_dt, plot_dt=plot_dt,
+                           on_stop=lambda t, c, k, grid: got.append((t, c, k, grid.download())))
+    final = g.download()
+    g.close()
+    assert (t, cyc) == (t_w, cyc_w) and cyc > 3
+    assert len(got) == len(stops_w) and n == len(stops_w) - 1
+    for (tg, cg, kg, sg), (tw, cw, kw, sw) in zip(got, stops_w):
+        assert (tg, cg, kg) == (tw, cw, kw)
+        for a, b in zip(sg, sw):
+            assert np.array_equal(a, b)
+    for a, b in zip(final, final_w):
+        assert np.array_equal(a, b)
