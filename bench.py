@@ -72,6 +72,24 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(values, device):
+    """Each of ``values`` maxed over the ranks of the default process group (the
+    values themselves when no group is up or it has one rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    tt = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return tt.tolist()
+
+
+def replica_throughput(world, units_per_rank, ms_per_step):
+    """Whole-job units/s of ``world`` replicas that each process ``units_per_rank``
+    units per step, timed by the slowest rank's ``ms_per_step``."""
+    return world * units_per_rank / (ms_per_step * 1e-3)
+
+
 # ----------------------------------------------------------------------------
 # CPU legs (oracle = CPU restatement of the reference algorithm)
 # ----------------------------------------------------------------------------
@@ -526,14 +544,10 @@ def run_ours(a):
     # max over ranks
     ms_per = ms_total / a.steps
     ms_e2e_per = ms_e2e / e2e_steps
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms_per, ms_e2e_per], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_per, ms_e2e_per = tt.tolist()
+    ms_per, ms_e2e_per = max_over_ranks([ms_per, ms_e2e_per], dev)
     zones = n * n
-    value = world * zones / (ms_per * 1e-3)
-    e2e_value = world * zones / (ms_e2e_per * 1e-3)
+    value = replica_throughput(world, zones, ms_per)
+    e2e_value = replica_throughput(world, zones, ms_e2e_per)
 
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs")
