@@ -536,6 +536,16 @@ def run_ours(a):
     e3.record(stream)
     e3.synchronize()
     ms_e2e = e2.elapsed_time(e3)
+    # the copies alone, after the e2e loop: the link rate that e2e pays on this host
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(stream)
+    g.upload(hp, hc, hbx, hby)
+    ev[1].record(stream)
+    g.download(0, hp, hc, hbx, hby)
+    ev[2].record(stream)
+    ev[2].synchronize()
+    copy_gbs = {"h2d": h2d / (ev[0].elapsed_time(ev[1]) * 1e-3) / 1e9,
+                "d2h": d2h / (ev[1].elapsed_time(ev[2]) * 1e-3) / 1e9}
     clk = clocks.stop()
     dev_bytes = g.device_bytes()
     if not np.isfinite(hp).all():
@@ -603,7 +613,7 @@ def run_ours(a):
                        "arith": a.arith, "cells": zones, "l2": "state 2.4 GB >> 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": e2e_steps, "ms_per_step": ms_e2e_per},
+                    "steps": e2e_steps, "ms_per_step": ms_e2e_per, "copy_gbs": copy_gbs},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "device_bytes": dev_bytes, "final_cycle": cyc, "final_time": t, "batched": batched,
             "adjoint": adjoint, "hydro3d": hydro_3d, "mhd3d": mhd_3d}
