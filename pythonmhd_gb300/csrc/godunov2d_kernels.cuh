@@ -166,7 +166,7 @@ __device__ __forceinline__ void limited_slopes(const double* wl, const double* w
     dc[k] = wr[k] - wl[k];
     dl[k] = wc[k] - wl[k];
     dr[k] = wr[k] - wc[k];
-    wt[k] = (dl[k] * dr[k] > 0.0) ? (2.0 * dl[k] * dr[k]) / (dl[k] + dr[k]) : 0.0;
+    wt[k] = is_pos(dl[k] * dr[k]) ? (2.0 * dl[k] * dr[k]) / (dl[k] + dr[k]) : 0.0;
   }
   double sc[NV];
 #pragma unroll
@@ -176,7 +176,7 @@ __device__ __forceinline__ void limited_slopes(const double* wl, const double* w
     const double cr = project<S>(e, i, dr);
     const double cw = project<S>(e, i, wt);
     double s = 0.0;
-    if (cl * cr > 0.0) {
+    if (is_pos(cl * cr)) {
       const double lim1 = dmin(fabs(cl), fabs(cr));
       const double lim2 = dmin(0.5 * fabs(cc), fabs(cw));
       s = signed_mag(cc, dmin(2.0 * lim1, lim2));
@@ -246,8 +246,8 @@ __device__ __forceinline__ void put_face(double* buf, size_t fplane, size_t fidx
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
     double x = v[k];
-    if (k == 0 && x < min_d) x = min_d;
-    if (k == NV - 1 && x < min_p) x = min_p;
+    if (k == 0 && dlt(x, min_d)) x = min_d;
+    if (k == NV - 1 && dlt(x, min_p)) x = min_p;
     if (k == S::SB && add_src) x = x + bsrc;
     buf[k * fplane + fidx] = x;
   }
@@ -311,7 +311,7 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
     for (int side = 0; side < 2; ++side) {
 #pragma unroll
       for (int i = 0; i < NV; ++i) {
-        if (side == 0 ? lam[i] <= 0.0 : lam[i] >= 0.0) {
+        if (side == 0 ? is_nonpos(lam[i]) : is_nonneg(lam[i])) {
           const double v3 = 0.5 * dtdx * lam[side == 0 ? 0 : NV - 1] - 0.5 * dtdx * lam[i];
           double fac = 0.0;
           bool first = true;
@@ -342,12 +342,12 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
       const double dprod = (b - wc[k]) * (wc[k] - a);
       const double idiff = b - a;
       const double adiff = 6.0 * (wc[k] - 0.5 * (a + b));
-      if (dprod <= 0.0) {
+      if (is_nonpos(dprod)) {
         a = wc[k];
         b = wc[k];
-      } else if ((idiff * adiff) > sq(idiff)) {
+      } else if (dgt(idiff * adiff, sq(idiff))) {
         a = (6.0 * wc[k] - 4.0 * b) / 2.0;
-      } else if ((idiff * adiff) < (-1.0 * sq(idiff))) {
+      } else if (dlt(idiff * adiff, -1.0 * sq(idiff))) {
         b = (6.0 * wc[k] - 4.0 * a) / 2.0;
       }
       a = dmax(dmin(wc[k], wl[k]), a);
@@ -376,7 +376,7 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
     }
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-      if (lam[i] <= 0.0) {
+      if (is_nonpos(lam[i])) {
         const double v1 = 0.5 * dtdx * lam[0];
         const double v2 = 0.5 * dtdx * lam[i];
         const double v3 = v1 - v2;
@@ -399,7 +399,7 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
     }
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-      if (lam[i] >= 0.0) {
+      if (is_nonneg(lam[i])) {
         const double v1 = 0.5 * dtdx * lam[NV - 1];
         const double v2 = 0.5 * dtdx * lam[i];
         const double v3 = v1 - v2;
@@ -594,18 +594,18 @@ __device__ __forceinline__ void b_emf(const Grid& G, const StateBuf& in, int I, 
   const double eu = cell_ez<STAGE>(G, in, jm, ic);
   const double eul = cell_ez<STAGE>(G, in, jm, im);
   double x1 = 0.0, x2 = 0.0, y1 = 0.0, y2 = 0.0;
-  if (lt0 > 0.0) x1 = lt5 - ul4 - eul;
-  else if (lt0 < 0.0) x1 = lt5 - l4 - el;
-  else if (lt0 == 0.0) x1 = lt5 - 0.5 * (l4 + ul4 + el + eul);
-  if (top0 > 0.0) x2 = top5 - ul4 - eu;
-  else if (top0 < 0.0) x2 = top5 - l4 - ec;
-  else if (top0 == 0.0) x2 = top5 - 0.5 * (l4 + ul4 + ec + eu);
-  if (ul0 > 0.0) y1 = -ul4 + lt5 - eul;
-  else if (ul0 < 0.0) y1 = -ul4 + top5 - eu;
-  else if (ul0 == 0.0) y1 = -ul4 + 0.5 * (lt5 + top5 - eul - eu);
-  if (l0 > 0.0) y2 = -l4 + lt5 - el;
-  else if (l0 < 0.0) y2 = -l4 + top5 - ec;
-  else if (l0 == 0.0) y2 = -l4 + 0.5 * (lt5 + top5 - el - ec);
+  if (is_pos(lt0)) x1 = lt5 - ul4 - eul;
+  else if (is_neg(lt0)) x1 = lt5 - l4 - el;
+  else if (is_zero(lt0)) x1 = lt5 - 0.5 * (l4 + ul4 + el + eul);
+  if (is_pos(top0)) x2 = top5 - ul4 - eu;
+  else if (is_neg(top0)) x2 = top5 - l4 - ec;
+  else if (is_zero(top0)) x2 = top5 - 0.5 * (l4 + ul4 + ec + eu);
+  if (is_pos(ul0)) y1 = -ul4 + lt5 - eul;
+  else if (is_neg(ul0)) y1 = -ul4 + top5 - eu;
+  else if (is_zero(ul0)) y1 = -ul4 + 0.5 * (lt5 + top5 - eul - eu);
+  if (is_pos(l0)) y2 = -l4 + lt5 - el;
+  else if (is_neg(l0)) y2 = -l4 + top5 - ec;
+  else if (is_zero(l0)) y2 = -l4 + 0.5 * (lt5 + top5 - el - ec);
   G.emf[(size_t)J * (nx + 1) + I] = 0.25 * (x1 + x2 + y1 + y2);
 }
 
@@ -719,8 +719,8 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
                                    : (-half_dtdt * (fh[k] - flo[k]) + half_dt * src[k]);
       u[k] = u[k] + corr;
     }
-    if (u[0] < G.min_d) u[0] = G.min_d;
-    if (u[6] < G.min_e) u[6] = G.min_e;
+    if (dlt(u[0], G.min_d)) u[0] = G.min_d;
+    if (dlt(u[6], G.min_e)) u[6] = G.min_e;
     double w2[7];
     cons_to_prim7(u, nb, G.gamma, w2);
 #pragma unroll

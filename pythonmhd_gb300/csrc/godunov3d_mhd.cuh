@@ -134,14 +134,14 @@ __global__ void k3m_begin(Grid3 G) {
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ double b3_limit(double nch, double tch, bool zero_when_t_zero) {
   double r = 0.0;
-  if (nch >= 0.0) {
-    if (nch < -tch) r = nch;
-    else r = (zero_when_t_zero && tch == 0.0) ? 0.0 : -tch;
-    if (r < 0.0) r = 0.0;
+  if (is_nonneg(nch)) {
+    if (dlt(nch, -tch)) r = nch;
+    else r = (zero_when_t_zero && is_zero(tch)) ? 0.0 : -tch;
+    if (is_neg(r)) r = 0.0;
   } else {
-    if (nch > -tch) r = nch;
-    else r = (zero_when_t_zero && tch == 0.0) ? 0.0 : -tch;
-    if (r > 0.0) r = 0.0;
+    if (dgt(nch, -tch)) r = nch;
+    else r = (zero_when_t_zero && is_zero(tch)) ? 0.0 : -tch;
+    if (is_pos(r)) r = 0.0;
   }
   return r;
 }
@@ -252,8 +252,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k3m_faces(Grid3 G, StateBu
     double w[7], u[7];
 #pragma unroll
     for (int k = 0; k < 7; ++k) w[k] = v[k];
-    if (w[0] < G.min_d) w[0] = G.min_d;
-    if (w[6] < G.min_p) w[6] = G.min_p;
+    if (dlt(w[0], G.min_d)) w[0] = G.min_d;
+    if (dlt(w[6], G.min_p)) w[6] = G.min_p;
     w[4] = w[4] + cr[0];
     w[5] = w[5] + cr[1];
     p2c_frame<S::N, S::T1, S::T2>(w, in.fb[D][fi], G.gamma, u);
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(kBlock) k3m_cell_e(Grid3 G, StateBuf3 in) {
 // direction (Source/CornerEMF_HelperModule.py:546-951)
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ double upwind3(double s, double pos, double neg, double zero) {
-  return s > 0.0 ? pos : (s < 0.0 ? neg : (s == 0.0 ? zero : 0.0));
+  return is_pos(s) ? pos : (is_neg(s) ? neg : (is_zero(s) ? zero : 0.0));
 }
 
 // slot k of the flux of direction A at point (x, y, z) of its face array
@@ -436,8 +436,8 @@ __global__ void __launch_bounds__(kBlock) k3m_ct(Grid3 G, StateBuf3 in, StateBuf
 // back to prims with the half-step face B.
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ double minmod3(double nch, double tch) {
-  if (nch > 0.0 && tch < 0.0) return tch > -nch ? tch : -nch;
-  if (nch < 0.0 && tch > 0.0) return tch < -nch ? tch : -nch;
+  if (is_pos(nch) && is_neg(tch)) return dgt(tch, -nch) ? tch : -nch;
+  if (is_neg(nch) && is_pos(tch)) return dlt(tch, -nch) ? tch : -nch;
   return 0.0;
 }
 
@@ -464,7 +464,7 @@ __device__ __forceinline__ void ctu3m_step(const Grid3& G, const int* p, double 
   };
   const double delta = ((em(1, 0) - em(0, 0)) + em(1, 1)) - em(0, 1);
   const double upd = (half * 0.5) * delta;
-  u[slot] = sign > 0.0 ? u[slot] + upd : u[slot] - upd;
+  u[slot] = is_pos(sign) ? u[slot] + upd : u[slot] - upd;
 }
 
 template <int D>

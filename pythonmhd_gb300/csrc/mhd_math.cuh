@@ -22,15 +22,39 @@ constexpr double SMALL_VALUE = 0.000000000001;   // Source/PythonMHD_Constants.p
 constexpr double FOUR_THIRDS = 1.333333333333333;  // Source/PythonMHD_Constants.py:8 (truncated)
 
 __device__ __forceinline__ double sq(double x) { return x * x; }
+
+// ---------------------------------------------------------------------------
+// Comparisons on the IEEE-754 bit pattern.  An FP64 compare (DSETP, and the
+// select of an FP64 max/min) issues on the FP64 pipe at the DFMA rate, and that
+// pipe bounds every kernel of the step; the same test on the 64-bit pattern runs
+// on the integer pipe at about 7x the rate.  Each helper equals the IEEE
+// comparison for every non-NaN operand, zeros of either sign included.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+// order key: okey(a) < okey(b) <=> a < b for non-NaN a, b; +0 and -0 both map to 0
+__device__ __forceinline__ long long okey(double x) {
+  const long long b = dbits(x);
+  return b < 0 ? (-0x7fffffffffffffffLL - 1) - b : b;
+}
+__device__ __forceinline__ bool is_pos(double x) { return dbits(x) > 0; }       // x > 0
+__device__ __forceinline__ bool is_nonpos(double x) { return dbits(x) <= 0; }   // x <= 0
+__device__ __forceinline__ bool is_neg(double x) { return okey(x) < 0; }        // x < 0
+__device__ __forceinline__ bool is_nonneg(double x) { return okey(x) >= 0; }    // x >= 0
+__device__ __forceinline__ bool is_zero(double x) {                             // x == 0
+  return (static_cast<unsigned long long>(dbits(x)) << 1) == 0ULL;
+}
+__device__ __forceinline__ bool dgt(double a, double b) { return okey(a) > okey(b); }  // a > b
+__device__ __forceinline__ bool dlt(double a, double b) { return okey(a) < okey(b); }  // a < b
+
 // np.sign(x) with 0 -> 1 (Source/RiemannSolvers_MHD_Roe_HelperModule.py:286-287)
-__device__ __forceinline__ double sign_one(double x) { return x < 0.0 ? -1.0 : 1.0; }
+__device__ __forceinline__ double sign_one(double x) { return is_neg(x) ? -1.0 : 1.0; }
 // np.sign(x) * m for m >= 0 (0 for x == 0)
 __device__ __forceinline__ double signed_mag(double x, double m) {
-  return x > 0.0 ? m : (x < 0.0 ? -m : 0.0);
+  return is_pos(x) ? m : (is_neg(x) ? -m : 0.0);
 }
-// numpy maximum / minimum (no NaN handling needed on finite data)
-__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
-__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+// numpy maximum / minimum (a > b ? a : b, a < b ? a : b; finite data)
+__device__ __forceinline__ double dmax(double a, double b) { return dgt(a, b) ? a : b; }
+__device__ __forceinline__ double dmin(double a, double b) { return dlt(a, b) ? a : b; }
 
 // ---------------------------------------------------------------------------
 // Structural non-zero patterns of the eigenmatrices (row i, column j)
@@ -168,15 +192,15 @@ __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, d
   const double cs = sqrt(cs2);
 
   double b1 = 0.0, b2 = 0.0;
-  if (bt == 0.0) b1 = 1.0;
-  if (bt > 0.0) { b1 = w[4] / bt; b2 = w[5] / bt; }
+  if (is_zero(bt)) b1 = 1.0;
+  if (is_pos(bt)) { b1 = w[4] / bt; b2 = w[5] / bt; }
 
   double fa = 0.0, sa = 0.0;
-  if (ssqrt == 0.0) {
+  if (is_zero(ssqrt)) {
     fa = 1.0;
-  } else if ((a2 - cs2) <= 0.0) {
+  } else if (is_nonpos(a2 - cs2)) {
     sa = 1.0;
-  } else if ((cf2 - a2) <= 0.0) {
+  } else if (is_nonpos(cf2 - a2)) {
     fa = 1.0;
   } else {
     fa = sqrt((a2 - cs2) / ssqrt);
@@ -345,19 +369,19 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
       const double x = lam[k];
-      if (fabs(x) < 2.0 * eps && x != 0.0) {
+      if (dlt(fabs(x), 2.0 * eps) && !is_zero(x)) {
         const double corr = eps + sq(x) / (4.0 * eps);
-        lam[k] = x > 0.0 ? x + corr : x - corr;
+        lam[k] = is_pos(x) ? x + corr : x - corr;
       }
     }
   }
 
   double fa = 0.0, sa = 0.0;
-  if (cf2 - cs2 == 0.0) {
+  if (is_zero(cf2 - cs2)) {
     fa = 1.0;
-  } else if (a2 - cs2 <= 0.0) {
+  } else if (is_nonpos(a2 - cs2)) {
     sa = 1.0;
-  } else if (cf2 - a2 <= 0.0) {
+  } else if (is_nonpos(cf2 - a2)) {
     fa = 1.0;
   } else {
     fa = sqrt((a2 - cs2) / (cf2 - cs2));
@@ -372,8 +396,8 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   const double asp = a * sa * isrd;
 
   double bh1 = 0.0, bh2 = 0.0;
-  if (bt == 0.0) bh1 = 1.0;
-  if (bt > 0.0) { bh1 = b1 / bt; bh2 = b2 / bt; }
+  if (is_zero(bt)) bh1 = 1.0;
+  if (is_pos(bt)) { bh1 = b1 / bt; bh2 = b2 / bt; }
   const double den = sqrt((gamma - 1.0) - (gamma - 2.0) * rc);
   const double b1s = bh1 / den;
   const double b2s = bh2 / den;
@@ -474,12 +498,12 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   double fl[7], fr[7];
   cell_flux7<N, T1, T2>(wl, ul, bn, hbl, fl);
   cell_flux7<N, T1, T2>(wr, ur, bn, hbr, fr);
-  if (lam[6] <= 0.0) {
+  if (is_nonpos(lam[6])) {
 #pragma unroll
     for (int i = 0; i < 7; ++i) flux[i] = fr[i];
     return;
   }
-  if (lam[0] >= 0.0) {
+  if (is_nonneg(lam[0])) {
 #pragma unroll
     for (int i = 0; i < 7; ++i) flux[i] = fl[i];
     return;
@@ -641,9 +665,9 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const double x = lam[k];
-      if (fabs(x) < 2.0 * eps && x != 0.0) {
+      if (dlt(fabs(x), 2.0 * eps) && !is_zero(x)) {
         const double corr = eps + sq(x) / (4.0 * eps);
-        lam[k] = x > 0.0 ? x + corr : x - corr;
+        lam[k] = is_pos(x) ? x + corr : x - corr;
       }
     }
   }
@@ -654,12 +678,12 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
   fl[3] = ul[n] * wl[3]; fr[3] = ur[n] * wr[3];
   fl[n] = fl[n] + wl[4]; fr[n] = fr[n] + wr[4];
   fl[4] = (ul[4] + wl[4]) * wl[n]; fr[4] = (ur[4] + wr[4]) * wr[n];
-  if (lam[4] <= 0.0) {
+  if (is_nonpos(lam[4])) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) flux[i] = fr[i];
     return;
   }
-  if (lam[0] >= 0.0) {
+  if (is_nonneg(lam[0])) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) flux[i] = fl[i];
     return;
