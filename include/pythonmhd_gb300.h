@@ -227,7 +227,7 @@ int mhd2d_adj_forward(void* handle, const double* state_in, int steps, double cf
  * sweep, otherwise each cycle is recomputed again right before its reverse. */
 int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initial);
 /* Bytes the backward pass may hold to keep a whole segment resident
- * (0 = 60% of the free device memory at mhd2d_adj_forward time). */
+ * (0 = 85% of the free device memory at mhd2d_adj_forward time). */
 int mhd2d_adj_configure(void* handle, size_t segment_bytes);
 /* Re-target a handle to another grid with the same reconstruction, entropy fix
  * and floors (drops its forward record).  Device memory is reused while large

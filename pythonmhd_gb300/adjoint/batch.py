@@ -34,7 +34,7 @@ class BatchAdjoint:
 
     ``grids``: dicts with nx, ny, dx, dy, gamma and optionally bcx, bcy (default
     periodic).  ``recon`` 0, 1 or 2 (PPM).  ``budget`` bytes the backward pass may
-    use to keep a segment resident (0: 60% of free memory at that time).
+    use to keep a segment resident (0: 85% of free memory at that time).
     """
 
     def __init__(self, grids, recon=2, entropy_fix=False, eps=0.5, min_d=1e-12, min_p=1e-12, min_e=1e-12,

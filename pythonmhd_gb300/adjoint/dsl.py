@@ -224,6 +224,25 @@ def _reverse_needs(t, act):
 _PY_BIN = {"add": "+", "sub": "-", "mul": "*", "div": "/"}
 _C_RN = {"add": "__dadd_rn", "sub": "__dsub_rn", "mul": "__dmul_rn", "div": "__ddiv_rn"}
 _CMP = {"gt": ">", "ge": ">=", "lt": "<", "le": "<=", "eq": "=="}
+# CUDA comparisons on the IEEE bit pattern (``dsl_*`` in the emitted preamble): an FP64
+# compare issues on the FP64 pipe at the DFMA rate, the pattern test on the integer pipe;
+# both agree for every non-NaN operand, zeros of either sign included
+_C_CMP = {op: f"dsl_{op}" for op in _CMP}
+_C_PREAMBLE = (
+    "#ifndef MHD_DSL_NZ\n#define MHD_DSL_NZ\n"
+    "__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }\n"
+    "__device__ __forceinline__ long long dsl_key(double x) {\n"
+    "  const long long b = __double_as_longlong(x);\n"
+    "  return b < 0 ? (-0x7fffffffffffffffLL - 1) - b : b;\n"
+    "}\n"
+    "__device__ __forceinline__ bool dsl_gt(double a, double b) { return dsl_key(a) > dsl_key(b); }\n"
+    "__device__ __forceinline__ bool dsl_ge(double a, double b) { return dsl_key(a) >= dsl_key(b); }\n"
+    "__device__ __forceinline__ bool dsl_lt(double a, double b) { return dsl_key(a) < dsl_key(b); }\n"
+    "__device__ __forceinline__ bool dsl_le(double a, double b) { return dsl_key(a) <= dsl_key(b); }\n"
+    "__device__ __forceinline__ bool dsl_eq(double a, double b) { return dsl_key(a) == dsl_key(b); }\n"
+    "__device__ __forceinline__ bool dsl_pos(double x) { return __double_as_longlong(x) > 0; }\n"
+    "__device__ __forceinline__ bool dsl_nonneg(double x) { return dsl_key(x) >= 0; }\n"
+    "#endif")
 
 
 def _fwd_lines(t, live, lang):
@@ -255,7 +274,7 @@ def _fwd_lines(t, live, lang):
         elif op == "abs":
             L.append((v, f"np.abs({a[0]})" if lang == "py" else f"fabs({a[0]})", kind))
         elif op in _CMP:
-            L.append((v, f"{a[0]} {_CMP[op]} {a[1]}", kind))
+            L.append((v, f"{a[0]} {_CMP[op]} {a[1]}" if lang == "py" else f"{_C_CMP[op]}({a[0]}, {a[1]})", kind))
         elif op == "and":
             L.append((v, f"{a[0]} & {a[1]}" if lang == "py" else f"{a[0]} && {a[1]}", kind))
         elif op == "or":
@@ -332,9 +351,9 @@ def _rev_lines_c(t, act, first_of=None):
             acc(args[0], f"q{i}")
             acc(args[1], f"q{i} * v{i}", guard=f"g{i}", neg=True)
         elif op == "sqrt":
-            acc(args[0], f"(0.5 * {b}) / v{i}", guard=f"(nz({b}) && v{i} > 0.0)")
+            acc(args[0], f"(0.5 * {b}) / v{i}", guard=f"(nz({b}) && dsl_pos(v{i}))")
         elif op == "abs":
-            acc(args[0], f"(v{args[0]} >= 0.0 ? {b} : -{b})")
+            acc(args[0], f"(dsl_nonneg(v{args[0]}) ? {b} : -{b})")
         elif op == "sel":
             acc(args[1], f"(v{args[0]} ? {b} : 0.0)")
             acc(args[2], f"(v{args[0]} ? 0.0 : {b})")
@@ -381,7 +400,7 @@ def _rev_lines(t, act, lang):
             acc(args[0], where(f"v{i} > 0.0", f"({b} * 0.5) / v{i}"))
         elif op == "abs":
             acc(args[0], f"np.where(v{args[0]} >= 0.0, {b}, -{b})" if lang == "py"
-                else f"(v{args[0]} >= 0.0 ? {b} : -{b})")
+                else f"(dsl_nonneg(v{args[0]}) ? {b} : -{b})")
         elif op == "sel":
             acc(args[1], where(f"v{args[0]}", b))
             nc = f"~v{args[0]}" if lang == "py" else f"!v{args[0]}"
@@ -476,9 +495,7 @@ def emit_cuda(t, reverse=True):
     need_out = set(t.outputs)
     out = []
     live = _live_forward(t, need_out)
-    out.append("#ifndef MHD_DSL_NZ\n#define MHD_DSL_NZ\n"
-               "__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }\n"
-               "#endif")
+    out.append(_C_PREAMBLE)
     out.append(f"__device__ __forceinline__ void {t.name}_fwd(const double* __restrict__ x, "
                f"const double* __restrict__ p, double* __restrict__ y) {{")
     for v, e, kind in _fwd_lines(t, live, "c"):

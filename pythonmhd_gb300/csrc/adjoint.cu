@@ -96,7 +96,7 @@ __device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a
       _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) yb_[k_] = *OUTS[k_].b; \
       g_##NAME##_rev(x_, PAR, yb_, xb_);                                          \
       _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_)               \
-        if (xb_[k_] != 0.0) atomicAdd(INS[k_].b, xb_[k_]);                        \
+        if (nz(xb_[k_])) atomicAdd(INS[k_].b, xb_[k_]);                          \
     }                                                                             \
   } while (0)
 
@@ -115,7 +115,7 @@ __device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a
       _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) yb_[k_] = *OUTS[k_].b; \
       g_##NAME##_revt(x_, PAR, yb_, xb_, TP, ST);                                 \
       _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_)               \
-        if (xb_[k_] != 0.0) atomicAdd(INS[k_].b, xb_[k_]);                        \
+        if (nz(xb_[k_])) atomicAdd(INS[k_].b, xb_[k_]);                          \
     }                                                                             \
   } while (0)
 
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
         *E.pv(7 + k, me) = *A.P.pv(slots[k], me);
       } else {
         const double g = *E.pb(k, me) + *E.pb(7 + k, me);
-        if (g != 0.0) atomicAdd(A.P.pb(slots[k], me), g);
+        if (nz(g)) atomicAdd(A.P.pb(slots[k], me), g);
       }
     }
   }
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(kT) k_final(Adj A) {
 // ---------------------------------------------------------------------------
 // CFL dt of the input state (Source/TimestepCalculations_HelperModule.py:239-289)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double dmax2(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double dmax2(double a, double b) { return dsl_gt(a, b) ? a : b; }
 
 __device__ __forceinline__ double M(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double Ad(double a, double b) { return __dadd_rn(a, b); }
@@ -613,7 +613,7 @@ struct Handle {
                                // PPM slopes x, y
   int nsets = 0;
   double* red = nullptr;       // CFL maxima (2) + dt (1)
-  size_t budget = 0;           // bytes the stored-segment mode may use (0: 60% of free memory)
+  size_t budget = 0;           // bytes the stored-segment mode may use (0: 85% of free memory)
   // forward record: uniform segments of `every` cycles over the first steps - tail
   // cycles, then (stored mode) a tail segment whose cycles the forward pass runs with
   // the taped kernels and leaves resident, so the backward pass reverses them at once
@@ -884,7 +884,7 @@ int prepare_record(Handle* h, int steps, int& every, bool own_ckpt, bool allow_t
   const size_t set_bytes = (h->W + h->TW) * sizeof(double);
   const size_t held_all = (h->vals_cap + h->tapes_cap) * sizeof(double);
   const size_t held = held_all > set_bytes ? held_all - set_bytes : 0;
-  const size_t budget = h->budget ? h->budget : (size_t)(0.6 * (double)(free_b + held));
+  const size_t budget = h->budget ? h->budget : (size_t)(0.85 * (double)(free_b + held));
   const size_t extra = ((size_t)every - 1) * set_bytes;
   h->stored = every > 1 && extra <= budget;
   int tail = 0;
