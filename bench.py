@@ -528,14 +528,22 @@ def run_ours(a):
     torch.cuda.synchronize()
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)
+    # per step: upload | cycle | download, each ended by the call's own stream sync
+    ph = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(e2e_steps)]
     e2.record(stream)
-    for _ in range(e2e_steps):
+    for k in range(e2e_steps):
+        ph[k][0].record(stream)
         g.upload(hp, hc, hbx, hby)
+        ph[k][1].record(stream)
         t, cyc, _ = g.advance(t, big, cyc, cyc + 1, 0.4)
+        ph[k][2].record(stream)
         g.download(0, hp, hc, hbx, hby)
+        ph[k][3].record(stream)
     e3.record(stream)
     e3.synchronize()
     ms_e2e = e2.elapsed_time(e3)
+    phase_ms = {name: sum(ph[k][i].elapsed_time(ph[k][i + 1]) for k in range(e2e_steps)) / e2e_steps
+                for i, name in enumerate(("upload", "cycle", "download"))}
     # the copies alone, after the e2e loop: the link rate that e2e pays on this host
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     ev[0].record(stream)
@@ -613,7 +621,8 @@ def run_ours(a):
                        "arith": a.arith, "cells": zones, "l2": "state 2.4 GB >> 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": e2e_steps, "ms_per_step": ms_e2e_per, "copy_gbs": copy_gbs},
+                    "steps": e2e_steps, "ms_per_step": ms_e2e_per, "copy_gbs": copy_gbs,
+                    "phase_ms": phase_ms},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
             "device_bytes": dev_bytes, "final_cycle": cyc, "final_time": t, "batched": batched,
             "adjoint": adjoint, "hydro3d": hydro_3d, "mhd3d": mhd_3d}
