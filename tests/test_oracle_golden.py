@@ -112,3 +112,14 @@ def test_oracle_3d_mhd_matches_reference_bitwise(path):
 
 def test_golden_3d_mhd_set_is_complete():
     assert len(golden_files("mhd3d")) >= 15
+
+
+def test_ot128_full_run_oracle_pinned_to_reference():
+    """The oracle's 407-cycle PPM Orszag-Tang run (128², t 0 -> 0.5) has the same
+    final-state digest as the reference's own run (tests/golden/make_ot128_digests.py)."""
+    import json
+    from tests.golden import make_ot128_digests as ot
+    with open(ot.OUT) as f:
+        d = json.load(f)
+    assert d["reference_ppm"] == d["oracle_ppm"]
+    assert d["reference_ppm"]["cycle"] > 300 and d["oracle_plm"]["t"] == 0.5
