@@ -123,3 +123,15 @@ def test_ot128_full_run_oracle_pinned_to_reference():
         d = json.load(f)
     assert d["reference_ppm"] == d["oracle_ppm"]
     assert d["reference_ppm"]["cycle"] > 300 and d["oracle_plm"]["t"] == 0.5
+
+
+def test_long_run_digests_cover_every_run():
+    """tests/golden/long_run_digests.json holds a digest of the reference's own run for
+    every run of tests/golden/make_long_run_digests.py (the generator checks the
+    oracle's runs against them)."""
+    import json
+    from tests.golden import make_long_run_digests as lr
+    with open(lr.OUT) as f:
+        d = json.load(f)
+    assert set(d) == set(lr.RUNS)
+    assert all(len(v["sha256"]) == 64 and v["cycle"] > 10 for v in d.values())
