@@ -123,3 +123,21 @@ def test_3d_mhd_div_b_and_conservation_at_size():
     for k in (0, 7):
         scale = float(np.sum(np.abs(cons[k])))
         assert abs(float(np.sum(c2[k])) - float(np.sum(cons[k]))) <= 1e-12 * scale, k
+
+
+def test_3d_mhd_40_cycles_vs_reference():
+    """40 cycles of evolve_3D_mhd on a periodic 10³ box against the reference's own run
+    (tests/golden/make_mhd3d_long.py): within 1e-12 relative per field (observed
+    1.1e-13: the reference's long-double predictor terms), and bit for bit against the
+    oracle's FP64-predictor form."""
+    from tests.golden import make_mhd3d_long as m
+    prim, cons, fbx, fby, fbz, dx, dy, dz = m.initial_state()
+    o = np.load(m.OUT)
+    got = evolve.evolve_3D_mhd(m.grid_of(prim, cons, fbx, fby, fbz, dx, dy, dz), *m.ARGS, arith="exact")
+    assert int(got[6]) == int(o["cycle"]) == m.CYCLES
+    for k, v in zip(m.KEYS, got[:7]):
+        if k != "cycle":
+            assert _close(v, o[k], 1e-12), k
+    want = mhd3d.evolve(prim, cons, fbx, fby, fbz, dx, dy, dz, 1, 1, 1, *m.ARGS, long_double=False)
+    for k, a, b in zip(m.KEYS, got[:7], want[:7]):
+        assert np.array_equal(np.asarray(a), np.asarray(b)), k

@@ -135,3 +135,34 @@ def test_long_run_digests_cover_every_run():
         d = json.load(f)
     assert set(d) == set(lr.RUNS)
     assert all(len(v["sha256"]) == 64 and v["cycle"] > 10 for v in d.values())
+
+
+def _field_rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    if a.ndim == 4:
+        return max(float(np.max(np.abs(a[i] - b[i]))) / max(float(np.max(np.abs(b[i]))), 1e-300)
+                   for i in range(a.shape[0]))
+    return float(np.max(np.abs(a - b))) / max(float(np.max(np.abs(b))), 1e-300)
+
+
+def test_oracle_3d_mhd_40_cycles_vs_reference():
+    """40 cycles of the reference's evolve_3D_mhd (tests/golden/make_mhd3d_long.py):
+    the oracle with the reference's long-double predictor terms equals it bit for bit
+    on an x86 host; its FP64-predictor form (the CUDA step's) stays within 1e-12."""
+    import platform
+
+    from oracle import mhd3d
+    from tests.golden import make_mhd3d_long as m
+    prim, cons, fbx, fby, fbz, dx, dy, dz = m.initial_state()
+    o = np.load(m.OUT)
+    exact = platform.machine() in ("x86_64", "AMD64")
+    r = mhd3d.evolve(prim, cons, fbx, fby, fbz, dx, dy, dz, 1, 1, 1, *m.ARGS, long_double=True)
+    for k, v in zip(m.KEYS, r[:7]):
+        if exact:
+            assert np.array_equal(np.asarray(v), o[k]), k
+        else:
+            assert _field_rel(v, o[k]) <= 1e-12, k
+    r = mhd3d.evolve(prim, cons, fbx, fby, fbz, dx, dy, dz, 1, 1, 1, *m.ARGS, long_double=False)
+    assert int(r[6]) == int(o["cycle"]) == m.CYCLES
+    for k, v in zip(m.KEYS[:5], r[:5]):
+        assert _field_rel(v, o[k]) <= 1e-12, k
