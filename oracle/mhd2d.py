@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .common import (FOUR_THIRDS, FRAME_X, FRAME_Y, OUTFLOW, PERIODIC,
+from .common import (FOUR_THIRDS, FRAME_X, FRAME_Y, OUTFLOW,
                      SMALL_VALUE, Frame, apply_floors_inplace, np_sign_one,
                      take_x, take_y, wrap_index)
 

@@ -14,8 +14,6 @@ from __future__ import annotations
 
 import ctypes
 
-import numpy as np
-
 from . import _lib
 from .solver import Grid2D, Grid3D, default_arith
 
