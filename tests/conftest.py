@@ -25,3 +25,21 @@ def pytest_collection_modifyitems(config, items):
     for item in items:
         if "gpu" in item.keywords:
             item.add_marker(skip)
+
+
+@pytest.fixture(autouse=True)
+def _release_device_memory(request):
+    """After each GPU test, collect garbage so that handles caught in reference cycles
+    free their device arenas (an adjoint handle may hold most of the HBM) before the
+    next test allocates, and return torch's cached blocks."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    import gc
+    gc.collect()
+    try:
+        import torch
+        if torch.cuda.is_available() and torch.cuda.is_initialized():
+            torch.cuda.empty_cache()
+    except Exception:  # pragma: no cover
+        pass
