@@ -121,3 +121,26 @@ def test_3d_entry_points_reject_bad_arguments(lib):
     assert lib.mhd3d_upload(None, None, None, None, None, None) == 1
     assert lib.mhd3d_download(None, 0, None, None, None, None, None) == 1
     lib.mhd3d_destroy(None)
+
+
+def test_save_mat_writes_the_reference_layout_with_face_b(tmp_path):
+    """driver.save_mat: the reference's .mat keys (Source/FileSaver.py:212-231) plus the
+    face-centred B a restart needs, faceBz included for a 3D grid."""
+    import numpy as np
+    import scipy.io
+    from pythonmhd_gb300 import driver
+    rng = np.random.default_rng(3)
+    prim, cons = rng.random((8, 3, 4, 2)), rng.random((8, 3, 4, 2))
+    fbx, fby, fbz = rng.random((3, 5, 2)), rng.random((4, 4, 2)), rng.random((3, 4, 3))
+    driver.save_mat(str(tmp_path / "s.mat"), prim, cons, fbx, fby, fbz)
+    d = scipy.io.loadmat(str(tmp_path / "s.mat"))
+    for k, i in (("density", 0), ("vx", 1), ("vy", 2), ("vz", 3), ("Bx", 4), ("By", 5), ("Bz", 6), ("pressure", 7)):
+        np.testing.assert_array_equal(d[k], prim[i])
+    np.testing.assert_array_equal(d["energy"], cons[7])
+    for k, a in (("faceBx", fbx), ("faceBy", fby), ("faceBz", fbz)):
+        np.testing.assert_array_equal(d[k], a)
+    # hydro: no face arrays
+    driver.save_mat(str(tmp_path / "h.mat"), prim[:5], cons[:5])
+    h = scipy.io.loadmat(str(tmp_path / "h.mat"))
+    np.testing.assert_array_equal(h["pressure"], prim[4])
+    assert "faceBx" not in h
