@@ -213,16 +213,54 @@ def profile_summary(arith):
         return None
 
 
+PROBE_SRC = os.path.join(ROOT, "fp64_probe.cu")
+PROBE_EXE = os.path.join(ROOT, "_build", "fp64_probe")
+
+
+def build_probe() -> str:
+    """Build the FP64 pipe throughput probe (fp64_probe.cu beside this file) for sm_103a."""
+    from pythonmhd_gb300 import build as _build
+    if os.path.exists(PROBE_EXE) and os.path.getmtime(PROBE_EXE) > os.path.getmtime(PROBE_SRC):
+        return PROBE_EXE
+    os.makedirs(os.path.dirname(PROBE_EXE), exist_ok=True)
+    r = subprocess.run([_build.nvcc_path(), _build.ARCH, "-O3", "-o", PROBE_EXE, PROBE_SRC],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("probe build failed:\n" + r.stdout.decode(errors="replace"))
+    return PROBE_EXE
+
+
 def fp64_peak():
-    """DFMA lane-ops/s of this GPU from the FP64 probe (pythonmhd_gb300/csrc/fp64_probe.cu)."""
+    """DFMA / DADD / DMUL lane-ops/s of this GPU from the FP64 probe (fp64_probe.cu)."""
     try:
-        from pythonmhd_gb300 import build as _build
-        exe = _build.build_probe()
+        exe = build_probe()
         out = subprocess.run([exe, "--json"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
                              timeout=120).stdout
         return json.loads(out.strip().splitlines()[-1])
     except Exception:
         return None
+
+
+def fp64_roof(prof, probe, zones, ms_per):
+    """FP64-issue roof of one step: each instruction class at its own measured rate.
+
+    The floor is dfma/r_fma + (dadd + dmul)/r_add lane-instructions' worth of time per
+    step; ``frac`` = floor / measured step time.  ``peak`` is the mix-weighted rate
+    (total instructions / floor), so achieved / peak = frac as well."""
+    dfma, dadd, dmul = (prof.get(k) for k in ("dfma_per_zone", "dadd_per_zone", "dmul_per_zone"))
+    if None in (dfma, dadd, dmul) or not probe:
+        return None
+    r_fma, r_add, r_mul = probe["dfma_gops"], probe["dadd_gops"], probe["dmul_gops"]
+    floor_s = zones * (dfma / r_fma + dadd / r_add + dmul / r_mul) / 1e9
+    ops = (dfma + dadd + dmul) * zones
+    ach = ops / (ms_per * 1e-3) / 1e9
+    peak = ops / floor_s / 1e9
+    return {"achieved": ach, "peak": peak, "unit": "G FP64 lane-instr/s", "frac": ach / peak,
+            "floor_ms_per_step": floor_s * 1e3,
+            "ops_per_zone": {"dfma": dfma, "dadd": dadd, "dmul": dmul},
+            "rates_gops": {"dfma": r_fma, "dadd": r_add, "dmul": r_mul},
+            "peak_source": "mix-weighted measured DFMA/DADD/DMUL rates (fp64_probe.cu, same box)",
+            "ops_source": prof.get("source")}
 
 
 # ----------------------------------------------------------------------------
@@ -580,14 +618,7 @@ def run_ours(a):
         scale = zones / prof.get("zones", zones)
         if prof.get("dram_bytes_per_cycle"):
             traffic = prof["dram_bytes_per_cycle"] * scale
-        if prof.get("fp64_lane_ops_per_zone"):
-            ops = prof["fp64_lane_ops_per_zone"] * zones
-            ach = ops / (ms_per * 1e-3) / 1e9
-            peak = probe["dfma_gops"] if probe else None
-            fp64 = {"achieved": ach, "peak": peak, "unit": "G FP64 lane-instr/s",
-                    "frac": ach / peak if peak else None, "ops_per_zone": prof["fp64_lane_ops_per_zone"],
-                    "peak_source": "measured DFMA rate (fp64_probe, same box)" if probe else None,
-                    "ops_source": prof.get("source")}
+        fp64 = fp64_roof(prof, probe, zones, ms_per)
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "traffic": traffic,
             "kernel": "one full cycle (CUDA graph of 17 kernels), 128 algorithmic B/zone",

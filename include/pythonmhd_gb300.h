@@ -152,7 +152,12 @@ int mhd2d_stream(void* handle, void** stream);
  * (cudaGetSymbolAddress), so make it before any stream capture.  All calls share
  * the array: calls that overlap on the GPU (different streams, or different
  * host threads with the same device) race and may return a wrong dt.  The result
- * equals the dt the exact-arithmetic step uses, bit for bit. */
+ * equals the dt the exact-arithmetic step uses, bit for bit; a state holding a
+ * NaN gives a NaN dt.  The cached array address is not refreshed after a
+ * cudaDeviceReset of that device, so calling this entry point after such a
+ * reset is not supported.  If a CUDA error is already pending on the calling
+ * thread, the call launches nothing, leaves that error pending and returns
+ * MHD_ERR_CUDA; otherwise MHD_ERR_CUDA reports a failure of its own launches. */
 int mhd2d_cfl_dt_noalloc(int physics, int ny, int nx, double dx, double dy, double gamma,
                          double cfl, const double* cons, const double* faceBx,
                          const double* faceBy, double* dt_out, void* stream);
@@ -172,9 +177,15 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
 int mhdb_upload(void* handle, int instance, const double* prim, const double* cons,
                 const double* faceBx, const double* faceBy);
 /* Per-instance t0/t_end/cycle0/max_cycles arrays; every instance runs the
- * reference loop (while t < t_end and cycle < max_cycles) with its own dt. */
+ * reference loop (while t < t_end and cycle < max_cycles) with its own dt.  An
+ * instance whose time or dt becomes non-finite stops there while the others run
+ * to their ends; t_out / cycle_out are written for every instance, and the call
+ * then returns MHD_ERR_NONFINITE (mhdb_instance_status names the instances). */
 int mhdb_advance(void* handle, const double* t0, const double* t_end, const long long* cycle0,
                  const long long* max_cycles, double cfl, double* t_out, long long* cycle_out);
+/* Per-instance status of the last mhdb_advance (count ints: MHD_OK or
+ * MHD_ERR_NONFINITE). */
+int mhdb_instance_status(void* handle, int* status);
 int mhdb_download(void* handle, int instance, int which, double* prim, double* cons,
                   double* faceBx, double* faceBy);
 /* Launch shape of a batched cycle (the autotuner's knobs): tile_width work

@@ -25,7 +25,6 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpythonmhd_gb300.so")
-PROBE = os.path.join(PKG, "fp64_probe")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 UNITS = [
@@ -50,7 +49,7 @@ def nvcc_path() -> str:
 
 
 def _sources():
-    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f != "fp64_probe.cu"]
+    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     srcs += [os.path.join(ADJ_PY, f) for f in os.listdir(ADJ_PY) if f.endswith(".py")]
     srcs.append(os.path.join(ROOT, "include", "pythonmhd_gb300.h"))
     srcs.append(os.path.abspath(__file__))
@@ -106,18 +105,6 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
     os.replace(tmp, LIB)
     return LIB
-
-
-def build_probe(force: bool = False) -> str:
-    """Build the FP64 throughput probe executable (used by bench.py for the FP64 roof)."""
-    src = os.path.join(CSRC, "fp64_probe.cu")
-    if not force and os.path.exists(PROBE) and os.path.getmtime(PROBE) > os.path.getmtime(src):
-        return PROBE
-    r = subprocess.run([nvcc_path(), ARCH, "-O3", "-o", PROBE, src], stdout=subprocess.PIPE,
-                       stderr=subprocess.STDOUT)
-    if r.returncode != 0:
-        raise RuntimeError("probe build failed:\n" + r.stdout.decode(errors="replace"))
-    return PROBE
 
 
 if __name__ == "__main__":

@@ -144,6 +144,7 @@ struct BatchHandle {
   unsigned blocks = 0;
   long long last_launches = 0;
   std::vector<int> uploaded;
+  std::vector<int> inst_status;    // per-instance status of the last mhdb_advance
 };
 
 void enqueue_batch(BatchHandle* b) {
@@ -562,6 +563,7 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
   b->nvars = physics == MHD2D_MHD ? 8 : 5;
   b->grids.resize(count);
   b->uploaded.assign(count, 0);
+  b->inst_status.assign(count, MHD_OK);
   cudaError_t e = cudaGetDevice(&b->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
@@ -690,6 +692,7 @@ int mhdb_advance(void* handle, const double* t0, const double* t_end, const long
     L.t = t0[i]; L.t_end = t_end[i]; L.t_prev = t0[i]; L.cfl = cfl;
     L.cycle = cycle0[i]; L.max_cycles = max_cycles[i]; L.cur = cur;
   }
+  b->inst_status.assign(b->count, MHD_OK);
   CK(cudaMemcpyAsync(b->d_loops, b->h_loops, b->count * sizeof(LoopState), cudaMemcpyHostToDevice, b->stream));
   int rc = build_batch_graph(b);
   if (rc) return rc;
@@ -715,14 +718,25 @@ int mhdb_advance(void* handle, const double* t0, const double* t_end, const long
     b->last_launches += budget * (long long)b->graph_nodes;
     CK(cudaMemcpyAsync(b->h_loops, b->d_loops, b->count * sizeof(LoopState), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
+    // An instance whose time or dt went non-finite has stopped by itself (NaN < t_end
+    // is false, so its kernels skip it); the others keep advancing.
     for (int i = 0; i < b->count; ++i)
-      if (!std::isfinite(b->h_loops[i].t) || !std::isfinite(b->h_loops[i].dt)) return MHD_ERR_NONFINITE;
+      if (!std::isfinite(b->h_loops[i].t) || !std::isfinite(b->h_loops[i].dt)) b->inst_status[i] = MHD_ERR_NONFINITE;
     budget = std::max(1LL, std::min(remaining - budget, 512LL));
   }
+  int rc_all = MHD_OK;
   for (int i = 0; i < b->count; ++i) {
     if (t_out) t_out[i] = b->h_loops[i].t;
     if (cycle_out) cycle_out[i] = b->h_loops[i].cycle;
+    if (b->inst_status[i] != MHD_OK) rc_all = b->inst_status[i];
   }
+  return rc_all;
+}
+
+int mhdb_instance_status(void* handle, int* status) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || !status) return MHD_ERR_ARG;
+  for (int i = 0; i < b->count; ++i) status[i] = b->inst_status[i];
   return MHD_OK;
 }
 

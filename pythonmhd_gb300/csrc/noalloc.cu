@@ -9,12 +9,16 @@
 // loads this library holds until the process exits.
 //
 // Built with -fmad=false, so the per-cell arithmetic, and with it the result, is
-// the same as the exact-arithmetic step's CFL reduction bit for bit.
+// the same as the exact-arithmetic step's CFL reduction bit for bit.  Maxima and
+// minima use the step's order-key compares (mhdk::dmax / dmin), which let a NaN
+// signal speed win where a plain `a > b ? a : b` would drop it: a state with a NaN
+// gives a NaN dt here, as it makes the step report MHD_ERR_NONFINITE.
 #include <cuda_runtime.h>
 
 #include <mutex>
 
 #include "../../include/pythonmhd_gb300.h"
+#include "mhd_math.cuh"
 
 namespace {
 
@@ -31,11 +35,12 @@ static __device__ __align__(256) double g_row_max[2 * kMaxRows];
 std::mutex g_setup_lock;
 double* g_scratch[kMaxDevices] = {};
 
-__device__ __forceinline__ double dmax2(double a, double b) { return a > b ? a : b; }
+using mhdk::dmax;
+using mhdk::dmin;
 
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = dmax2(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = dmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
@@ -76,19 +81,19 @@ __global__ void __launch_bounds__(kThreads) k_row_speeds(int mhd, int ny, int nx
       const double by = c5 + fabs(fby[(size_t)j * nx + i] - c5);
       const double bz = cons[6 * plane + idx];
       const double bsq = bx * bx + by * by + bz * bz;
-      const double p = dmax2((gamma - 1.0) * (cons[7 * plane + idx] - 0.5 * cons[idx] * vsq - 0.5 * bsq), kSmall);
+      const double p = dmax((gamma - 1.0) * (cons[7 * plane + idx] - 0.5 * cons[idx] * vsq - 0.5 * bsq), kSmall);
       const double a2 = gamma * p * inv_d;
       const double ssum = bsq * inv_d + a2;
       const double sdiff = bsq * inv_d - a2;
       const double cfx2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (by * by + bz * bz) * inv_d));
       const double cfy2 = 0.5 * (ssum + sqrt(sdiff * sdiff + 4.0 * a2 * (bx * bx + bz * bz) * inv_d));
-      mx = dmax2(mx, fabs(vx) + sqrt(cfx2));
-      my = dmax2(my, fabs(vy) + sqrt(cfy2));
+      mx = dmax(mx, fabs(vx) + sqrt(cfx2));
+      my = dmax(my, fabs(vy) + sqrt(cfy2));
     } else {
-      const double p = dmax2((gamma - 1.0) * (cons[4 * plane + idx] - 0.5 * cons[idx] * vsq), kSmall);
+      const double p = dmax((gamma - 1.0) * (cons[4 * plane + idx] - 0.5 * cons[idx] * vsq), kSmall);
       const double a = sqrt(gamma * p * inv_d);
-      mx = dmax2(mx, fabs(vx) + a);
-      my = dmax2(my, fabs(vy) + a);
+      mx = dmax(mx, fabs(vx) + a);
+      my = dmax(my, fabs(vy) + a);
     }
   }
   __shared__ double sx[kThreads / 32], sy[kThreads / 32];
@@ -104,20 +109,20 @@ __global__ void __launch_bounds__(kThreads) k_finish_dt(int mhd, int ny, double 
                                                         const double* __restrict__ rows, double* dt_out) {
   double mx = 0.0, my = 0.0;
   for (int j = threadIdx.x; j < ny; j += blockDim.x) {
-    mx = dmax2(mx, rows[2 * j]);
-    my = dmax2(my, rows[2 * j + 1]);
+    mx = dmax(mx, rows[2 * j]);
+    my = dmax(my, rows[2 * j + 1]);
   }
   __shared__ double sx[kThreads / 32], sy[kThreads / 32];
   block_max2(mx, my, sx, sy);
   if (threadIdx.x == 0) {
     double dt;
     if (mhd) {
-      const double inv = dmax2(mx / dx, my / dy);
+      const double inv = dmax(mx / dx, my / dy);
       dt = cfl / inv;
     } else {
       const double dtx = cfl / (mx / dx);
       const double dty = cfl / (my / dy);
-      dt = dtx < dty ? dtx : dty;
+      dt = dmin(dtx, dty);
     }
     *dt_out = dt;
   }
@@ -149,6 +154,9 @@ extern "C" int mhd2d_cfl_dt_noalloc(int physics, int ny, int nx, double dx, doub
   if (ny < 1 || nx < 1 || !(dx > 0.0) || !(dy > 0.0) || !cons || !dt_out) return MHD_ERR_ARG;
   if (physics == MHD2D_MHD && (!faceBx || !faceBy)) return MHD_ERR_ARG;
   if (ny > kMaxRows) return MHD_ERR_TOO_LARGE;
+  // An error left pending by earlier work on this thread is not ours to clear or
+  // to blame on this call: report it and launch nothing.
+  if (cudaPeekAtLastError() != cudaSuccess) return MHD_ERR_CUDA;
   double* rows = nullptr;
   const int rc = scratch_for_current_device(&rows);
   if (rc != MHD_OK) return rc;

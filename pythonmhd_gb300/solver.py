@@ -387,9 +387,21 @@ class Batch2D:
         mc = np.broadcast_to(np.asarray(max_cycles, dtype=np.int64), (n,)).copy()
         t_out = np.empty(n)
         c_out = np.empty(n, dtype=np.int64)
-        _lib.check(self.lib.mhdb_advance(self._h, t0.ctypes.data, te.ctypes.data, c0.ctypes.data, mc.ctypes.data,
-                                         float(cfl), t_out.ctypes.data, c_out.ctypes.data), "mhdb_advance")
+        rc = self.lib.mhdb_advance(self._h, t0.ctypes.data, te.ctypes.data, c0.ctypes.data, mc.ctypes.data,
+                                   float(cfl), t_out.ctypes.data, c_out.ctypes.data)
+        if rc != 0:
+            err = _lib.MhdError(rc, "mhdb_advance")
+            # the healthy instances ran to their ends; say which ones did not
+            err.t_out, err.cycle_out = t_out, c_out
+            err.instance_status = self.instance_status() if rc == 5 else None
+            raise err
         return t_out, c_out
+
+    def instance_status(self):
+        """Per-instance status of the last advance (0 ok, 5 the time or dt went non-finite)."""
+        st = np.zeros(self.count, dtype=np.int32)
+        _lib.check(self.lib.mhdb_instance_status(self._h, st.ctypes.data), "mhdb_instance_status")
+        return st
 
     def download(self, k, which=0):
         ny, nx = self.shapes[k]

@@ -3,7 +3,9 @@
 Run in a checkout that has the reference next to it (the fixtures are committed,
 so the tests do not need the reference):
 
-    python -B tests/golden/make_golden.py /root/reference/PythonMHD
+    python -B tests/golden/make_golden.py <PythonMHD checkout> [2d|1d|3d|all]
+
+(or set ``PYTHONMHD_REFERENCE`` to the checkout)
 
 For every case in ``tests/golden/cases.py`` (2D; the 1D cases with
 ``evolve_1D_mhd`` / ``evolve_1D_hydro``; the 3D cases with ``evolve_3D_hydro``) this imports the reference's own
@@ -154,8 +156,9 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    # make_golden.py [reference root] [2d|1d|3d|all]
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/PythonMHD"
+    # make_golden.py <reference root> [2d|1d|3d|all]
+    from tests.golden.refpath import reference_root
+    root = reference_root()
     which = sys.argv[2] if len(sys.argv) > 2 else "all"
     if which in ("2d", "all"):
         main(root)

@@ -2,7 +2,7 @@
 checks after hundreds of cycles (the fixtures in ``tests/golden/*.npz`` hold 1-6
 cycles each).
 
-    python -B tests/golden/make_long_run_digests.py /root/reference/PythonMHD
+    python -B tests/golden/make_long_run_digests.py <PythonMHD checkout>
 
 Writes ``tests/golden/long_run_digests.json``: per run, the final time, the cycle
 count and the SHA-256 of the final prim and cons arrays (C-contiguous little-endian
@@ -137,4 +137,5 @@ def main(ref_root):
 
 if __name__ == "__main__":
     sys.dont_write_bytecode = True
-    main(sys.argv[1])
+    from tests.golden.refpath import reference_root
+    main(reference_root())

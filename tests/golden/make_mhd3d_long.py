@@ -1,7 +1,7 @@
 """A 40-cycle run of the reference's own ``evolve_3D_mhd`` (the 3D MHD fixtures in
 ``tests/golden/mhd3d_*.npz`` hold 1-6 cycles each).
 
-    python -B tests/golden/make_mhd3d_long.py /root/reference/PythonMHD
+    python -B tests/golden/make_mhd3d_long.py <PythonMHD checkout>
 
 State: ``cases._random_mhd_3d(10, 10, 10, seed=71)`` (smooth random flow, rms Mach
 ~0.6, divergence-free face B), periodic in x, y and z, gamma 5/3, PPM, the entropy
@@ -55,4 +55,5 @@ def main(ref_root):
 
 if __name__ == "__main__":
     sys.dont_write_bytecode = True
-    main(sys.argv[1])
+    from tests.golden.refpath import reference_root
+    main(reference_root())

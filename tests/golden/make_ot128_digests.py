@@ -2,7 +2,7 @@
 from t = 0 to t = 0.5 (about 400 cycles), the workload of the plain CPU-runnable
 configuration.
 
-    python -B tests/golden/make_ot128_digests.py [/root/reference/PythonMHD]
+    python -B tests/golden/make_ot128_digests.py [<PythonMHD checkout>]
 
 Writes ``tests/golden/ot128_t05_digests.json`` with, per run, the final time, the
 cycle count and the SHA-256 of the final prim, cons, faceBx and faceBy arrays
@@ -85,4 +85,5 @@ def main(ref_root=None):
 
 if __name__ == "__main__":
     sys.dont_write_bytecode = True
-    main(sys.argv[1] if len(sys.argv) > 1 else None)
+    from tests.golden.refpath import reference_root
+    main(reference_root(required=False))

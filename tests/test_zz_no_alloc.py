@@ -71,6 +71,20 @@ def test_noalloc_dt_matches_handle_dt_on_two_calls_in_a_row():
     assert got2 == want2
 
 
+def test_noalloc_dt_is_nan_for_a_state_with_a_nan():
+    # the handle's step reports MHD_ERR_NONFINITE on such a state; this entry point
+    # must not hide the NaN behind a finite dt
+    prim, cons, fbx, fby, dx, dy = ic.turbulence(64, seed=2, gamma=G)
+    cons = cons.copy()
+    cons[7, 40, 17] = np.nan
+    assert np.isnan(_dt_noalloc(True, cons, fbx, fby, dx, dy, G))
+    hp = np.ones((5, 24, 32))
+    hp[1:4] = 0.1
+    hc = ic.prim_to_cons_hydro(hp, 1.4)
+    hc[1, 3, 5] = np.nan
+    assert np.isnan(_dt_noalloc(False, hc, None, None, 1 / 32, 1 / 24, 1.4))
+
+
 def test_noalloc_rejects_grids_above_its_row_limit():
     import torch
     lib = _lib.load()
