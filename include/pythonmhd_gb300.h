@@ -130,6 +130,26 @@ int mhd2d_last_launches(void* handle, long long* launches);
 /* Bytes of device memory the handle holds. */
 int mhd2d_device_bytes(void* handle, size_t* bytes);
 
+/* Failure counters of the state since the last upload (SURVEY-planned stats; the
+ * reference clamps floors silently, Source/PrimCons_HelperModule.py:499-554, and
+ * builds a warning it never prints):
+ *   floor_hits: how many values the density / pressure / energy floors raised,
+ *               counted per face-state value as the reference's applyFloors
+ *               calls clamp them (reconstructed prim states and CTU cons states);
+ *   nan_flag:   1 if a cycle wrote a NaN or Inf into the state, or an advance
+ *               ended with MHD_ERR_NONFINITE.
+ * Either pointer may be NULL.  Waits for the handle's stream. */
+int mhd2d_stats(void* handle, long long* floor_hits, int* nan_flag);
+
+/* Check the current state as the reference's validatePrimVars does before a run
+ * (Source/SimulationGrid_HelperModule.py:282-410): energy per cell in the
+ * reference's arithmetic, then counts[7] = { cells with a NaN/Inf prim value,
+ * density < 0, density < min_d, pressure < 0, pressure < min_p, energy < 0,
+ * energy < min_e }.  The reference raises RuntimeError on the first nonzero
+ * class (negative before below-floor, density, then pressure, then energy);
+ * the Python mirror (solver.Grid2D.check_state) does the same from these counts. */
+int mhd2d_validate(void* handle, long long* counts);
+
 /* The CUDA stream the handle's work runs on (a cudaStream_t). */
 int mhd2d_stream(void* handle, void** stream);
 
@@ -186,6 +206,8 @@ int mhdb_advance(void* handle, const double* t0, const double* t_end, const long
 /* Per-instance status of the last mhdb_advance (count ints: MHD_OK or
  * MHD_ERR_NONFINITE). */
 int mhdb_instance_status(void* handle, int* status);
+/* mhd2d_stats per instance: count entries in each array (either may be NULL). */
+int mhdb_stats(void* handle, long long* floor_hits, int* nan_flag);
 int mhdb_download(void* handle, int instance, int which, double* prim, double* cons,
                   double* faceBx, double* faceBy);
 /* Launch shape of a batched cycle (the autotuner's knobs): tile_width work
@@ -194,6 +216,18 @@ int mhdb_download(void* handle, int instance, int which, double* prim, double* c
  * launches of a stage as one launch, blocks = blocks of each persistent launch
  * (default 2 per SM).  Results do not depend on these. */
 int mhdb_configure(void* handle, int tile_width, int fuse, int blocks);
+/* Work lists: a batched cycle runs, per index space, a list of row tiles
+ * {instance, row, x0, 0} (4 ints each) that its persistent blocks stride through.
+ * Spaces: 0 cells (nx x ny), 1 x-extended cells (nx+2 x ny), 2 y-extended cells
+ * (nx x ny+2), 3 x-faces (nx+1 x ny), 4 y-faces (nx x ny+1), 5 corners
+ * (nx+1 x ny+1); x0 is a multiple of the tile width.  mhdb_get_tiles copies the
+ * installed list of a space (tiles NULL: just its length); mhdb_set_tiles installs a
+ * caller's order of it, e.g. largest instances first.  The list is checked on the
+ * host before anything is copied or launched: every tile of every instance exactly
+ * once and nothing out of range, else MHD_ERR_ARG and the installed list stays.
+ * mhdb_configure with a new tile width rebuilds every list in the default order. */
+int mhdb_get_tiles(void* handle, int space, int* tiles, long long capacity, long long* count);
+int mhdb_set_tiles(void* handle, int space, const int* tiles, long long count);
 /* mhdb_upload from device memory of the handle's GPU. */
 int mhdb_upload_device(void* handle, int inst, const double* prim, const double* cons,
                        const double* faceBx, const double* faceBy);

@@ -62,16 +62,34 @@ def take_y(a: np.ndarray, idx: np.ndarray) -> np.ndarray:
     return np.take(a, idx, axis=-2)
 
 
+_floor_tally = {"hits": 0}
+
+
+def reset_floor_tally() -> None:
+    """Zero the running count of floored values (see ``apply_floors_inplace``)."""
+    _floor_tally["hits"] = 0
+
+
+def floor_tally() -> int:
+    """Values raised by the floors since the last ``reset_floor_tally``."""
+    return _floor_tally["hits"]
+
+
 def apply_floors_inplace(v: np.ndarray, min_d: float, min_last: float) -> np.ndarray:
     """Density floor on slot 0 and pressure/energy floor on the last slot.
 
-    Follows Source/PrimCons_HelperModule.py:499-554 (the warning text the
-    reference builds there is discarded, so only the clamps matter).
+    Follows Source/PrimCons_HelperModule.py:499-554.  The reference counts the
+    values it clamps for a warning text that it then discards; the oracle adds that
+    count to a running tally (``floor_tally``) that tests compare with the GPU's
+    floor-hit counter.  The clamps themselves are unchanged.
     """
     d = v[0]
-    d[d < min_d] = min_d
+    low = d < min_d
+    d[low] = min_d
     last = v[v.shape[0] - 1]
-    last[last < min_last] = min_last
+    low_last = last < min_last
+    last[low_last] = min_last
+    _floor_tally["hits"] += int(np.count_nonzero(low)) + int(np.count_nonzero(low_last))
     return v
 
 

@@ -75,6 +75,12 @@ SIGNATURES = {
     "mhdb_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t),
                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p)]),
     "mhdb_instance_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mhdb_get_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
+                                      ctypes.POINTER(ctypes.c_longlong)]),
+    "mhdb_set_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong]),
+    "mhdb_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mhd2d_validate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "mhd2d_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]),
     "mhdb_destroy": (None, [ctypes.c_void_p]),
     "mhd2d_adj_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,

@@ -9,6 +9,7 @@ shared library with a plain C ABI (``include/pythonmhd_gb300.h``):
 * ``csrc/kernels3d_exact.cu`` / ``csrc/kernels3d_fast.cu`` -- the 3D hydro step kernels
 * ``csrc/capi3d.cu``         -- the 3D handle and its evolve loop
 * ``csrc/noalloc.cu``        -- the CFL timestep for callers that cannot allocate
+* ``csrc/validate.cu``       -- the initial-state check (the reference's validatePrimVars)
 * ``csrc/adjoint.cu``        -- the reverse-mode adjoint of the MHD step; its pointwise
   stage functions (``csrc/adjoint_gen.cuh``) are generated from ``adjoint/stages.py``
   first
@@ -35,6 +36,7 @@ UNITS = [
     ("kernels3d_fast.cu", ["-fmad=true"]),
     ("capi3d.cu", []),
     ("noalloc.cu", ["-fmad=false"]),
+    ("validate.cu", ["-fmad=false"]),
     ("adjoint.cu", []),
 ]
 ADJ_GEN = os.path.join(CSRC, "adjoint_gen.cuh")

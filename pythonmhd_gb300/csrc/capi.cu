@@ -19,6 +19,8 @@ void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
 void enqueue_cycle_batch_tuned(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, int fuse,
                                cudaStream_t s);
 }  // namespace exact
+void enqueue_validate(int mhd, size_t plane, double gamma, double min_d, double min_p, double min_e,
+                      const double* prim, unsigned long long* counts, int blocks, cudaStream_t s);
 namespace fast {
 void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
 void enqueue_cycle_batch_tuned(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, int fuse,
@@ -47,6 +49,8 @@ struct Handle {
   long long last_launches = 0;
   size_t graph_nodes[2] = {0, 0};
   int dt_blocks = 0;
+  int nonfinite_seen = 0;  // an advance since the last upload ended with MHD_ERR_NONFINITE
+  unsigned long long* d_check = nullptr;  // 7 counters of mhd2d_validate (device)
 };
 
 int cuda_fail(cudaError_t e) {
@@ -145,6 +149,9 @@ struct BatchHandle {
   long long last_launches = 0;
   std::vector<int> uploaded;
   std::vector<int> inst_status;    // per-instance status of the last mhdb_advance
+  std::vector<std::vector<int4>> host_tiles;  // the installed work lists
+  int* d_status = nullptr;         // per-instance device error words
+  unsigned long long* d_floor_hits = nullptr;  // per-instance floor-hit counts
 };
 
 void enqueue_batch(BatchHandle* b) {
@@ -156,17 +163,42 @@ void enqueue_batch(BatchHandle* b) {
                                           b->stream);
 }
 
-// (Re)build the per-space work lists for tiles of `width` items.
-int build_tiles(BatchHandle* b, int width) {
-  std::vector<int4> tiles[mhdk::kNumSpaces];
+// Width and height of index space `sp` of grid g (work items per row, rows).
+void space_extent(const Grid& g, int sp, int* w, int* h) {
+  const int ws[mhdk::kNumSpaces] = {g.nx, g.nx + 2, g.nx, g.nx + 1, g.nx, g.nx + 1};
+  const int hs[mhdk::kNumSpaces] = {g.ny, g.ny, g.ny + 2, g.ny, g.ny + 1, g.ny + 1};
+  *w = ws[sp];
+  *h = hs[sp];
+}
+
+// A work list for space sp must name every row tile {instance, row, x0} of every
+// instance exactly once (x0 a multiple of `width` below the row width).  A tile out
+// of range would make a kernel index past its instance's arrays; a missing or
+// repeated tile would skip or race on work items.  Checked on the host, before
+// anything is copied or launched.
+bool tiles_valid(const BatchHandle* b, int sp, int width, const std::vector<int4>& t) {
+  std::vector<size_t> first(b->count + 1, 0);
   for (int i = 0; i < b->count; ++i) {
-    const Grid& g = b->grids[i];
-    const int w[mhdk::kNumSpaces] = {g.nx, g.nx + 2, g.nx, g.nx + 1, g.nx, g.nx + 1};
-    const int hgt[mhdk::kNumSpaces] = {g.ny, g.ny, g.ny + 2, g.ny, g.ny + 1, g.ny + 1};
-    for (int sp = 0; sp < mhdk::kNumSpaces; ++sp)
-      for (int r = 0; r < hgt[sp]; ++r)
-        for (int x0 = 0; x0 < w[sp]; x0 += width) tiles[sp].push_back(make_int4(i, r, x0, 0));
+    int w, h;
+    space_extent(b->grids[i], sp, &w, &h);
+    first[i + 1] = first[i] + (size_t)h * ((w + width - 1) / width);
   }
+  if (t.size() != first[b->count]) return false;
+  std::vector<unsigned char> seen(t.size(), 0);
+  for (const int4& q : t) {
+    if (q.x < 0 || q.x >= b->count || q.w != 0) return false;
+    int w, h;
+    space_extent(b->grids[q.x], sp, &w, &h);
+    if (q.y < 0 || q.y >= h || q.z < 0 || q.z >= w || q.z % width != 0) return false;
+    const size_t slot = first[q.x] + (size_t)q.y * ((w + width - 1) / width) + q.z / width;
+    if (seen[slot]) return false;
+    seen[slot] = 1;
+  }
+  return true;
+}
+
+// Install per-space work lists (already validated) on the device.
+int install_tiles(BatchHandle* b, int width, std::vector<int4> (&tiles)[mhdk::kNumSpaces]) {
   size_t total = 0;
   for (auto& t : tiles) total += t.size();
   int4* d = nullptr;
@@ -187,7 +219,23 @@ int build_tiles(BatchHandle* b, int width) {
   b->d_tiles = d;
   b->view = v;
   b->tile_width = width;
+  b->host_tiles.resize(mhdk::kNumSpaces);
+  for (int sp = 0; sp < mhdk::kNumSpaces; ++sp) b->host_tiles[sp] = tiles[sp];
   return MHD_OK;
+}
+
+// (Re)build the per-space work lists for tiles of `width` items, row-major per instance.
+int build_tiles(BatchHandle* b, int width) {
+  std::vector<int4> tiles[mhdk::kNumSpaces];
+  for (int i = 0; i < b->count; ++i) {
+    for (int sp = 0; sp < mhdk::kNumSpaces; ++sp) {
+      int w, h;
+      space_extent(b->grids[i], sp, &w, &h);
+      for (int r = 0; r < h; ++r)
+        for (int x0 = 0; x0 < w; x0 += width) tiles[sp].push_back(make_int4(i, r, x0, 0));
+    }
+  }
+  return install_tiles(b, width, tiles);
 }
 
 int build_batch_graph(BatchHandle* b) {
@@ -264,7 +312,8 @@ static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, d
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   h->dt_blocks = std::max(1, sms) * 8;
 
-  const size_t total = carve_grid(g, h->nvars, nullptr) + align256(sizeof(LoopState)) + align256(sizeof(int));
+  const size_t total = carve_grid(g, h->nvars, nullptr) + align256(sizeof(LoopState)) + align256(sizeof(int)) +
+                       align256(sizeof(unsigned long long)) + align256(7 * sizeof(unsigned long long));
   e = cudaMalloc(&h->arena, total);
   if (e != cudaSuccess) {
     cudaStreamDestroy(h->stream);
@@ -277,6 +326,10 @@ static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, d
   g.loop = reinterpret_cast<LoopState*>(base + off);
   off += align256(sizeof(LoopState));
   g.status = reinterpret_cast<int*>(base + off);
+  off += align256(sizeof(int));
+  g.floor_hits = reinterpret_cast<unsigned long long*>(base + off);
+  off += align256(sizeof(unsigned long long));
+  h->d_check = reinterpret_cast<unsigned long long*>(base + off);
   e = cudaMemsetAsync(h->arena, 0, total, h->stream);
   if (e == cudaSuccess) e = cudaMallocHost(&h->host_loop, sizeof(LoopState));
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -357,9 +410,13 @@ static int upload_state(void* handle, const double* prim, const double* cons, co
     CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(h->g) * sizeof(double), kind, h->stream));
     CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(h->g) * sizeof(double), kind, h->stream));
   }
+  // a new state starts with clean counters (floor hits, error word)
+  CK(cudaMemsetAsync(h->g.status, 0, sizeof(int), h->stream));
+  CK(cudaMemsetAsync(h->g.floor_hits, 0, sizeof(unsigned long long), h->stream));
   CK(cudaStreamSynchronize(h->stream));
   h->have_state = 1;
   h->last_cycles_run = 0;
+  h->nonfinite_seen = 0;
   return MHD_OK;
 }
 
@@ -408,6 +465,7 @@ int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0, long 
     if (!std::isfinite(st.t) || !std::isfinite(st.dt)) {
       h->cur = st.cur;
       h->last_cycles_run = st.cycles_run;
+      h->nonfinite_seen = 1;
       return MHD_ERR_NONFINITE;
     }
     // size the next chunk from the remaining cycles (graphs past the end are no-ops)
@@ -529,6 +587,34 @@ int mhd2d_device_bytes(void* handle, size_t* bytes) {
   return MHD_OK;
 }
 
+int mhd2d_stats(void* handle, long long* floor_hits, int* nan_flag) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return MHD_ERR_ARG;
+  unsigned long long hits = 0;
+  int status = 0;
+  CK(cudaMemcpyAsync(&hits, h->g.floor_hits, sizeof(hits), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(&status, h->g.status, sizeof(status), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (floor_hits) *floor_hits = (long long)hits;
+  if (nan_flag) *nan_flag = ((status & mhdk::kStatusNonfinite) || h->nonfinite_seen) ? 1 : 0;
+  return MHD_OK;
+}
+
+int mhd2d_validate(void* handle, long long* counts) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || !counts) return MHD_ERR_ARG;
+  if (!h->have_state) return MHD_ERR_STATE;
+  unsigned long long c[7] = {};
+  CK(cudaMemsetAsync(h->d_check, 0, sizeof(c), h->stream));
+  mhdk::enqueue_validate(h->g.physics == MHD2D_MHD, mhdk::cell_plane(h->g), h->g.gamma, h->g.min_d, h->g.min_p,
+                         h->g.min_e, h->g.st[h->cur].prim, h->d_check, h->dt_blocks, h->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c, h->d_check, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < 7; ++k) counts[k] = (long long)c[k];
+  return MHD_OK;
+}
+
 int mhd2d_stream(void* handle, void** stream) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !stream) return MHD_ERR_ARG;
@@ -581,7 +667,7 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
     grid_bytes += carve_grid(g, b->nvars, nullptr);
   }
   const size_t total = grid_bytes + align256(count * sizeof(LoopState)) + align256(count * sizeof(Grid)) +
-                       align256(sizeof(int));
+                       align256(count * sizeof(int)) + align256(count * sizeof(unsigned long long));
   e = cudaMalloc(&b->arena, total);
   if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
   b->arena_bytes = total;
@@ -593,9 +679,14 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
   b->d_grids = reinterpret_cast<Grid*>(base + off);
   off += align256(count * sizeof(Grid));
   int* status = reinterpret_cast<int*>(base + off);
+  off += align256(count * sizeof(int));
+  unsigned long long* hits = reinterpret_cast<unsigned long long*>(base + off);
+  b->d_status = status;
+  b->d_floor_hits = hits;
   for (int i = 0; i < count; ++i) {
     b->grids[i].loop = b->d_loops + i;
-    b->grids[i].status = status;
+    b->grids[i].status = status + i;
+    b->grids[i].floor_hits = hits + i;
   }
   e = cudaMemsetAsync(b->arena, 0, total, b->stream);
   b->view.grids = b->d_grids;
@@ -631,6 +722,8 @@ static int batch_upload(void* handle, int inst, const double* prim, const double
     CK(cudaMemcpyAsync(s.fbx, faceBx, mhdk::xface_plane(g) * sizeof(double), kind, b->stream));
     CK(cudaMemcpyAsync(s.fby, faceBy, mhdk::yface_plane(g) * sizeof(double), kind, b->stream));
   }
+  CK(cudaMemsetAsync(b->d_status + inst, 0, sizeof(int), b->stream));
+  CK(cudaMemsetAsync(b->d_floor_hits + inst, 0, sizeof(unsigned long long), b->stream));
   CK(cudaStreamSynchronize(b->stream));
   b->uploaded[inst] = 1;
   b->h_loops[inst].cycles_run = 0;
@@ -733,6 +826,22 @@ int mhdb_advance(void* handle, const double* t0, const double* t_end, const long
   return rc_all;
 }
 
+int mhdb_stats(void* handle, long long* floor_hits, int* nan_flag) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b) return MHD_ERR_ARG;
+  std::vector<unsigned long long> hits(b->count);
+  std::vector<int> st(b->count);
+  CK(cudaMemcpyAsync(hits.data(), b->d_floor_hits, b->count * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     b->stream));
+  CK(cudaMemcpyAsync(st.data(), b->d_status, b->count * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < b->count; ++i) {
+    if (floor_hits) floor_hits[i] = (long long)hits[i];
+    if (nan_flag) nan_flag[i] = ((st[i] & mhdk::kStatusNonfinite) || b->inst_status[i] != MHD_OK) ? 1 : 0;
+  }
+  return MHD_OK;
+}
+
 int mhdb_instance_status(void* handle, int* status) {
   BatchHandle* b = static_cast<BatchHandle*>(handle);
   if (!b || !status) return MHD_ERR_ARG;
@@ -771,6 +880,35 @@ int mhdb_configure(void* handle, int tile_width, int fuse, int blocks) {
   b->fuse = fuse;
   b->blocks = (unsigned)blocks;
   if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  return MHD_OK;
+}
+
+int mhdb_set_tiles(void* handle, int space, const int* tiles, long long count) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || space < 0 || space >= mhdk::kNumSpaces || count < 0 || (count > 0 && !tiles)) return MHD_ERR_ARG;
+  std::vector<int4> t((size_t)count);
+  for (long long k = 0; k < count; ++k)
+    t[k] = make_int4(tiles[4 * k], tiles[4 * k + 1], tiles[4 * k + 2], tiles[4 * k + 3]);
+  if (!tiles_valid(b, space, b->tile_width, t)) return MHD_ERR_ARG;
+  std::vector<int4> all[mhdk::kNumSpaces];
+  for (int sp = 0; sp < mhdk::kNumSpaces; ++sp) all[sp] = sp == space ? t : b->host_tiles[sp];
+  CK(cudaStreamSynchronize(b->stream));
+  const int rc = install_tiles(b, b->tile_width, all);
+  if (rc != MHD_OK) return rc;
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  return MHD_OK;
+}
+
+int mhdb_get_tiles(void* handle, int space, int* tiles, long long capacity, long long* count) {
+  BatchHandle* b = static_cast<BatchHandle*>(handle);
+  if (!b || space < 0 || space >= mhdk::kNumSpaces || !count) return MHD_ERR_ARG;
+  const std::vector<int4>& t = b->host_tiles[space];
+  *count = (long long)t.size();
+  if (!tiles) return MHD_OK;
+  if (capacity < (long long)t.size()) return MHD_ERR_ARG;
+  for (size_t k = 0; k < t.size(); ++k) {
+    tiles[4 * k] = t[k].x; tiles[4 * k + 1] = t[k].y; tiles[4 * k + 2] = t[k].z; tiles[4 * k + 3] = t[k].w;
+  }
   return MHD_OK;
 }
 

@@ -238,19 +238,31 @@ __device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, 
 }
 
 // Write one reconstructed state to a face: floors (Source/PrimCons_HelperModule.py:499-554),
-// then the transverse-B source term (Source/EvolveFunctions_MHD.py:524-535).
+// then the transverse-B source term (Source/EvolveFunctions_MHD.py:524-535).  Returns how
+// many of its values the floors raised (the reference counts them for a warning it
+// then discards; here they reach mhd2d_stats).
 template <class S>
-__device__ __forceinline__ void put_face(double* buf, size_t fplane, size_t fidx, const double* v,
-                                         double min_d, double min_p, double bsrc, bool add_src = true) {
+__device__ __forceinline__ unsigned put_face(double* buf, size_t fplane, size_t fidx, const double* v,
+                                             double min_d, double min_p, double bsrc, bool add_src = true) {
   constexpr int NV = S::NV;
+  unsigned hits = 0;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
     double x = v[k];
-    if (k == 0 && dlt(x, min_d)) x = min_d;
-    if (k == NV - 1 && dlt(x, min_p)) x = min_p;
+    if (k == 0 && dlt(x, min_d)) { x = min_d; ++hits; }
+    if (k == NV - 1 && dlt(x, min_p)) { x = min_p; ++hits; }
     if (k == S::SB && add_src) x = x + bsrc;
     buf[k * fplane + fidx] = x;
   }
+  return hits;
+}
+
+// Publish a thread's floor hits / a non-finite output with one atomic (rare events).
+__device__ __forceinline__ void note_floor_hits(const Grid& G, unsigned hits) {
+  if (hits && G.floor_hits) atomicAdd(G.floor_hits, (unsigned long long)hits);
+}
+__device__ __forceinline__ void note_nonfinite(const Grid& G, bool bad) {
+  if (bad && G.status) atomicOr(G.status, kStatusNonfinite);
 }
 
 // B source term of one face state: half_dt * v_t(cell) * ((fb[f2] - fb[f1]) * inv_dn)
@@ -492,16 +504,17 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
       else s_lo = bsource<AX>(in.prim, fb, plane, Ls - 1, Ls - 1, 0, t, g.nx, half_dt, inv_dn);
     }
   }
-  put_face<S>(outR, fplane, face_index<AX>(c, t, g.nx), lia, G.min_d, G.min_p, s_mid, src);
-  put_face<S>(outL, fplane, face_index<AX>(c + 1, t, g.nx), ria, G.min_d, G.min_p, s_mid, src);
+  unsigned hits = put_face<S>(outR, fplane, face_index<AX>(c, t, g.nx), lia, G.min_d, G.min_p, s_mid, src);
+  hits += put_face<S>(outL, fplane, face_index<AX>(c + 1, t, g.nx), ria, G.min_d, G.min_p, s_mid, src);
   if (c == 0) {
-    if (g.bc == OUTFLOW) put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), lia, G.min_d, G.min_p, s_lo, src);
-    else put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), lia, G.min_d, G.min_p, s_hi, src);
+    if (g.bc == OUTFLOW) hits += put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), lia, G.min_d, G.min_p, s_lo, src);
+    else hits += put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), lia, G.min_d, G.min_p, s_hi, src);
   }
   if (c == Ls - 1) {
-    if (g.bc == OUTFLOW) put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), ria, G.min_d, G.min_p, s_hi, src);
-    else put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), ria, G.min_d, G.min_p, s_lo, src);
+    if (g.bc == OUTFLOW) hits += put_face<S>(outR, fplane, face_index<AX>(Ls, t, g.nx), ria, G.min_d, G.min_p, s_hi, src);
+    else hits += put_face<S>(outL, fplane, face_index<AX>(0, t, g.nx), ria, G.min_d, G.min_p, s_lo, src);
   }
+  note_floor_hits(G, hits);
 }
 
 // ----------------------------------------------------------------------------
@@ -652,6 +665,7 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
 
   double* Wout[2] = {AX == 0 ? G.xl : G.yl, AX == 0 ? G.xr : G.yr};
   double* Uout[2] = {AX == 0 ? G.uxl : G.uyl, AX == 0 ? G.uxr : G.uyr};
+  unsigned hits = 0;
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
     double w[7], u[7];
@@ -719,8 +733,8 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
                                    : (-half_dtdt * (fh[k] - flo[k]) + half_dt * src[k]);
       u[k] = u[k] + corr;
     }
-    if (dlt(u[0], G.min_d)) u[0] = G.min_d;
-    if (dlt(u[6], G.min_e)) u[6] = G.min_e;
+    if (dlt(u[0], G.min_d)) { u[0] = G.min_d; ++hits; }
+    if (dlt(u[6], G.min_e)) { u[6] = G.min_e; ++hits; }
     double w2[7];
     cons_to_prim7(u, nb, G.gamma, w2);
 #pragma unroll
@@ -729,6 +743,7 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
       Wout[side][k * nf + fl] = w2[k];
     }
   }
+  note_floor_hits(G, hits);
 }
 
 // Hydro CTU (Source/EvolveFunctions_Hydro.py:460-489): cons -= half dt/dn * transverse
@@ -844,11 +859,16 @@ __device__ __forceinline__ void b_final_mhd(const Grid& G, const StateBuf& in, c
   cons_to_prim7(u, cbx, G.gamma, w);
   const double po[8] = {w[0], w[1], w[2], w[3], cbx, w[4], w[5], w[6]};
   const double co[8] = {u[0], u[1], u[2], u[3], cbx, u[4], u[5], u[6]};
+  bool bad = false;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     out.prim[k * plane + idx] = po[k];
     out.cons[k * plane + idx] = co[k];
+    bad |= is_nonfinite(co[k]) | is_nonfinite(po[k]);
   }
+  if (i == nx - 1) bad |= is_nonfinite(bxr);
+  if (j == ny - 1) bad |= is_nonfinite(byb);
+  note_nonfinite(G, bad | is_nonfinite(bxl) | is_nonfinite(byt));
 }
 
 __device__ __forceinline__ void b_final_hydro(const Grid& G, const StateBuf& in, const StateBuf& out, int i,
@@ -871,11 +891,14 @@ __device__ __forceinline__ void b_final_hydro(const Grid& G, const StateBuf& in,
     u[k] = v;
   }
   hcons_to_prim<0>(u, G.gamma, w);
+  bool bad = false;
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     out.prim[k * plane + idx] = w[k];
     out.cons[k * plane + idx] = u[k];
+    bad |= is_nonfinite(u[k]) | is_nonfinite(w[k]);
   }
+  note_nonfinite(G, bad);
 }
 
 // ----------------------------------------------------------------------------
@@ -1101,24 +1124,30 @@ __global__ void __launch_bounds__(kBlock) k_update_1d(Grid G, StateBuf in, State
     for (int k = 0; k < 7; ++k)
       u[k] = __ldg(in.cons + src[k] * plane + i) - dtdx * (G.fx[k * fp + i + 1] - G.fx[k * fp + i]);
     cons_to_prim7(u, G.bx1d, G.gamma, w);
+    bool bad = false;
 #pragma unroll
     for (int k = 0; k < 7; ++k) {
       out.prim[src[k] * plane + i] = w[k];
       out.cons[src[k] * plane + i] = u[k];
+      bad |= is_nonfinite(u[k]) | is_nonfinite(w[k]);
     }
     out.prim[4 * plane + i] = G.bx1d;
     out.cons[4 * plane + i] = G.bx1d;
+    note_nonfinite(G, bad);
   } else {
     double u[5], w[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k)
       u[k] = __ldg(in.cons + k * plane + i) - dtdx * (G.fx[k * fp + i + 1] - G.fx[k * fp + i]);
     hcons_to_prim<0>(u, G.gamma, w);
+    bool bad = false;
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       out.prim[k * plane + i] = w[k];
       out.cons[k * plane + i] = u[k];
+      bad |= is_nonfinite(u[k]) | is_nonfinite(w[k]);
     }
+    note_nonfinite(G, bad);
   }
 }
 

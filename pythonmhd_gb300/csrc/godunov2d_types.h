@@ -70,7 +70,8 @@ struct Grid {
   double* eig_y;               // can run at once)
   size_t ext_plane;            // plane stride of slopes / eig (max of x/y extended sizes)
   LoopState* loop;             // device
-  int* status;                 // device error word (0 = ok)
+  int* status;                 // device error word (0 = ok; kStatusNonfinite, kStatusIndex bits)
+  unsigned long long* floor_hits;  // device count of floored values (may be null)
   // 1D grids (ny = 1): the x sweep only, no transverse or CT stages; MHD keeps
   // B_x uniform at bx1d (the reference's evolve_1D_mhd)
   int one_d;
@@ -80,6 +81,10 @@ struct Grid {
   double* dt_log;
   long long dt_log_cap;
 };
+
+// bits of the device error word Grid::status
+constexpr int kStatusNonfinite = 1;  // a NaN or Inf was written to the state by a cycle
+constexpr int kStatusIndex = 2;      // checked builds: an index fell outside its array
 
 // index spaces of the batched work lists
 enum Space : int { SPACE_CELL = 0, SPACE_EXT_X, SPACE_EXT_Y, SPACE_XFACE, SPACE_YFACE, SPACE_CORNER, kNumSpaces };

@@ -43,6 +43,10 @@ __device__ __forceinline__ bool is_nonneg(double x) { return okey(x) >= 0; }    
 __device__ __forceinline__ bool is_zero(double x) {                             // x == 0
   return (static_cast<unsigned long long>(dbits(x)) << 1) == 0ULL;
 }
+// x is NaN or +-Inf (exponent field all ones), tested on the integer pipe
+__device__ __forceinline__ bool is_nonfinite(double x) {
+  return (static_cast<unsigned long long>(dbits(x)) & 0x7ff0000000000000ULL) == 0x7ff0000000000000ULL;
+}
 __device__ __forceinline__ bool dgt(double a, double b) { return okey(a) > okey(b); }  // a > b
 __device__ __forceinline__ bool dlt(double a, double b) { return okey(a) < okey(b); }  // a < b
 

@@ -149,6 +149,39 @@ class Grid2D:
         _lib.check(self.lib.mhd2d_device_bytes(self._h, ctypes.byref(n)), "mhd2d_device_bytes")
         return n.value
 
+    def validate(self):
+        """Counts of the current state's bad values (``mhd2d_validate``)."""
+        c = np.zeros(7, dtype=np.int64)
+        _lib.check(self.lib.mhd2d_validate(self._h, c.ctypes.data), "mhd2d_validate")
+        keys = ("nonfinite", "density_negative", "density_low", "pressure_negative", "pressure_low",
+                "energy_negative", "energy_low")
+        return dict(zip(keys, (int(x) for x in c)))
+
+    def check_state(self):
+        """Raise RuntimeError as the reference's validatePrimVars would
+        (Source/SimulationGrid_HelperModule.py:282-410): negative values before
+        values below the floor, density before pressure before energy; a NaN or
+        Inf anywhere is reported first."""
+        c = self.validate()
+        if c["nonfinite"]:
+            raise RuntimeError(f"{c['nonfinite']} cells of the state hold a NaN or Inf value")
+        names = (("density", "primitive"), ("pressure", "primitive"), ("energy", "conservative"))
+        for name, kind in names:
+            if c[f"{name}_negative"]:
+                raise RuntimeError(f"You have at least one negative {name} value in your {kind} variables matrix "
+                                   f"({c[name + '_negative']} values).")
+            if c[f"{name}_low"]:
+                raise RuntimeError(f"You have at least one {name} value in your {kind} variables matrix that is "
+                                   f"less than the minimum {name} value for the simulation "
+                                   f"({c[name + '_low']} values).")
+
+    def stats(self):
+        """Failure counters since the last upload: ``{"floor_hits": n, "nan": bool}``."""
+        hits = ctypes.c_longlong()
+        nan = ctypes.c_int()
+        _lib.check(self.lib.mhd2d_stats(self._h, ctypes.byref(hits), ctypes.byref(nan)), "mhd2d_stats")
+        return {"floor_hits": hits.value, "nan": bool(nan.value)}
+
     def state_ptrs(self, which=0):
         ptrs = [ctypes.c_void_p() for _ in range(4)]
         _lib.check(self.lib.mhd2d_state_ptrs(self._h, int(which), *[ctypes.byref(p) for p in ptrs]),
@@ -396,6 +429,27 @@ class Batch2D:
             err.instance_status = self.instance_status() if rc == 5 else None
             raise err
         return t_out, c_out
+
+    def get_tiles(self, space):
+        """The installed work list of an index space as an (n, 4) int32 array."""
+        n = ctypes.c_longlong()
+        _lib.check(self.lib.mhdb_get_tiles(self._h, int(space), None, 0, ctypes.byref(n)), "mhdb_get_tiles")
+        t = np.zeros((n.value, 4), dtype=np.int32)
+        _lib.check(self.lib.mhdb_get_tiles(self._h, int(space), t.ctypes.data, n.value, ctypes.byref(n)),
+                   "mhdb_get_tiles")
+        return t
+
+    def set_tiles(self, space, tiles):
+        """Install a caller's order of an index space's work list (checked on the host)."""
+        t = np.ascontiguousarray(tiles, dtype=np.int32).reshape(-1, 4)
+        _lib.check(self.lib.mhdb_set_tiles(self._h, int(space), t.ctypes.data, len(t)), "mhdb_set_tiles")
+
+    def stats(self):
+        """Per-instance failure counters since each upload: (floor_hits, nan flags)."""
+        hits = np.zeros(self.count, dtype=np.int64)
+        nan = np.zeros(self.count, dtype=np.int32)
+        _lib.check(self.lib.mhdb_stats(self._h, hits.ctypes.data, nan.ctypes.data), "mhdb_stats")
+        return hits, nan.astype(bool)
 
     def instance_status(self):
         """Per-instance status of the last advance (0 ok, 5 the time or dt went non-finite)."""

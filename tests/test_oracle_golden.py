@@ -166,3 +166,38 @@ def test_oracle_3d_mhd_40_cycles_vs_reference():
     assert int(r[6]) == int(o["cycle"]) == m.CYCLES
     for k, v in zip(m.KEYS[:5], r[:5]):
         assert _field_rel(v, o[k]) <= 1e-12, k
+
+
+def _floor_counts():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "floor_counts.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("path", golden_files("mhd") + golden_files("hydro") + golden_files("mhd1d")
+                         + golden_files("hydro1d"), ids=case_id)
+def test_oracle_floor_tally_matches_reference_counts(path):
+    """The oracle's floor tally equals the number of values the reference's own floor
+    routine raised on the same case (tests/golden/make_floor_counts.py wraps
+    Source/PrimCons_HelperModule.py:499-554 to count them)."""
+    from oracle import common, evolve1d
+    name = case_id(path)
+    p, i, _ = load(path)
+    common.reset_floor_tally()
+    tail = (p["t_start"], p["t_end"], p["start_cycle"], p["max_cycles"], p["gamma"], p["cfl"], p["min_d"],
+            p["min_p"], p["min_e"], p["order"], p["efix"], p["eps"])
+    if name.startswith("mhd1d"):
+        evolve1d.evolve_mhd(i["prim"], i["cons"], p["dx"], p["bcx"], *tail)
+    elif name.startswith("hydro1d"):
+        evolve1d.evolve_hydro(i["prim"], i["cons"], p["dx"], p["bcx"], *tail)
+    elif name.startswith("mhd"):
+        mhd2d.evolve(i["prim"], i["cons"], i["fbx"], i["fby"], p["dx"], p["dy"], p["bcx"], p["bcy"], *tail)
+    else:
+        hydro2d.evolve(i["prim"], i["cons"], p["dx"], p["dy"], p["bcx"], p["bcy"], *tail)
+    assert common.floor_tally() == _floor_counts()[name]
+
+
+def test_floor_counts_cover_the_floor_cases():
+    c = _floor_counts()
+    assert c["mhd_floors"] > 0 and c["hydro_floors"] > 0 and c["mhd1d_floors"] > 0
