@@ -150,3 +150,65 @@ def test_3d_mhd_driver_matches_oracle_driver(t_lim, save_dt, plot_dt, order):
             assert np.array_equal(a, b)
     for a, b in zip(final, final_w):
         assert np.array_equal(a, b)
+
+
+def _driver_cases():
+    from tests.test_oracle_golden import _driver_digests
+    return sorted(_driver_digests())
+
+
+@pytest.mark.parametrize("case", _driver_cases())
+def test_device_driver_matches_the_reference_driver(case):
+    """mhd2d_run against the reference's own Simulation.run() (digests recorded by
+    tests/golden/make_driver_digests.py): every stop's time, cycle, kind and state and the
+    final state, bit for bit."""
+    from tests.test_oracle_golden import run_driver_case
+
+    def run(state, w, sp, pp):
+        mhd = len(state) == 4
+        ny, nx = state[0].shape[1:]
+        g = Grid2D(ny, nx, w["dx"], w["dy"], w["bcx"], w["bcy"], w["gamma"], mhd=mhd,
+                   recon=2 if w["order"] == 2 else 0, arith="exact")
+        got = []
+        try:
+            g.upload(*state)
+            t, cyc, _ = driver.run(g, w["t_lim"], w["max_cycles"], w["cfl"], save_dt=w["save_dt"], save_prec=sp,
+                                   plot_dt=w["plot_dt"], plot_prec=pp,
+                                   on_stop=lambda t, c, k, grid: got.append((t, c, k, grid.download())))
+            return t, cyc, got, g.download()
+        finally:
+            g.close()
+
+    run_driver_case(case, run)
+
+
+@pytest.mark.parametrize("case", _driver_cases())
+def test_dropin_evolve_under_the_driver_loop_matches_the_reference_driver(case):
+    """The drop-in evolve functions (evolve_2D_mhd / evolve_2D_hydro on the GPU), called by
+    the driver loop as Source/Simulation.py:345-413 calls them (the oracle's restatement
+    of that loop, itself pinned to the reference's runs), reproduce the reference's stops."""
+    from types import SimpleNamespace
+
+    from pythonmhd_gb300 import evolve
+    from tests.test_oracle_golden import run_driver_case
+
+    def run(state, w, sp, pp):
+        mhd = len(state) == 4
+        ny, nx = state[0].shape[1:]
+
+        def step(st, t0, t_end, cyc0):
+            g = SimpleNamespace(primVars=st[0], consVars=st[1], dx=w["dx"], dy=w["dy"], BcX=w["bcx"], BcY=w["bcy"],
+                                numXCells=nx, numYCells=ny)
+            if mhd:
+                g.faceBx, g.faceBy = st[2], st[3]
+                r = evolve.evolve_2D_mhd(g, t0, t_end, cyc0, w["max_cycles"], w["gamma"], w["cfl"], 1e-12, 1e-12,
+                                         1e-12, w["order"], False, 0.5, arith="exact")
+                return tuple(np.copy(a) for a in r[:4]), r[4], r[5], tuple(r[6:10]), r[10]
+            r = evolve.evolve_2D_hydro(g, t0, t_end, cyc0, w["max_cycles"], w["gamma"], w["cfl"], 1e-12, 1e-12,
+                                       1e-12, w["order"], False, 0.5, arith="exact")
+            return tuple(np.copy(a) for a in r[:2]), r[2], r[3], tuple(r[4:6]), r[6]
+
+        return odriver._drive(tuple(a.copy() for a in state), step, w["t_lim"], w["max_cycles"], w["save_dt"], sp,
+                              w["plot_dt"], pp)
+
+    run_driver_case(case, run)

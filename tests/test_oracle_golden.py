@@ -201,3 +201,45 @@ def test_oracle_floor_tally_matches_reference_counts(path):
 def test_floor_counts_cover_the_floor_cases():
     c = _floor_counts()
     assert c["mhd_floors"] > 0 and c["hydro_floors"] > 0 and c["mhd1d_floors"] > 0
+
+
+def _driver_digests():
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "driver_digests.json")) as f:
+        return json.load(f)
+
+
+def run_driver_case(case, run_fn):
+    """Run one of the reference driver's recorded workloads with ``run_fn(state, w, save_prec,
+    plot_prec)`` -> (t, cycle, stops [(t, cycle, kinds, state)], final_state) and compare
+    every stop and the end with the reference's digests."""
+    from pythonmhd_gb300 import driver
+    from tests.golden import make_driver_digests as mdd
+    want = _driver_digests()[case]
+    w = want["workload"]
+    state, dx, dy, bcx, bcy = mdd.initial_state(case)
+    state = tuple(a for a in state if a is not None)
+    assert mdd.digest(*state) == want["initial_sha256"]
+    sp = driver.time_precision(w["save_dt"], w["t_lim"]) if w["save_dt"] > 0 else 0
+    pp = driver.time_precision(w["plot_dt"], w["t_lim"]) if w["plot_dt"] > 0 else 0
+    t, cyc, stops, final = run_fn(state, w, sp, pp)
+    got = [{"t": float(s[0]), "cycle": int(s[1]), "kinds": int(s[2]), "sha256": mdd.digest(*s[3])} for s in stops]
+    assert got == want["stops"]
+    assert {"t": float(t), "cycle": int(cyc), "sha256": mdd.digest(*final)} == want["final"]
+
+
+@pytest.mark.parametrize("case", sorted(_driver_digests()))
+def test_oracle_driver_matches_the_reference_driver(case):
+    """oracle/driver.py against the reference's own Simulation.run() (Source/Simulation.py:
+    277-434, run headless by tests/golden/make_driver_digests.py): every stop's time, cycle,
+    kind and state, and the final state, bit for bit."""
+    from oracle import driver as odriver
+
+    def run(state, w, sp, pp):
+        fb = state[2:] if len(state) == 4 else (None, None)
+        return odriver.run(state[0], state[1], fb[0], fb[1], w["dx"], w["dy"], w["bcx"], w["bcy"], w["t_lim"],
+                           w["max_cycles"], w["gamma"], w["cfl"], 1e-12, 1e-12, 1e-12, w["order"], False, 0.5,
+                           save_dt=w["save_dt"], save_prec=sp, plot_dt=w["plot_dt"], plot_prec=pp)
+
+    run_driver_case(case, run)
