@@ -84,6 +84,19 @@ int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0,
                   long long max_cycles, double cfl, double* t_out, long long* cycle_out,
                   double* t_second_last);
 
+/* Domain decomposition support.  A grid split into blocks over several GPUs
+ * advances each block (with a halo of neighbour cells) on its own handle; all
+ * blocks must use the one global dt, the minimum over blocks of their CFL dts
+ * (exact: dt = cfl / max(speed), and a correctly rounded division is monotone, so
+ * the minimum of the blocks' dts is the dt of the whole grid; the reference takes
+ * the global maximum speed, Source/EvolveFunctions_MHD.py:472-475).
+ * mhd2d_cfl_dt: the CFL dt of the current state before the t_end clip, in the
+ * exact step's arithmetic (2D handles).  mhd2d_advance_dt: one cycle from (t0,
+ * cycle0) with the given dt, clipped to t_end as the step clips its own; t_out
+ * gets the time after it. */
+int mhd2d_cfl_dt(void* handle, double cfl, double* dt);
+int mhd2d_advance_dt(void* handle, double t0, double t_end, long long cycle0, double dt, double* t_out);
+
 /* The reference driver's time loop (Source/Simulation.py:290-413) with the state
  * kept on the device: from t = 0 and cycle 0 it advances to each stop time (the
  * next save every save_dt and plot every plot_dt, rounded to save_prec /
@@ -112,6 +125,10 @@ int mhd2d_set_dt_log(void* handle, double* dt_log, long long capacity);
  * NULL to skip that array. */
 int mhd2d_download(void* handle, int which, double* prim, double* cons,
                    double* faceBx, double* faceBy);
+
+/* mhd2d_download into device memory of the handle's GPU (no host round trip). */
+int mhd2d_download_device(void* handle, int which, double* prim, double* cons,
+                          double* faceBx, double* faceBy);
 
 /* Device pointers of the current state (for zero-copy use from a framework on
  * the same device).  Pointers stay valid until the next advance/upload. */
@@ -300,6 +317,23 @@ int mhd2d_adj_info(void* handle, size_t* state_words, size_t* device_bytes, int*
 int mhd2d_adj_set_tail(void* handle, int max_cycles);
 /* The last record: its cycles, checkpoint interval and tail length (0: none). */
 int mhd2d_adj_record(void* handle, int* steps, int* every, int* tail);
+/* Branch-frozen forward passes, for checking the backward pass by finite
+ * differences.  The discrete step is piecewise smooth: limiter and floor clamps,
+ * the Roe upwind switch, the entropy-fix window, the corner-EMF upwinding and |x|
+ * change branch at kinks, and over hundreds of cycles a perturbation of 1e-6
+ * crosses some of them, so free central differences measure a different piece
+ * than the one the adjoint differentiates.  mode 1 runs `steps` cycles from
+ * state_in with the host dts `dt` and records every branch decision of every
+ * stage (conditions and the sign of each |x|) in the handle; mode 2 runs the same
+ * cycles from another state with each decision replayed from that record, i.e. on
+ * the recorded piece.  Mode 2 from the recorded initial state reproduces mode 1
+ * bit for bit; it needs a record of at least `steps` cycles (else MHD_ERR_STATE).
+ * Both reuse the first value arena, so a pending resident tail of the forward
+ * record is recomputed from its checkpoint by the next mhd2d_adj_backward.  The
+ * record takes 4 bytes x (tape words per cycle) x steps of device memory (about
+ * 92 B per cell and cycle for PLM). */
+int mhd2d_adj_branches(void* handle, int mode, const double* state_in, int steps, const double* dt,
+                       double* state_out);
 void mhd2d_adj_destroy(void* handle);
 
 /* ---------------------------------------------------------------------------

@@ -50,6 +50,10 @@ SIGNATURES = {
                                      ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double)]),
     "mhd2d_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, c_double_p, c_double_p,
                                       c_double_p]),
+    "mhd2d_cfl_dt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "mhd2d_advance_dt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_longlong,
+                                        ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "mhd2d_download_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4),
     "mhd2d_set_dt_log": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]),
     "mhd2d_state_ptrs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_void_p)] * 4),
     "mhd2d_peek": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_size_t]),
@@ -99,6 +103,8 @@ SIGNATURES = {
                                              ctypes.POINTER(ctypes.c_size_t)]),
     "mhd2d_adj_restore": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_double_p]),
     "mhd2d_adj_set_tail": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "mhd2d_adj_branches": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, c_double_p,
+                                          ctypes.c_void_p]),
     "mhd2d_adj_record": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 3),
     "mhd2d_adj_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
                                       ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_int)]),

@@ -39,8 +39,9 @@ STAGES = [
 ]
 
 HEADER = """// GENERATED by pythonmhd_gb300/adjoint/codegen.py from adjoint/stages.py -- do not edit.
-// Forward (<stage>_fwd) and reverse-mode (<stage>_rev) device functions of the
-// pointwise stages of one MHD CTU+CT cycle.
+// Forward (<stage>_fwd), branch-recording / branch-replaying forward (<stage>_fwdb)
+// and reverse-mode (<stage>_rev) device functions of the pointwise stages of one
+// MHD CTU+CT cycle.
 #pragma once
 """
 
@@ -51,7 +52,7 @@ def generate() -> str:
         t = dsl.trace(f"g_{name}", fn, nin, npar, **kw)
         parts.append(f"// ---- {name}: {nin} inputs, {npar} params, {len(t.outputs)} outputs\n")
         parts.append(f"constexpr int g_{name}_NI = {nin}, g_{name}_NP = {max(npar, 1)}, g_{name}_NO = {len(t.outputs)}, "
-                     f"g_{name}_NT = {dsl.tape_words(t)};\n")
+                     f"g_{name}_NT = {dsl.tape_words(t)}, g_{name}_NB = {dsl.branch_words(t)};\n")
         parts.append(dsl.emit_cuda(t))
     return "\n".join(parts)
 

@@ -170,6 +170,19 @@ class Adjoint2D:
         self._ckpt_ref = checkpoints
         self.dts = dts.copy()
 
+    def branches(self, mode, state, dts):
+        """``len(dts)`` cycles from ``state`` with the given dts, recording ("record") or
+        replaying ("replay") every branch decision (``mhd2d_adj_branches``); returns the
+        final packed state.  Replaying from nearby states evaluates the piece of the
+        step the recorded run was on, which is what the backward pass differentiates."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        out = self._new()
+        self._sync()
+        _lib.check(self.lib.mhd2d_adj_branches(self._h, {"record": 1, "replay": 2}[mode], _dptr(state), len(dts),
+                                               dts.ctypes.data_as(_lib.c_double_p), _dptr(out)),
+                   "mhd2d_adj_branches")
+        return out
+
     def backward(self, bar_final):
         """Adjoint of the last :meth:`forward` with respect to its initial state."""
         bar0 = self._new()

@@ -480,6 +480,20 @@ def tape_words(t):
     return len(fl) + (len(bl) + 31) // 32
 
 
+def branch_layout(t):
+    """Every branch decision of a forward sweep, in node order: each live condition
+    node, and the sign of each live |x| (the kink of the absolute value).  A forward
+    sweep that records these bits and one that replays them (``emit_cuda``'s
+    ``_fwdb<1>`` / ``_fwdb<2>``) evaluate the same smooth piece of the function at
+    nearby inputs -- the piece whose derivative the reverse sweep returns."""
+    live = _live_forward(t, set(t.outputs))
+    return [i for i, (op, args, meta, kind) in enumerate(t.nodes) if live[i] and (kind == "b" or op == "abs")]
+
+
+def branch_words(t):
+    return (len(branch_layout(t)) + 31) // 32
+
+
 def emit_cuda(t, reverse=True):
     """CUDA source for one item of a traced function:
 
@@ -504,6 +518,7 @@ def emit_cuda(t, reverse=True):
     for k, o in enumerate(t.outputs):
         out.append(f"  y[{k}] = v{o};")
     out.append("}")
+    out.append(_emit_branch_forward(t, live))
     if not reverse:
         return "\n".join(out) + "\n"
     need = need_out | _reverse_needs_c(t, act)
@@ -580,6 +595,49 @@ def emit_cuda(t, reverse=True):
         out.append(f"  xbar[{k}] = {'b%d' % i if i in declared else '0.0'};")
     out.append("}")
     return "\n".join(out) + "\n"
+
+
+def _emit_branch_forward(t, live):
+    """``<name>_fwdb<MODE>(x, p, y, bt, stride)``: the forward sweep with its branch
+    decisions (``branch_layout``) on a bit tape of 32-bit words at bt[k * stride].
+    MODE 1 records them; MODE 2 replays them -- each condition takes its recorded
+    value and each |x| its recorded sign -- so that the sweep stays on the piece of
+    the function it was on when they were recorded."""
+    bl = branch_layout(t)
+    bslot = {i: (k // 32, k % 32) for k, i in enumerate(bl)}
+    nw = (len(bl) + 31) // 32
+    out = [f"template <int MODE>",
+           f"__device__ __forceinline__ void {t.name}_fwdb(const double* __restrict__ x, "
+           f"const double* __restrict__ p, double* __restrict__ y, unsigned int* __restrict__ bt, size_t stride) {{"]
+    for w in range(nw):
+        out.append(f"  unsigned int bw{w} = MODE == 2 ? bt[{w} * stride] : 0u;")
+    if nw == 0:
+        out.append("  (void)bt; (void)stride;")
+    for v, e, kind in _fwd_lines(t, live, "c"):
+        i = int(v[1:])
+        ty = "double" if kind == "f" else "bool"
+        if i not in bslot:
+            out.append(f"  const {ty} {v} = {e};")
+            continue
+        w, bit = bslot[i]
+        op, args, meta, _ = t.nodes[i]
+        if kind == "b":
+            out.append(f"  const bool {v} = MODE == 2 ? (((bw{w} >> {bit}) & 1u) != 0u) : ({e});")
+            out.append(f"  if (MODE == 1) bw{w} |= (unsigned int){v} << {bit};")
+        else:  # |x|: the sign of x is the decision
+            a = f"v{args[0]}"
+            out.append(f"  const bool s{i} = MODE == 2 ? (((bw{w} >> {bit}) & 1u) != 0u) : dsl_nonneg({a});")
+            out.append(f"  if (MODE == 1) bw{w} |= (unsigned int)s{i} << {bit};")
+            out.append(f"  const double {v} = s{i} ? {a} : -{a};")
+    if nw:
+        out.append("  if (MODE == 1) {")
+        for w in range(nw):
+            out.append(f"    bt[{w} * stride] = bw{w};")
+        out.append("  }")
+    for k, o in enumerate(t.outputs):
+        out.append(f"  y[{k}] = v{o};")
+    out.append("}")
+    return "\n".join(out)
 
 
 def emit_torch(t):

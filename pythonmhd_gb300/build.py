@@ -12,7 +12,8 @@ shared library with a plain C ABI (``include/pythonmhd_gb300.h``):
 * ``csrc/validate.cu``       -- the initial-state check (the reference's validatePrimVars)
 * ``csrc/adjoint.cu``        -- the reverse-mode adjoint of the MHD step; its pointwise
   stage functions (``csrc/adjoint_gen.cuh``) are generated from ``adjoint/stages.py``
-  first
+  first, its stage kernels are in ``csrc/adjoint_kernels.cuh``
+* ``csrc/adjoint_branch.cu`` -- the adjoint's branch-recording / -replaying forward sweep
 """
 from __future__ import annotations
 
@@ -38,6 +39,7 @@ UNITS = [
     ("noalloc.cu", ["-fmad=false"]),
     ("validate.cu", ["-fmad=false"]),
     ("adjoint.cu", []),
+    ("adjoint_branch.cu", []),
 ]
 ADJ_GEN = os.path.join(CSRC, "adjoint_gen.cuh")
 ADJ_PY = os.path.join(PKG, "adjoint")

@@ -21,502 +21,12 @@
 #include <vector>
 
 #include "../../include/pythonmhd_gb300.h"
-#include "adjoint_gen.cuh"
+
+#include "adjoint_kernels.cuh"
 
 namespace {
 
-constexpr int kT = 128;
-// resident blocks per SM the heavy reverse kernels are compiled for (1: up to 255
-// registers a thread; more blocks cap the registers and trade spills for occupancy)
-#ifndef MHD_ADJ_REV_MIN_BLOCKS
-#define MHD_ADJ_REV_MIN_BLOCKS 1
-#endif
-constexpr int kRevMinBlocks = MHD_ADJ_REV_MIN_BLOCKS;
-static_assert(g_plm0_NT == g_plm1_NT && g_roe1_0_NT == g_roe1_1_NT && g_roe2_0_NT == g_roe2_1_NT &&
-                  g_ctu0_NT == g_ctu1_NT && g_ppm0_NT == g_ppm1_NT && g_pslope0_NT == g_pslope1_NT &&
-                  g_roe1_0_efix_NT == g_roe1_1_efix_NT && g_roe2_0_efix_NT == g_roe2_1_efix_NT,
-              "the x and y sweeps of a stage store tapes of the same length");
-
-struct Arr {
-  double* v = nullptr;   // values
-  double* b = nullptr;   // adjoints
-  size_t ps = 0;         // plane stride
-  __device__ __forceinline__ double* pv(int slot, size_t i) const { return v + (size_t)slot * ps + i; }
-  __device__ __forceinline__ double* pb(int slot, size_t i) const { return b + (size_t)slot * ps + i; }
-};
-
-struct Adj {
-  int nx, ny, bcx, bcy, recon, efix;
-  double dx, dy, gamma, eps, min_d, min_p, min_e;
-  double dt;                       // dt of the cycle being processed
-  Arr P, C, FX, FY;                // input state
-  Arr EX, EY;                      // edge states per cell (lia 7 + ria 7), x and y sweeps
-  Arr SX, SY;                      // PPM: limited slopes of the sweep-extended cells
-  Arr XL, XR, YL, YR;              // reconstructed face states
-  Arr F1X, F1Y, EZ, E1, NBX, NBY;  // stage-1 fluxes, cell Ez, corner EMF, half-step faces
-  Arr UXL, UXR, UYL, UYR, WXL, WXR, WYL, WYR;  // CTU-corrected face cons / prim
-  Arr HEZ, F2X, F2Y, E2;           // half-step Ez, stage-2 fluxes and EMF
-  Arr NP, NC, NFX, NFY;            // output state
-  double* red;                     // 2 doubles: CFL maxima (bits)
-  // tapes of the heavy stages (values their reverse sweeps read), plane-major:
-  // PLM per cell and sweep, Roe per face, stage and sweep
-  double* tplm[2];
-  double* troe[2][2];              // [stage-1][axis]
-  double* tctu[2];                 // CTU per (face, side) and sweep
-  double* tslope[2];               // PPM slopes per extended cell and sweep
-};
-
-__device__ __forceinline__ int wrapc(int c, int L, int bc) {
-  if (bc == 1) {
-    int m = c % L;
-    return m < 0 ? m + L : m;
-  }
-  return c < 0 ? 0 : (c >= L ? L - 1 : c);
-}
-
-struct IO {
-  double* v;
-  double* b;
-};
-
-__device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a.pv(slot, i), a.pb(slot, i)}; }
-
-// forward: gather inputs, call fwd, write outputs; reverse: gather inputs, read output
-// adjoints, call rev, scatter input adjoints.
-#define MHD_ADJ_APPLY(NAME, REV, INS, OUTS, PAR)                                  \
-  do {                                                                            \
-    double x_[g_##NAME##_NI];                                                     \
-    _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_) x_[k_] = *INS[k_].v; \
-    if constexpr (!(REV)) {                                                       \
-      double y_[g_##NAME##_NO];                                                   \
-      g_##NAME##_fwd(x_, PAR, y_);                                                \
-      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) *OUTS[k_].v = y_[k_]; \
-    } else {                                                                      \
-      double yb_[g_##NAME##_NO], xb_[g_##NAME##_NI];                              \
-      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) yb_[k_] = *OUTS[k_].b; \
-      g_##NAME##_rev(x_, PAR, yb_, xb_);                                          \
-      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_)               \
-        if (nz(xb_[k_])) atomicAdd(INS[k_].b, xb_[k_]);                          \
-    }                                                                             \
-  } while (0)
-
-// the same with a tape: the forward stores what the reverse reads, the reverse
-// reads it back instead of recomputing the forward
-#define MHD_ADJ_APPLY_T(NAME, REV, INS, OUTS, PAR, TP, ST)                        \
-  do {                                                                            \
-    double x_[g_##NAME##_NI];                                                     \
-    _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_) x_[k_] = *INS[k_].v; \
-    if constexpr (!(REV)) {                                                       \
-      double y_[g_##NAME##_NO];                                                   \
-      g_##NAME##_fwdt(x_, PAR, y_, TP, ST);                                       \
-      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) *OUTS[k_].v = y_[k_]; \
-    } else {                                                                      \
-      double yb_[g_##NAME##_NO], xb_[g_##NAME##_NI];                              \
-      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NO; ++k_) yb_[k_] = *OUTS[k_].b; \
-      g_##NAME##_revt(x_, PAR, yb_, xb_, TP, ST);                                 \
-      _Pragma("unroll") for (int k_ = 0; k_ < g_##NAME##_NI; ++k_)               \
-        if (nz(xb_[k_])) atomicAdd(INS[k_].b, xb_[k_]);                          \
-    }                                                                             \
-  } while (0)
-
-// taped or plain application of a stage
-#define MHD_ADJ_STAGE(NAME, REV, TAPE, INS, OUTS, PAR, TP, ST)                    \
-  do {                                                                            \
-    if constexpr (TAPE) MHD_ADJ_APPLY_T(NAME, REV, INS, OUTS, PAR, TP, ST);       \
-    else MHD_ADJ_APPLY(NAME, REV, INS, OUTS, PAR);                                \
-  } while (0)
-
-// ---------------------------------------------------------------------------
-// stage kernels (REV = false: forward with stored intermediates; true: reverse)
-// ---------------------------------------------------------------------------
-// limited slopes of the sweep-extended cells e = 0 .. L+1 (cell e-1), PPM only
-template <int AX, bool REV, bool TAPE>
-__global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_slope(Adj A) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y;
-  const int Wd = AX == 0 ? A.nx + 2 : A.nx, H = AX == 0 ? A.ny : A.ny + 2;
-  if (col >= Wd || row >= H) return;
-  const int e = AX == 0 ? col : row, t = AX == 0 ? row : col;
-  const int L = AX == 0 ? A.nx : A.ny;
-  const int bc = AX == 0 ? A.bcx : A.bcy;
-  const size_t me = (size_t)row * Wd + col;
-  const int slots[7] = {0, 1, 2, 3, AX == 0 ? 5 : 6, AX == 0 ? 6 : 4, 7};
-  IO in[22];
-  IO out[7];
-#pragma unroll
-  for (int o = -1; o <= 1; ++o) {
-    const int c = wrapc(e - 1 + o, L, bc);
-    const size_t ci = AX == 0 ? (size_t)t * A.nx + c : (size_t)c * A.nx + t;
-#pragma unroll
-    for (int k = 0; k < 7; ++k) in[(o + 1) * 7 + k] = io(A.P, slots[k], ci);
-  }
-  {
-    const int c = wrapc(e - 1, L, bc);
-    in[21] = io(A.P, AX == 0 ? 4 : 5, AX == 0 ? (size_t)t * A.nx + c : (size_t)c * A.nx + t);
-  }
-  const Arr& S = AX == 0 ? A.SX : A.SY;
-#pragma unroll
-  for (int k = 0; k < 7; ++k) out[k] = io(S, k, me);
-  const double par[1] = {A.gamma};
-  double* tp = A.tslope[AX] + me;
-  const size_t st = (size_t)Wd * H;
-  if (AX == 0) MHD_ADJ_STAGE(pslope0, REV, TAPE, in, out, par, tp, st);
-  else MHD_ADJ_STAGE(pslope1, REV, TAPE, in, out, par, tp, st);
-}
-
-// edge states of each cell: first order (copies), PLM, or PPM from the slopes
-template <int AX, bool REV, bool TAPE, int RECON>
-__global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
-  const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
-  if (c0 >= A.nx || t0 >= A.ny) return;
-  const size_t me = (size_t)t0 * A.nx + c0;
-  const Arr& E = AX == 0 ? A.EX : A.EY;
-  const int slots[7] = {0, 1, 2, 3, AX == 0 ? 5 : 6, AX == 0 ? 6 : 4, 7};
-  if constexpr (RECON >= 1) {
-    const int bc = AX == 0 ? A.bcx : A.bcy;
-    IO in[RECON == 1 ? 22 : 43];
-    IO out[14];
-#pragma unroll
-    for (int o = -1; o <= 1; ++o) {
-      const int jj = AX == 0 ? t0 : wrapc(t0 + o, A.ny, bc);
-      const int ii = AX == 0 ? wrapc(c0 + o, A.nx, bc) : c0;
-      const size_t ci = (size_t)jj * A.nx + ii;
-#pragma unroll
-      for (int k = 0; k < 7; ++k) in[(o + 1) * 7 + k] = io(A.P, slots[k], ci);
-    }
-    if constexpr (RECON == 2) {
-      // slopes of cells c-1, c, c+1 sit at extended indices c, c+1, c+2
-      const Arr& S = AX == 0 ? A.SX : A.SY;
-#pragma unroll
-      for (int o = 0; o < 3; ++o) {
-        const size_t si = AX == 0 ? (size_t)t0 * (A.nx + 2) + c0 + o : (size_t)(t0 + o) * A.nx + c0;
-#pragma unroll
-        for (int k = 0; k < 7; ++k) in[21 + o * 7 + k] = io(S, k, si);
-      }
-    }
-    in[RECON == 1 ? 21 : 42] = io(A.P, AX == 0 ? 4 : 5, me);
-#pragma unroll
-    for (int k = 0; k < 14; ++k) out[k] = io(E, k, me);
-    const double par[2] = {A.gamma, A.dt / (AX == 0 ? A.dx : A.dy)};
-    double* tp = A.tplm[AX] + me;
-    const size_t st = (size_t)A.nx * A.ny;
-    if constexpr (RECON == 1) {
-      if (AX == 0) MHD_ADJ_STAGE(plm0, REV, TAPE, in, out, par, tp, st);
-      else MHD_ADJ_STAGE(plm1, REV, TAPE, in, out, par, tp, st);
-    } else {
-      if (AX == 0) MHD_ADJ_STAGE(ppm0, REV, TAPE, in, out, par, tp, st);
-      else MHD_ADJ_STAGE(ppm1, REV, TAPE, in, out, par, tp, st);
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-      if (!REV) {
-        *E.pv(k, me) = *A.P.pv(slots[k], me);
-        *E.pv(7 + k, me) = *A.P.pv(slots[k], me);
-      } else {
-        const double g = *E.pb(k, me) + *E.pb(7 + k, me);
-        if (nz(g)) atomicAdd(A.P.pb(slots[k], me), g);
-      }
-    }
-  }
-}
-
-// launch the reconstruction of both sweeps (PPM: slopes first)
-template <bool REV, bool TAPE>
-void launch_recon(const Adj& A, cudaStream_t s) {
-  const int nx = A.nx, ny = A.ny;
-  const dim3 gc((unsigned)((nx + kT - 1) / kT), (unsigned)ny);
-  const dim3 gsx((unsigned)((nx + 2 + kT - 1) / kT), (unsigned)ny);
-  const dim3 gsy((unsigned)((nx + kT - 1) / kT), (unsigned)(ny + 2));
-  switch (A.recon) {
-    case 0:
-      k_recon<0, REV, TAPE, 0><<<gc, kT, 0, s>>>(A);
-      k_recon<1, REV, TAPE, 0><<<gc, kT, 0, s>>>(A);
-      break;
-    case 1:
-      k_recon<0, REV, TAPE, 1><<<gc, kT, 0, s>>>(A);
-      k_recon<1, REV, TAPE, 1><<<gc, kT, 0, s>>>(A);
-      break;
-    default:
-      if constexpr (!REV) {
-        k_slope<0, false, TAPE><<<gsx, kT, 0, s>>>(A);
-        k_slope<1, false, TAPE><<<gsy, kT, 0, s>>>(A);
-        k_recon<0, false, TAPE, 2><<<gc, kT, 0, s>>>(A);
-        k_recon<1, false, TAPE, 2><<<gc, kT, 0, s>>>(A);
-      } else {
-        k_recon<1, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
-        k_recon<0, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
-        k_slope<1, true, TAPE><<<gsy, kT, 0, s>>>(A);
-        k_slope<0, true, TAPE><<<gsx, kT, 0, s>>>(A);
-      }
-  }
-}
-
-// face states of one sweep: item = (face, side)
-template <int AX, bool REV>
-__global__ void __launch_bounds__(kT) k_face(Adj A) {
-  const int L = AX == 0 ? A.nx : A.ny;
-  const int Wd = AX == 0 ? A.nx + 1 : A.nx;   // row width of the face array
-  const int H = AX == 0 ? A.ny : A.ny + 1;
-  const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y, side = blockIdx.z;
-  if (col >= Wd || row >= H) return;
-  const int f = AX == 0 ? col : row;   // face index along the sweep
-  const int t = AX == 0 ? row : col;   // transverse index
-  const int bc = AX == 0 ? A.bcx : A.bcy;
-  int cell, sd, vc, f1, f2;
-  if (side == 0) {
-    if (bc == 0) {
-      cell = f == 0 ? 0 : f - 1; sd = f == 0 ? 0 : 7;
-      vc = f == 0 ? 0 : f - 1; f1 = f == 0 ? 0 : f - 1; f2 = f == 0 ? 0 : f;
-    } else {
-      cell = f == 0 ? L - 1 : f - 1; sd = 7;
-      vc = cell; f1 = f == 0 ? L - 1 : f - 1; f2 = f;
-    }
-  } else {
-    if (bc == 0) {
-      cell = f == L ? L - 1 : f; sd = f == L ? 7 : 0;
-      vc = cell; f1 = f == L ? L : f; f2 = f == L ? L : f + 1;
-    } else {
-      cell = f == L ? 0 : f; sd = 0;
-      vc = cell; f1 = f == L ? L : f; f2 = f == L ? 1 : f + 1;
-    }
-  }
-  const Arr& E = AX == 0 ? A.EX : A.EY;
-  const Arr& FB = AX == 0 ? A.FX : A.FY;
-  const Arr& OUT = AX == 0 ? (side == 0 ? A.XL : A.XR) : (side == 0 ? A.YL : A.YR);
-  const size_t ci = AX == 0 ? (size_t)t * A.nx + cell : (size_t)cell * A.nx + t;
-  const size_t vi = AX == 0 ? (size_t)t * A.nx + vc : (size_t)vc * A.nx + t;
-  const size_t fi1 = AX == 0 ? (size_t)t * (A.nx + 1) + f1 : (size_t)f1 * A.nx + t;
-  const size_t fi2 = AX == 0 ? (size_t)t * (A.nx + 1) + f2 : (size_t)f2 * A.nx + t;
-  const size_t me = (size_t)row * Wd + col;
-  IO in[10];
-  IO out[7];
-#pragma unroll
-  for (int k = 0; k < 7; ++k) in[k] = io(E, sd + k, ci);
-  in[7] = io(A.P, AX == 0 ? 2 : 1, vi);
-  in[8] = io(FB, 0, fi1);
-  in[9] = io(FB, 0, fi2);
-#pragma unroll
-  for (int k = 0; k < 7; ++k) out[k] = io(OUT, k, me);
-  const double par[4] = {A.min_d, A.min_p, 0.5 * A.dt, 1.0 / (AX == 0 ? A.dx : A.dy)};
-  if (AX == 0) MHD_ADJ_APPLY(face0, REV, in, out, par);
-  else MHD_ADJ_APPLY(face1, REV, in, out, par);
-}
-
-template <int AX, int STAGE, bool REV, bool TAPE>
-__global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_roe(Adj A) {
-  const size_t nf = AX == 0 ? (size_t)(A.nx + 1) * A.ny : (size_t)A.nx * (A.ny + 1);
-  const size_t f = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= nf) return;
-  const Arr& WL = STAGE == 1 ? (AX == 0 ? A.XL : A.YL) : (AX == 0 ? A.WXL : A.WYL);
-  const Arr& WR = STAGE == 1 ? (AX == 0 ? A.XR : A.YR) : (AX == 0 ? A.WXR : A.WYR);
-  const Arr& BN = STAGE == 1 ? (AX == 0 ? A.FX : A.FY) : (AX == 0 ? A.NBX : A.NBY);
-  const Arr& F = STAGE == 1 ? (AX == 0 ? A.F1X : A.F1Y) : (AX == 0 ? A.F2X : A.F2Y);
-  const double par[2] = {A.gamma, A.eps};
-  double* tp = A.troe[STAGE - 1][AX] + f;
-  IO out[7];
-#pragma unroll
-  for (int k = 0; k < 7; ++k) out[k] = io(F, k, f);
-  if (STAGE == 1) {
-    IO in[15];
-#pragma unroll
-    for (int k = 0; k < 7; ++k) { in[k] = io(WL, k, f); in[7 + k] = io(WR, k, f); }
-    in[14] = io(BN, 0, f);
-    if (A.efix) {
-      if (AX == 0) MHD_ADJ_STAGE(roe1_0_efix, REV, TAPE, in, out, par, tp, nf);
-      else MHD_ADJ_STAGE(roe1_1_efix, REV, TAPE, in, out, par, tp, nf);
-    } else {
-      if (AX == 0) MHD_ADJ_STAGE(roe1_0, REV, TAPE, in, out, par, tp, nf);
-      else MHD_ADJ_STAGE(roe1_1, REV, TAPE, in, out, par, tp, nf);
-    }
-  } else {
-    const Arr& UL = AX == 0 ? A.UXL : A.UYL;
-    const Arr& UR = AX == 0 ? A.UXR : A.UYR;
-    IO in[29];
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-      in[k] = io(WL, k, f); in[7 + k] = io(WR, k, f);
-      in[14 + k] = io(UL, k, f); in[21 + k] = io(UR, k, f);
-    }
-    in[28] = io(BN, 0, f);
-    if (A.efix) {
-      if (AX == 0) MHD_ADJ_STAGE(roe2_0_efix, REV, TAPE, in, out, par, tp, nf);
-      else MHD_ADJ_STAGE(roe2_1_efix, REV, TAPE, in, out, par, tp, nf);
-    } else {
-      if (AX == 0) MHD_ADJ_STAGE(roe2_0, REV, TAPE, in, out, par, tp, nf);
-      else MHD_ADJ_STAGE(roe2_1, REV, TAPE, in, out, par, tp, nf);
-    }
-  }
-}
-
-template <bool REV>
-__global__ void __launch_bounds__(kT) k_ez(Adj A) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (i >= A.nx || j >= A.ny) return;
-  const size_t me = (size_t)j * A.nx + i;
-  IO in[4] = {io(A.P, 2, me), io(A.P, 4, me), io(A.P, 1, me), io(A.P, 5, me)};
-  IO out[1] = {io(A.EZ, 0, me)};
-  const double* par = nullptr;
-  MHD_ADJ_APPLY(ez, REV, in, out, par);
-}
-
-template <int STAGE, bool REV>
-__global__ void __launch_bounds__(kT) k_emf(Adj A) {
-  const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y;
-  const int nx = A.nx, ny = A.ny;
-  if (I > nx || J > ny) return;
-  const Arr& FXa = STAGE == 1 ? A.F1X : A.F2X;
-  const Arr& FYa = STAGE == 1 ? A.F1Y : A.F2Y;
-  const Arr& EZa = STAGE == 1 ? A.EZ : A.HEZ;
-  const Arr& OUT = STAGE == 1 ? A.E1 : A.E2;
-  const int ic = wrapc(I, nx, A.bcx), im = wrapc(I - 1, nx, A.bcx);
-  const int jc = wrapc(J, ny, A.bcy), jm = wrapc(J - 1, ny, A.bcy);
-  IO in[12] = {io(FYa, 0, (size_t)J * nx + im), io(FYa, 5, (size_t)J * nx + im),
-               io(FYa, 0, (size_t)J * nx + ic), io(FYa, 5, (size_t)J * nx + ic),
-               io(FXa, 0, (size_t)jc * (nx + 1) + I), io(FXa, 4, (size_t)jc * (nx + 1) + I),
-               io(FXa, 0, (size_t)jm * (nx + 1) + I), io(FXa, 4, (size_t)jm * (nx + 1) + I),
-               io(EZa, 0, (size_t)jc * nx + ic), io(EZa, 0, (size_t)jc * nx + im),
-               io(EZa, 0, (size_t)jm * nx + ic), io(EZa, 0, (size_t)jm * nx + im)};
-  IO out[1] = {io(OUT, 0, (size_t)J * (nx + 1) + I)};
-  const double* par = nullptr;
-  MHD_ADJ_APPLY(emf, REV, in, out, par);
-}
-
-// half-step (FULL=false, from E1 into NBX/NBY) or full-step (FULL=true, from E2 into NFX/NFY) faces
-template <int AX, bool FULL, bool REV>
-__global__ void __launch_bounds__(kT) k_fhalf(Adj A) {
-  const int nx = A.nx, ny = A.ny;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  const int w = AX == 0 ? nx + 1 : nx, h = AX == 0 ? ny : ny + 1;
-  if (i >= w || j >= h) return;
-  const Arr& E = FULL ? A.E2 : A.E1;
-  const size_t me = (size_t)j * w + i;
-  const size_t cw = nx + 1;
-  if (AX == 0) {
-    IO in[3] = {io(A.FX, 0, me), io(E, 0, (size_t)(j + 1) * cw + i), io(E, 0, (size_t)j * cw + i)};
-    IO out[1] = {io(FULL ? A.NFX : A.NBX, 0, me)};
-    const double par[1] = {FULL ? A.dt / A.dy : 0.5 * (A.dt / A.dy)};
-    MHD_ADJ_APPLY(fhx, REV, in, out, par);
-  } else {
-    IO in[3] = {io(A.FY, 0, me), io(E, 0, (size_t)j * cw + i + 1), io(E, 0, (size_t)j * cw + i)};
-    IO out[1] = {io(FULL ? A.NFY : A.NBY, 0, me)};
-    const double par[1] = {FULL ? A.dt / A.dx : 0.5 * (A.dt / A.dx)};
-    MHD_ADJ_APPLY(fhy, REV, in, out, par);
-  }
-}
-
-template <int AX, bool REV, bool TAPE>
-__global__ void __launch_bounds__(kT) k_ctu(Adj A) {
-  const int nx = A.nx, ny = A.ny;
-  const int Wd = AX == 0 ? nx + 1 : nx, H = AX == 0 ? ny : ny + 1;
-  const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y, side = blockIdx.z;
-  if (col >= Wd || row >= H) return;
-  const int f = AX == 0 ? col : row, t = AX == 0 ? row : col;
-  const int L = AX == 0 ? nx : ny;
-  const int bc = AX == 0 ? A.bcx : A.bcy;
-  const size_t me = (size_t)row * Wd + col;
-  const int kpad = f + side;
-  int scell, lb, rb;
-  if (AX == 0) {
-    scell = wrapc(kpad - 1, L, bc);
-    if (bc == 0) { lb = kpad - 1 < 0 ? 0 : (kpad - 1 > L ? L : kpad - 1); rb = kpad > L ? L : kpad; }
-    else { lb = kpad == 0 ? L - 1 : kpad - 1; rb = kpad == L + 1 ? 1 : kpad; }
-  } else {
-    if (bc == 0) {
-      scell = kpad == 0 ? 1 : (kpad - 1 > L - 1 ? L - 1 : kpad - 1);
-      lb = kpad == 0 ? 1 : kpad - 1; rb = kpad == L + 1 ? L - 1 : kpad;
-    } else {
-      scell = wrapc(kpad - 1, L, bc);
-      lb = kpad == 0 ? L - 1 : kpad - 1; rb = kpad == L + 1 ? 1 : kpad;
-    }
-  }
-  const int fc = wrapc(f - 1 + side, L, bc);
-  const Arr& W = AX == 0 ? (side == 0 ? A.XL : A.XR) : (side == 0 ? A.YL : A.YR);
-  const Arr& U = AX == 0 ? (side == 0 ? A.UXL : A.UXR) : (side == 0 ? A.UYL : A.UYR);
-  const Arr& W2 = AX == 0 ? (side == 0 ? A.WXL : A.WXR) : (side == 0 ? A.WYL : A.WYR);
-  const Arr& FB = AX == 0 ? A.FX : A.FY;
-  const Arr& NB = AX == 0 ? A.NBX : A.NBY;
-  const Arr& FT = AX == 0 ? A.F1Y : A.F1X;
-  size_t hi, lo, si, lbi, rbi;
-  if (AX == 0) {
-    hi = (size_t)(t + 1) * nx + fc; lo = (size_t)t * nx + fc;
-    si = (size_t)t * nx + scell;
-    lbi = (size_t)t * (nx + 1) + lb; rbi = (size_t)t * (nx + 1) + rb;
-  } else {
-    hi = (size_t)fc * (nx + 1) + t + 1; lo = (size_t)fc * (nx + 1) + t;
-    si = (size_t)scell * nx + t;
-    lbi = (size_t)lb * nx + t; rbi = (size_t)rb * nx + t;
-  }
-  IO in[29];
-  IO out[14];
-#pragma unroll
-  for (int k = 0; k < 7; ++k) in[k] = io(W, k, me);
-  in[7] = io(FB, 0, me);
-#pragma unroll
-  for (int k = 0; k < 7; ++k) { in[8 + k] = io(FT, k, hi); in[15 + k] = io(FT, k, lo); }
-  in[22] = io(A.P, 4, si); in[23] = io(A.P, 5, si); in[24] = io(A.P, 6, si); in[25] = io(A.P, 3, si);
-  in[26] = io(FB, 0, lbi); in[27] = io(FB, 0, rbi);
-  in[28] = io(NB, 0, me);
-#pragma unroll
-  for (int k = 0; k < 7; ++k) { out[k] = io(U, k, me); out[7 + k] = io(W2, k, me); }
-  const double par[6] = {A.gamma, 0.5 * A.dt, 1.0 / (AX == 0 ? A.dx : A.dy),
-                         0.5 * (A.dt / (AX == 0 ? A.dy : A.dx)), A.min_d, A.min_e};
-  const size_t nf = (size_t)H * Wd;
-  double* tp = A.tctu[AX] + side * nf + me;
-  if (AX == 0) MHD_ADJ_STAGE(ctu0, REV, TAPE, in, out, par, tp, 2 * nf);
-  else MHD_ADJ_STAGE(ctu1, REV, TAPE, in, out, par, tp, 2 * nf);
-}
-
-template <bool REV>
-__global__ void __launch_bounds__(kT) k_half(Adj A) {
-  const int nx = A.nx;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (i >= nx || j >= A.ny) return;
-  const size_t me = (size_t)j * nx + i;
-  const size_t xl = (size_t)j * (nx + 1) + i, yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
-  IO in[19];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    in[k] = io(A.C, k, me);
-    in[3 + k] = io(A.F1X, k, xl);
-    in[6 + k] = io(A.F1X, k, xl + 1);
-    in[9 + k] = io(A.F1Y, k, yt);
-    in[12 + k] = io(A.F1Y, k, yb);
-  }
-  in[15] = io(A.NBX, 0, xl); in[16] = io(A.NBX, 0, xl + 1);
-  in[17] = io(A.NBY, 0, yt); in[18] = io(A.NBY, 0, yb);
-  IO out[1] = {io(A.HEZ, 0, me)};
-  const double par[2] = {0.5 * (A.dt / A.dx), 0.5 * (A.dt / A.dy)};
-  MHD_ADJ_APPLY(half, REV, in, out, par);
-}
-
-template <bool REV>
-__global__ void __launch_bounds__(kT) k_final(Adj A) {
-  const int nx = A.nx;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (i >= nx || j >= A.ny) return;
-  const size_t me = (size_t)j * nx + i;
-  const size_t xl = (size_t)j * (nx + 1) + i, yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
-  const size_t cw = nx + 1;
-  const int xs[7] = {0, 1, 2, 3, 5, 6, 7};
-  IO in[43];
-  in[0] = io(A.FX, 0, xl); in[1] = io(A.FX, 0, xl + 1);
-  in[2] = io(A.FY, 0, yt); in[3] = io(A.FY, 0, yb);
-  in[4] = io(A.E2, 0, (size_t)j * cw + i); in[5] = io(A.E2, 0, (size_t)(j + 1) * cw + i);
-  in[6] = io(A.E2, 0, (size_t)j * cw + i + 1); in[7] = io(A.E2, 0, (size_t)(j + 1) * cw + i + 1);
-#pragma unroll
-  for (int k = 0; k < 7; ++k) {
-    in[8 + k] = io(A.C, xs[k], me);
-    in[15 + k] = io(A.F2X, k, xl);
-    in[22 + k] = io(A.F2X, k, xl + 1);
-    in[29 + k] = io(A.F2Y, k, yt);
-    in[36 + k] = io(A.F2Y, k, yb);
-  }
-  IO out[16];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) { out[k] = io(A.NP, k, me); out[8 + k] = io(A.NC, k, me); }
-  const double par[3] = {A.dt / A.dx, A.dt / A.dy, A.gamma};
-  MHD_ADJ_APPLY(final, REV, in, out, par);
-}
+using namespace mhdadj;
 
 // ---------------------------------------------------------------------------
 // CFL dt of the input state (Source/TimestepCalculations_HelperModule.py:239-289)
@@ -577,6 +87,7 @@ __global__ void k_cfl_finish(Adj A, double cfl, double* dt_slot) {
   A.red[1] = 0.0;
 }
 
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -631,6 +142,11 @@ struct Handle {
   size_t ckpt_bytes = 0, seg_bytes = 0;
   size_t state_words = 0;
   void* solver = nullptr;      // exact-arithmetic production step: the CFL forward pass
+  // branch arena of the branch-recording / -replaying forward sweeps: BW words per
+  // cycle (offsets btoff per stage slot), recorded for br_steps cycles
+  unsigned int* br = nullptr;
+  size_t br_cap = 0, BW = 0, btoff[kNumBt] = {};
+  int br_steps = 0;
 };
 
 int fail(cudaError_t e) { return e == cudaErrorMemoryAllocation ? MHD_ERR_NOMEM : MHD_ERR_CUDA; }
@@ -686,8 +202,32 @@ int alloc_sets(Handle* h, int n) {
 
 size_t device_bytes(const Handle* h) {
   return (h->bars_cap + h->vals_cap + h->tapes_cap + 4 + h->dtlog_cap) * sizeof(double) + h->ckpt_bytes +
-         h->seg_bytes;
+         h->seg_bytes + h->br_cap * sizeof(unsigned int);
 }
+
+// Words of one cycle's branch tapes and each stage slot's offset (items x words of
+// the stage, 128-byte aligned).
+void branch_layout(int nx, int ny, int recon, int efix, size_t* off, size_t* BW) {
+  const size_t cells = (size_t)nx * ny, xf = (size_t)(nx + 1) * ny, yf = (size_t)nx * (ny + 1);
+  const size_t corners = (size_t)(nx + 1) * (ny + 1);
+  const int nb_recon = recon == 1 ? std::max(g_plm0_NB, g_plm1_NB) : (recon == 2 ? std::max(g_ppm0_NB, g_ppm1_NB) : 0);
+  const int nb_slope = recon == 2 ? std::max(g_pslope0_NB, g_pslope1_NB) : 0;
+  const int nb_roe1 = efix ? std::max(g_roe1_0_efix_NB, g_roe1_1_efix_NB) : std::max(g_roe1_0_NB, g_roe1_1_NB);
+  const int nb_roe2 = efix ? std::max(g_roe2_0_efix_NB, g_roe2_1_efix_NB) : std::max(g_roe2_0_NB, g_roe2_1_NB);
+  const size_t items[kNumBt] = {(size_t)(nx + 2) * ny, (size_t)nx * (ny + 2), cells, cells, 2 * xf, 2 * yf,
+                                xf, yf, xf, yf, corners, corners, 2 * xf, 2 * yf};
+  const int words[kNumBt] = {nb_slope, nb_slope, nb_recon, nb_recon, std::max(g_face0_NB, g_face1_NB),
+                             std::max(g_face0_NB, g_face1_NB), nb_roe1, nb_roe1, nb_roe2, nb_roe2, g_emf_NB, g_emf_NB,
+                             std::max(g_ctu0_NB, g_ctu1_NB), std::max(g_ctu0_NB, g_ctu1_NB)};
+  size_t w = 0;
+  for (int i = 0; i < kNumBt; ++i) {
+    off[i] = w;
+    w += items[i] * (size_t)words[i];
+    w = (w + 31) & ~(size_t)31;
+  }
+  *BW = w;
+}
+
 
 // segments of a record: ceil(head / every) uniform segments over the first
 // head = steps - tail cycles, then the tail segment when tail > 0
@@ -727,8 +267,6 @@ int unpack(Handle* h, const double* src, Arr& P, Arr& C, Arr& FX, Arr& FY, bool 
   return MHD_OK;
 }
 
-dim3 g2(int w, int h, int z = 1) { return dim3((unsigned)((w + kT - 1) / kT), (unsigned)h, (unsigned)z); }
-unsigned g1(size_t n) { return (unsigned)((n + kT - 1) / kT); }
 
 // forward sweep of one cycle from the input arrays (P, C, FX, FY) with A.dt set;
 // TAPE: the PLM and Roe stages also write the tapes their reverse sweeps read
@@ -760,6 +298,14 @@ int fwd_cycle_t(Handle* h) {
 }
 
 int fwd_cycle(Handle* h, bool tape) { return tape ? fwd_cycle_t<true>(h) : fwd_cycle_t<false>(h); }
+
+// forward sweep of one cycle that records (BR 1) or replays (BR 2) every branch
+// decision on the bit tapes A.bt (set to the cycle's region of the branch arena)
+template <int BR>
+int fwd_cycle_b(Handle* h) {
+  CK(launch_fwd_branch<BR>(h->A, h->stream));
+  return MHD_OK;
+}
 
 // reverse sweep: output adjoints in NP/NC/NFX/NFY .b -> input adjoints in P/C/FX/FY .b
 // (reads the tapes of the last taped forward sweep of the selected arena)
@@ -822,6 +368,47 @@ int bars_in_to_out(Handle* h) {
   CK(cudaMemcpyAsync(A.NC.b, A.C.b, 8 * cp * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemcpyAsync(A.NFX.b, A.FX.b, A.FX.ps * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
   CK(cudaMemcpyAsync(A.NFY.b, A.FY.b, A.FY.ps * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  return MHD_OK;
+}
+
+// `steps` cycles with the host dts `dt` from state_in, recording (mode 1) or
+// replaying (mode 2) every branch decision; the final state goes to state_out.
+int run_branches(Handle* h, int mode, const double* state_in, int steps, const double* dt, double* state_out) {
+  Adj& A = h->A;
+  int rc;
+  if (mode == 1) {
+    const size_t need = (size_t)std::max(steps, 1) * h->BW;
+    if (need > h->br_cap) {
+      cudaFree(h->br);
+      h->br = nullptr;
+      h->br_cap = 0;
+      CK(cudaMalloc(&h->br, need * sizeof(unsigned int)));
+      h->br_cap = need;
+    }
+    h->br_steps = 0;
+  } else if (steps > h->br_steps) {
+    return MHD_ERR_STATE;
+  }
+  if (h->nsets < 1 && (rc = alloc_sets(h, 1))) return rc;
+  h->tail_resident = false;   // arena 0 is reused: a pending tail is recomputed from its checkpoint
+  select_set(h, 0);
+  if ((rc = unpack(h, state_in, A.P, A.C, A.FX, A.FY, false))) return rc;
+  if (steps == 0) {
+    if ((rc = pack(h, state_out, A.P, A.C, A.FX, A.FY, false))) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return MHD_OK;
+  }
+  for (int c = 0; c < steps; ++c) {
+    if (!std::isfinite(dt[c])) return MHD_ERR_ARG;
+    for (int i = 0; i < kNumBt; ++i) A.bt[i] = h->br + (size_t)c * h->BW + h->btoff[i];
+    A.dt = dt[c];
+    rc = mode == 1 ? fwd_cycle_b<1>(h) : fwd_cycle_b<2>(h);
+    if (rc) return rc;
+    if (c + 1 < steps && (rc = output_to_input(h, 0, 0))) return rc;
+  }
+  if ((rc = pack(h, state_out, A.NP, A.NC, A.NFX, A.NFY, false))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  if (mode == 1) h->br_steps = steps;
   return MHD_OK;
 }
 
@@ -1014,6 +601,7 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
   A.nx = nx; A.ny = ny; A.dx = dx; A.dy = dy; A.bcx = bcx; A.bcy = bcy; A.recon = recon;
   A.efix = entropy_fix ? 1 : 0; A.gamma = gamma; A.eps = eps; A.min_d = min_d; A.min_p = min_p; A.min_e = min_e;
   layout(nx, ny, recon, A.efix, h->off, h->ps, &h->W, h->toff, &h->TW);
+  branch_layout(nx, ny, recon, A.efix, h->btoff, &h->BW);
   h->state_words = state_words(A);
   int rc = MHD_OK;
   cudaError_t e = cudaMalloc(&h->bars, h->W * sizeof(double));
@@ -1049,6 +637,7 @@ void mhd2d_adj_destroy(void* handle) {
   cudaFree(h->dtlog);
   if (h->ckpt_owned) cudaFree(h->ckpt);
   cudaFree(h->seg);
+  cudaFree(h->br);
   if (h->solver) mhd2d_destroy(h->solver);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1062,6 +651,8 @@ int mhd2d_adj_reshape(void* handle, int ny, int nx, double dx, double dy, int bc
   Adj& A = h->A;
   A.nx = nx; A.ny = ny; A.dx = dx; A.dy = dy; A.bcx = bcx; A.bcy = bcy; A.gamma = gamma;
   layout(nx, ny, A.recon, A.efix, h->off, h->ps, &h->W, h->toff, &h->TW);
+  branch_layout(nx, ny, A.recon, A.efix, h->btoff, &h->BW);
+  h->br_steps = 0;
   h->state_words = state_words(A);
   if (h->W > h->bars_cap) {
     cudaFree(h->bars);
@@ -1275,6 +866,13 @@ int mhd2d_adj_backward(void* handle, const double* bar_final, double* bar_initia
   if ((rc = pack(h, bar_initial, A.NP, A.NC, A.NFX, A.NFY, true))) return rc;
   CK(cudaStreamSynchronize(h->stream));
   return MHD_OK;
+}
+
+int mhd2d_adj_branches(void* handle, int mode, const double* state_in, int steps, const double* dt,
+                       double* state_out) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h || (mode != 1 && mode != 2) || steps < 0 || !state_in || !state_out || (steps > 0 && !dt)) return MHD_ERR_ARG;
+  return run_branches(h, mode, state_in, steps, dt, state_out);
 }
 
 int mhd2d_adj_set_tail(void* handle, int max_cycles) {

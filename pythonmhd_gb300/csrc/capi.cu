@@ -51,6 +51,7 @@ struct Handle {
   int dt_blocks = 0;
   int nonfinite_seen = 0;  // an advance since the last upload ended with MHD_ERR_NONFINITE
   unsigned long long* d_check = nullptr;  // 7 counters of mhd2d_validate (device)
+  double* d_dt = nullptr;                 // mhd2d_cfl_dt's result (device)
 };
 
 int cuda_fail(cudaError_t e) {
@@ -313,7 +314,8 @@ static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, d
   h->dt_blocks = std::max(1, sms) * 8;
 
   const size_t total = carve_grid(g, h->nvars, nullptr) + align256(sizeof(LoopState)) + align256(sizeof(int)) +
-                       align256(sizeof(unsigned long long)) + align256(7 * sizeof(unsigned long long));
+                       align256(sizeof(unsigned long long)) + align256(7 * sizeof(unsigned long long)) +
+                       align256(sizeof(double));
   e = cudaMalloc(&h->arena, total);
   if (e != cudaSuccess) {
     cudaStreamDestroy(h->stream);
@@ -330,6 +332,8 @@ static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, d
   g.floor_hits = reinterpret_cast<unsigned long long*>(base + off);
   off += align256(sizeof(unsigned long long));
   h->d_check = reinterpret_cast<unsigned long long*>(base + off);
+  off += align256(7 * sizeof(unsigned long long));
+  h->d_dt = reinterpret_cast<double*>(base + off);
   e = cudaMemsetAsync(h->arena, 0, total, h->stream);
   if (e == cudaSuccess) e = cudaMallocHost(&h->host_loop, sizeof(LoopState));
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -430,9 +434,37 @@ int mhd2d_upload_device(void* handle, const double* prim, const double* cons, co
   return upload_state(handle, prim, cons, faceBx, faceBy, cudaMemcpyDeviceToDevice);
 }
 
+static int advance_impl(Handle* h, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
+                        double dt_fixed, double* t_out, long long* cycle_out, double* t_second_last);
+
 int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
                   double* t_out, long long* cycle_out, double* t_second_last) {
+  return advance_impl(static_cast<Handle*>(handle), t0, t_end, cycle0, max_cycles, cfl, 0.0, t_out, cycle_out,
+                      t_second_last);
+}
+
+int mhd2d_advance_dt(void* handle, double t0, double t_end, long long cycle0, double dt, double* t_out) {
+  if (!(dt > 0.0) || !std::isfinite(dt)) return MHD_ERR_ARG;
+  return advance_impl(static_cast<Handle*>(handle), t0, t_end, cycle0, cycle0 + 1, 0.0, dt, t_out, nullptr, nullptr);
+}
+
+int mhd2d_cfl_dt(void* handle, double cfl, double* dt) {
   Handle* h = static_cast<Handle*>(handle);
+  if (!h || !dt) return MHD_ERR_ARG;
+  if (!h->have_state) return MHD_ERR_STATE;
+  if (h->g.one_d) return MHD_ERR_STATE;
+  const mhdk::StateBuf& st = h->g.st[h->cur];
+  const bool mhd = h->g.physics == MHD2D_MHD;
+  int rc = mhd2d_cfl_dt_noalloc(h->g.physics, h->g.ny, h->g.nx, h->g.dx, h->g.dy, h->g.gamma, cfl, st.cons,
+                                mhd ? st.fbx : nullptr, mhd ? st.fby : nullptr, h->d_dt, h->stream);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(dt, h->d_dt, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+static int advance_impl(Handle* h, double t0, double t_end, long long cycle0, long long max_cycles, double cfl,
+                        double dt_fixed, double* t_out, long long* cycle_out, double* t_second_last) {
   if (!h) return MHD_ERR_ARG;
   if (!h->have_state) return MHD_ERR_STATE;
   if (!(t0 <= t_end) || cycle0 < 0) return MHD_ERR_ARG;
@@ -442,6 +474,7 @@ int mhd2d_advance(void* handle, double t0, double t_end, long long cycle0, long 
   init.t_end = t_end;
   init.t_prev = t0;
   init.dt = 0.0;
+  init.dt_fixed = dt_fixed;
   init.cfl = cfl;
   init.cycle = cycle0;
   init.max_cycles = max_cycles;
@@ -517,7 +550,19 @@ int mhd2d_set_dt_log(void* handle, double* dt_log, long long capacity) {
   return MHD_OK;
 }
 
+static int download_state(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy,
+                          cudaMemcpyKind kind);
+
 int mhd2d_download(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy) {
+  return download_state(handle, which, prim, cons, faceBx, faceBy, cudaMemcpyDeviceToHost);
+}
+
+int mhd2d_download_device(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy) {
+  return download_state(handle, which, prim, cons, faceBx, faceBy, cudaMemcpyDeviceToDevice);
+}
+
+static int download_state(void* handle, int which, double* prim, double* cons, double* faceBx, double* faceBy,
+                          cudaMemcpyKind kind) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || (which != 0 && which != 1)) return MHD_ERR_ARG;
   if (!h->have_state) return MHD_ERR_STATE;
@@ -525,11 +570,11 @@ int mhd2d_download(void* handle, int which, double* prim, double* cons, double* 
   if (which == 1 && h->last_cycles_run > 0) b ^= 1;
   const mhdk::StateBuf& s = h->g.st[b];
   const size_t cb = (size_t)h->nvars * mhdk::cell_plane(h->g) * sizeof(double);
-  if (prim) CK(cudaMemcpyAsync(prim, s.prim, cb, cudaMemcpyDeviceToHost, h->stream));
-  if (cons) CK(cudaMemcpyAsync(cons, s.cons, cb, cudaMemcpyDeviceToHost, h->stream));
+  if (prim) CK(cudaMemcpyAsync(prim, s.prim, cb, kind, h->stream));
+  if (cons) CK(cudaMemcpyAsync(cons, s.cons, cb, kind, h->stream));
   if (h->g.physics == MHD2D_MHD) {
-    if (faceBx) CK(cudaMemcpyAsync(faceBx, s.fbx, mhdk::xface_plane(h->g) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    if (faceBy) CK(cudaMemcpyAsync(faceBy, s.fby, mhdk::yface_plane(h->g) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (faceBx) CK(cudaMemcpyAsync(faceBx, s.fbx, mhdk::xface_plane(h->g) * sizeof(double), kind, h->stream));
+    if (faceBy) CK(cudaMemcpyAsync(faceBy, s.fby, mhdk::yface_plane(h->g) * sizeof(double), kind, h->stream));
   }
   CK(cudaStreamSynchronize(h->stream));
   return MHD_OK;

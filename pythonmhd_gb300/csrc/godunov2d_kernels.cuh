@@ -984,7 +984,9 @@ __device__ __forceinline__ void b_begin(const Grid& G) {
     const double mx = __longlong_as_double((long long)L->max_sx);
     const double my = __longlong_as_double((long long)L->max_sy);
     double dt;
-    if (PHYS == MHD) {
+    if (is_pos(L->dt_fixed)) {
+      dt = L->dt_fixed;
+    } else if (PHYS == MHD) {
       const double inv = dmax(mx / G.dx, my / G.dy);
       dt = L->cfl / inv;
     } else {

@@ -34,6 +34,8 @@ struct LoopState {
   int cur;              // state buffer (0/1) holding the current state
   int pad[2];
   unsigned long long max_sz;  // 3D grids: bits of max(|vz| + c) over cells
+  double dt_fixed;      // > 0: the cycle uses this dt (before the t_end clip) instead of
+                        // the CFL dt of the grid (a domain-decomposed run's global dt)
 };
 
 // One state buffer: SoA planes, row-major (x fastest).

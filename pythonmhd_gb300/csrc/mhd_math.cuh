@@ -24,6 +24,18 @@ constexpr double FOUR_THIRDS = 1.333333333333333;  // Source/PythonMHD_Constants
 __device__ __forceinline__ double sq(double x) { return x * x; }
 
 // ---------------------------------------------------------------------------
+// Operations the compiler never fuses into a multiply-add.  The fast build lets
+// nvcc contract a*b+c into one rounding; these keep two.  They are used for the
+// scalars that decide the reference's branches (wave speeds, the Roe-averaged
+// sound speed, the fast/slow normalisations) so that both builds take the same
+// branch from the same inputs; in the exact build they are the plain operators.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double nmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double nadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double nsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double nsq(double x) { return __dmul_rn(x, x); }
+
+// ---------------------------------------------------------------------------
 // Comparisons on the IEEE-754 bit pattern.  An FP64 compare (DSETP, and the
 // select of an FP64 max/min) issues on the FP64 pipe at the DFMA rate, and that
 // pipe bounds every kernel of the step; the same test on the 64-bit pattern runs
@@ -177,7 +189,7 @@ __device__ __forceinline__ double prim_R(const PrimEig& e, int i, int j) {
 
 template <int N, int T1, int T2>
 __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, double gamma, PrimEig& e) {
-  const double bt2 = sq(w[4]) + sq(w[5]);
+  const double bt2 = nadd(nsq(w[4]), nsq(w[5]));
   const double bt = sqrt(bt2);
   const double gp = gamma * w[6];
   const double inv_d = 1.0 / w[0];
@@ -189,7 +201,7 @@ __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, d
   const double ca = sqrt(ca2);
   const double ssum = ca2 + red_bt2 + a2;
   const double sdiff = ca2 + red_bt2 - a2;
-  const double ssqrt = sqrt(sdiff * sdiff + 4.0 * a2 * red_bt2);
+  const double ssqrt = sqrt(nadd(nsq(sdiff), nmul(4.0 * a2, red_bt2)));
   const double cf2 = 0.5 * (ssum + ssqrt);
   const double cf = sqrt(cf2);
   const double cs2 = a2 * ca2 / cf2;
@@ -338,30 +350,30 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   const double rd = sl * sr;
   double v[4];
 #pragma unroll
-  for (int k = 1; k <= 3; ++k) v[k] = (sl * wl[k] + sr * wr[k]) * isum;
-  const double vsq = v[N] * v[N] + v[T1] * v[T1] + v[T2] * v[T2];
-  const double b1 = (sr * wl[4] + sl * wr[4]) * isum;
-  const double b2 = (sr * wl[5] + sl * wr[5]) * isum;
-  const double hbl = 0.5 * (sq(bn) + sq(wl[4]) + sq(wl[5]));
-  const double hbr = 0.5 * (sq(bn) + sq(wr[4]) + sq(wr[5]));
+  for (int k = 1; k <= 3; ++k) v[k] = nadd(nmul(sl, wl[k]), nmul(sr, wr[k])) * isum;
+  const double vsq = nadd(nadd(nsq(v[N]), nsq(v[T1])), nsq(v[T2]));
+  const double b1 = nadd(nmul(sr, wl[4]), nmul(sl, wr[4])) * isum;
+  const double b2 = nadd(nmul(sr, wl[5]), nmul(sl, wr[5])) * isum;
+  const double hbl = 0.5 * nadd(nadd(nsq(bn), nsq(wl[4])), nsq(wl[5]));
+  const double hbr = 0.5 * nadd(nadd(nsq(bn), nsq(wr[4])), nsq(wr[5]));
   const double H = ((ul[6] + wl[6] + hbl) / sl + (ur[6] + wr[6] + hbr) / sr) * isum;
 
   const double ird = 1.0 / rd;
-  const double btc = 0.5 * (sq(wl[4] - wr[4]) + sq(wl[5] - wr[5])) / sq(sl + sr);
+  const double btc = 0.5 * nadd(nsq(wl[4] - wr[4]), nsq(wl[5] - wr[5])) / sq(sl + sr);
   const double rc = 0.5 * (wl[0] + wr[0]) / rd;
-  const double bt2 = b1 * b1 + b2 * b2;
+  const double bt2 = nadd(nsq(b1), nsq(b2));
   const double bt = sqrt(bt2);
-  const double bts2 = ((gamma - 1.0) - (gamma - 2.0) * rc) * bt2;
+  const double bts2 = nsub(gamma - 1.0, nmul(gamma - 2.0, rc)) * bt2;
   const double bts = sqrt(bts2);
   const double rbts2 = bts2 * ird;
   const double ca2 = bn * bn * ird;
   const double ca = sqrt(ca2);
-  const double hmb = H - (ca2 + bt2 * ird);
-  const double a2 = dmax((gamma - 1.0) * (hmb - 0.5 * vsq) - (gamma - 2.0) * btc, SMALL_VALUE);
+  const double hmb = H - nadd(ca2, nmul(bt2, ird));
+  const double a2 = dmax(nsub(nmul(gamma - 1.0, hmb - 0.5 * vsq), nmul(gamma - 2.0, btc)), SMALL_VALUE);
   const double a = sqrt(a2);
   const double ssum = ca2 + rbts2 + a2;
   const double sdiff = ca2 + rbts2 - a2;
-  const double ssqrt = sqrt(sdiff * sdiff + 4.0 * a2 * rbts2);
+  const double ssqrt = sqrt(nadd(nsq(sdiff), nmul(4.0 * a2, rbts2)));
   const double cf2 = 0.5 * (ssum + ssqrt);
   const double cf = sqrt(cf2);
   const double cs2 = a2 * ca2 / cf2;
@@ -402,7 +414,7 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   double bh1 = 0.0, bh2 = 0.0;
   if (is_zero(bt)) bh1 = 1.0;
   if (is_pos(bt)) { bh1 = b1 / bt; bh2 = b2 / bt; }
-  const double den = sqrt((gamma - 1.0) - (gamma - 2.0) * rc);
+  const double den = sqrt(nsub(gamma - 1.0, nmul(gamma - 2.0, rc)));
   const double b1s = bh1 / den;
   const double b2s = bh2 / den;
   const double vb = v[T1] * b1s + v[T2] * b2s;

@@ -104,6 +104,21 @@ class Grid2D:
         _lib.check(self.lib.mhd2d_upload_device(self._h, ptr(prim), ptr(cons), ptr(fbx), ptr(fby)),
                    "mhd2d_upload_device")
 
+    def download_device(self, which, prim, cons, fbx=None, fby=None):
+        """Copy the current (which=0) or second-last (which=1) state into contiguous float64
+        CUDA tensors of the handle's device."""
+        import torch
+
+        def ptr(t):
+            if t is None:
+                return None
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError("download_device expects contiguous float64 CUDA tensors")
+            return ctypes.c_void_p(t.data_ptr())
+        torch.cuda.current_stream(prim.device).synchronize()
+        _lib.check(self.lib.mhd2d_download_device(self._h, int(which), ptr(prim), ptr(cons), ptr(fbx), ptr(fby)),
+                   "mhd2d_download_device")
+
     def download(self, which=0, prim=None, cons=None, fbx=None, fby=None):
         """Copy the current (which=0) or second-last (which=1) state into new or given arrays."""
         prim = np.empty(self.cell_shape()) if prim is None else prim
@@ -127,6 +142,20 @@ class Grid2D:
                    "mhd2d_advance")
         self.last_cycles = c.value - int(cycle0)
         return t.value, c.value, tsl.value
+
+    def cfl_dt(self, cfl):
+        """The CFL dt of the current state before the t_end clip (exact arithmetic)."""
+        dt = ctypes.c_double()
+        _lib.check(self.lib.mhd2d_cfl_dt(self._h, float(cfl), ctypes.byref(dt)), "mhd2d_cfl_dt")
+        return dt.value
+
+    def advance_dt(self, t0, t_end, cycle0, dt):
+        """One cycle with the given dt (clipped to t_end); returns the new time."""
+        t = ctypes.c_double()
+        _lib.check(self.lib.mhd2d_advance_dt(self._h, float(t0), float(t_end), int(cycle0), float(dt),
+                                             ctypes.byref(t)), "mhd2d_advance_dt")
+        self.last_cycles = 1
+        return t.value
 
     def peek(self, what):
         """Intermediates of the last cycle (see mhd2d_peek in include/pythonmhd_gb300.h)."""

@@ -16,6 +16,15 @@ Checked against
   finite differences scatter around the derivative; they are reported, and
   checked for gross disagreement over the default 40 cycles.
 
+A third check freezes the branches: the forward pass is run once more from the
+unperturbed state with every branch decision recorded (limiter, clamp, floor,
+upwind, entropy-fix and |x| decisions of every stage), and the perturbed runs of
+the central differences replay them, so the differences measure the derivative of
+the piece the adjoint differentiates.  Along 16 seeded directions in all five
+fields (rho, vx, vy, p, A_z) they must agree with the adjoint to 1e-6 relative at
+eps = 1e-6 (40 cycles by default; PYTHONMHD_GB300_ADJ_FROZEN_STEPS=400 runs the
+workload's length).
+
 By default 40 cycles and 3 directions (about a minute);
 PYTHONMHD_GB300_ADJ_STEPS=400 PYTHONMHD_GB300_ADJ_DIRS=16 runs the full workload
 (about ten minutes, most of it in the torch transcription; PYTHONMHD_GB300_ADJ_TORCH=0
@@ -118,3 +127,64 @@ def test_turbulence_gradient_against_torch_and_finite_differences():
     # to 25% at its best step; over hundreds of cycles the scatter is only reported
     if steps <= 40:
         assert all(min(errs.values()) < 0.25 for _, errs in rows)
+
+
+def _direction(rng, fl, keys):
+    """A seeded direction in the fields, each scaled by the field's spread (by its mean
+    for p, which is uniform at the generator's state)."""
+    return {k: rng.standard_normal(fl[k].shape) * (np.mean(fl[k]) if k == "p" else np.std(fl[k])) for k in keys}
+
+
+def test_turbulence_gradient_against_branch_frozen_differences():
+    n = 512
+    steps = int(os.environ.get("PYTHONMHD_GB300_ADJ_FROZEN_STEPS", "40"))
+    ndir = 16
+    dev = torch.device("cuda", 0)
+    fl = fields.turbulence_fields(n, seed=1, kmax_v=16, kmax_a=16)
+    g0, dx, dy = fl["gamma"], fl["dx"], fl["dy"]
+    tgt = fields.perturbed(fl, 0.02, seed=2)
+    a = Adjoint2D(n, n, dx, dy, 1, 1, g0, recon=1)
+    st_t = fields.state_from_fields(*fields.fields_to_torch(tgt, dev), g0, dx, dy).contiguous()
+    target = a.unpack(a.forward(st_t, steps, cfl=0.4))[0][0].clone()
+    xs = fields.fields_to_torch(fl, dev, requires_grad=True)
+    out = evolve(fields.state_from_fields(*xs, g0, dx, dy), a, steps, cfl=0.4)
+    loss = torch.mean((a.unpack(out)[0][0] - target) ** 2)
+    loss.backward()
+    gnp = {k: x.grad.detach().cpu().numpy() for k, x in zip(KEYS, xs)}
+    dts = a.dts.copy()
+    s0 = fields.state_from_fields(*fields.fields_to_torch(fl, dev), g0, dx, dy).contiguous()
+    assert torch.equal(a.branches("record", s0, dts), out.detach())
+
+    def frozen_loss(f):
+        st = fields.state_from_fields(*fields.fields_to_torch(f, dev), g0, dx, dy).contiguous()
+        return float(torch.mean((a.unpack(a.branches("replay", st, dts))[0][0] - target) ** 2))
+
+    def free_loss(f):
+        st = fields.state_from_fields(*fields.fields_to_torch(f, dev), g0, dx, dy).contiguous()
+        return float(torch.mean((a.unpack(a.forward(st, steps, dts=dts))[0][0] - target) ** 2))
+
+    assert frozen_loss(fl) == float(loss.detach())
+    rng = np.random.default_rng(29)
+    rows = []
+    for _ in range(ndir):
+        d = _direction(rng, fl, KEYS)
+        ad = sum(float(np.sum(gnp[k] * d[k])) for k in KEYS)
+        row = {"adjoint": ad}
+        for eps in (1e-5, 1e-6, 1e-7):
+            fp = dict(fl, **{k: fl[k] + eps * d[k] for k in KEYS})
+            fm = dict(fl, **{k: fl[k] - eps * d[k] for k in KEYS})
+            fd = (frozen_loss(fp) - frozen_loss(fm)) / (2 * eps)
+            row[f"frozen {eps:.0e}"] = abs(fd - ad) / abs(fd)
+        eps = 1e-6
+        fp = dict(fl, **{k: fl[k] + eps * d[k] for k in KEYS})
+        fm = dict(fl, **{k: fl[k] - eps * d[k] for k in KEYS})
+        fd = (free_loss(fp) - free_loss(fm)) / (2 * eps)
+        row["free 1e-06"] = abs(fd - ad) / abs(fd)   # reported, not checked
+        rows.append(row)
+        print("direction:", " ".join(f"{k}: {v:.3e}" for k, v in row.items()))
+    report = os.environ.get("PYTHONMHD_GB300_ADJ_REPORT")
+    if report:
+        with open(report, "w") as f:
+            json.dump({"n": n, "steps": steps, "loss": float(loss.detach()), "directions": rows}, f, indent=1)
+    a.close()
+    assert max(r["frozen 1e-06"] for r in rows) <= 1e-6

@@ -35,3 +35,33 @@ def test_ot128_full_run_bitwise(key, order):
     assert np.max(np.abs(rho - rho[::-1, ::-1])) <= 1e-11 * np.max(rho)
     div = (r[2][:, 1:] - r[2][:, :-1]) / dx + (r[3][1:, :] - r[3][:-1, :]) / dy
     assert np.max(np.abs(div)) * dx <= 1e-13 * np.max(np.abs(r[2]))
+
+
+def test_ot128_full_run_fast_arithmetic_per_cycle():
+    """The fast arithmetic (FMA contraction, branch-deciding scalars uncontracted) along
+    the whole reference PPM run: at every one of its ~400 cycles, one fast cycle from
+    the reference's state (the exact chain, whose end is checked against the
+    reference's digest) stays within 1e-12 of the reference's next state."""
+    from pythonmhd_gb300.solver import Grid2D
+    from tests.gpu_util import field_rel_err
+    with open(ot.OUT) as f:
+        want = json.load(f)["reference_ppm"]
+    prim, cons, fbx, fby, dx, dy = ot.initial_state()
+    ge = Grid2D(ot.N, ot.N, dx, dy, 1, 1, ot.GAMMA, mhd=True, recon=2, arith="exact")
+    gf = Grid2D(ot.N, ot.N, dx, dy, 1, 1, ot.GAMMA, mhd=True, recon=2, arith="fast")
+    try:
+        st, t, c, worst = (prim, cons, fbx, fby), 0.0, 0, 0.0
+        while t < ot.T_END and c < ot.MAX_CYCLES:
+            ge.upload(*st)
+            gf.upload(*st)
+            te, ce, _ = ge.advance(t, ot.T_END, c, c + 1, ot.CFL)
+            tf, cf, _ = gf.advance(t, ot.T_END, c, c + 1, ot.CFL)
+            nxt = ge.download(0)
+            assert cf == ce and abs(tf - te) <= 1e-12 * te
+            worst = max(worst, max(field_rel_err(a, b) for a, b in zip(gf.download(0), nxt)))
+            st, t, c = nxt, te, ce
+        assert (t, c) == (want["t"], want["cycle"]) and ot.digest(*st) == want["sha256"]
+        assert worst <= 1e-12, worst
+    finally:
+        ge.close()
+        gf.close()

@@ -3,8 +3,14 @@ evolve functions.
 
 * arith="exact": every output of every golden case equals the reference's own
   output bit for bit (the fixtures come from running Source/EvolveFunctions_*.py).
-* arith="fast" (FMA contraction): every field within 1e-12 of the reference,
-  relative to the field's largest magnitude, over the 1-3 cycles of a case.
+* arith="fast" (FMA contraction, the branch-deciding scalars uncontracted):
+  per cycle, from the reference's own state at that cycle, every field within
+  1e-12 of the reference, relative to the field's largest magnitude -- on every
+  case where the reference itself is well conditioned.  Two cases sit on exact
+  ties of the reference's branches (tests/conditioning.py): there a one-ulp change
+  of the input moves the reference's own output by 1e-11 (mhd_ot_order0) and 1e-5
+  (mhd_zero_btran), and the fast mode is required to stay within ten times that
+  measured sensitivity instead.
 """
 import numpy as np
 import pytest
@@ -13,22 +19,8 @@ from tests.golden_io import HYDRO_KEYS, MHD_KEYS, case_id, golden_files, load
 from tests.gpu_util import field_rel_err, run_dropin
 
 FAST_TOL = 1e-12
-# States whose eigen-branch choice in the reference is an exact floating-point tie
-# (B == 0 everywhere: c_f^2 == a^2; B_t == 0: the slow/Alfven degeneracy).  Any
-# change in the last bit of a^2 -- such as a fused multiply-add -- may take the
-# other branch, so only the exact arithmetic mode can reproduce them.
-EXACT_TIE_CASES = {"mhd_zero_b", "mhd_zero_btran"}
 
 pytestmark = pytest.mark.gpu
-
-
-def _fast_cases():
-    out = []
-    for f in golden_files("mhd") + golden_files("hydro"):
-        marks = [pytest.mark.xfail(reason="exact tie in the reference's eigen-branch test", strict=False)] \
-            if case_id(f) in EXACT_TIE_CASES else []
-        out.append(pytest.param(f, marks=marks, id=case_id(f)))
-    return out
 
 
 @pytest.mark.parametrize("path", golden_files("mhd") + golden_files("hydro"), ids=case_id)
@@ -45,17 +37,40 @@ def test_exact_matches_reference_bitwise(path):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("path", _fast_cases())
-def test_fast_within_tolerance(path):
-    physics = "mhd" if case_id(path).startswith("mhd") else "hydro"
+@pytest.mark.parametrize("path", golden_files("mhd") + golden_files("hydro"), ids=case_id)
+def test_fast_within_tolerance_per_cycle(path):
+    """Each cycle of the case from the reference's state at its start (the exact mode
+    reproduces the reference's states bit for bit, so it supplies them): one fast
+    cycle against one exact cycle."""
+    from pythonmhd_gb300.solver import Grid2D
+    from tests.conditioning import sensitivity
+    mhd = case_id(path).startswith("mhd")
     p, i, o = load(path)
-    grid, res = run_dropin(physics, p, i, "fast")
-    keys = MHD_KEYS if physics == "mhd" else HYDRO_KEYS
-    for k, v in zip(keys, res):
-        if k in ("cycle",):
-            assert int(v) == int(o[k])
-            continue
-        assert field_rel_err(v, o[k]) <= FAST_TOL, k
+    ny, nx = i["prim"].shape[1:]
+    tol = max(FAST_TOL, 10.0 * sensitivity(path))
+    hs = [Grid2D(ny, nx, p["dx"], p["dy"], p["bcx"], p["bcy"], p["gamma"], mhd=mhd,
+                 recon=2 if p["order"] == 2 else 0, entropy_fix=p["efix"], eps=p["eps"], min_d=p["min_d"],
+                 min_p=p["min_p"], min_e=p["min_e"], arith=m) for m in ("exact", "fast")]
+    try:
+        st = (i["prim"], i["cons"], i["fbx"], i["fby"]) if mhd else (i["prim"], i["cons"])
+        t, c = p["t_start"], p["start_cycle"]
+        while t < p["t_end"] and c < p["max_cycles"]:
+            outs = []
+            for g in hs:
+                g.upload(*st)
+                outs.append((g.advance(t, p["t_end"], c, c + 1, p["cfl"]), g.download(0)))
+            (te, ce, _), want = outs[0]
+            (tf, cf, _), got = outs[1]
+            assert cf == ce and abs(tf - te) <= FAST_TOL * abs(te)
+            for a, w in zip(got, want):
+                assert field_rel_err(a, w) <= tol
+            st, t, c = want, te, ce
+        # and the exact mode's chain is the reference's own run
+        for a, w in zip(st, (o["prim"], o["cons"], o.get("fbx"), o.get("fby"))):
+            assert np.array_equal(a, w)
+    finally:
+        for g in hs:
+            g.close()
 
 
 @pytest.mark.parametrize("arith", ["exact", "fast"])
