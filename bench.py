@@ -275,12 +275,19 @@ def run_batch(a, torch):
     handle vs a loop of single-grid handles advancing each instance in turn."""
     from pythonmhd_gb300 import initial_conditions as ic
     from pythonmhd_gb300.solver import Batch2D, Grid2D
-    insts = ic.orszag_tang_batch(count=a.batch_count, seed=0)
+    # the instances are built on the GPU (the project's generator kernels); the host
+    # copies serve the autotuner and the per-instance loop's uploads
+    dev_insts = ic.orszag_tang_batch_device(count=a.batch_count, seed=0)
+    insts = [dict(d, prim=d["prim"].cpu().numpy(), cons=d["cons"].cpu().numpy(), fbx=d["fbx"].cpu().numpy(),
+                  fby=d["fby"].cpu().numpy()) for d in dev_insts]
     zones = sum(i["nx"] * i["ny"] for i in insts)
     k, w = a.batch_steps, 1
     from pythonmhd_gb300 import autotune
     b = Batch2D(insts, mhd=True, recon=1, arith=a.arith)
     tuned = autotune.tune_batch(b, insts, recon=1, cycles=1)
+    for j, d in enumerate(dev_insts):
+        b.upload_device(j, d["prim"], d["cons"], d["fbx"], d["fby"])
+    del dev_insts
     b.advance(0.0, 1e30, 0, w, 0.4)
     torch.cuda.synchronize()
     t0 = time.perf_counter()

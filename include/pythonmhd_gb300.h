@@ -40,11 +40,18 @@ enum mhd2d_status {
   MHD_ERR_STATE = 4,       /* call out of order (e.g. advance before upload) */
   MHD_ERR_NONFINITE = 5,   /* the time or dt became NaN/Inf during advance */
   MHD_ERR_TOO_LARGE = 6,   /* size above a fixed limit of the entry point */
-  MHD_ERR_ABORTED = 7      /* mhd2d_run: the stop callback asked to stop */
+  MHD_ERR_ABORTED = 7,     /* mhd2d_run: the stop callback asked to stop */
+  MHD_ERR_INDEX = 8        /* checked arithmetic: an index fell outside its array */
 };
 
 enum mhd2d_physics { MHD2D_HYDRO = 0, MHD2D_MHD = 1 };
-enum mhd2d_arith { MHD2D_ARITH_EXACT = 0, MHD2D_ARITH_FAST = 1 };
+/* EXACT: the reference's float64 arithmetic bit for bit; FAST: multiply-adds fused
+ * except in the scalars that decide branches; CHECKED: EXACT's arithmetic with
+ * every global index of the 2D and 1D kernels (single and batched) checked before
+ * use -- a failed check never touches memory outside the array, sets the handle's
+ * error word and makes the advance call return MHD_ERR_INDEX (mhd2d_check_info
+ * says where).  A debugging build of the same source, slower. */
+enum mhd2d_arith { MHD2D_ARITH_EXACT = 0, MHD2D_ARITH_FAST = 1, MHD2D_ARITH_CHECKED = 2 };
 
 /* Create a handle for an ny x nx grid.  bcx/bcy: 0 outflow, 1 periodic
  * (Source/PythonMHD_Constants.py:11-12).  recon: 0 first order, 2 PPM
@@ -167,6 +174,10 @@ int mhd2d_stats(void* handle, long long* floor_hits, int* nan_flag);
  * the Python mirror (solver.Grid2D.check_state) does the same from these counts. */
 int mhd2d_validate(void* handle, long long* counts);
 
+/* Checked arithmetic: the kernel source line and the index of the first failed
+ * index check since the last upload (0, 0: none). */
+int mhd2d_check_info(void* handle, long long* line, long long* index);
+
 /* The CUDA stream the handle's work runs on (a cudaStream_t). */
 int mhd2d_stream(void* handle, void** stream);
 
@@ -198,6 +209,34 @@ int mhd2d_stream(void* handle, void** stream);
 int mhd2d_cfl_dt_noalloc(int physics, int ny, int nx, double dx, double dy, double gamma,
                          double cfl, const double* cons, const double* faceBx,
                          const double* faceBy, double* dt_out, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Initial states on the GPU (inputs of the runs; the reference builds its initial
+ * states on the host in its initialization files, e.g. the Orszag-Tang vortex of
+ * InitializationFiles/SampleSimulations/2D_MHD/OrszagTang_InitializationFile.py:134-194).
+ * All pointers are device pointers of the current GPU; the work is queued on
+ * `stream` (NULL: the default stream).
+ *
+ * mhd_ic_scatter_spectrum: spec[idx[k]] = re[k] + i im[k] for k < count, into an
+ *   interleaved complex half-spectrum the caller zeroed (the in-band coefficients
+ *   of a seeded Gaussian random field, drawn on the host).
+ * mhd_ic_turbulence_2d: the driven-free turbulence state of an n x n periodic unit
+ *   box from the four inverse-transformed fields g, vx, vy, A_z (in that order of
+ *   the random stream): rho = exp(0.1 g / std g), p = 1/gamma, velocities scaled to
+ *   rms Mach `mach`, face B from A_z scaled to plasma beta `beta`, prim, cons,
+ *   faceBx (n, n+1), faceBy (n+1, n).  `work` holds mhd_ic_work_words() doubles.
+ * mhd_ic_orszag_tang: the Orszag-Tang vortex on nx x ny with B0 scaled by b0_scale,
+ *   face B from the corner vector potential, and the density multiplied by
+ *   (1 + rho_perturb noise) when `noise` (ny, nx) is not NULL.
+ * ------------------------------------------------------------------------- */
+long long mhd_ic_work_words(void);
+int mhd_ic_scatter_spectrum(long long count, const int* idx, const double* re, const double* im, double* spec,
+                            void* stream);
+int mhd_ic_turbulence_2d(int n, double gamma, double mach, double beta, const double* g, const double* vx,
+                         const double* vy, const double* az, double* prim, double* cons, double* fbx, double* fby,
+                         double* work, long long work_words, void* stream);
+int mhd_ic_orszag_tang(int nx, int ny, double gamma, double b0_scale, double rho_perturb, const double* noise,
+                       double* prim, double* cons, double* fbx, double* fby, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Batched form: many independent grids (uneven sizes, per-instance gamma, dx,

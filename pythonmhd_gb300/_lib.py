@@ -83,6 +83,8 @@ SIGNATURES = {
                                       ctypes.POINTER(ctypes.c_longlong)]),
     "mhdb_set_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong]),
     "mhdb_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mhd2d_check_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                        ctypes.POINTER(ctypes.c_longlong)]),
     "mhd2d_validate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "mhd2d_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]),
     "mhdb_destroy": (None, [ctypes.c_void_p]),
@@ -117,6 +119,12 @@ SIGNATURES = {
                                  ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                  ctypes.POINTER(ctypes.c_longlong)]),
+    "mhd_ic_work_words": (ctypes.c_longlong, []),
+    "mhd_ic_scatter_spectrum": (ctypes.c_int, [ctypes.c_longlong] + [ctypes.c_void_p] * 5),
+    "mhd_ic_turbulence_2d": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+                             + [ctypes.c_void_p] * 9 + [ctypes.c_longlong, ctypes.c_void_p]),
+    "mhd_ic_orszag_tang": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double] + [ctypes.c_void_p] * 6),
     "mhd2d_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "mhd2d_destroy": (None, [ctypes.c_void_p]),
 }

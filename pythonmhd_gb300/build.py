@@ -5,11 +5,13 @@ shared library with a plain C ABI (``include/pythonmhd_gb300.h``):
 
 * ``csrc/kernels_exact.cu``  -- the step kernels with ``-fmad=false``
 * ``csrc/kernels_fast.cu``   -- the same kernels with FMA contraction
+* ``csrc/kernels_checked.cu`` -- the exact kernels with every global index checked
 * ``csrc/capi.cu``           -- handles, copies and the CUDA-graph evolve loop
 * ``csrc/kernels3d_exact.cu`` / ``csrc/kernels3d_fast.cu`` -- the 3D hydro step kernels
 * ``csrc/capi3d.cu``         -- the 3D handle and its evolve loop
 * ``csrc/noalloc.cu``        -- the CFL timestep for callers that cannot allocate
 * ``csrc/validate.cu``       -- the initial-state check (the reference's validatePrimVars)
+* ``csrc/icgen.cu``          -- initial states on the GPU (turbulence field algebra, Orszag-Tang)
 * ``csrc/adjoint.cu``        -- the reverse-mode adjoint of the MHD step; its pointwise
   stage functions (``csrc/adjoint_gen.cuh``) are generated from ``adjoint/stages.py``
   first, its stage kernels are in ``csrc/adjoint_kernels.cuh``
@@ -32,12 +34,14 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 UNITS = [
     ("kernels_exact.cu", ["-fmad=false"]),
     ("kernels_fast.cu", ["-fmad=true"]),
+    ("kernels_checked.cu", ["-fmad=false"]),
     ("capi.cu", []),
     ("kernels3d_exact.cu", ["-fmad=false"]),
     ("kernels3d_fast.cu", ["-fmad=true"]),
     ("capi3d.cu", []),
     ("noalloc.cu", ["-fmad=false"]),
     ("validate.cu", ["-fmad=false"]),
+    ("icgen.cu", ["-fmad=false", "--extended-lambda"]),
     ("adjoint.cu", []),
     ("adjoint_branch.cu", []),
 ]

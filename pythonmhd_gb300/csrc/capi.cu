@@ -26,6 +26,11 @@ void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
 void enqueue_cycle_batch_tuned(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, int fuse,
                                cudaStream_t s);
 }  // namespace fast
+namespace checked {
+void enqueue_cycle(const Grid& g, int parity, int dt_blocks, cudaStream_t s);
+void enqueue_cycle_batch_tuned(const BatchView& V, int physics, int recon, unsigned blocks, unsigned tw, int fuse,
+                               cudaStream_t s);
+}  // namespace checked
 }  // namespace mhdk
 
 using mhdk::Grid;
@@ -106,6 +111,7 @@ size_t carve_grid(Grid& g, int nvars, char* base) {
 
 void enqueue(Handle* h, int parity) {
   if (h->arith == MHD2D_ARITH_EXACT) mhdk::exact::enqueue_cycle(h->g, parity, h->dt_blocks, h->stream);
+  else if (h->arith == MHD2D_ARITH_CHECKED) mhdk::checked::enqueue_cycle(h->g, parity, h->dt_blocks, h->stream);
   else mhdk::fast::enqueue_cycle(h->g, parity, h->dt_blocks, h->stream);
 }
 
@@ -159,6 +165,9 @@ void enqueue_batch(BatchHandle* b) {
   if (b->arith == MHD2D_ARITH_EXACT)
     mhdk::exact::enqueue_cycle_batch_tuned(b->view, b->physics, b->recon, b->blocks, (unsigned)b->tile_width, b->fuse,
                                            b->stream);
+  else if (b->arith == MHD2D_ARITH_CHECKED)
+    mhdk::checked::enqueue_cycle_batch_tuned(b->view, b->physics, b->recon, b->blocks, (unsigned)b->tile_width,
+                                             b->fuse, b->stream);
   else
     mhdk::fast::enqueue_cycle_batch_tuned(b->view, b->physics, b->recon, b->blocks, (unsigned)b->tile_width, b->fuse,
                                           b->stream);
@@ -279,6 +288,7 @@ const char* mhd2d_strerror(int status) {
     case MHD_ERR_NONFINITE: return "time or timestep became non-finite";
     case MHD_ERR_TOO_LARGE: return "size above the entry point's fixed limit";
     case MHD_ERR_ABORTED: return "stopped by the caller's stop callback";
+    case MHD_ERR_INDEX: return "an index fell outside its array (checked build)";
     default: return "unknown status";
   }
 }
@@ -292,7 +302,7 @@ static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, d
   if ((bcx != 0 && bcx != 1) || (bcy != 0 && bcy != 1)) return MHD_ERR_ARG;
   if (physics != MHD2D_HYDRO && physics != MHD2D_MHD) return MHD_ERR_ARG;
   if (recon != 0 && recon != 1 && recon != 2) return MHD_ERR_ARG;
-  if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST) return MHD_ERR_ARG;
+  if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST && arith != MHD2D_ARITH_CHECKED) return MHD_ERR_ARG;
   if ((long long)nx * ny > (1LL << 31)) return MHD_ERR_TOO_LARGE;
 
   Handle* h = new (std::nothrow) Handle();
@@ -315,7 +325,7 @@ static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, d
 
   const size_t total = carve_grid(g, h->nvars, nullptr) + align256(sizeof(LoopState)) + align256(sizeof(int)) +
                        align256(sizeof(unsigned long long)) + align256(7 * sizeof(unsigned long long)) +
-                       align256(sizeof(double));
+                       align256(sizeof(double)) + align256(2 * sizeof(long long));
   e = cudaMalloc(&h->arena, total);
   if (e != cudaSuccess) {
     cudaStreamDestroy(h->stream);
@@ -334,6 +344,8 @@ static int create_grid(int ny, int nx, double dx, double dy, int bcx, int bcy, d
   h->d_check = reinterpret_cast<unsigned long long*>(base + off);
   off += align256(7 * sizeof(unsigned long long));
   h->d_dt = reinterpret_cast<double*>(base + off);
+  off += align256(sizeof(double));
+  g.bad = reinterpret_cast<long long*>(base + off);
   e = cudaMemsetAsync(h->arena, 0, total, h->stream);
   if (e == cudaSuccess) e = cudaMallocHost(&h->host_loop, sizeof(LoopState));
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -417,6 +429,7 @@ static int upload_state(void* handle, const double* prim, const double* cons, co
   // a new state starts with clean counters (floor hits, error word)
   CK(cudaMemsetAsync(h->g.status, 0, sizeof(int), h->stream));
   CK(cudaMemsetAsync(h->g.floor_hits, 0, sizeof(unsigned long long), h->stream));
+  CK(cudaMemsetAsync(h->g.bad, 0, 2 * sizeof(long long), h->stream));
   CK(cudaStreamSynchronize(h->stream));
   h->have_state = 1;
   h->last_cycles_run = 0;
@@ -493,8 +506,16 @@ static int advance_impl(Handle* h, double t0, double t_end, long long cycle0, lo
     for (long long k = 0; k < budget_pairs; ++k) CK(cudaGraphLaunch(h->graph[parity], h->stream));
     h->last_launches += budget_pairs * (long long)h->graph_nodes[parity];
     CK(cudaMemcpyAsync(h->host_loop, h->g.loop, sizeof(LoopState), cudaMemcpyDeviceToHost, h->stream));
+    int status = 0;
+    if (h->arith == MHD2D_ARITH_CHECKED)
+      CK(cudaMemcpyAsync(&status, h->g.status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     st = *h->host_loop;
+    if (status & mhdk::kStatusIndex) {
+      h->cur = st.cur;
+      h->last_cycles_run = st.cycles_run;
+      return MHD_ERR_INDEX;
+    }
     if (!std::isfinite(st.t) || !std::isfinite(st.dt)) {
       h->cur = st.cur;
       h->last_cycles_run = st.cycles_run;
@@ -660,6 +681,17 @@ int mhd2d_validate(void* handle, long long* counts) {
   return MHD_OK;
 }
 
+int mhd2d_check_info(void* handle, long long* line, long long* index) {
+  Handle* h = static_cast<Handle*>(handle);
+  if (!h) return MHD_ERR_ARG;
+  long long bad[2] = {0, 0};
+  CK(cudaMemcpyAsync(bad, h->g.bad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (line) *line = bad[0];
+  if (index) *index = bad[1];
+  return MHD_OK;
+}
+
 int mhd2d_stream(void* handle, void** stream) {
   Handle* h = static_cast<Handle*>(handle);
   if (!h || !stream) return MHD_ERR_ARG;
@@ -679,7 +711,7 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
   if (count < 1 || !ny || !nx || !dx || !dy || !bcx || !bcy || !gamma) return MHD_ERR_ARG;
   if (physics != MHD2D_HYDRO && physics != MHD2D_MHD) return MHD_ERR_ARG;
   if (recon != 0 && recon != 1 && recon != 2) return MHD_ERR_ARG;
-  if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST) return MHD_ERR_ARG;
+  if (arith != MHD2D_ARITH_EXACT && arith != MHD2D_ARITH_FAST && arith != MHD2D_ARITH_CHECKED) return MHD_ERR_ARG;
   for (int i = 0; i < count; ++i) {
     if (nx[i] < 2 || ny[i] < 2 || !(dx[i] > 0.0) || !(dy[i] > 0.0)) return MHD_ERR_ARG;
     if ((bcx[i] != 0 && bcx[i] != 1) || (bcy[i] != 0 && bcy[i] != 1)) return MHD_ERR_ARG;
@@ -712,7 +744,8 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
     grid_bytes += carve_grid(g, b->nvars, nullptr);
   }
   const size_t total = grid_bytes + align256(count * sizeof(LoopState)) + align256(count * sizeof(Grid)) +
-                       align256(count * sizeof(int)) + align256(count * sizeof(unsigned long long));
+                       align256(count * sizeof(int)) + align256(count * sizeof(unsigned long long)) +
+                       align256(2 * sizeof(long long));
   e = cudaMalloc(&b->arena, total);
   if (e != cudaSuccess) { free_batch(b); return cuda_fail(e); }
   b->arena_bytes = total;
@@ -726,12 +759,15 @@ int mhdb_create(int count, const int* ny, const int* nx, const double* dx, const
   int* status = reinterpret_cast<int*>(base + off);
   off += align256(count * sizeof(int));
   unsigned long long* hits = reinterpret_cast<unsigned long long*>(base + off);
+  off += align256(count * sizeof(unsigned long long));
+  long long* bad = reinterpret_cast<long long*>(base + off);
   b->d_status = status;
   b->d_floor_hits = hits;
   for (int i = 0; i < count; ++i) {
     b->grids[i].loop = b->d_loops + i;
     b->grids[i].status = status + i;
     b->grids[i].floor_hits = hits + i;
+    b->grids[i].bad = bad;
   }
   e = cudaMemsetAsync(b->arena, 0, total, b->stream);
   b->view.grids = b->d_grids;
@@ -856,6 +892,12 @@ int mhdb_advance(void* handle, const double* t0, const double* t_end, const long
     b->last_launches += budget * (long long)b->graph_nodes;
     CK(cudaMemcpyAsync(b->h_loops, b->d_loops, b->count * sizeof(LoopState), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
+    if (b->arith == MHD2D_ARITH_CHECKED) {
+      std::vector<int> st(b->count);
+      CK(cudaMemcpy(st.data(), b->d_status, b->count * sizeof(int), cudaMemcpyDeviceToHost));
+      for (int i = 0; i < b->count; ++i)
+        if (st[i] & mhdk::kStatusIndex) return MHD_ERR_INDEX;
+    }
     // An instance whose time or dt went non-finite has stopped by itself (NaN < t_end
     // is false, so its kernels skip it); the others keep advancing.
     for (int i = 0; i < b->count; ++i)

@@ -40,6 +40,53 @@ __device__ __forceinline__ int wrapc(int c, int L, int bc) {
 }
 
 // ----------------------------------------------------------------------------
+// Checked build (MHD_CHECKED, the "checked" arithmetic mode): every global access
+// of the per-item bodies below is preceded by MHD_GUARD(G, base, idx), which
+// requires the in-plane index idx to lie inside one plane of the array that starts
+// at `base` (each access is base[k * plane + idx] with k a compile-time slot below
+// the array's plane count).  A violation sets kStatusIndex in the grid's error
+// word, records the first offending source line and index, and skips the item: it
+// never traps and never touches memory outside the array.  In the other builds
+// MHD_GUARD is empty.
+// ----------------------------------------------------------------------------
+#ifdef MHD_CHECKED
+// elements in one plane of the grid array that starts at base (0: not an array of G)
+__device__ __forceinline__ size_t plane_extent(const Grid& G, const void* base) {
+  const size_t cp = cell_plane(G), xp = xface_plane(G), yp = yface_plane(G), kp = corner_plane(G);
+  for (int b = 0; b < 2; ++b) {
+    if (base == G.st[b].prim || base == G.st[b].cons) return cp;
+    if (base == G.st[b].fbx) return xp;
+    if (base == G.st[b].fby) return yp;
+  }
+  if (base == G.xl || base == G.xr || base == G.fx || base == G.uxl || base == G.uxr || base == G.nfbx) return xp;
+  if (base == G.yl || base == G.yr || base == G.fy || base == G.uyl || base == G.uyr || base == G.nfby) return yp;
+  if (base == G.emf) return kp;
+  if (base == G.hez) return cp;
+  if (base == G.slopes || base == G.eig || base == G.slopes_y || base == G.eig_y) return G.ext_plane;
+  if (base == G.dt_log) return (size_t)G.dt_log_cap;
+  return 0;
+}
+__device__ __noinline__ void report_index(const Grid& G, int line, size_t idx) {
+  if (G.status) atomicOr(G.status, kStatusIndex);
+  if (G.bad && atomicCAS(reinterpret_cast<unsigned long long*>(G.bad), 0ull, (unsigned long long)line) == 0ull)
+    G.bad[1] = (long long)idx;
+}
+#define MHD_GUARD(G, base, idx)                                               \
+  do {                                                                        \
+    const size_t i_ = (idx);                                                  \
+    if (!(i_ < plane_extent((G), (base)))) { report_index((G), __LINE__, i_); return; } \
+  } while (0)
+#define MHD_GUARD_RET(G, base, idx, ret)                                      \
+  do {                                                                        \
+    const size_t i_ = (idx);                                                  \
+    if (!(i_ < plane_extent((G), (base)))) { report_index((G), __LINE__, i_); return (ret); } \
+  } while (0)
+#else
+#define MHD_GUARD(G, base, idx) do {} while (0)
+#define MHD_GUARD_RET(G, base, idx, ret) do {} while (0)
+#endif
+
+// ----------------------------------------------------------------------------
 // Sweep policies
 // ----------------------------------------------------------------------------
 // Sweep vectors [rho, v, B_t1, B_t2, p] in the frame (n, t1, t2): x (vx, vy, vz) with
@@ -145,9 +192,10 @@ __device__ __forceinline__ size_t face_index(int f, int t, int nx) {
 }
 
 template <class S, int AX>
-__device__ __forceinline__ void load_sweep_cell(const double* prim, size_t plane, int c, int t,
+__device__ __forceinline__ void load_sweep_cell(const Grid& G, const double* prim, size_t plane, int c, int t,
                                                 const SweepGeom& g, double* w) {
   const size_t idx = cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx);
+  MHD_GUARD(G, prim, idx);
 #pragma unroll
   for (int k = 0; k < S::NV; ++k) w[k] = __ldg(prim + S::src(k) * plane + idx);
 }
@@ -219,10 +267,11 @@ __device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, 
   const size_t plane = cell_plane(G);
   constexpr int NV = S::NV;
   double wl[NV], wc[NV], wr[NV];
-  load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
-  load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
-  load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
+  load_sweep_cell<S, AX>(G, in.prim, plane, c - 1, t, g, wl);
+  load_sweep_cell<S, AX>(G, in.prim, plane, c, t, g, wc);
+  load_sweep_cell<S, AX>(G, in.prim, plane, c + 1, t, g, wr);
   double bn = 0.0;
+  MHD_GUARD(G, in.prim, cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx));
   if (S::BN >= 0)
     bn = G.one_d ? G.bx1d
                  : __ldg(in.prim + (size_t)(S::BN >= 0 ? S::BN : 0) * plane + cell_index<AX>(wrapc(c, g.Ls, g.bc), t, g.nx));
@@ -232,6 +281,8 @@ __device__ __forceinline__ void b_ppm_slopes(const Grid& G, const StateBuf& in, 
   limited_slopes<S>(wl, wc, wr, e, ps);
   const size_t xi = ext_index<AX>(c, t, g.nx);
   const size_t es = G.ext_plane;
+  MHD_GUARD(G, AX == 0 ? G.slopes : G.slopes_y, xi);
+  MHD_GUARD(G, AX == 0 ? G.eig : G.eig_y, xi);
 #pragma unroll
   for (int i = 0; i < NV; ++i) (AX == 0 ? G.slopes : G.slopes_y)[i * es + xi] = ps[i];
   S::store(e, (AX == 0 ? G.eig : G.eig_y) + xi, es);
@@ -268,9 +319,12 @@ __device__ __forceinline__ void note_nonfinite(const Grid& G, bool bad) {
 // B source term of one face state: half_dt * v_t(cell) * ((fb[f2] - fb[f1]) * inv_dn)
 // (Source/Reconstruction_PPM_MHD_HelperModule.py:1193-1239)
 template <int AX>
-__device__ __forceinline__ double bsource(const double* prim, const double* fb, size_t plane, int cell, int f1,
-                                          int f2, int t, int nx, double half_dt, double inv_dn) {
+__device__ __forceinline__ double bsource(const Grid& G, const double* prim, const double* fb, size_t plane, int cell,
+                                          int f1, int f2, int t, int nx, double half_dt, double inv_dn) {
   const int vslot = AX == 0 ? 2 : 1;
+  MHD_GUARD_RET(G, prim, cell_index<AX>(cell, t, nx), 0.0);
+  MHD_GUARD_RET(G, fb, face_index<AX>(f2, t, nx), 0.0);
+  MHD_GUARD_RET(G, fb, face_index<AX>(f1, t, nx), 0.0);
   const double vt = __ldg(prim + vslot * plane + cell_index<AX>(cell, t, nx));
   const double b2 = __ldg(fb + face_index<AX>(f2, t, nx));
   const double b1 = __ldg(fb + face_index<AX>(f1, t, nx));
@@ -466,10 +520,10 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
   const double dn = AX == 0 ? G.dx : G.dy;
   double lia[NV], ria[NV];
   double wc[NV], wl[NV], wr[NV];
-  load_sweep_cell<S, AX>(in.prim, plane, c, t, g, wc);
+  load_sweep_cell<S, AX>(G, in.prim, plane, c, t, g, wc);
   if (MODE != 0) {
-    load_sweep_cell<S, AX>(in.prim, plane, c - 1, t, g, wl);
-    load_sweep_cell<S, AX>(in.prim, plane, c + 1, t, g, wr);
+    load_sweep_cell<S, AX>(G, in.prim, plane, c - 1, t, g, wl);
+    load_sweep_cell<S, AX>(G, in.prim, plane, c + 1, t, g, wr);
   }
   {
     const size_t es = G.ext_plane;
@@ -477,6 +531,11 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
     const double* sl = AX == 0 ? G.slopes : G.slopes_y;
     const double* eg = AX == 0 ? G.eig : G.eig_y;
     const size_t step = AX == 0 ? 1 : (size_t)g.nx;
+    if (MODE != 0) {
+      MHD_GUARD(G, sl, xc - step);
+      MHD_GUARD(G, sl, xc + step);
+      MHD_GUARD(G, eg, xc);
+    }
     edge_states<S, MODE>(
         wl, wc, wr, [&](int k, int d) { return sl[k * es + xc + (ptrdiff_t)d * (ptrdiff_t)step]; },
         [&](typename S::Eig& e) { S::load(e, eg + xc, es); }, dt, dn, lia, ria);
@@ -494,16 +553,20 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
     const double* fb = AX == 0 ? in.fbx : in.fby;
     const double half_dt = 0.5 * dt;
     const double inv_dn = 1.0 / dn;
-    s_mid = bsource<AX>(in.prim, fb, plane, c, c, c + 1, t, g.nx, half_dt, inv_dn);
+    s_mid = bsource<AX>(G, in.prim, fb, plane, c, c, c + 1, t, g.nx, half_dt, inv_dn);
     if (c == 0) {
-      if (g.bc == OUTFLOW) s_lo = bsource<AX>(in.prim, fb, plane, 0, 0, 0, t, g.nx, half_dt, inv_dn);
-      else s_hi = bsource<AX>(in.prim, fb, plane, 0, Ls, 1, t, g.nx, half_dt, inv_dn);
+      if (g.bc == OUTFLOW) s_lo = bsource<AX>(G, in.prim, fb, plane, 0, 0, 0, t, g.nx, half_dt, inv_dn);
+      else s_hi = bsource<AX>(G, in.prim, fb, plane, 0, Ls, 1, t, g.nx, half_dt, inv_dn);
     }
     if (c == Ls - 1) {
-      if (g.bc == OUTFLOW) s_hi = bsource<AX>(in.prim, fb, plane, Ls - 1, Ls, Ls, t, g.nx, half_dt, inv_dn);
-      else s_lo = bsource<AX>(in.prim, fb, plane, Ls - 1, Ls - 1, 0, t, g.nx, half_dt, inv_dn);
+      if (g.bc == OUTFLOW) s_hi = bsource<AX>(G, in.prim, fb, plane, Ls - 1, Ls, Ls, t, g.nx, half_dt, inv_dn);
+      else s_lo = bsource<AX>(G, in.prim, fb, plane, Ls - 1, Ls - 1, 0, t, g.nx, half_dt, inv_dn);
     }
   }
+  MHD_GUARD(G, outR, face_index<AX>(c, t, g.nx));
+  MHD_GUARD(G, outL, face_index<AX>(c + 1, t, g.nx));
+  MHD_GUARD(G, outL, face_index<AX>(0, t, g.nx));
+  MHD_GUARD(G, outR, face_index<AX>(Ls, t, g.nx));
   unsigned hits = put_face<S>(outR, fplane, face_index<AX>(c, t, g.nx), lia, G.min_d, G.min_p, s_mid, src);
   hits += put_face<S>(outL, fplane, face_index<AX>(c + 1, t, g.nx), ria, G.min_d, G.min_p, s_mid, src);
   if (c == 0) {
@@ -531,6 +594,14 @@ __device__ __forceinline__ void b_roe_mhd(const Grid& G, const StateBuf& in, siz
   constexpr int N = AX == 0 ? 1 : 2, T1 = AX == 0 ? 2 : 3, T2 = AX == 0 ? 3 : 1;
   const double* WL = AX == 0 ? G.xl : G.yl;
   const double* WR = AX == 0 ? G.xr : G.yr;
+  MHD_GUARD(G, WL, f);
+  MHD_GUARD(G, WR, f);
+  MHD_GUARD(G, AX == 0 ? G.fx : G.fy, f);
+  MHD_GUARD(G, STAGE == 1 ? (AX == 0 ? in.fbx : in.fby) : (AX == 0 ? G.nfbx : G.nfby), f);
+  if (STAGE == 2) {
+    MHD_GUARD(G, AX == 0 ? G.uxl : G.uyl, f);
+    MHD_GUARD(G, AX == 0 ? G.uxr : G.uyr, f);
+  }
   double wl[7], wr[7], ul[7], ur[7];
 #pragma unroll
   for (int k = 0; k < 7; ++k) { wl[k] = WL[k * nf + f]; wr[k] = WR[k * nf + f]; }
@@ -560,6 +631,9 @@ __device__ __forceinline__ void b_roe_hydro(const Grid& G, size_t f) {
   if (f >= nf) return;
   const double* WL = AX == 0 ? G.xl : G.yl;
   const double* WR = AX == 0 ? G.xr : G.yr;
+  MHD_GUARD(G, WL, f);
+  MHD_GUARD(G, WR, f);
+  MHD_GUARD(G, AX == 0 ? G.fx : G.fy, f);
   double wl[5], wr[5], flux[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) { wl[k] = WL[k * nf + f]; wr[k] = WR[k * nf + f]; }
@@ -577,6 +651,7 @@ __device__ __forceinline__ void b_roe_hydro(const Grid& G, size_t f) {
 template <int STAGE>
 __device__ __forceinline__ double cell_ez(const Grid& G, const StateBuf& in, int j, int i) {
   const size_t idx = (size_t)j * G.nx + i;
+  MHD_GUARD_RET(G, G.hez, idx, 0.0);
   if (STAGE == 2) return G.hez[idx];
   const size_t plane = cell_plane(G);
   return __ldg(in.prim + 2 * plane + idx) * __ldg(in.prim + 4 * plane + idx)
@@ -592,6 +667,11 @@ __device__ __forceinline__ void b_emf(const Grid& G, const StateBuf& in, int I, 
   const int ic = wrapc(I, nx, G.bcx), im = wrapc(I - 1, nx, G.bcx);
   const int jc = wrapc(J, ny, G.bcy), jm = wrapc(J - 1, ny, G.bcy);
   const size_t yfp = yface_plane(G), xfp = xface_plane(G);
+  MHD_GUARD(G, G.fy, (size_t)J * nx + ic);
+  MHD_GUARD(G, G.fy, (size_t)J * nx + im);
+  MHD_GUARD(G, G.fx, (size_t)jc * (nx + 1) + I);
+  MHD_GUARD(G, G.fx, (size_t)jm * (nx + 1) + I);
+  MHD_GUARD(G, G.emf, (size_t)J * (nx + 1) + I);
   // y-face fluxes of row J at columns I (top) and I-1 (ltop)
   const double top0 = G.fy[0 * yfp + (size_t)J * nx + ic];
   const double top5 = G.fy[5 * yfp + (size_t)J * nx + ic];
@@ -646,7 +726,26 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
   const double half_dtdt = 0.5 * (dt / (AX == 0 ? G.dy : G.dx));   // transverse
   const size_t plane = cell_plane(G);
   const double* fb = AX == 0 ? in.fbx : in.fby;
-  auto fbv = [&](int ff) { return fb[face_index<AX>(ff, t, nx)]; };
+  auto fbv = [&](int ff) -> double {
+    const size_t ii = face_index<AX>(ff, t, nx);
+#ifdef MHD_CHECKED
+    if (!(ii < plane_extent(G, fb))) { report_index(G, __LINE__, ii); return 0.0; }
+#endif
+    return fb[ii];
+  };
+  MHD_GUARD(G, fb, fl);
+  MHD_GUARD(G, AX == 0 ? G.nfbx : G.nfby, fl);
+  MHD_GUARD(G, AX == 0 ? G.xl : G.yl, fl);
+  MHD_GUARD(G, AX == 0 ? G.xr : G.yr, fl);
+  MHD_GUARD(G, AX == 0 ? G.uxl : G.uyl, fl);
+  MHD_GUARD(G, AX == 0 ? G.uxr : G.uyr, fl);
+  if (AX == 0) {
+    MHD_GUARD(G, G.emf, (size_t)(row + 1) * (nx + 1) + col);
+    MHD_GUARD(G, G.emf, (size_t)row * (nx + 1) + col);
+  } else {
+    MHD_GUARD(G, G.emf, (size_t)row * (nx + 1) + col + 1);
+    MHD_GUARD(G, G.emf, (size_t)row * (nx + 1) + col);
+  }
   const double bn = fb[fl];
 
   // half-step face B from the stage-1 corner EMF (Source/EvolveFunctions_MHD.py:579-586)
@@ -699,6 +798,7 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
     }
     const double dB = rb - lb;
     const size_t sidx = cell_index<AX>(scell, t, nx);
+    MHD_GUARD(G, in.prim, sidx);
     const double cbx = __ldg(in.prim + 4 * plane + sidx);
     const double cby = __ldg(in.prim + 5 * plane + sidx);
     const double cbz = __ldg(in.prim + 6 * plane + sidx);
@@ -719,6 +819,8 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
     size_t i_lo, i_hi;  // lower/upper transverse face of cell (fc, t)
     if (AX == 0) { i_lo = (size_t)t * nx + fc; i_hi = (size_t)(t + 1) * nx + fc; }
     else { i_lo = (size_t)fc * (nx + 1) + t; i_hi = (size_t)fc * (nx + 1) + t + 1; }
+    MHD_GUARD(G, F, i_lo);
+    MHD_GUARD(G, F, i_hi);
     double fh[7], flo[7];
 #pragma unroll
     for (int k = 0; k < 7; ++k) { fh[k] = F[k * tfp + i_hi]; flo[k] = F[k * tfp + i_lo]; }
@@ -765,6 +867,8 @@ __device__ __forceinline__ void b_ctu_hydro(const Grid& G, size_t fl) {
   double* Wout[2] = {AX == 0 ? G.xl : G.yl, AX == 0 ? G.xr : G.yr};
   const double* F = AX == 0 ? G.fy : G.fx;
   const size_t tfp = AX == 0 ? yface_plane(G) : xface_plane(G);
+  MHD_GUARD(G, Wout[0], fl);
+  MHD_GUARD(G, Wout[1], fl);
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
     double w[5], u[5];
@@ -775,6 +879,8 @@ __device__ __forceinline__ void b_ctu_hydro(const Grid& G, size_t fl) {
     size_t i_lo, i_hi;
     if (AX == 0) { i_lo = (size_t)t * nx + fc; i_hi = (size_t)(t + 1) * nx + fc; }
     else { i_lo = (size_t)fc * (nx + 1) + t; i_hi = (size_t)fc * (nx + 1) + t + 1; }
+    MHD_GUARD(G, F, i_lo);
+    MHD_GUARD(G, F, i_hi);
 #pragma unroll
     for (int k = 0; k < 5; ++k) u[k] = u[k] - half_dtdt * (F[k * tfp + i_hi] - F[k * tfp + i_lo]);
     hcons_to_prim<AX>(u, G.gamma, w);
@@ -796,6 +902,16 @@ __device__ __forceinline__ void b_half_ez(const Grid& G, const StateBuf& in, int
   const size_t idx = (size_t)j * nx + i;
   const size_t xr = (size_t)j * (nx + 1) + i + 1, xlf = (size_t)j * (nx + 1) + i;
   const size_t yb = (size_t)(j + 1) * nx + i, yt = (size_t)j * nx + i;
+  MHD_GUARD(G, in.cons, idx);
+  MHD_GUARD(G, G.hez, idx);
+  MHD_GUARD(G, G.fx, xr);
+  MHD_GUARD(G, G.fx, xlf);
+  MHD_GUARD(G, G.fy, yb);
+  MHD_GUARD(G, G.fy, yt);
+  MHD_GUARD(G, G.nfbx, xr);
+  MHD_GUARD(G, G.nfbx, xlf);
+  MHD_GUARD(G, G.nfby, yb);
+  MHD_GUARD(G, G.nfby, yt);
   double hu[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -827,6 +943,23 @@ __device__ __forceinline__ void b_final_mhd(const Grid& G, const StateBuf& in, c
   const size_t yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
   const size_t cw = nx + 1;
   const double* E = G.emf;
+  MHD_GUARD(G, in.cons, idx);
+  MHD_GUARD(G, out.prim, idx);
+  MHD_GUARD(G, out.cons, idx);
+  MHD_GUARD(G, in.fbx, xlf);
+  MHD_GUARD(G, in.fbx, xr);
+  MHD_GUARD(G, in.fby, yt);
+  MHD_GUARD(G, in.fby, yb);
+  MHD_GUARD(G, out.fbx, xlf);
+  MHD_GUARD(G, out.fbx, xr);
+  MHD_GUARD(G, out.fby, yt);
+  MHD_GUARD(G, out.fby, yb);
+  MHD_GUARD(G, G.fx, xlf);
+  MHD_GUARD(G, G.fx, xr);
+  MHD_GUARD(G, G.fy, yt);
+  MHD_GUARD(G, G.fy, yb);
+  MHD_GUARD(G, E, (size_t)j * cw + i);
+  MHD_GUARD(G, E, (size_t)(j + 1) * cw + i + 1);
   // full-step face B (Source/EvolveFunctions_MHD.py:644-645)
   const double bxl = in.fbx[xlf] - dtdy * (E[(size_t)(j + 1) * cw + i] - E[(size_t)j * cw + i]);
   const double bxr = in.fbx[xr] - dtdy * (E[(size_t)(j + 1) * cw + i + 1] - E[(size_t)j * cw + i + 1]);
@@ -882,6 +1015,13 @@ __device__ __forceinline__ void b_final_hydro(const Grid& G, const StateBuf& in,
   const size_t idx = (size_t)j * nx + i;
   const size_t xlf = (size_t)j * (nx + 1) + i, xr = xlf + 1;
   const size_t yt = (size_t)j * nx + i, yb = (size_t)(j + 1) * nx + i;
+  MHD_GUARD(G, in.cons, idx);
+  MHD_GUARD(G, out.prim, idx);
+  MHD_GUARD(G, out.cons, idx);
+  MHD_GUARD(G, G.fx, xlf);
+  MHD_GUARD(G, G.fx, xr);
+  MHD_GUARD(G, G.fy, yt);
+  MHD_GUARD(G, G.fy, yb);
   double u[5], w[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
@@ -919,6 +1059,11 @@ __device__ __forceinline__ void b_dt_cell(const Grid& G, const StateBuf& in, siz
   const size_t plane = cell_plane(G);
   const double gamma = G.gamma;
   const double* c = in.cons;
+  MHD_GUARD(G, c, idx);
+  if (PHYS == MHD) {
+    MHD_GUARD(G, in.fbx, (size_t)(idx / nx) * (nx + 1) + idx % nx);
+    MHD_GUARD(G, in.fby, idx);
+  }
   const double inv_d = 1.0 / c[idx];
   const double vx = c[plane + idx] * inv_d;
   const double vy = c[2 * plane + idx] * inv_d;
@@ -1004,7 +1149,14 @@ __device__ __forceinline__ void b_begin(const Grid& G) {
 __device__ __forceinline__ void b_end(const Grid& G) {
   LoopState* L = G.loop;
   if (!L->active) return;
-  if (G.dt_log && L->cycle >= 0 && L->cycle < G.dt_log_cap) G.dt_log[L->cycle] = L->dt;
+  if (G.dt_log && L->cycle >= 0 && L->cycle < G.dt_log_cap) {
+#ifdef MHD_CHECKED
+    // (no early return here: the loop bookkeeping below must run)
+    if (!((size_t)L->cycle < plane_extent(G, G.dt_log))) report_index(G, __LINE__, (size_t)L->cycle);
+    else
+#endif
+    G.dt_log[L->cycle] = L->dt;
+  }
   L->t_prev = L->t;
   L->t = L->t + L->dt;
   L->cycle = L->cycle + 1;
@@ -1082,6 +1234,7 @@ __device__ __forceinline__ void b_dt_cell_1d(const Grid& G, const StateBuf& in, 
   const size_t plane = cell_plane(G);
   const double gamma = G.gamma;
   const double* c = in.cons;
+  MHD_GUARD(G, c, i);
   const double inv_d = 1.0 / c[i];
   const double vx = c[plane + i] * inv_d;
   const double vy = c[2 * plane + i] * inv_d;
@@ -1119,6 +1272,10 @@ __global__ void __launch_bounds__(kBlock) k_update_1d(Grid G, StateBuf in, State
   if (i >= G.nx) return;
   const double dtdx = G.loop->dt / G.dx;
   const size_t plane = cell_plane(G), fp = xface_plane(G);
+  MHD_GUARD(G, in.cons, (size_t)i);
+  MHD_GUARD(G, out.prim, (size_t)i);
+  MHD_GUARD(G, out.cons, (size_t)i);
+  MHD_GUARD(G, G.fx, (size_t)i + 1);
   if (PHYS == MHD) {
     constexpr int src[7] = {0, 1, 2, 3, 5, 6, 7};
     double u[7], w[7];

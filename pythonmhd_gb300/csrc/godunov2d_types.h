@@ -74,6 +74,7 @@ struct Grid {
   LoopState* loop;             // device
   int* status;                 // device error word (0 = ok; kStatusNonfinite, kStatusIndex bits)
   unsigned long long* floor_hits;  // device count of floored values (may be null)
+  long long* bad;                  // checked builds: first failed index check (source line, index)
   // 1D grids (ny = 1): the x sweep only, no transverse or CT stages; MHD keeps
   // B_x uniform at bx1d (the reference's evolve_1D_mhd)
   int one_d;

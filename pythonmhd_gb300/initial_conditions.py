@@ -214,63 +214,108 @@ def orszag_tang_batch(count=256, seed=0, sizes=tuple(range(64, 513, 32)), gamma_
 # ---------------------------------------------------------------------------
 # the same generator with the transforms and field algebra on the GPU
 # ---------------------------------------------------------------------------
-def _gaussian_field_device(rng, n, slope, kmin, kmax, device):
-    """``_gaussian_field`` with the inverse FFT on the device (cuFFT through torch).
-
-    The random coefficients come from the same NumPy generator in the same order,
-    so the field equals the host one up to the transform's rounding."""
-    import torch
+def _band(rng, n, slope, kmin, kmax):
+    """The in-band coefficients of ``_gaussian_field``'s spectrum: flat indices into the
+    (n, n//2 + 1) half-spectrum and the real and imaginary parts, drawn from the same
+    NumPy stream in the same order (whole arrays of normals, then the band's share)."""
     kx = np.fft.rfftfreq(n, d=1.0 / n)
     ky = np.fft.fftfreq(n, d=1.0 / n)
     KX, KY = np.meshgrid(kx, ky)
     k = np.sqrt(KX * KX + KY * KY)
     mask = (k >= kmin) & (k <= kmax)
-    amp = np.zeros_like(k)
-    amp[mask] = k[mask] ** (-slope / 2.0)
+    amp = k[mask] ** (-slope / 2.0)
     re = rng.standard_normal(k.shape)
     im = rng.standard_normal(k.shape)
-    c = torch.complex(torch.from_numpy(re * amp), torch.from_numpy(im * amp)).to(device)
-    f = torch.fft.irfft2(c, s=(n, n))
-    return f - f.mean()
+    return np.flatnonzero(mask).astype(np.int32), re[mask] * amp, im[mask] * amp
+
+
+def _gaussian_field_device(lib, rng, n, slope, kmin, kmax, device, stream):
+    """``_gaussian_field`` before its zero-mean shift, on the device: the band's
+    coefficients (a few thousand) are uploaded and scattered into the half-spectrum
+    by the project's kernel (``mhd_ic_scatter_spectrum``), and cuFFT inverts it."""
+    import ctypes
+
+    import torch
+    idx, re, im = _band(rng, n, slope, kmin, kmax)
+    spec = torch.zeros((n, n // 2 + 1), dtype=torch.complex128, device=device)
+    t_idx = torch.from_numpy(idx).to(device)
+    t_re = torch.from_numpy(np.ascontiguousarray(re)).to(device)
+    t_im = torch.from_numpy(np.ascontiguousarray(im)).to(device)
+    rc = lib.mhd_ic_scatter_spectrum(len(idx), ctypes.c_void_p(t_idx.data_ptr()), ctypes.c_void_p(t_re.data_ptr()),
+                                     ctypes.c_void_p(t_im.data_ptr()), ctypes.c_void_p(spec.data_ptr()), stream)
+    from . import _lib
+    _lib.check(rc, "mhd_ic_scatter_spectrum")
+    return torch.fft.irfft2(spec, s=(n, n)).contiguous()
 
 
 def turbulence_device(n, seed=1, gamma=5.0 / 3.0, kmax_v=32, kmax_a=16, mach=1.0, beta=1.0, device="cuda"):
     """``turbulence`` generated on the GPU: returns (prim, cons, faceBx, faceBy) as
     float64 torch tensors on ``device`` plus dx, dy, ready for
-    ``mhd2d_upload_device`` -- no n^2 transform or field array on the host.  The
-    state equals ``turbulence``'s to rounding (the transforms and reductions are
-    evaluated differently)."""
+    ``mhd2d_upload_device`` -- no n^2 field on the host.  The random coefficients
+    come from the same seeded NumPy stream; the inverse transforms run in cuFFT and
+    the field algebra in the project's kernels (``mhd_ic_turbulence_2d``), so the
+    state equals ``turbulence``'s to rounding."""
+    import ctypes
+
     import torch
+
+    from . import _lib
+    lib = _lib.load()
+    device = torch.device(device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
     rng = np.random.default_rng(seed)
-    g = _gaussian_field_device(rng, n, 2.0, 1.0, kmax_v, device)
-    g = g / g.std(unbiased=False)
-    vx = _gaussian_field_device(rng, n, 2.0, 1.0, kmax_v, device)
-    vy = _gaussian_field_device(rng, n, 2.0, 1.0, kmax_v, device)
-    az = _gaussian_field_device(rng, n, 3.0, 1.0, kmax_a, device)
-    dx = dy = 1.0 / n
-    rho = torch.exp(0.1 * g)
-    p = torch.full((n, n), 1.0 / gamma, dtype=torch.float64, device=device)
-    cs2 = gamma * p / rho
-    vscale = mach / torch.sqrt(torch.mean((vx * vx + vy * vy) / cs2))
-    vx = vx * vscale
-    vy = vy * vscale
-    bxf = torch.roll(az, -1, dims=0) - az
-    byf = -(torch.roll(az, -1, dims=1) - az)
-    fbx = torch.cat([bxf, bxf[:, :1]], dim=1) / dy
-    fby = torch.cat([byf, byf[:1, :]], dim=0) / dx
-    cbx = (fbx[:, :-1] + fbx[:, 1:]) / 2.0
-    cby = (fby[:-1, :] + fby[1:, :]) / 2.0
-    bscale = torch.sqrt(2.0 * (1.0 / gamma) / beta / torch.mean(cbx * cbx + cby * cby))
-    fbx = fbx * bscale
-    fby = fby * bscale
-    cbx = (fbx[:, :-1] + fbx[:, 1:]) / 2.0
-    cby = (fby[:-1, :] + fby[1:, :]) / 2.0
-    zero = torch.zeros_like(rho)
-    prim = torch.stack([rho, vx, vy, zero, cbx, cby, zero, p])
-    e = p / (gamma - 1.0) + 0.5 * rho * (vx * vx + vy * vy + zero * zero)
-    e = e + 0.5 * (cbx * cbx + cby * cby + zero * zero)
-    cons = torch.stack([rho, rho * vx, rho * vy, rho * zero, cbx, cby, zero, e])
-    return prim.contiguous(), cons.contiguous(), fbx.contiguous(), fby.contiguous(), dx, dy
+    fields = [_gaussian_field_device(lib, rng, n, sl, 1.0, km, device, stream)
+              for sl, km in ((2.0, kmax_v), (2.0, kmax_v), (2.0, kmax_v), (3.0, kmax_a))]
+    prim = torch.empty((8, n, n), dtype=torch.float64, device=device)
+    cons = torch.empty_like(prim)
+    fbx = torch.empty((n, n + 1), dtype=torch.float64, device=device)
+    fby = torch.empty((n + 1, n), dtype=torch.float64, device=device)
+    words = int(lib.mhd_ic_work_words())
+    work = torch.empty(words, dtype=torch.float64, device=device)
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    _lib.check(lib.mhd_ic_turbulence_2d(n, float(gamma), float(mach), float(beta), *[ptr(f) for f in fields],
+                                        ptr(prim), ptr(cons), ptr(fbx), ptr(fby), ptr(work), words, stream),
+               "mhd_ic_turbulence_2d")
+    torch.cuda.current_stream(device).synchronize()
+    return prim, cons, fbx, fby, 1.0 / n, 1.0 / n
+
+
+def orszag_tang_batch_device(count=256, seed=0, sizes=tuple(range(64, 513, 32)), gamma_range=(1.4, 5.0 / 3.0),
+                             b0_range=(0.5, 2.0), rho_perturb=0.01, device="cuda"):
+    """``orszag_tang_batch`` with the states built on the GPU (``mhd_ic_orszag_tang``):
+    the same draws from the same seeded streams (sizes, gamma, B0 scale, and each
+    instance's density noise, uploaded), the vortex evaluated on the device.  The
+    instances' prim, cons, fbx, fby are float64 torch tensors on ``device``; they
+    equal the host generator's to rounding (device sin/cos)."""
+    import ctypes
+
+    import torch
+
+    from . import _lib
+    lib = _lib.load()
+    device = torch.device(device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        nx = int(rng.choice(sizes))
+        ny = int(rng.choice(sizes))
+        gamma = float(rng.uniform(*gamma_range))
+        b0 = float(rng.uniform(*b0_range))
+        noise = None
+        if rho_perturb:
+            noise = torch.from_numpy(np.random.default_rng(seed * 100003 + k).standard_normal((ny, nx))).to(device)
+        prim = torch.empty((8, ny, nx), dtype=torch.float64, device=device)
+        cons = torch.empty_like(prim)
+        fbx = torch.empty((ny, nx + 1), dtype=torch.float64, device=device)
+        fby = torch.empty((ny + 1, nx), dtype=torch.float64, device=device)
+        ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        _lib.check(lib.mhd_ic_orszag_tang(nx, ny, gamma, b0, float(rho_perturb), ptr(noise), ptr(prim), ptr(cons),
+                                          ptr(fbx), ptr(fby), stream), "mhd_ic_orszag_tang")
+        out.append(dict(prim=prim, cons=cons, fbx=fbx, fby=fby, dx=1.0 / nx, dy=1.0 / ny, nx=nx, ny=ny, gamma=gamma,
+                        bcx=PERIODIC, bcy=PERIODIC))
+    torch.cuda.current_stream(device).synchronize()
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -8,7 +8,7 @@ import numpy as np
 
 from . import _lib
 
-ARITH = {"exact": 0, "fast": 1}
+ARITH = {"exact": 0, "fast": 1, "checked": 2}
 
 
 def default_arith() -> str:
@@ -203,6 +203,13 @@ class Grid2D:
                 raise RuntimeError(f"You have at least one {name} value in your {kind} variables matrix that is "
                                    f"less than the minimum {name} value for the simulation "
                                    f"({c[name + '_low']} values).")
+
+    def check_info(self):
+        """Checked arithmetic: (kernel source line, index) of the first failed index check
+        since the last upload, or (0, 0)."""
+        line, idx = ctypes.c_longlong(), ctypes.c_longlong()
+        _lib.check(self.lib.mhd2d_check_info(self._h, ctypes.byref(line), ctypes.byref(idx)), "mhd2d_check_info")
+        return line.value, idx.value
 
     def stats(self):
         """Failure counters since the last upload: ``{"floor_hits": n, "nan": bool}``."""
@@ -440,6 +447,23 @@ class Batch2D:
             raise ValueError(f"instance {k}: prim/cons must be {(self.nvars, ny, nx)}")
         _lib.check(self.lib.mhdb_upload(self._h, int(k), _ptr(prim), _ptr(cons), _ptr(fbx), _ptr(fby)),
                    "mhdb_upload")
+
+    def upload_device(self, k, prim, cons, fbx=None, fby=None):
+        """Upload instance k from contiguous float64 CUDA tensors of the batch's device."""
+        import torch
+
+        def ptr(t):
+            if t is None:
+                return None
+            if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError("upload_device expects contiguous float64 CUDA tensors")
+            return ctypes.c_void_p(t.data_ptr())
+        ny, nx = self.shapes[k]
+        if tuple(prim.shape) != (self.nvars, ny, nx) or tuple(cons.shape) != tuple(prim.shape):
+            raise ValueError(f"instance {k}: prim/cons must be {(self.nvars, ny, nx)}")
+        torch.cuda.current_stream(prim.device).synchronize()
+        _lib.check(self.lib.mhdb_upload_device(self._h, int(k), ptr(prim), ptr(cons), ptr(fbx), ptr(fby)),
+                   "mhdb_upload_device")
 
     def advance(self, t0, t_end, cycle0, max_cycles, cfl):
         n = self.count

@@ -16,7 +16,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(mhd(?:1d|2d|3d|b)_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mhd(?:1d|2d|3d|b)_\w+|mhd_ic_\w+)\s*\(", text)))
 
 
 @pytest.fixture(scope="module")
@@ -42,7 +42,7 @@ def test_ctypes_signatures_cover_the_header():
 
 
 def test_strerror_names_every_status(lib):
-    for code in range(0, 7):
+    for code in range(0, 9):
         assert lib.mhd2d_strerror(code).decode() not in ("", "unknown status")
     assert lib.mhd2d_strerror(99).decode() == "unknown status"
 
