@@ -66,21 +66,26 @@ def turbulence_fields(n, seed=1, gamma=5.0 / 3.0, kmax_v=16, kmax_a=16, mach=1.0
 
 
 def turbulence_batch(count=64, seed=0, sizes=tuple(range(128, 1025, 64)), gamma_range=(1.4, 5.0 / 3.0),
-                     kmax=16, mach=1.0, cells_per_wave=None):
+                     kmax=16, mach=1.0, cells_per_wave=None, kmax_v=None, kmax_a=None):
     """Uneven batch of turbulence fields: Nx and Ny drawn independently and uniformly
     from ``sizes``, gamma uniformly from ``gamma_range``, rms Mach ``mach``, instance k
-    generated with seed ``seed * 100003 + k``.  With ``cells_per_wave`` the spectral
-    cutoff of an instance is min(kmax, min(Nx, Ny) // cells_per_wave), so its
-    shortest wave spans at least that many cells.  Returns a list of field dicts
-    with nx, ny added."""
+    generated with seed ``seed * 100003 + k``.  The density and velocity spectra end at
+    ``kmax_v`` and the vector potential's at ``kmax_a`` (both default to ``kmax``).
+    With ``cells_per_wave`` each cutoff is further limited to min(Nx, Ny) //
+    cells_per_wave, so the shortest wave spans at least that many cells.  Returns a
+    list of field dicts with nx, ny added."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
         nx = int(rng.choice(sizes))
         ny = int(rng.choice(sizes))
         gamma = float(rng.uniform(*gamma_range))
-        km = kmax if cells_per_wave is None else max(1, min(kmax, min(nx, ny) // cells_per_wave))
-        f = turbulence_fields(nx, seed=seed * 100003 + k, gamma=gamma, kmax_v=km, kmax_a=km, ny=ny, mach=mach)
+        kv = kmax if kmax_v is None else kmax_v
+        ka = kmax if kmax_a is None else kmax_a
+        if cells_per_wave is not None:
+            kv = max(1, min(kv, min(nx, ny) // cells_per_wave))
+            ka = max(1, min(ka, min(nx, ny) // cells_per_wave))
+        f = turbulence_fields(nx, seed=seed * 100003 + k, gamma=gamma, kmax_v=kv, kmax_a=ka, ny=ny, mach=mach)
         f.update(nx=nx, ny=ny)
         out.append(f)
     return out
