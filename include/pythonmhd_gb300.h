@@ -338,6 +338,16 @@ int mhd2d_adj_reshape(void* handle, int ny, int nx, double dx, double dy, int bc
  * tapes) for an ny x nx grid: a whole checkpoint segment stays resident when
  * `every` times this fits the segment budget. */
 int mhd2d_adj_cycle_bytes(int ny, int nx, int recon, int entropy_fix, size_t* bytes);
+/* q[i] = b[i] / v[i] as the reverse sweeps compute it (n elements, device
+ * pointers; blocks until done): a refined reciprocal within two ulps of the
+ * correctly rounded quotient for divisors of magnitude 2^-1000 .. 2^1000, the
+ * correctly rounded quotient otherwise.  Exposed so that bound can be tested. */
+int mhd2d_adj_quotient(const double* b, const double* v, double* q, long long n);
+/* q[i] = x[i] / 6 as the exact-arithmetic kernels compute it in the PPM interface
+ * values (n elements, device pointers; blocks until done): one multiply and two FMAs
+ * (Markstein's remainder correction), correctly rounded, so equal bit for bit to
+ * the IEEE division.  Exposed so that the equality can be tested. */
+int mhd_quotient6(const double* x, double* q, long long n);
 /* Install a forward record made elsewhere (e.g. by the batched step): `steps`
  * cycles with the host dts `dt`, and the packed device states at cycles 0,
  * every, 2*every, ... in `checkpoints` (ceil(steps/every) states, one after the

@@ -111,6 +111,8 @@ SIGNATURES = {
     "mhd2d_adj_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
                                       ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_int)]),
     "mhd2d_adj_destroy": (None, [ctypes.c_void_p]),
+    "mhd2d_adj_quotient": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]),
+    "mhd_quotient6": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]),
     "mhd3d_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),

@@ -230,6 +230,7 @@ _CMP = {"gt": ">", "ge": ">=", "lt": "<", "le": "<=", "eq": "=="}
 _C_CMP = {op: f"dsl_{op}" for op in _CMP}
 _C_PREAMBLE = (
     "#ifndef MHD_DSL_NZ\n#define MHD_DSL_NZ\n"
+    "#include \"mhd_math.cuh\"\n"
     "__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }\n"
     "__device__ __forceinline__ long long dsl_key(double x) {\n"
     "  const long long b = __double_as_longlong(x);\n"
@@ -242,6 +243,24 @@ _C_PREAMBLE = (
     "__device__ __forceinline__ bool dsl_eq(double a, double b) { return dsl_key(a) == dsl_key(b); }\n"
     "__device__ __forceinline__ bool dsl_pos(double x) { return __double_as_longlong(x) > 0; }\n"
     "__device__ __forceinline__ bool dsl_nonneg(double x) { return dsl_key(x) >= 0; }\n"
+    # b / v for the reverse statements, which need not round like NumPy: Newton-Raphson
+    # refinement of the reciprocal (r <- r + r(1 - v r), error squared per step) from the
+    # hardware estimate (PTX rcp.approx.ftz.f64), then one residual correction of the
+    # quotient q <- q + r(b - v q) (Markstein's final step).  Divisors whose exponent lies
+    # outside [2^-1000, 2^1000] (zero, subnormal, huge, inf, NaN) take the correctly rounded
+    # division, so those keep its IEEE results.
+    "__device__ __forceinline__ double dsl_div(double b, double v) {\n"
+    "  const unsigned int ex = ((unsigned int)__double2hiint(v) >> 20) & 0x7ffu;\n"
+    "  if (ex - 23u > 2000u) return b / v;\n"
+    "  double r;\n"
+    "  asm(\"rcp.approx.ftz.f64 %0, %1;\" : \"=d\"(r) : \"d\"(v));\n"
+    "  double e = fma(-v, r, 1.0);\n"
+    "  r = fma(r, e, r);\n"
+    "  e = fma(-v, r, 1.0);\n"
+    "  r = fma(r, e, r);\n"
+    "  const double q = b * r;\n"
+    "  return fma(r, fma(-v, q, b), q);\n"
+    "}\n"
     "#endif")
 
 
@@ -262,6 +281,12 @@ def _fwd_lines(t, live, lang):
         elif op in _PY_BIN:
             if lang == "py":
                 L.append((v, f"{a[0]} {_PY_BIN[op]} {a[1]}", kind))
+            elif op == "div" and t.nodes[args[1]][0] == "const" and t.nodes[args[1]][2] == 6.0:
+                # correctly rounded x / 6 without an IEEE division (mhdk::div6)
+                L.append((v, f"mhdk::div6({a[0]})", kind))
+            elif op == "div" and t.nodes[args[1]][0] == "const" and _pow2(t.nodes[args[1]][2]):
+                # x / 2^k and x * 2^-k are the same real number, rounded once
+                L.append((v, f"__dmul_rn({a[0]}, {_c_lit(1.0 / t.nodes[args[1]][2])})", kind))
             else:
                 # round-to-nearest intrinsics are never contracted into an FMA, so
                 # the forward values round exactly like NumPy's even in a unit
@@ -288,6 +313,12 @@ def _fwd_lines(t, live, lang):
     return L
 
 
+def _pow2(x):
+    """x is +-2^k with 2^-k a normal double."""
+    m, e = math.frexp(abs(x))
+    return x != 0.0 and m == 0.5 and -1021 <= 1 - e <= 1022
+
+
 def _c_lit(x):
     if math.isinf(x) or math.isnan(x):
         raise ValueError("non-finite constant")
@@ -305,9 +336,11 @@ def _rev_lines_c(t, act, first_of=None):
     by a forward value is guarded by ``nz(b)``: a branch not taken may hold a
     non-finite value (e.g. w/bt with bt == 0) and 0 * inf must not reach the
     result.  Sums, differences and selects pass the adjoint through unguarded.
-    A quotient's two contributions share one division.  These statements may
-    contract into FMAs: the adjoint is not required to round like the NumPy
-    reverse sweep.
+    A quotient's two contributions share one division, and the divisions of the
+    quotient and square-root rules go through ``dsl_div`` (a refined reciprocal,
+    within two ulps of the correctly rounded quotient); a constant divisor becomes
+    a multiply by its reciprocal.  These statements may contract into FMAs: the
+    adjoint is not required to round like the NumPy reverse sweep.
     """
     L = []
     declared = set() if first_of is None else first_of
@@ -347,11 +380,15 @@ def _rev_lines_c(t, act, first_of=None):
         elif op == "div":
             # the quotient may be non-finite on a branch not taken: guard its use
             L.append(f"const bool g{i} = nz({b})")
-            L.append(f"const double q{i} = g{i} ? {b} / v{args[1]} : 0.0")
+            if t.nodes[args[1]][0] == "const" and t.nodes[args[1]][2] != 0.0:
+                # a constant divisor: multiply by its reciprocal (within an ulp)
+                L.append(f"const double q{i} = {b} * {_c_lit(1.0 / t.nodes[args[1]][2])}")
+            else:
+                L.append(f"const double q{i} = g{i} ? dsl_div({b}, v{args[1]}) : 0.0")
             acc(args[0], f"q{i}")
             acc(args[1], f"q{i} * v{i}", guard=f"g{i}", neg=True)
         elif op == "sqrt":
-            acc(args[0], f"(0.5 * {b}) / v{i}", guard=f"(nz({b}) && dsl_pos(v{i}))")
+            acc(args[0], f"dsl_div(0.5 * {b}, v{i})", guard=f"(nz({b}) && dsl_pos(v{i}))")
         elif op == "abs":
             acc(args[0], f"(dsl_nonneg(v{args[0]}) ? {b} : -{b})")
         elif op == "sel":

@@ -87,6 +87,14 @@ __global__ void k_cfl_finish(Adj A, double cfl, double* dt_slot) {
   A.red[1] = 0.0;
 }
 
+// the reverse statements' quotient, elementwise (its error bound is tested against
+// the correctly rounded division)
+__global__ void k_quotient(const double* __restrict__ b, const double* __restrict__ v, double* __restrict__ q,
+                           long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    q[i] = dsl_div(b[i], v[i]);
+}
+
 
 // ---------------------------------------------------------------------------
 // host side
@@ -901,6 +909,16 @@ int mhd2d_adj_info(void* handle, size_t* state_words_out, size_t* device_bytes_o
     *device_bytes_out = device_bytes(h) + solver_bytes;
   }
   if (segment_sets) *segment_sets = h->stored ? h->every : 1;
+  return MHD_OK;
+}
+
+int mhd2d_adj_quotient(const double* b, const double* v, double* q, long long n) {
+  if (n < 0 || (n > 0 && (!b || !v || !q))) return MHD_ERR_ARG;
+  if (n == 0) return MHD_OK;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  k_quotient<<<(unsigned)blocks, 256>>>(b, v, q, n);
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
   return MHD_OK;
 }
 

@@ -403,8 +403,8 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
       const double s_l = slope_at(k, -1);
       const double s_c = slope_at(k, 0);
       const double s_r = slope_at(k, 1);
-      double a = 0.5 * (wc[k] + wl[k]) - (s_c - s_l) / 6.0;
-      double b = 0.5 * (wr[k] + wc[k]) - (s_r - s_c) / 6.0;
+      double a = 0.5 * (wc[k] + wl[k]) - div6(s_c - s_l);
+      double b = 0.5 * (wr[k] + wc[k]) - div6(s_r - s_c);
       const double dprod = (b - wc[k]) * (wc[k] - a);
       const double idiff = b - a;
       const double adiff = 6.0 * (wc[k] - 0.5 * (a + b));

@@ -36,6 +36,32 @@ __device__ __forceinline__ double nsub(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ double nsq(double x) { return __dmul_rn(x, x); }
 
 // ---------------------------------------------------------------------------
+// x / 6, correctly rounded, in one multiply and two FMAs (Markstein's remainder
+// correction, IBM J. Res. Dev. 34(1), 1990), against about ten FP64 slots for an
+// IEEE division.  With z = RN(1/6) = (1 - 2^-54) / 6, let u = ulp(x/6); x lies two
+// or three binades above x/6, so it is a multiple of 4u.
+//  * q0 = RN(x z) lies within 1.5u of x/6 (x z is within u/2 of x/6, and the
+//    rounding adds at most another ulp of q0's binade);
+//  * r = x - 6 q0 is then a multiple of 2u of magnitude <= 9u, so it is a double and
+//    the FMA computes it exactly;
+//  * q0 + r z = x/6 - r 2^-54 / 6 exactly, within 1.5u 2^-54 of x/6, and the final
+//    FMA rounds it once.
+// x/6 is never that close to a rounding boundary: a midpoint m = (2k+1) u/2 of the
+// binade of x/6 gives 6m - x = u (6k + 3 - x/u), an odd multiple of u, so
+// |x/6 - m| >= u/6 (and the boundary below the binade is u/4 away from it).  The
+// rounding of q0 + r z therefore equals that of x/6.  The argument needs x/6 and q0
+// in the normal range; other exponents (zeros, subnormals, huge values, inf, NaN)
+// take the IEEE division, which also keeps the sign of a zero.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double div6(double x) {
+  const unsigned int ex = ((unsigned int)__double2hiint(x) >> 20) & 0x7ffu;
+  if (ex - 24u > 1998u) return x / 6.0;
+  const double z = 0.16666666666666666;   // RN(1/6)
+  const double q0 = __dmul_rn(x, z);
+  return __fma_rn(__fma_rn(-6.0, q0, x), z, q0);
+}
+
+// ---------------------------------------------------------------------------
 // Comparisons on the IEEE-754 bit pattern.  An FP64 compare (DSETP, and the
 // select of an FP64 max/min) issues on the FP64 pipe at the DFMA rate, and that
 // pipe bounds every kernel of the step; the same test on the 64-bit pattern runs

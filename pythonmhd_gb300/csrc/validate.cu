@@ -10,6 +10,7 @@
 // the reference's NumPy expression does.
 #include <cuda_runtime.h>
 
+#include "../../include/pythonmhd_gb300.h"
 #include "godunov2d_types.h"
 #include "mhd_math.cuh"
 
@@ -55,3 +56,23 @@ void enqueue_validate(int mhd, size_t plane, double gamma, double min_d, double 
 }
 
 }  // namespace mhdk
+
+// ---------------------------------------------------------------------------
+// The exact kernels' x / 6 (div6), elementwise, so that it can be compared bit for
+// bit with the IEEE division.
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void k_quotient6(const double* __restrict__ x, double* __restrict__ q, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    q[i] = mhdk::div6(x[i]);
+}
+}  // namespace
+
+extern "C" int mhd_quotient6(const double* x, double* q, long long n) {
+  if (n < 0 || (n > 0 && (!x || !q))) return MHD_ERR_ARG;
+  if (n == 0) return MHD_OK;
+  const long long blocks = (n + 255) / 256 < 152LL * 16 ? (n + 255) / 256 : 152LL * 16;
+  k_quotient6<<<(unsigned)blocks, 256>>>(x, q, n);
+  if (cudaGetLastError() != cudaSuccess) return MHD_ERR_CUDA;
+  return cudaDeviceSynchronize() == cudaSuccess ? MHD_OK : MHD_ERR_CUDA;
+}

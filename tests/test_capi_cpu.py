@@ -16,7 +16,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(mhd(?:1d|2d|3d|b)_\w+|mhd_ic_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mhd(?:1d|2d|3d|b)?_\w+)\s*\(", text)))
 
 
 @pytest.fixture(scope="module")

@@ -285,3 +285,36 @@ def test_gradient_matches_branch_frozen_differences(recon, efix):
         worst = max(worst, min(errs))
     a.close()
     assert worst <= 1e-6, worst
+
+
+def test_reverse_quotient_within_two_ulps_of_the_division():
+    """The reverse statements divide by a refined reciprocal (``dsl_div``).  For divisors
+    of magnitude 2^-1000 .. 2^1000 its quotient lies within two ulps of the correctly
+    rounded division (NumPy's); other divisors (zeros, subnormals, huge, inf, NaN) take
+    the IEEE division itself, so the result is the same bits."""
+    from pythonmhd_gb300 import _lib
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    # quotients stay in the normal range: |b| in [1e-20, 2e20], |v| in [2^-950, 2^951)
+    b = np.sign(rng.standard_normal(n)) * rng.uniform(1, 2, n) * 10.0 ** rng.uniform(-20, 20, n)
+    v = np.sign(rng.standard_normal(n)) * rng.uniform(1, 2, n) * 2.0 ** rng.integers(-950, 951, n)
+    edge = np.array([2.0 ** -1000, -(2.0 ** -1000), 2.0 ** 1000 * 1.9999, 2.0 ** -1001, 2.0 ** 1001, 0.0, -0.0,
+                     5e-324, -2.2e-308, 1e308, np.inf, -np.inf, np.nan, 1.0, -3.0, 0.1])
+    v = np.concatenate([v, edge, edge])
+    b = np.concatenate([b, np.ones(edge.size), np.full(edge.size, -7.5)])
+    bd, vd = torch.from_numpy(b).to(dev), torch.from_numpy(v).to(dev)
+    qd = torch.empty_like(bd)
+    _lib.check(lib.mhd2d_adj_quotient(bd.data_ptr(), vd.data_ptr(), qd.data_ptr(), b.size), "mhd2d_adj_quotient")
+    with np.errstate(all="ignore"):
+        q, ref = qd.cpu().numpy(), b / v
+    ex = (v.view(np.int64) >> 52) & 0x7ff
+    fast = (ex >= 23) & (ex <= 2023)
+    assert fast.sum() >= n
+    qi, ri = q[fast].view(np.int64), ref[fast].view(np.int64)
+    assert np.all(np.isfinite(ref[fast])) and np.all(np.sign(q[fast]) == np.sign(ref[fast]))
+    assert int(np.max(np.abs(qi - ri))) <= 2
+    qs, rs = q[~fast], ref[~fast]
+    assert np.array_equal(np.isnan(qs), np.isnan(rs))
+    np.testing.assert_array_equal(qs[~np.isnan(rs)].view(np.int64), rs[~np.isnan(rs)].view(np.int64))
