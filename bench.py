@@ -35,7 +35,6 @@ sys.path.insert(0, ROOT)
 METRIC = "zone-updates/s @4096^2 FP64 MHD (PPM+Roe+CTU+CT)"
 UNIT = "zone-updates/s"
 ALG_BYTES_PER_ZONE = 128          # 8 state words read + 8 written per zone-update (MHD)
-KERNELS_PER_CYCLE_MHD_PPM = 17
 
 
 def parse():
@@ -48,6 +47,9 @@ def parse():
     ap.add_argument("--other-arith-steps", type=int, default=10,
                     help="cycles timed in the other arithmetic mode beside the headline (0 = skip)")
     ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--recon", type=int, choices=[0, 1, 2], default=2,
+                    help="reconstruction of the single-grid workload (2 = PPM, the headline; 1 = PLM and "
+                         "0 = first order serve instruction-mix captures)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=512, help="grid size of the CPU baseline sample")
     ap.add_argument("--cpu-steps", type=int, default=2)
@@ -208,10 +210,13 @@ def measured_peaks():
         return {}
 
 
-def profile_summary(arith):
+RECON_NAME = {0: "first", 1: "plm", 2: "ppm"}
+
+
+def profile_summary(arith, recon=2):
     """Per-cycle DRAM traffic / FP64 instruction counts from the committed ncu summary."""
     try:
-        with open(os.path.join(ROOT, "profiles", f"mhd_ppm_cycle_ncu_{arith}.json")) as f:
+        with open(os.path.join(ROOT, "profiles", f"mhd_{RECON_NAME[recon]}_cycle_ncu_{arith}.json")) as f:
             return json.load(f)
     except Exception:
         return None
@@ -234,15 +239,37 @@ def build_probe() -> str:
     return PROBE_EXE
 
 
+_PROBE = {}
+
+
 def fp64_peak():
-    """DFMA / DADD / DMUL lane-ops/s of this GPU from the FP64 probe (fp64_probe.cu)."""
+    """DFMA / DADD / DMUL lane-ops/s of this GPU from the FP64 probe (fp64_probe.cu),
+    measured once per run."""
+    if "rates" not in _PROBE:
+        try:
+            exe = build_probe()
+            out = subprocess.run([exe, "--json"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                                 timeout=120).stdout
+            _PROBE["rates"] = json.loads(out.strip().splitlines()[-1])
+        except Exception:
+            _PROBE["rates"] = None
+    return _PROBE["rates"]
+
+
+def fp64_roof_3d(kind, arith, zones, ms_per):
+    """The FP64-issue roof of a 3D cycle from its committed instruction mix
+    (profiles/<kind>_cycle_ncu_<arith>.json), flattened for the bench line."""
     try:
-        exe = build_probe()
-        out = subprocess.run([exe, "--json"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
-                             timeout=120).stdout
-        return json.loads(out.strip().splitlines()[-1])
+        with open(os.path.join(ROOT, "profiles", f"{kind}_cycle_ncu_{arith}.json")) as f:
+            prof = json.load(f)
     except Exception:
-        return None
+        return {}
+    r = fp64_roof(prof, fp64_peak(), zones, ms_per)
+    if not r:
+        return {}
+    return {"fp64_frac_of_floor": r["frac"], "fp64_floor_ms": r["floor_ms_per_step"],
+            "fp64_achieved_ginstr_s": r["achieved"], "fp64_peak_ginstr_s": r["peak"],
+            "fp64_ops_source": r["ops_source"]}
 
 
 def fp64_roof(prof, probe, zones, ms_per):
@@ -318,6 +345,14 @@ def run_batch(a, torch):
     ts = time.perf_counter() - t0
     for g in singles:
         g.close()
+    # the FP64-issue roof from the single-grid PLM cycle's instruction mix: the batched
+    # kernels run the same per-zone bodies (tile edges add a little on top)
+    roof = {}
+    plm = profile_summary(a.arith, 1)
+    r = fp64_roof(plm, fp64_peak(), zones * k, tb * 1e3) if plm else None
+    if r:
+        roof = {"fp64_frac_of_floor": r["frac"], "fp64_floor_s": r["floor_ms_per_step"] * 1e-3,
+                "looped_fp64_frac_of_floor": r["frac"] * tb / tl, "fp64_ops_source": r["ops_source"]}
     return {"workload": f"{len(insts)} Orszag-Tang instances, Nx,Ny uniform in 64..512 step 32, gamma in "
                         f"[1.4,5/3], B0 x U[0.5,2], 1% density perturbation, PLM+Roe+CTU+CT, per-instance dt",
             "zones_per_step": zones, "steps": k,
@@ -327,7 +362,7 @@ def run_batch(a, torch):
                              "autotuned": True, "from_cache": tuned["cached"]},
             "loop": "one single-grid handle per instance, each advanced k cycles in turn (CUDA graphs)",
             "step_major_loop_zone_updates_per_s": zones * ks / ts, "step_major_steps": ks,
-            "speedup_vs_step_major_loop": (ts / ks) / (tb / k),
+            "speedup_vs_step_major_loop": (ts / ks) / (tb / k), **roof,
             "timing": "host wall clock around device-synchronised calls"}
 
 
@@ -380,7 +415,7 @@ def run_hydro3d(a, torch):
             "gpu_launches": launches, "device_bytes": dev_bytes,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "kernel": "one full 3D cycle (19 kernels per cycle, CUDA graphs), 80 algorithmic B/zone",
-                         "compute_bound": "fp64"},
+                         "compute_bound": "fp64", **fp64_roof_3d("hydro3d", a.arith, zones, ms)},
             "cpu_baseline": {"value": m ** 3 * 2 / cpu_s, "unit": "zone-updates/s", "cores": 1, "kind": "port",
                              "sample": f"oracle/hydro3d.py, {m}^3 periodic turbulence, 2 PPM cycles"},
             "timing": "CUDA events on the handle's stream; state 0.67 GB per buffer >> 129 MB L2"}
@@ -434,7 +469,8 @@ def run_mhd3d(a, torch):
             "gpu_launches": launches, "device_bytes": dev_bytes,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "kernel": "one full 3D MHD cycle (29 kernels, CUDA graphs), 176 algorithmic B/zone "
-                                   "(8 conserved and 3 face-B words in and out)", "compute_bound": "fp64"},
+                                   "(8 conserved and 3 face-B words in and out)", "compute_bound": "fp64",
+                         **fp64_roof_3d("mhd3d", a.arith, zones, ms)},
             "cpu_baseline": {"value": m ** 3 * 2 / cpu_s, "unit": "zone-updates/s", "cores": 1, "kind": "port",
                              "sample": f"oracle/mhd3d.py, {m}^3 periodic turbulence, 2 PPM cycles"},
             "timing": "CUDA events on the handle's stream; state 1.3 GB per buffer >> 129 MB L2"}
@@ -538,7 +574,7 @@ def run_ours(a):
     gamma = 5.0 / 3.0
     # the seeded state, generated on the device (same generator as the host one, to rounding)
     prim, cons, fbx, fby, dx, dy = ic.turbulence_device(n, seed=a.seed + rank, gamma=gamma, device=dev)
-    g = Grid2D(n, n, dx, dy, 1, 1, gamma, mhd=True, recon=2, arith=a.arith)
+    g = Grid2D(n, n, dx, dy, 1, 1, gamma, mhd=True, recon=a.recon, arith=a.arith)
     g.upload_device(prim, cons, fbx, fby)
     shapes = (tuple(prim.shape), tuple(cons.shape), tuple(fbx.shape), tuple(fby.shape))
     del prim, cons, fbx, fby
@@ -623,7 +659,7 @@ def run_ours(a):
     peak_src = "measured" if hbm_peak else "fallback"
     hbm_peak = hbm_peak or 6800.0
     achieved = ALG_BYTES_PER_ZONE * zones / (ms_per * 1e-3) / 1e9
-    prof = profile_summary(a.arith)
+    prof = profile_summary(a.arith, a.recon)
     probe = fp64_peak() if rank == 0 else None
     traffic = None
     fp64 = None
@@ -634,7 +670,7 @@ def run_ours(a):
         fp64 = fp64_roof(prof, probe, zones, ms_per)
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak, "traffic": traffic,
-            "kernel": "one full cycle (CUDA graph of 17 kernels), 128 algorithmic B/zone",
+            "kernel": f"one full cycle (CUDA graph of {launches // max(a.steps, 1)} kernels), 128 algorithmic B/zone",
             "peak_source": peak_src, "compute_bound": "fp64", "fp64": fp64}
     if fp64:
         # the binding roof, flat: fraction of the FP64-issue floor (each instruction class
@@ -648,7 +684,7 @@ def run_ours(a):
         other_mode = "fast" if a.arith == "exact" else "exact"
         torch.cuda.synchronize()
         prim0, cons0, fbx0, fby0, _, _ = ic.turbulence_device(n, seed=a.seed + rank, gamma=gamma, device=dev)
-        g2 = Grid2D(n, n, dx, dy, 1, 1, gamma, mhd=True, recon=2, arith=other_mode)
+        g2 = Grid2D(n, n, dx, dy, 1, 1, gamma, mhd=True, recon=a.recon, arith=other_mode)
         g2.upload_device(prim0, cons0, fbx0, fby0)
         del prim0, cons0, fbx0, fby0
         torch.cuda.empty_cache()
@@ -689,11 +725,13 @@ def run_ours(a):
         g.close()
         mhd_3d = run_mhd3d(a, torch)
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+    recon_label = {0: "first-order", 1: "PLM", 2: "PPM"}[a.recon]
+    metric = METRIC if a.recon == 2 else METRIC.replace("PPM", recon_label)
+    line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_per, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"2D ideal-MHD driven-free turbulence {n}x{n} periodic, gamma=5/3, "
-                                   f"PPM+Roe+CTU+CT, CFL 0.4, FP64, seeded (seed {a.seed})",
+                                   f"{recon_label}+Roe+CTU+CT, CFL 0.4, FP64, seeded (seed {a.seed})",
                        "arith": a.arith, "cells": zones, "l2": "state 2.4 GB >> 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
