@@ -77,18 +77,25 @@ def run(grid, t_lim, max_cycles, cfl, save_dt=-1.0, save_prec=None, plot_dt=-1.0
     return t.value, c.value, n.value
 
 
+# the reference's variable names (Source/PythonMHD_Constants.py:86-104), the keys
+# of its .mat files (Source/FileSaver.py:212-231)
+MAT_KEYS_MHD = ("Density", "Vx", "Vy", "Vz", "Bx", "By", "Bz", "Pressure")
+MAT_KEYS_HYDRO = ("Density", "Vx", "Vy", "Vz", "Pressure")
+
+
 def save_mat(path, prim, cons, fbx=None, fby=None, fbz=None):
-    """A stop's state in the reference's .mat layout, plus faceBx/faceBy (and faceBz
-    for a 3D grid) for MHD."""
+    """A stop's state in the reference's .mat layout (the primitive variables and the
+    energy under the reference's keys), plus faceBx/faceBy (and faceBz for a 3D grid)
+    for MHD, which a restart needs."""
     import scipy.io
     if prim.shape[0] == 8:
-        d = {"density": prim[0], "vx": prim[1], "vy": prim[2], "vz": prim[3], "Bx": prim[4], "By": prim[5],
-             "Bz": prim[6], "pressure": prim[7], "energy": cons[7], "faceBx": fbx, "faceBy": fby}
+        d = dict(zip(MAT_KEYS_MHD, prim))
+        d.update({"Energy": cons[7], "faceBx": fbx, "faceBy": fby})
         if fbz is not None:
             d["faceBz"] = fbz
     else:
-        d = {"density": prim[0], "vx": prim[1], "vy": prim[2], "vz": prim[3], "pressure": prim[4],
-             "energy": cons[4]}
+        d = dict(zip(MAT_KEYS_HYDRO, prim))
+        d["Energy"] = cons[4]
     scipy.io.savemat(path, d)
 
 

@@ -134,13 +134,17 @@ def test_save_mat_writes_the_reference_layout_with_face_b(tmp_path):
     fbx, fby, fbz = rng.random((3, 5, 2)), rng.random((4, 4, 2)), rng.random((3, 4, 3))
     driver.save_mat(str(tmp_path / "s.mat"), prim, cons, fbx, fby, fbz)
     d = scipy.io.loadmat(str(tmp_path / "s.mat"))
-    for k, i in (("density", 0), ("vx", 1), ("vy", 2), ("vz", 3), ("Bx", 4), ("By", 5), ("Bz", 6), ("pressure", 7)):
+    # Source/PythonMHD_Constants.py:86-104: DENSITY "Density", VX "Vx", ..., BX "Bx", ...,
+    # PRESSURE "Pressure", ENERGY "Energy"
+    for k, i in (("Density", 0), ("Vx", 1), ("Vy", 2), ("Vz", 3), ("Bx", 4), ("By", 5), ("Bz", 6), ("Pressure", 7)):
         np.testing.assert_array_equal(d[k], prim[i])
-    np.testing.assert_array_equal(d["energy"], cons[7])
+    np.testing.assert_array_equal(d["Energy"], cons[7])
     for k, a in (("faceBx", fbx), ("faceBy", fby), ("faceBz", fbz)):
         np.testing.assert_array_equal(d[k], a)
     # hydro: no face arrays
     driver.save_mat(str(tmp_path / "h.mat"), prim[:5], cons[:5])
     h = scipy.io.loadmat(str(tmp_path / "h.mat"))
-    np.testing.assert_array_equal(h["pressure"], prim[4])
+    np.testing.assert_array_equal(h["Pressure"], prim[4])
+    np.testing.assert_array_equal(h["Energy"], cons[4])
+    assert not any(k.startswith("face") for k in h)
     assert "faceBx" not in h

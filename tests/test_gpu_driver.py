@@ -86,7 +86,7 @@ def test_driver_stop_callback_can_end_the_run(tmp_path):
     import scipy.io
     d = scipy.io.loadmat(str(tmp_path / "snap_0.mat"))
     np.testing.assert_array_equal(d["faceBx"], c["fbx"])
-    np.testing.assert_array_equal(d["density"], c["prim"][0])
+    np.testing.assert_array_equal(d["Density"], c["prim"][0])
 
 
 @pytest.mark.parametrize("t_lim,save_dt,plot_dt,order", [(0.03, 0.01, 0.0075, 2), (0.02, -1.0, 0.005, 0)])
