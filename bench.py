@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=400,
                     help="cycles of the 512^2 PLM adjoint workload (0 = skip it)")
     ap.add_argument("--adjoint-n", type=int, default=512)
+    ap.add_argument("--adjoint-recon", type=int, choices=[0, 1, 2], default=1,
+                    help="reconstruction of the adjoint workload (1 = PLM, as stated; 2 = PPM)")
     ap.add_argument("--adjoint-tail", type=int, default=-1,
                     help="cycles the adjoint's forward pass leaves resident (-1 as many as fit, 0 none)")
     ap.add_argument("--hydro3d-steps", type=int, default=10,
@@ -480,8 +482,8 @@ def run_mhd3d(a, torch):
 # adjoint: gradient of a density-matching loss through many cycles
 # ----------------------------------------------------------------------------
 def run_adjoint(a, torch):
-    """512^2 periodic MHD turbulence (seeded, k <= 16), PLM + Roe + CTU+CT, 400 cycles
-    at CFL 0.4; loss = mean squared difference between the final density and the
+    """512^2 periodic MHD turbulence (seeded, k <= 16), PLM + Roe + CTU+CT (PPM with
+    --adjoint-recon 2), 400 cycles at CFL 0.4; loss = mean squared difference between the final density and the
     final density of a run from a smoothly 2%-perturbed initial state; gradient
     with respect to the initial rho, vx, vy, p, A_z by the hand-written backward
     pass with sqrt(N) checkpoints (the last cycles run with tapes in the forward pass
@@ -495,7 +497,8 @@ def run_adjoint(a, torch):
     fl = fields.turbulence_fields(n, seed=1, kmax_v=16, kmax_a=16)
     tgt = fields.perturbed(fl, 0.02, seed=2)
     g0 = fl["gamma"]
-    adj = Adjoint2D(n, n, fl["dx"], fl["dy"], 1, 1, g0, recon=1)
+    recon = a.adjoint_recon
+    adj = Adjoint2D(n, n, fl["dx"], fl["dy"], 1, 1, g0, recon=recon)
     adj.configure(0, tail=a.adjoint_tail)
     st_t = fields.state_from_fields(*fields.fields_to_torch(tgt, dev), g0, fl["dx"], fl["dy"]).contiguous()
     target = adj.unpack(adj.forward(st_t, steps, cfl=0.4))[0][0].clone()
@@ -503,7 +506,7 @@ def run_adjoint(a, torch):
     xs = fields.fields_to_torch(fl, dev)
     s0 = fields.state_from_fields(*xs, g0, fl["dx"], fl["dy"]).contiguous()
     prim, cons, fbx, fby = [t.cpu().numpy() for t in adj.unpack(s0)]
-    grid = Grid2D(n, n, fl["dx"], fl["dy"], 1, 1, g0, mhd=True, recon=1, arith="exact")
+    grid = Grid2D(n, n, fl["dx"], fl["dy"], 1, 1, g0, mhd=True, recon=recon, arith="exact")
     grid.upload(prim, cons, fbx, fby)
     grid.advance(0.0, 1e30, 0, 3, 0.4)
     grid.upload(prim, cons, fbx, fby)
@@ -535,7 +538,8 @@ def run_adjoint(a, torch):
     rec = adj.record()
     gnorm = float(sum(float(torch.sum(x.grad * x.grad)) for x in xs)) ** 0.5
     adj.close()
-    return {"workload": f"{n}x{n} periodic MHD turbulence (seeded, k<=16), PLM+Roe+CTU+CT, {steps} cycles, CFL 0.4; "
+    label = {0: "first-order", 1: "PLM", 2: "PPM"}[recon]
+    return {"workload": f"{n}x{n} periodic MHD turbulence (seeded, k<=16), {label}+Roe+CTU+CT, {steps} cycles, CFL 0.4; "
                         "loss = mean((rho_final - rho_target)^2), target from a smoothly 2%-perturbed state; "
                         "gradient w.r.t. initial rho, vx, vy, p, A_z; dt frozen",
             "steps": steps, "loss": float(loss.detach()), "grad_norm": gnorm,
