@@ -704,8 +704,11 @@ def run_ours(a):
         ms2 = f0.elapsed_time(f1) / a.other_arith_steps
         g2.close()
         torch.cuda.empty_cache()
+        r2 = fp64_roof(profile_summary(other_mode, a.recon) or {}, probe, zones, ms2) if probe else None
         other = {"arith": other_mode, "value": zones / (ms2 * 1e-3), "ms_per_step": ms2,
                  "steps": a.other_arith_steps, "speed_vs_headline": ms_per / ms2,
+                 "fp64_frac_of_floor": r2["frac"] if r2 else None,
+                 "fp64_floor_ms": r2["floor_ms_per_step"] if r2 else None,
                  "parity": "per cycle within 1e-12 of the reference on every well-conditioned golden state and "
                            "along the full Orszag-Tang run (exact: bit for bit)"}
 
