@@ -40,8 +40,15 @@ def signed_mag(x, m):
 # ---------------------------------------------------------------------------
 # primitive eigensystem (mhd_math.cuh: prim_eigensystem)
 # ---------------------------------------------------------------------------
-def prim_eig(w, bn, gamma, axis):
-    N, T1, T2 = FRAMES[axis]
+EIG_BASE = 16   # words of eig_base
+
+
+def eig_base(w, bn, gamma):
+    """The costly part of the primitive eigensystem of one cell state: its square
+    roots, divisions and signs, as the list [a2, a, ca, cf, cs, fa, sa, b1, b2, sgn,
+    sqrt_d, inv_d, nf, l14, l15, l36].  ``eig_from_base`` builds lam, L and R from
+    them with multiplies only, so a stage can take them as inputs from the stage that
+    formed them instead of recomputing them."""
     bt2 = w[4] * w[4] + w[5] * w[5]
     bt = sqrt(bt2)
     gp = gamma * w[6]
@@ -67,6 +74,18 @@ def prim_eig(w, bn, gamma, axis):
     fa = select(c_f1, 1.0, select(c_s1, 0.0, select(c_f2, 1.0, sqrt((a2 - cs2) / ssqrt))))
     sa = select(c_f1, 0.0, select(c_s1, 1.0, select(c_f2, 0.0, sqrt((cf2 - a2) / ssqrt))))
     sgn = sign_one(bn)
+    nf = 0.5 / a2
+    l14 = -0.5 * b2 * sgn / sqrt_d
+    l15 = 0.5 * b1 * sgn / sqrt_d
+    l36 = -1.0 / a2
+    return [a2, a, ca, cf, cs, fa, sa, b1, b2, sgn, sqrt_d, inv_d, nf, l14, l15, l36]
+
+
+def eig_from_base(base, w, axis):
+    """lam, L and R (mhd_math.cuh: prim_eigensystem) of the cell state w from its
+    ``eig_base`` words, in the same operation order."""
+    N, T1, T2 = FRAMES[axis]
+    a2, a, ca, cf, cs, fa, sa, b1, b2, sgn, sqrt_d, inv_d, nf, l14, l15, l36 = base
     qf = cf * fa * sgn
     qs = cs * sa * sgn
     af = a * fa * sqrt_d
@@ -90,7 +109,6 @@ def prim_eig(w, bn, gamma, axis):
     R[4, 0] = r40; R[4, 1] = r41; R[4, 2] = r42; R[4, 4] = r42; R[4, 5] = r41; R[4, 6] = r40
     r50 = as_ * b2; r51 = b1 * sgn * sqrt_d; r52 = -af * b2
     R[5, 0] = r50; R[5, 1] = r51; R[5, 2] = r52; R[5, 4] = r52; R[5, 5] = r51; R[5, 6] = r50
-    nf = 0.5 / a2
     qf_n = nf * qf
     qs_n = nf * qs
     afp = nf * af * inv_d
@@ -101,7 +119,6 @@ def prim_eig(w, bn, gamma, axis):
     L[0, N] = l0n; L[0, T1] = l0t1; L[0, T2] = l0t2; L[0, 6] = l06; L[0, 4] = l04; L[0, 5] = l05
     L[6, N] = -l0n; L[6, T1] = -l0t1; L[6, T2] = -l0t2; L[6, 6] = l06; L[6, 4] = l04; L[6, 5] = l05
     l1t1 = -0.5 * b2; l1t2 = 0.5 * b1
-    l14 = -0.5 * b2 * sgn / sqrt_d; l15 = 0.5 * b1 * sgn / sqrt_d
     L[1, T1] = l1t1; L[1, T2] = l1t2; L[1, 4] = l14; L[1, 5] = l15
     L[5, T1] = -l1t1; L[5, T2] = -l1t2; L[5, 4] = l14; L[5, 5] = l15
     l2n = -nf * cs * sa; l2t1 = -qf_n * b1; l2t2 = -qf_n * b2; l26 = nf * sa * inv_d
@@ -109,7 +126,7 @@ def prim_eig(w, bn, gamma, axis):
     L[2, N] = l2n; L[2, T1] = l2t1; L[2, T2] = l2t2; L[2, 6] = l26; L[2, 4] = l24; L[2, 5] = l25
     L[4, N] = -l2n; L[4, T1] = -l2t1; L[4, T2] = -l2t2; L[4, 6] = l26; L[4, 4] = l24; L[4, 5] = l25
     L[3, 0] = 1.0
-    L[3, 6] = -1.0 / a2
+    L[3, 6] = l36
     return lam, L, R
 
 
@@ -123,8 +140,10 @@ def _project(L, i, v, order):
 
 
 def char_slopes(wl, wc, wr, bn, gamma, axis):
-    """The reference's limited slope of one cell (k_ppm_slopes) and its eigensystem."""
-    lam, L, R = prim_eig(wc, bn, gamma, axis)
+    """The reference's limited slope of one cell (k_ppm_slopes), its eigensystem and
+    the eigensystem's base words."""
+    base = eig_base(wc, bn, gamma)
+    lam, L, R = eig_from_base(base, wc, axis)
     order = _order(axis)
     dc = [wr[k] - wl[k] for k in range(7)]
     dl = [wc[k] - wl[k] for k in range(7)]
@@ -140,17 +159,19 @@ def char_slopes(wl, wc, wr, bn, gamma, axis):
         lim2 = dmin(0.5 * fabs(cc), fabs(cw))
         sc.append(select(cl * cr > 0.0, signed_mag(cc, dmin(2.0 * lim1, lim2)), 0.0))
     s = [_sum_first([sc[j] * R[i, j] for j in range(7) if (i, j) in R]) for i in range(7)]
-    return s, lam, L, R
+    return s, lam, L, R, base
 
 
-def plm_cell(ins, pars, axis):
-    """PLM edge states of one cell (k_faces MODE 1).
+def plm_edge(ins, pars, axis):
+    """PLM edge states of one cell (k_faces MODE 1) from its limited slope and its
+    eigensystem's base words (both formed by ``ppm_slope``).
 
-    ins = wl(7) + wc(7) + wr(7) + bn ; pars = [gamma, dtdx] -> lia(7) + ria(7)
+    ins = wl(7) + wc(7) + wr(7) + sc(7) + base(EIG_BASE) ; pars = [gamma, dtdx] -> lia(7) + ria(7)
     """
-    wl, wc, wr, bn = ins[0:7], ins[7:14], ins[14:21], ins[21]
-    gamma, dtdx = pars
-    s, lam, L, R = char_slopes(wl, wc, wr, bn, gamma, axis)
+    wl, wc, wr, s = ins[0:7], ins[7:14], ins[14:21], ins[21:28]
+    base = ins[28:28 + EIG_BASE]
+    dtdx = pars[1]
+    lam, L, R = eig_from_base(base, wc, axis)
     order = _order(axis)
     lia, ria = [], []
     for k in range(7):
@@ -180,27 +201,28 @@ def plm_cell(ins, pars, axis):
 
 
 def ppm_slope(ins, pars, axis):
-    """Characteristic-limited primitive slope of one (sweep-extended) cell (k_ppm_slopes).
+    """Characteristic-limited primitive slope of one (sweep-extended) cell (k_ppm_slopes)
+    and the base words of its eigensystem, which the edge stages (PLM and PPM) read.
 
-    ins = wl(7) + wc(7) + wr(7) + bn ; pars = [gamma] -> s(7)
+    ins = wl(7) + wc(7) + wr(7) + bn ; pars = [gamma] -> s(7) + base(EIG_BASE)
     """
     wl, wc, wr, bn = ins[0:7], ins[7:14], ins[14:21], ins[21]
-    s, _, _, _ = char_slopes(wl, wc, wr, bn, pars[0], axis)
-    return s
+    s, _, _, _, base = char_slopes(wl, wc, wr, bn, pars[0], axis)
+    return s + base
 
 
 def ppm_cell(ins, pars, axis):
     """PPM edge states of one cell with dt/2 characteristic tracing (k_faces MODE 2;
     oracle.mhd2d.ppm_sweep).
 
-    ins = wl(7) + wc(7) + wr(7) + sl(7) + sc(7) + sr(7) + bn ; pars = [gamma, dtdx]
-    -> lia(7) + ria(7)
+    ins = wl(7) + wc(7) + wr(7) + sl(7) + sc(7) + sr(7) + base(EIG_BASE), base the
+    cell's eigensystem words from ``ppm_slope`` ; pars = [gamma, dtdx] -> lia(7) + ria(7)
     """
     wl, wc, wr = ins[0:7], ins[7:14], ins[14:21]
     sl, sc, sr = ins[21:28], ins[28:35], ins[35:42]
-    bn = ins[42]
-    gamma, dtdx = pars
-    lam, L, R = prim_eig(wc, bn, gamma, axis)
+    base = ins[42:42 + EIG_BASE]
+    dtdx = pars[1]
+    lam, L, R = eig_from_base(base, wc, axis)
     order = _order(axis)
     lia, ria = [], []
     for k in range(7):

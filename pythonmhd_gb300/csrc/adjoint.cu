@@ -108,7 +108,7 @@ struct Slot {
 };
 const Slot kSlots[] = {
     {&Adj::P, 8, 0},   {&Adj::C, 8, 0},   {&Adj::FX, 1, 1},  {&Adj::FY, 1, 2},  {&Adj::EX, 14, 0},
-    {&Adj::EY, 14, 0}, {&Adj::SX, 7, 4},  {&Adj::SY, 7, 5},  {&Adj::XL, 7, 1},  {&Adj::XR, 7, 1},  {&Adj::YL, 7, 2},  {&Adj::YR, 7, 2},
+    {&Adj::EY, 14, 0}, {&Adj::SX, g_pslope0_NO, 4},  {&Adj::SY, g_pslope0_NO, 5},  {&Adj::XL, 7, 1},  {&Adj::XR, 7, 1},  {&Adj::YL, 7, 2},  {&Adj::YR, 7, 2},
     {&Adj::F1X, 7, 1}, {&Adj::F1Y, 7, 2}, {&Adj::EZ, 1, 0},  {&Adj::E1, 1, 3},  {&Adj::NBX, 1, 1},
     {&Adj::NBY, 1, 2}, {&Adj::UXL, 7, 1}, {&Adj::UXR, 7, 1}, {&Adj::UYL, 7, 2}, {&Adj::UYR, 7, 2},
     {&Adj::WXL, 7, 1}, {&Adj::WXR, 7, 1}, {&Adj::WYL, 7, 2}, {&Adj::WYR, 7, 2}, {&Adj::HEZ, 1, 0},
@@ -219,7 +219,7 @@ void branch_layout(int nx, int ny, int recon, int efix, size_t* off, size_t* BW)
   const size_t cells = (size_t)nx * ny, xf = (size_t)(nx + 1) * ny, yf = (size_t)nx * (ny + 1);
   const size_t corners = (size_t)(nx + 1) * (ny + 1);
   const int nb_recon = recon == 1 ? std::max(g_plm0_NB, g_plm1_NB) : (recon == 2 ? std::max(g_ppm0_NB, g_ppm1_NB) : 0);
-  const int nb_slope = recon == 2 ? std::max(g_pslope0_NB, g_pslope1_NB) : 0;
+  const int nb_slope = recon >= 1 ? std::max(g_pslope0_NB, g_pslope1_NB) : 0;
   const int nb_roe1 = efix ? std::max(g_roe1_0_efix_NB, g_roe1_1_efix_NB) : std::max(g_roe1_0_NB, g_roe1_1_NB);
   const int nb_roe2 = efix ? std::max(g_roe2_0_efix_NB, g_roe2_1_efix_NB) : std::max(g_roe2_0_NB, g_roe2_1_NB);
   const size_t items[kNumBt] = {(size_t)(nx + 2) * ny, (size_t)nx * (ny + 2), cells, cells, 2 * xf, 2 * yf,
@@ -434,9 +434,9 @@ void layout(int nx, int ny, int recon, int efix, size_t* off, size_t* ps, size_t
   }
   *W = w;
   // tapes: PLM/PPM per cell and sweep (first order has no reconstruction stage), Roe per
-  // face, stage and sweep, CTU per face side and sweep, PPM slopes per extended cell and sweep
+  // face, stage and sweep, CTU per face side and sweep, PLM/PPM slopes per extended cell and sweep
   const int nt_plm = recon == 1 ? g_plm0_NT : (recon == 2 ? g_ppm0_NT : 0);
-  const int nt_slope = recon == 2 ? g_pslope0_NT : 0;
+  const int nt_slope = recon >= 1 ? g_pslope0_NT : 0;
   const int nt_roe[2] = {efix ? g_roe1_0_efix_NT : g_roe1_0_NT, efix ? g_roe2_0_efix_NT : g_roe2_0_NT};
   const size_t items[10] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2],
                             plane[4], plane[5]};
