@@ -24,8 +24,8 @@ OUTFLOW, PERIODIC = 0, 1
 @functools.lru_cache(maxsize=None)
 def _fn(name, efix=False, backend="numpy", device=None):
     spec = {
-        "plm0": (stages.plm_edge, 28 + stages.EIG_BASE, 2, dict(axis=0)),
-        "plm1": (stages.plm_edge, 28 + stages.EIG_BASE, 2, dict(axis=1)),
+        "plm0": (stages.plm_cell, 22, 2, dict(axis=0)),
+        "plm1": (stages.plm_cell, 22, 2, dict(axis=1)),
         "pslope0": (stages.ppm_slope, 22, 1, dict(axis=0)),
         "pslope1": (stages.ppm_slope, 22, 1, dict(axis=1)),
         "ppm0": (stages.ppm_cell, 42 + stages.EIG_BASE, 2, dict(axis=0)),
@@ -158,7 +158,11 @@ class Cycle:
                     return (J, _wrap(I + off, nx, bc))
                 return (_wrap(J + off, ny, bc), I)
             bslot = 4 if ax == 0 else 5
-            if self.order >= 1:
+            if self.order == 1:
+                ins = [(P, s, cell(off)) for off in (-1, 0, 1) for s in slots]
+                ins.append((P, bslot, cell(0)))
+                self._rec(f"plm{ax}", ins, [g, dt / dn], [(E, k, (J, I)) for k in range(14)])
+            elif self.order == 2:
                 # slopes of the sweep-extended cells -1 .. L (extended index e = cell + 1),
                 # each with its eigensystem's base words (planes 7 ..)
                 ns = 7 + stages.EIG_BASE
@@ -178,16 +182,12 @@ class Cycle:
                 ins.append((P, bslot, ecell(0)))
                 self._rec(f"pslope{ax}", ins, [g], [(S, k, (SJ, SE) if ax == 0 else (SE, SJ)) for k in range(ns)])
                 ins = [(P, s, cell(off)) for off in (-1, 0, 1) for s in slots]
+                for off in (0, 1, 2):
+                    sidx = (J, I + off) if ax == 0 else (J + off, I)
+                    ins += [(S, k, sidx) for k in range(7)]
                 own = (J, I + 1) if ax == 0 else (J + 1, I)
-                if self.order == 1:
-                    ins += [(S, k, own) for k in range(7)]
-                else:
-                    for off in (0, 1, 2):
-                        sidx = (J, I + off) if ax == 0 else (J + off, I)
-                        ins += [(S, k, sidx) for k in range(7)]
                 ins += [(S, 7 + k, own) for k in range(stages.EIG_BASE)]
-                name = f"plm{ax}" if self.order == 1 else f"ppm{ax}"
-                self._rec(name, ins, [g, dt / dn], [(E, k, (J, I)) for k in range(14)])
+                self._rec(f"ppm{ax}", ins, [g, dt / dn], [(E, k, (J, I)) for k in range(14)])
             else:
                 for k, s in enumerate(slots):
                     self._rec_copy(P, s, E, k)

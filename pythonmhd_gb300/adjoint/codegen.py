@@ -12,8 +12,8 @@ from . import dsl, stages
 
 # name, function, inputs, params, keyword arguments
 STAGES = [
-    ("plm0", stages.plm_edge, 28 + stages.EIG_BASE, 2, dict(axis=0)),
-    ("plm1", stages.plm_edge, 28 + stages.EIG_BASE, 2, dict(axis=1)),
+    ("plm0", stages.plm_cell, 22, 2, dict(axis=0)),
+    ("plm1", stages.plm_cell, 22, 2, dict(axis=1)),
     ("pslope0", stages.ppm_slope, 22, 1, dict(axis=0)),
     ("pslope1", stages.ppm_slope, 22, 1, dict(axis=1)),
     ("ppm0", stages.ppm_cell, 42 + stages.EIG_BASE, 2, dict(axis=0)),

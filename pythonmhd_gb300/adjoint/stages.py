@@ -162,16 +162,15 @@ def char_slopes(wl, wc, wr, bn, gamma, axis):
     return s, lam, L, R, base
 
 
-def plm_edge(ins, pars, axis):
-    """PLM edge states of one cell (k_faces MODE 1) from its limited slope and its
-    eigensystem's base words (both formed by ``ppm_slope``).
+def plm_cell(ins, pars, axis):
+    """PLM edge states of one cell (k_faces MODE 1), slope and eigensystem included:
+    one fused stage (splitting it like PPM measured slower).
 
-    ins = wl(7) + wc(7) + wr(7) + sc(7) + base(EIG_BASE) ; pars = [gamma, dtdx] -> lia(7) + ria(7)
+    ins = wl(7) + wc(7) + wr(7) + bn ; pars = [gamma, dtdx] -> lia(7) + ria(7)
     """
-    wl, wc, wr, s = ins[0:7], ins[7:14], ins[14:21], ins[21:28]
-    base = ins[28:28 + EIG_BASE]
-    dtdx = pars[1]
-    lam, L, R = eig_from_base(base, wc, axis)
+    wl, wc, wr, bn = ins[0:7], ins[7:14], ins[14:21], ins[21]
+    gamma, dtdx = pars
+    s, lam, L, R, _ = char_slopes(wl, wc, wr, bn, gamma, axis)
     order = _order(axis)
     lia, ria = [], []
     for k in range(7):
@@ -202,7 +201,7 @@ def plm_edge(ins, pars, axis):
 
 def ppm_slope(ins, pars, axis):
     """Characteristic-limited primitive slope of one (sweep-extended) cell (k_ppm_slopes)
-    and the base words of its eigensystem, which the edge stages (PLM and PPM) read.
+    and the base words of its eigensystem, which the PPM edge stage reads.
 
     ins = wl(7) + wc(7) + wr(7) + bn ; pars = [gamma] -> s(7) + base(EIG_BASE)
     """

@@ -219,7 +219,7 @@ void branch_layout(int nx, int ny, int recon, int efix, size_t* off, size_t* BW)
   const size_t cells = (size_t)nx * ny, xf = (size_t)(nx + 1) * ny, yf = (size_t)nx * (ny + 1);
   const size_t corners = (size_t)(nx + 1) * (ny + 1);
   const int nb_recon = recon == 1 ? std::max(g_plm0_NB, g_plm1_NB) : (recon == 2 ? std::max(g_ppm0_NB, g_ppm1_NB) : 0);
-  const int nb_slope = recon >= 1 ? std::max(g_pslope0_NB, g_pslope1_NB) : 0;
+  const int nb_slope = recon == 2 ? std::max(g_pslope0_NB, g_pslope1_NB) : 0;
   const int nb_roe1 = efix ? std::max(g_roe1_0_efix_NB, g_roe1_1_efix_NB) : std::max(g_roe1_0_NB, g_roe1_1_NB);
   const int nb_roe2 = efix ? std::max(g_roe2_0_efix_NB, g_roe2_1_efix_NB) : std::max(g_roe2_0_NB, g_roe2_1_NB);
   const size_t items[kNumBt] = {(size_t)(nx + 2) * ny, (size_t)nx * (ny + 2), cells, cells, 2 * xf, 2 * yf,
@@ -429,14 +429,16 @@ void layout(int nx, int ny, int recon, int efix, size_t* off, size_t* ps, size_t
   for (int i = 0; i < kNumSlots; ++i) {
     off[i] = w;
     ps[i] = plane[kSlots[i].kind];
-    w += (size_t)kSlots[i].planes * ps[i];
+    // the slope arrays (sweep-extended cells) exist only for PPM
+    const bool slope = kSlots[i].kind == 4 || kSlots[i].kind == 5;
+    w += (size_t)(slope && recon != 2 ? 0 : kSlots[i].planes) * ps[i];
     w = (w + 31) & ~(size_t)31;   // 256-byte aligned plane groups
   }
   *W = w;
   // tapes: PLM/PPM per cell and sweep (first order has no reconstruction stage), Roe per
   // face, stage and sweep, CTU per face side and sweep, PLM/PPM slopes per extended cell and sweep
   const int nt_plm = recon == 1 ? g_plm0_NT : (recon == 2 ? g_ppm0_NT : 0);
-  const int nt_slope = recon >= 1 ? g_pslope0_NT : 0;
+  const int nt_slope = recon == 2 ? g_pslope0_NT : 0;
   const int nt_roe[2] = {efix ? g_roe1_0_efix_NT : g_roe1_0_NT, efix ? g_roe2_0_efix_NT : g_roe2_0_NT};
   const size_t items[10] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2],
                             plane[4], plane[5]};

@@ -39,7 +39,7 @@ struct Adj {
   double dt;                       // dt of the cycle being processed
   Arr P, C, FX, FY;                // input state
   Arr EX, EY;                      // edge states per cell (lia 7 + ria 7), x and y sweeps
-  Arr SX, SY;                      // PLM/PPM: limited slopes of the sweep-extended cells and their
+  Arr SX, SY;                      // PPM: limited slopes of the sweep-extended cells and their
                                    // eigensystems' base words (g_pslope0_NO planes)
   Arr XL, XR, YL, YR;              // reconstructed face states
   Arr F1X, F1Y, EZ, E1, NBX, NBY;  // stage-1 fluxes, cell Ez, corner EMF, half-step faces
@@ -52,7 +52,7 @@ struct Adj {
   double* tplm[2];
   double* troe[2][2];              // [stage-1][axis]
   double* tctu[2];                 // CTU per (face, side) and sweep
-  double* tslope[2];               // PLM/PPM slopes per extended cell and sweep
+  double* tslope[2];               // PPM slopes per extended cell and sweep
   // branch tapes (32-bit words, item-major planes) of the branch-recording and
   // -replaying forward sweeps: kBt* below
   unsigned int* bt[14];
@@ -144,7 +144,7 @@ __device__ __forceinline__ IO io(const Arr& a, int slot, size_t i) { return IO{a
 // stage kernels (REV = false: forward with stored intermediates; true: reverse)
 // ---------------------------------------------------------------------------
 // limited slopes of the sweep-extended cells e = 0 .. L+1 (cell e-1) and the base
-// words of each cell's eigensystem, which the edge stages read (PLM and PPM)
+// words of each cell's eigensystem, which the PPM edge stage reads (PPM only)
 template <int AX, bool REV, bool TAPE, int BR = 0>
 __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_slope(Adj A) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x, row = blockIdx.y;
@@ -179,8 +179,8 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_slope(Adj A) {
   else MHD_ADJ_RUN(pslope1, REV, TAPE, BR, in, out, par, tp, st, bt);
 }
 
-// edge states of each cell: first order (copies), or PLM / PPM from the slopes and the
-// cell's eigensystem words (the slope stage's output planes 7 ..)
+// edge states of each cell: first order (copies), PLM (one fused stage), or PPM from
+// the slopes and the cell's eigensystem words (the slope stage's output planes 7 ..)
 template <int AX, bool REV, bool TAPE, int RECON, int BR = 0>
 __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
@@ -191,8 +191,8 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
   if constexpr (RECON >= 1) {
     const int bc = AX == 0 ? A.bcx : A.bcy;
     constexpr int NI = RECON == 1 ? g_plm0_NI : g_ppm0_NI;
-    constexpr int NS = RECON == 1 ? 7 : 21;   // slope words: the cell's, or cells c-1, c, c+1
-    static_assert(NI == 21 + NS + g_pslope0_NO - 7, "edge stage inputs: 3 cells, slopes, eigensystem words");
+    static_assert(g_plm0_NI == 22 && g_ppm0_NI == 21 + 21 + g_pslope0_NO - 7,
+                  "edge stage inputs: PLM 3 cells + B_n; PPM 3 cells, 3 slopes, eigensystem words");
     IO in[NI];
     IO out[14];
 #pragma unroll
@@ -203,19 +203,21 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
 #pragma unroll
       for (int k = 0; k < 7; ++k) in[(o + 1) * 7 + k] = io(A.P, slots[k], ci);
     }
-    // slopes of cells c-1, c, c+1 sit at extended indices c, c+1, c+2
-    const Arr& S = AX == 0 ? A.SX : A.SY;
-    const int o0 = RECON == 1 ? 1 : 0;
+    if constexpr (RECON == 2) {
+      // slopes of cells c-1, c, c+1 sit at extended indices c, c+1, c+2; the cell's own
+      // eigensystem words at c+1
+      const Arr& S = AX == 0 ? A.SX : A.SY;
 #pragma unroll
-    for (int o = o0; o < (RECON == 1 ? 2 : 3); ++o) {
-      const size_t si = AX == 0 ? (size_t)t0 * (A.nx + 2) + c0 + o : (size_t)(t0 + o) * A.nx + c0;
+      for (int o = 0; o < 3; ++o) {
+        const size_t si = AX == 0 ? (size_t)t0 * (A.nx + 2) + c0 + o : (size_t)(t0 + o) * A.nx + c0;
 #pragma unroll
-      for (int k = 0; k < 7; ++k) in[21 + (o - o0) * 7 + k] = io(S, k, si);
-    }
-    {
+        for (int k = 0; k < 7; ++k) in[21 + o * 7 + k] = io(S, k, si);
+      }
       const size_t si = AX == 0 ? (size_t)t0 * (A.nx + 2) + c0 + 1 : (size_t)(t0 + 1) * A.nx + c0;
 #pragma unroll
-      for (int k = 7; k < g_pslope0_NO; ++k) in[21 + NS + k - 7] = io(S, k, si);
+      for (int k = 7; k < g_pslope0_NO; ++k) in[42 + k - 7] = io(S, k, si);
+    } else {
+      in[21] = io(A.P, AX == 0 ? 4 : 5, me);
     }
 #pragma unroll
     for (int k = 0; k < 14; ++k) out[k] = io(E, k, me);
@@ -257,17 +259,8 @@ void launch_recon(const Adj& A, cudaStream_t s) {
       k_recon<1, REV, TAPE, 0, BR><<<gc, kT, 0, s>>>(A);
       break;
     case 1:
-      if constexpr (!REV) {
-        k_slope<0, false, TAPE, BR><<<gsx, kT, 0, s>>>(A);
-        k_slope<1, false, TAPE, BR><<<gsy, kT, 0, s>>>(A);
-        k_recon<0, false, TAPE, 1, BR><<<gc, kT, 0, s>>>(A);
-        k_recon<1, false, TAPE, 1, BR><<<gc, kT, 0, s>>>(A);
-      } else {
-        k_recon<1, true, TAPE, 1><<<gc, kT, 0, s>>>(A);
-        k_recon<0, true, TAPE, 1><<<gc, kT, 0, s>>>(A);
-        k_slope<1, true, TAPE><<<gsy, kT, 0, s>>>(A);
-        k_slope<0, true, TAPE><<<gsx, kT, 0, s>>>(A);
-      }
+      k_recon<0, REV, TAPE, 1, BR><<<gc, kT, 0, s>>>(A);
+      k_recon<1, REV, TAPE, 1, BR><<<gc, kT, 0, s>>>(A);
       break;
     default:
       if constexpr (!REV) {
