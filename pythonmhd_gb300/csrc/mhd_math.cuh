@@ -448,31 +448,21 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   const double afb = afp * bts * bs2;
   const double asb = asp * bts * bs2;
 
-  double R[7][7];
-  R[0][0] = fa; R[0][2] = sa; R[0][3] = 1.0; R[0][4] = sa; R[0][6] = fa;
-  R[N][0] = fa * lam[0]; R[N][2] = sa * lam[2]; R[N][3] = vn; R[N][4] = sa * lam[4]; R[N][6] = fa * lam[6];
-  {
-    const double fv = fa * v[T1], sv = sa * v[T1], qsb = qs * b1s, qfb = qf * b1s;
-    R[T1][0] = fv + qsb; R[T1][1] = -bh2; R[T1][2] = sv - qfb; R[T1][3] = v[T1];
-    R[T1][4] = sv + qfb; R[T1][5] = bh2; R[T1][6] = fv - qsb;
+  double fl[7], fr[7];
+  cell_flux7<N, T1, T2>(wl, ul, bn, hbl, fl);
+  cell_flux7<N, T1, T2>(wr, ur, bn, hbr, fr);
+  if (is_nonpos(lam[6])) {
+#pragma unroll
+    for (int i = 0; i < 7; ++i) flux[i] = fr[i];
+    return;
   }
-  {
-    const double fv = fa * v[T2], sv = sa * v[T2], qsb = qs * b2s, qfb = qf * b2s;
-    R[T2][0] = fv + qsb; R[T2][1] = bh1; R[T2][2] = sv - qfb; R[T2][3] = v[T2];
-    R[T2][4] = sv + qfb; R[T2][5] = -bh1; R[T2][6] = fv - qsb;
+  if (is_nonneg(lam[0])) {
+#pragma unroll
+    for (int i = 0; i < 7; ++i) flux[i] = fl[i];
+    return;
   }
-  R[6][0] = fa * (hmb - vn * cf) + qs * vb + asb;
-  R[6][1] = -(v[T1] * bh2 - v[T2] * bh1);
-  R[6][2] = sa * (hmb - vn * cs) - qf * vb - afb;
-  R[6][3] = 0.5 * vsq + (gamma - 2.0) * btc / (gamma - 1.0);
-  R[6][4] = sa * (hmb + vn * cs) + qf * vb - afb;
-  R[6][5] = -R[6][1];
-  R[6][6] = fa * (hmb + vn * cf) - qs * vb + asb;
-  R[4][0] = asp * b1s; R[4][1] = -bh2 * sgn * isrd; R[4][2] = -afp * b1s;
-  R[4][4] = R[4][2]; R[4][5] = R[4][1]; R[4][6] = R[4][0];
-  R[5][0] = asp * b2s; R[5][1] = bh1 * sgn * isrd; R[5][2] = -afp * b2s;
-  R[5][4] = R[5][2]; R[5][5] = R[5][1]; R[5][6] = R[5][0];
-
+  // L, the wave amplitudes, then R: each matrix is formed where it is used, after
+  // the supersonic exits (the same expressions, so the same roundings)
   double nf = 0.5 / a2;
   const double cff = nf * fa * cf;
   const double css = nf * sa * cs;
@@ -537,19 +527,6 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   L[6][4] = L[0][4];
   L[6][5] = L[0][5];
 
-  double fl[7], fr[7];
-  cell_flux7<N, T1, T2>(wl, ul, bn, hbl, fl);
-  cell_flux7<N, T1, T2>(wr, ur, bn, hbr, fr);
-  if (is_nonpos(lam[6])) {
-#pragma unroll
-    for (int i = 0; i < 7; ++i) flux[i] = fr[i];
-    return;
-  }
-  if (is_nonneg(lam[0])) {
-#pragma unroll
-    for (int i = 0; i < 7; ++i) flux[i] = fl[i];
-    return;
-  }
   double du[7];
 #pragma unroll
   for (int i = 0; i < 7; ++i) du[i] = ur[i] - ul[i];
@@ -570,6 +547,31 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
     }
     amps[i] = 0.5 * fabs(lam[i]) * acc;
   }
+  double R[7][7];
+  R[0][0] = fa; R[0][2] = sa; R[0][3] = 1.0; R[0][4] = sa; R[0][6] = fa;
+  R[N][0] = fa * lam[0]; R[N][2] = sa * lam[2]; R[N][3] = vn; R[N][4] = sa * lam[4]; R[N][6] = fa * lam[6];
+  {
+    const double fv = fa * v[T1], sv = sa * v[T1], qsb = qs * b1s, qfb = qf * b1s;
+    R[T1][0] = fv + qsb; R[T1][1] = -bh2; R[T1][2] = sv - qfb; R[T1][3] = v[T1];
+    R[T1][4] = sv + qfb; R[T1][5] = bh2; R[T1][6] = fv - qsb;
+  }
+  {
+    const double fv = fa * v[T2], sv = sa * v[T2], qsb = qs * b2s, qfb = qf * b2s;
+    R[T2][0] = fv + qsb; R[T2][1] = bh1; R[T2][2] = sv - qfb; R[T2][3] = v[T2];
+    R[T2][4] = sv + qfb; R[T2][5] = -bh1; R[T2][6] = fv - qsb;
+  }
+  R[6][0] = fa * (hmb - vn * cf) + qs * vb + asb;
+  R[6][1] = -(v[T1] * bh2 - v[T2] * bh1);
+  R[6][2] = sa * (hmb - vn * cs) - qf * vb - afb;
+  R[6][3] = 0.5 * vsq + (gamma - 2.0) * btc / (gamma - 1.0);
+  R[6][4] = sa * (hmb + vn * cs) + qf * vb - afb;
+  R[6][5] = -R[6][1];
+  R[6][6] = fa * (hmb + vn * cf) - qs * vb + asb;
+  R[4][0] = asp * b1s; R[4][1] = -bh2 * sgn * isrd; R[4][2] = -afp * b1s;
+  R[4][4] = R[4][2]; R[4][5] = R[4][1]; R[4][6] = R[4][0];
+  R[5][0] = asp * b2s; R[5][1] = bh1 * sgn * isrd; R[5][2] = -afp * b2s;
+  R[5][4] = R[5][2]; R[5][5] = R[5][1]; R[5][6] = R[5][0];
+
 #pragma unroll
   for (int i = 0; i < 7; ++i) {
     double acc = 0.5 * (fl[i] + fr[i]);
