@@ -124,6 +124,45 @@ def _cpu_worker(args):
     return _cpu_cycles(n, steps, warmup, seed)
 
 
+def _batch_cpu_instance(args):
+    """The oracle's PLM cycle on one batched instance (its own CFL dt): seconds for
+    ``steps`` cycles and the zone-updates done."""
+    inst, steps = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from oracle import mhd2d
+    prim, cons, fbx, fby = (inst[k].copy() for k in ("prim", "cons", "fbx", "fby"))
+    g, dx, dy = inst["gamma"], inst["dx"], inst["dy"]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt = mhd2d.calc_dt(cons, fbx, fby, g, 0.4, dx, dy)
+        prim, cons, fbx, fby = mhd2d.cycle(prim, cons, fbx, fby, dt, dx, dy, 1, 1, g, 1e-12, 1e-12, 1e-12,
+                                           1, False, 0.5)
+    return time.perf_counter() - t0, inst["nx"] * inst["ny"] * steps
+
+
+def batch_cpu_baseline(insts, count, steps):
+    """The oracle on a seeded subset of the batched workload's instances: one host core,
+    and one process per host core (the instances are independent); zone-updates/s."""
+    import multiprocessing as mp
+    sample = [dict((k, i[k]) for k in ("prim", "cons", "fbx", "fby", "gamma", "dx", "dy", "nx", "ny"))
+              for i in insts[:count]]
+    one = [_batch_cpu_instance((i, steps)) for i in sample]
+    t1, z1 = sum(t for t, _ in one), sum(z for _, z in one)
+    cores = os.cpu_count() or 1
+    work = [(sample[k % len(sample)], steps) for k in range(cores)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_batch_cpu_instance, work)
+    wall = time.perf_counter() - t0
+    zp = sum(z for _, z in res)
+    return {"value": z1 / t1, "unit": UNIT, "cores": 1, "kind": "port",
+            "processes_value": zp / wall, "processes": cores,
+            "sample": f"oracle (NumPy restatement of the reference step, PLM), the first {len(sample)} instances of "
+                      f"the batch x {steps} cycles each: {t1:.2f} s on 1 host core; {cores} processes over the same "
+                      f"instances in turn, {wall:.2f} s wall (pool start included); a sample, not the 256 x 200 run"}
+
+
 def cpu_baseline(n, steps):
     t = _cpu_cycles(n, steps, 1, 7)
     return {"value": n * n / t, "unit": UNIT, "cores": 1, "kind": "port",
@@ -349,6 +388,7 @@ def run_batch(a, torch):
         g.close()
     # the FP64-issue roof from the single-grid PLM cycle's instruction mix: the batched
     # kernels run the same per-zone bodies (tile edges add a little on top)
+    cpu = batch_cpu_baseline(insts, 8, 2) if not a.no_cpu else None
     roof = {}
     plm = profile_summary(a.arith, 1)
     r = fp64_roof(plm, fp64_peak(), zones * k, tb * 1e3) if plm else None
@@ -364,7 +404,7 @@ def run_batch(a, torch):
                              "autotuned": True, "from_cache": tuned["cached"]},
             "loop": "one single-grid handle per instance, each advanced k cycles in turn (CUDA graphs)",
             "step_major_loop_zone_updates_per_s": zones * ks / ts, "step_major_steps": ks,
-            "speedup_vs_step_major_loop": (ts / ks) / (tb / k), **roof,
+            "speedup_vs_step_major_loop": (ts / ks) / (tb / k), **roof, "cpu_baseline": cpu,
             "timing": "host wall clock around device-synchronised calls"}
 
 
