@@ -412,9 +412,9 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
         a = wc[k];
         b = wc[k];
       } else if (dgt(idiff * adiff, sq(idiff))) {
-        a = (6.0 * wc[k] - 4.0 * b) / 2.0;
+        a = (6.0 * wc[k] - 4.0 * b) * 0.5;   // x / 2 exactly
       } else if (dlt(idiff * adiff, -1.0 * sq(idiff))) {
-        b = (6.0 * wc[k] - 4.0 * a) / 2.0;
+        b = (6.0 * wc[k] - 4.0 * a) * 0.5;
       }
       a = dmax(dmin(wc[k], wl[k]), a);
       a = dmin(dmax(wc[k], wl[k]), a);
@@ -920,8 +920,8 @@ __device__ __forceinline__ void b_half_ez(const Grid& G, const StateBuf& in, int
     u = u - hy * (G.fy[k * yfp + yb] - G.fy[k * yfp + yt]);
     hu[k] = u;
   }
-  const double hbx = (G.nfbx[xlf] + G.nfbx[xr]) / 2.0;
-  const double hby = (G.nfby[yt] + G.nfby[yb]) / 2.0;
+  const double hbx = (G.nfbx[xlf] + G.nfbx[xr]) * 0.5;   // x / 2 exactly
+  const double hby = (G.nfby[yt] + G.nfby[yb]) * 0.5;
   const double hvx = hu[1] / hu[0];
   const double hvy = hu[2] / hu[0];
   G.hez[idx] = hvy * hbx - hvx * hby;
@@ -969,8 +969,8 @@ __device__ __forceinline__ void b_final_mhd(const Grid& G, const StateBuf& in, c
   if (i == nx - 1) out.fbx[xr] = bxr;
   out.fby[yt] = byt;
   if (j == ny - 1) out.fby[yb] = byb;
-  const double cbx = (bxl + bxr) / 2.0;
-  const double cby = (byt + byb) / 2.0;
+  const double cbx = (bxl + bxr) * 0.5;   // x / 2 exactly
+  const double cby = (byt + byb) * 0.5;
   // conservative update of the x-sweep cons vector [rho, mx, my, mz, By, Bz, E]
   const int cslot[7] = {0, 1, 2, 3, 5, 6, 7};
   double u[7];
