@@ -28,8 +28,10 @@ def _fn(name, efix=False, backend="numpy", device=None):
         "plm1": (stages.plm_cell, 22, 2, dict(axis=1)),
         "pslope0": (stages.ppm_slope, 22, 1, dict(axis=0)),
         "pslope1": (stages.ppm_slope, 22, 1, dict(axis=1)),
-        "ppm0": (stages.ppm_cell, 42 + stages.EIG_BASE, 2, dict(axis=0)),
-        "ppm1": (stages.ppm_cell, 42 + stages.EIG_BASE, 2, dict(axis=1)),
+        "ppmi0": (stages.ppm_iface, 42, 1, dict(axis=0)),
+        "ppmi1": (stages.ppm_iface, 42, 1, dict(axis=1)),
+        "ppmt0": (stages.ppm_trace, 21 + stages.EIG_BASE, 2, dict(axis=0)),
+        "ppmt1": (stages.ppm_trace, 21 + stages.EIG_BASE, 2, dict(axis=1)),
         "face0": (stages.face_state, 10, 4, dict(sb=4)),
         "face1": (stages.face_state, 10, 4, dict(sb=5)),
         "roe1_0": (stages.roe1, 15, 2, dict(axis=0, efix=efix)),
@@ -181,13 +183,17 @@ class Cycle:
                 ins = [(P, s, ecell(off)) for off in (-1, 0, 1) for s in slots]
                 ins.append((P, bslot, ecell(0)))
                 self._rec(f"pslope{ax}", ins, [g], [(S, k, (SJ, SE) if ax == 0 else (SE, SJ)) for k in range(ns)])
+                # interface values with monotonicity (E0), then the characteristic tracing
+                E0 = self._zeros((14, ny, nx))
                 ins = [(P, s, cell(off)) for off in (-1, 0, 1) for s in slots]
                 for off in (0, 1, 2):
                     sidx = (J, I + off) if ax == 0 else (J + off, I)
                     ins += [(S, k, sidx) for k in range(7)]
+                self._rec(f"ppmi{ax}", ins, [g], [(E0, k, (J, I)) for k in range(14)])
                 own = (J, I + 1) if ax == 0 else (J + 1, I)
+                ins = [(P, s, cell(0)) for s in slots] + [(E0, k, (J, I)) for k in range(14)]
                 ins += [(S, 7 + k, own) for k in range(stages.EIG_BASE)]
-                self._rec(f"ppm{ax}", ins, [g, dt / dn], [(E, k, (J, I)) for k in range(14)])
+                self._rec(f"ppmt{ax}", ins, [g, dt / dn], [(E, k, (J, I)) for k in range(14)])
             else:
                 for k, s in enumerate(slots):
                     self._rec_copy(P, s, E, k)

@@ -16,8 +16,10 @@ STAGES = [
     ("plm1", stages.plm_cell, 22, 2, dict(axis=1)),
     ("pslope0", stages.ppm_slope, 22, 1, dict(axis=0)),
     ("pslope1", stages.ppm_slope, 22, 1, dict(axis=1)),
-    ("ppm0", stages.ppm_cell, 42 + stages.EIG_BASE, 2, dict(axis=0)),
-    ("ppm1", stages.ppm_cell, 42 + stages.EIG_BASE, 2, dict(axis=1)),
+    ("ppmi0", stages.ppm_iface, 42, 1, dict(axis=0)),
+    ("ppmi1", stages.ppm_iface, 42, 1, dict(axis=1)),
+    ("ppmt0", stages.ppm_trace, 21 + stages.EIG_BASE, 2, dict(axis=0)),
+    ("ppmt1", stages.ppm_trace, 21 + stages.EIG_BASE, 2, dict(axis=1)),
     ("face0", stages.face_state, 10, 4, dict(sb=4)),
     ("face1", stages.face_state, 10, 4, dict(sb=5)),
     ("roe1_0", stages.roe1, 15, 2, dict(axis=0, efix=False)),

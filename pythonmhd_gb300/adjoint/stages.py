@@ -210,19 +210,14 @@ def ppm_slope(ins, pars, axis):
     return s + base
 
 
-def ppm_cell(ins, pars, axis):
-    """PPM edge states of one cell with dt/2 characteristic tracing (k_faces MODE 2;
-    oracle.mhd2d.ppm_sweep).
+def ppm_iface(ins, pars, axis):
+    """PPM interface values of one cell with the monotonicity tests and the clamps to
+    the neighbours (k_faces MODE 2, first half; oracle.mhd2d.ppm_sweep).
 
-    ins = wl(7) + wc(7) + wr(7) + sl(7) + sc(7) + sr(7) + base(EIG_BASE), base the
-    cell's eigensystem words from ``ppm_slope`` ; pars = [gamma, dtdx] -> lia(7) + ria(7)
+    ins = wl(7) + wc(7) + wr(7) + sl(7) + sc(7) + sr(7) ; pars = [gamma] -> a(7) + b(7)
     """
     wl, wc, wr = ins[0:7], ins[7:14], ins[14:21]
     sl, sc, sr = ins[21:28], ins[28:35], ins[35:42]
-    base = ins[42:42 + EIG_BASE]
-    dtdx = pars[1]
-    lam, L, R = eig_from_base(base, wc, axis)
-    order = _order(axis)
     lia, ria = [], []
     for k in range(7):
         a = 0.5 * (wc[k] + wl[k]) - (sc[k] - sl[k]) / 6.0
@@ -242,6 +237,20 @@ def ppm_cell(ins, pars, axis):
         b2 = dmin(dmax(wc[k], wr[k]), b2)
         lia.append(a2)
         ria.append(b2)
+    return lia + ria
+
+
+def ppm_trace(ins, pars, axis):
+    """dt/2 characteristic tracing of one cell's PPM edge values (k_faces MODE 2, second
+    half), with the eigensystem built from the slope stage's base words.
+
+    ins = wc(7) + a(7) + b(7) + base(EIG_BASE) ; pars = [gamma, dtdx] -> lia(7) + ria(7)
+    """
+    wc, lia, ria = ins[0:7], list(ins[7:14]), list(ins[14:21])
+    base = ins[21:21 + EIG_BASE]
+    dtdx = pars[1]
+    lam, L, R = eig_from_base(base, wc, axis)
+    order = _order(axis)
     c1 = [ria[k] - lia[k] for k in range(7)]
     c2 = [6.0 * (wc[k] - 0.5 * (lia[k] + ria[k])) for k in range(7)]
     c3 = 0.5 * dmax(lam[6], 0.0) * dtdx

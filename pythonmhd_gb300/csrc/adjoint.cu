@@ -108,7 +108,7 @@ struct Slot {
 };
 const Slot kSlots[] = {
     {&Adj::P, 8, 0},   {&Adj::C, 8, 0},   {&Adj::FX, 1, 1},  {&Adj::FY, 1, 2},  {&Adj::EX, 14, 0},
-    {&Adj::EY, 14, 0}, {&Adj::SX, g_pslope0_NO, 4},  {&Adj::SY, g_pslope0_NO, 5},  {&Adj::XL, 7, 1},  {&Adj::XR, 7, 1},  {&Adj::YL, 7, 2},  {&Adj::YR, 7, 2},
+    {&Adj::EY, 14, 0}, {&Adj::SX, g_pslope0_NO, 4},  {&Adj::SY, g_pslope0_NO, 5},  {&Adj::E0X, 14, 0}, {&Adj::E0Y, 14, 0},  {&Adj::XL, 7, 1},  {&Adj::XR, 7, 1},  {&Adj::YL, 7, 2},  {&Adj::YR, 7, 2},
     {&Adj::F1X, 7, 1}, {&Adj::F1Y, 7, 2}, {&Adj::EZ, 1, 0},  {&Adj::E1, 1, 3},  {&Adj::NBX, 1, 1},
     {&Adj::NBY, 1, 2}, {&Adj::UXL, 7, 1}, {&Adj::UXR, 7, 1}, {&Adj::UYL, 7, 2}, {&Adj::UYR, 7, 2},
     {&Adj::WXL, 7, 1}, {&Adj::WXR, 7, 1}, {&Adj::WYL, 7, 2}, {&Adj::WYR, 7, 2}, {&Adj::HEZ, 1, 0},
@@ -128,8 +128,8 @@ struct Handle {
   double* vals = nullptr;      // nsets value arenas
   size_t TW = 0;               // words of one tape arena
   double* tapes = nullptr;     // nsets tape arenas
-  size_t toff[10] = {};        // tape offsets: recon x, recon y, roe1 x, roe1 y, roe2 x, roe2 y, ctu x, ctu y,
-                               // PPM slopes x, y
+  size_t toff[12] = {};        // tape offsets: recon x, recon y, roe1 x, roe1 y, roe2 x, roe2 y, ctu x, ctu y,
+                               // PPM slopes x, y, PPM tracing x, y
   int nsets = 0;
   double* red = nullptr;       // CFL maxima (2) + dt (1)
   size_t budget = 0;           // bytes the stored-segment mode may use (0: 85% of free memory)
@@ -185,6 +185,8 @@ void select_set(Handle* h, int k) {
   h->A.tctu[1] = tb + h->toff[7];
   h->A.tslope[0] = tb + h->toff[8];
   h->A.tslope[1] = tb + h->toff[9];
+  h->A.ttrace[0] = tb + h->toff[10];
+  h->A.ttrace[1] = tb + h->toff[11];
 }
 
 // n value+tape arenas of the current layout.  Memory is kept while it is large
@@ -218,15 +220,16 @@ size_t device_bytes(const Handle* h) {
 void branch_layout(int nx, int ny, int recon, int efix, size_t* off, size_t* BW) {
   const size_t cells = (size_t)nx * ny, xf = (size_t)(nx + 1) * ny, yf = (size_t)nx * (ny + 1);
   const size_t corners = (size_t)(nx + 1) * (ny + 1);
-  const int nb_recon = recon == 1 ? std::max(g_plm0_NB, g_plm1_NB) : (recon == 2 ? std::max(g_ppm0_NB, g_ppm1_NB) : 0);
+  const int nb_recon = recon == 1 ? std::max(g_plm0_NB, g_plm1_NB) : (recon == 2 ? std::max(g_ppmi0_NB, g_ppmi1_NB) : 0);
+  const int nb_trace = recon == 2 ? std::max(g_ppmt0_NB, g_ppmt1_NB) : 0;
   const int nb_slope = recon == 2 ? std::max(g_pslope0_NB, g_pslope1_NB) : 0;
   const int nb_roe1 = efix ? std::max(g_roe1_0_efix_NB, g_roe1_1_efix_NB) : std::max(g_roe1_0_NB, g_roe1_1_NB);
   const int nb_roe2 = efix ? std::max(g_roe2_0_efix_NB, g_roe2_1_efix_NB) : std::max(g_roe2_0_NB, g_roe2_1_NB);
   const size_t items[kNumBt] = {(size_t)(nx + 2) * ny, (size_t)nx * (ny + 2), cells, cells, 2 * xf, 2 * yf,
-                                xf, yf, xf, yf, corners, corners, 2 * xf, 2 * yf};
+                                xf, yf, xf, yf, corners, corners, 2 * xf, 2 * yf, cells, cells};
   const int words[kNumBt] = {nb_slope, nb_slope, nb_recon, nb_recon, std::max(g_face0_NB, g_face1_NB),
                              std::max(g_face0_NB, g_face1_NB), nb_roe1, nb_roe1, nb_roe2, nb_roe2, g_emf_NB, g_emf_NB,
-                             std::max(g_ctu0_NB, g_ctu1_NB), std::max(g_ctu0_NB, g_ctu1_NB)};
+                             std::max(g_ctu0_NB, g_ctu1_NB), std::max(g_ctu0_NB, g_ctu1_NB), nb_trace, nb_trace};
   size_t w = 0;
   for (int i = 0; i < kNumBt; ++i) {
     off[i] = w;
@@ -429,23 +432,25 @@ void layout(int nx, int ny, int recon, int efix, size_t* off, size_t* ps, size_t
   for (int i = 0; i < kNumSlots; ++i) {
     off[i] = w;
     ps[i] = plane[kSlots[i].kind];
-    // the slope arrays (sweep-extended cells) exist only for PPM
-    const bool slope = kSlots[i].kind == 4 || kSlots[i].kind == 5;
-    w += (size_t)(slope && recon != 2 ? 0 : kSlots[i].planes) * ps[i];
+    // the slope arrays (sweep-extended cells) and the interface values exist only for PPM
+    const bool ppm_only = kSlots[i].kind == 4 || kSlots[i].kind == 5 || kSlots[i].arr == &Adj::E0X ||
+                          kSlots[i].arr == &Adj::E0Y;
+    w += (size_t)(ppm_only && recon != 2 ? 0 : kSlots[i].planes) * ps[i];
     w = (w + 31) & ~(size_t)31;   // 256-byte aligned plane groups
   }
   *W = w;
-  // tapes: PLM/PPM per cell and sweep (first order has no reconstruction stage), Roe per
+  // tapes: PLM / PPM interface values per cell and sweep (first order has no reconstruction stage), Roe per
   // face, stage and sweep, CTU per face side and sweep, PLM/PPM slopes per extended cell and sweep
-  const int nt_plm = recon == 1 ? g_plm0_NT : (recon == 2 ? g_ppm0_NT : 0);
+  const int nt_plm = recon == 1 ? g_plm0_NT : (recon == 2 ? g_ppmi0_NT : 0);
+  const int nt_trace = recon == 2 ? g_ppmt0_NT : 0;
   const int nt_slope = recon == 2 ? g_pslope0_NT : 0;
   const int nt_roe[2] = {efix ? g_roe1_0_efix_NT : g_roe1_0_NT, efix ? g_roe2_0_efix_NT : g_roe2_0_NT};
-  const size_t items[10] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2],
-                            plane[4], plane[5]};
-  const int words[10] = {nt_plm, nt_plm, nt_roe[0], nt_roe[0], nt_roe[1], nt_roe[1], g_ctu0_NT, g_ctu0_NT,
-                         nt_slope, nt_slope};
+  const size_t items[12] = {plane[0], plane[0], plane[1], plane[2], plane[1], plane[2], 2 * plane[1], 2 * plane[2],
+                            plane[4], plane[5], plane[0], plane[0]};
+  const int words[12] = {nt_plm, nt_plm, nt_roe[0], nt_roe[0], nt_roe[1], nt_roe[1], g_ctu0_NT, g_ctu0_NT,
+                         nt_slope, nt_slope, nt_trace, nt_trace};
   size_t tw = 0;
-  for (int i = 0; i < 10; ++i) {
+  for (int i = 0; i < 12; ++i) {
     toff[i] = tw;
     tw += items[i] * (size_t)words[i];
     tw = (tw + 31) & ~(size_t)31;
@@ -690,7 +695,7 @@ int mhd2d_adj_reshape(void* handle, int ny, int nx, double dx, double dy, int bc
 
 int mhd2d_adj_cycle_bytes(int ny, int nx, int recon, int entropy_fix, size_t* bytes) {
   if (!bytes || nx < 2 || ny < 2 || recon < 0 || recon > 2) return MHD_ERR_ARG;
-  size_t off[kNumSlots], ps[kNumSlots], toff[10], W = 0, TW = 0;
+  size_t off[kNumSlots], ps[kNumSlots], toff[12], W = 0, TW = 0;
   layout(nx, ny, recon, entropy_fix ? 1 : 0, off, ps, &W, toff, &TW);
   *bytes = (W + TW) * sizeof(double);
   return MHD_OK;

@@ -21,7 +21,8 @@ constexpr int kT = 128;
 #endif
 constexpr int kRevMinBlocks = MHD_ADJ_REV_MIN_BLOCKS;
 static_assert(g_plm0_NT == g_plm1_NT && g_roe1_0_NT == g_roe1_1_NT && g_roe2_0_NT == g_roe2_1_NT &&
-                  g_ctu0_NT == g_ctu1_NT && g_ppm0_NT == g_ppm1_NT && g_pslope0_NT == g_pslope1_NT &&
+                  g_ctu0_NT == g_ctu1_NT && g_ppmi0_NT == g_ppmi1_NT && g_ppmt0_NT == g_ppmt1_NT &&
+                  g_pslope0_NT == g_pslope1_NT &&
                   g_roe1_0_efix_NT == g_roe1_1_efix_NT && g_roe2_0_efix_NT == g_roe2_1_efix_NT,
               "the x and y sweeps of a stage store tapes of the same length");
 
@@ -41,6 +42,7 @@ struct Adj {
   Arr EX, EY;                      // edge states per cell (lia 7 + ria 7), x and y sweeps
   Arr SX, SY;                      // PPM: limited slopes of the sweep-extended cells and their
                                    // eigensystems' base words (g_pslope0_NO planes)
+  Arr E0X, E0Y;                    // PPM: interface values after the monotonicity tests (a 7 + b 7)
   Arr XL, XR, YL, YR;              // reconstructed face states
   Arr F1X, F1Y, EZ, E1, NBX, NBY;  // stage-1 fluxes, cell Ez, corner EMF, half-step faces
   Arr UXL, UXR, UYL, UYR, WXL, WXR, WYL, WYR;  // CTU-corrected face cons / prim
@@ -53,15 +55,21 @@ struct Adj {
   double* troe[2][2];              // [stage-1][axis]
   double* tctu[2];                 // CTU per (face, side) and sweep
   double* tslope[2];               // PPM slopes per extended cell and sweep
+  double* ttrace[2];               // PPM characteristic tracing per cell and sweep
   // branch tapes (32-bit words, item-major planes) of the branch-recording and
   // -replaying forward sweeps: kBt* below
-  unsigned int* bt[14];
+  unsigned int* bt[16];
 };
 
 // branch tape of each stage: PPM slopes x/y (extended cells), reconstruction x/y
-// (cells), face states x/y (face, side), Roe stage 1 x/y and stage 2 x/y (faces),
-// corner EMF stage 1/2 (corners), CTU x/y (face, side)
-enum BtSlot { kBtSlope = 0, kBtRecon = 2, kBtFace = 4, kBtRoe1 = 6, kBtRoe2 = 8, kBtEmf = 10, kBtCtu = 12, kNumBt = 14 };
+// (cells; PLM, or the PPM interface values), face states x/y (face, side), Roe stage 1
+// x/y and stage 2 x/y (faces), corner EMF stage 1/2 (corners), CTU x/y (face, side),
+// PPM tracing x/y (cells)
+enum BtSlot {
+  kBtSlope = 0, kBtRecon = 2, kBtFace = 4, kBtRoe1 = 6, kBtRoe2 = 8, kBtEmf = 10, kBtCtu = 12, kBtTrace = 14,
+  kNumBt = 16
+};
+static_assert(kNumBt == sizeof(Adj::bt) / sizeof(Adj::bt[0]), "one branch tape per stage slot");
 
 __device__ __forceinline__ int wrapc(int c, int L, int bc) {
   if (bc == 1) {
@@ -179,8 +187,8 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_slope(Adj A) {
   else MHD_ADJ_RUN(pslope1, REV, TAPE, BR, in, out, par, tp, st, bt);
 }
 
-// edge states of each cell: first order (copies), PLM (one fused stage), or PPM from
-// the slopes and the cell's eigensystem words (the slope stage's output planes 7 ..)
+// edge states of each cell: first order (copies), PLM (one fused stage), or the PPM
+// interface values after the monotonicity tests (into E0X/E0Y; k_trace finishes them)
 template <int AX, bool REV, bool TAPE, int RECON, int BR = 0>
 __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
@@ -190,9 +198,8 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
   const int slots[7] = {0, 1, 2, 3, AX == 0 ? 5 : 6, AX == 0 ? 6 : 4, 7};
   if constexpr (RECON >= 1) {
     const int bc = AX == 0 ? A.bcx : A.bcy;
-    constexpr int NI = RECON == 1 ? g_plm0_NI : g_ppm0_NI;
-    static_assert(g_plm0_NI == 22 && g_ppm0_NI == 21 + 21 + g_pslope0_NO - 7,
-                  "edge stage inputs: PLM 3 cells + B_n; PPM 3 cells, 3 slopes, eigensystem words");
+    constexpr int NI = RECON == 1 ? g_plm0_NI : g_ppmi0_NI;
+    static_assert(g_plm0_NI == 22 && g_ppmi0_NI == 42, "edge stage inputs: PLM 3 cells + B_n; PPM 3 cells, 3 slopes");
     IO in[NI];
     IO out[14];
 #pragma unroll
@@ -204,8 +211,7 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
       for (int k = 0; k < 7; ++k) in[(o + 1) * 7 + k] = io(A.P, slots[k], ci);
     }
     if constexpr (RECON == 2) {
-      // slopes of cells c-1, c, c+1 sit at extended indices c, c+1, c+2; the cell's own
-      // eigensystem words at c+1
+      // slopes of cells c-1, c, c+1 sit at extended indices c, c+1, c+2
       const Arr& S = AX == 0 ? A.SX : A.SY;
 #pragma unroll
       for (int o = 0; o < 3; ++o) {
@@ -213,14 +219,12 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
 #pragma unroll
         for (int k = 0; k < 7; ++k) in[21 + o * 7 + k] = io(S, k, si);
       }
-      const size_t si = AX == 0 ? (size_t)t0 * (A.nx + 2) + c0 + 1 : (size_t)(t0 + 1) * A.nx + c0;
-#pragma unroll
-      for (int k = 7; k < g_pslope0_NO; ++k) in[42 + k - 7] = io(S, k, si);
     } else {
       in[21] = io(A.P, AX == 0 ? 4 : 5, me);
     }
+    const Arr& O = RECON == 2 ? (AX == 0 ? A.E0X : A.E0Y) : E;
 #pragma unroll
-    for (int k = 0; k < 14; ++k) out[k] = io(E, k, me);
+    for (int k = 0; k < 14; ++k) out[k] = io(O, k, me);
     const double par[2] = {A.gamma, A.dt / (AX == 0 ? A.dx : A.dy)};
     double* tp = A.tplm[AX] + me;
     const size_t st = (size_t)A.nx * A.ny;
@@ -229,8 +233,8 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
       if (AX == 0) MHD_ADJ_RUN(plm0, REV, TAPE, BR, in, out, par, tp, st, bt);
       else MHD_ADJ_RUN(plm1, REV, TAPE, BR, in, out, par, tp, st, bt);
     } else {
-      if (AX == 0) MHD_ADJ_RUN(ppm0, REV, TAPE, BR, in, out, par, tp, st, bt);
-      else MHD_ADJ_RUN(ppm1, REV, TAPE, BR, in, out, par, tp, st, bt);
+      if (AX == 0) MHD_ADJ_RUN(ppmi0, REV, TAPE, BR, in, out, par, tp, st, bt);
+      else MHD_ADJ_RUN(ppmi1, REV, TAPE, BR, in, out, par, tp, st, bt);
     }
   } else {
 #pragma unroll
@@ -246,7 +250,38 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_recon(Adj A) {
   }
 }
 
-// launch the reconstruction of both sweeps (PPM: slopes first)
+// PPM: dt/2 characteristic tracing of each cell's interface values (E0X/E0Y -> EX/EY),
+// with the eigensystem from the slope stage's base words (extended index c+1)
+template <int AX, bool REV, bool TAPE, int BR = 0>
+__global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_trace(Adj A) {
+  const int c0 = blockIdx.x * blockDim.x + threadIdx.x, t0 = blockIdx.y;
+  if (c0 >= A.nx || t0 >= A.ny) return;
+  const size_t me = (size_t)t0 * A.nx + c0;
+  const int slots[7] = {0, 1, 2, 3, AX == 0 ? 5 : 6, AX == 0 ? 6 : 4, 7};
+  static_assert(g_ppmt0_NI == 21 + g_pslope0_NO - 7, "tracing inputs: the cell, its interface values, eigensystem words");
+  IO in[g_ppmt0_NI];
+  IO out[14];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) in[k] = io(A.P, slots[k], me);
+  const Arr& E0 = AX == 0 ? A.E0X : A.E0Y;
+#pragma unroll
+  for (int k = 0; k < 14; ++k) in[7 + k] = io(E0, k, me);
+  const Arr& S = AX == 0 ? A.SX : A.SY;
+  const size_t si = AX == 0 ? (size_t)t0 * (A.nx + 2) + c0 + 1 : (size_t)(t0 + 1) * A.nx + c0;
+#pragma unroll
+  for (int k = 7; k < g_pslope0_NO; ++k) in[21 + k - 7] = io(S, k, si);
+  const Arr& E = AX == 0 ? A.EX : A.EY;
+#pragma unroll
+  for (int k = 0; k < 14; ++k) out[k] = io(E, k, me);
+  const double par[2] = {A.gamma, A.dt / (AX == 0 ? A.dx : A.dy)};
+  double* tp = A.ttrace[AX] + me;
+  const size_t st = (size_t)A.nx * A.ny;
+  unsigned int* bt = BR ? A.bt[kBtTrace + AX] + me : nullptr;
+  if (AX == 0) MHD_ADJ_RUN(ppmt0, REV, TAPE, BR, in, out, par, tp, st, bt);
+  else MHD_ADJ_RUN(ppmt1, REV, TAPE, BR, in, out, par, tp, st, bt);
+}
+
+// launch the reconstruction of both sweeps (PPM: slopes, interface values, tracing)
 template <bool REV, bool TAPE, int BR = 0>
 void launch_recon(const Adj& A, cudaStream_t s) {
   const int nx = A.nx, ny = A.ny;
@@ -268,7 +303,11 @@ void launch_recon(const Adj& A, cudaStream_t s) {
         k_slope<1, false, TAPE, BR><<<gsy, kT, 0, s>>>(A);
         k_recon<0, false, TAPE, 2, BR><<<gc, kT, 0, s>>>(A);
         k_recon<1, false, TAPE, 2, BR><<<gc, kT, 0, s>>>(A);
+        k_trace<0, false, TAPE, BR><<<gc, kT, 0, s>>>(A);
+        k_trace<1, false, TAPE, BR><<<gc, kT, 0, s>>>(A);
       } else {
+        k_trace<1, true, TAPE><<<gc, kT, 0, s>>>(A);
+        k_trace<0, true, TAPE><<<gc, kT, 0, s>>>(A);
         k_recon<1, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
         k_recon<0, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
         k_slope<1, true, TAPE><<<gsy, kT, 0, s>>>(A);
