@@ -435,6 +435,84 @@ def roe_flux(wl, wr, ul, ur, bn, gamma, eps, efix, axis):
     bs2 = b1s * b1s + b2s * b2s
     afb = afp * bts * bs2
     asb = asp * bts * bs2
+    nf = 0.5 / a2
+    cff = nf * fa * cf
+    css = nf * sa * cs
+    qfn = qf * nf
+    qsn = qs * nf
+    af_ = nf * afp * rd
+    as_ = nf * asp * rd
+    afb2 = nf * afp * bts
+    asb2 = nf * asp * bts
+    nf = nf * (gamma - 1.0)
+    fan = fa * nf
+    san = sa * nf
+    b1c = b1s / bs2
+    b2c = b2s / bs2
+    vbs = v[T1] * b1c + v[T2] * b2c
+    nf = nf * 2.0
+    fl = _cell_flux(wl, ul, bn, hbl, axis)
+    fr = _cell_flux(wr, ur, bn, hbr, axis)
+    du = [ur[i] - ul[i] for i in range(7)]
+    order = _order(axis)
+    # L row by row, each wave amplitude right after its row (the same values; the
+    # reverse sweep then holds few of L's adjoints at a time)
+    amps = []
+    L = {}
+    L[0, 0] = fan * (vsq - hmb) + cff * (cf + vn) - qsn * vbs - asb2
+    L[0, N] = -1.0 * fan * vn - cff
+    L[0, T1] = -1.0 * fan * v[T1] + qsn * b1c
+    L[0, T2] = -1.0 * fan * v[T2] + qsn * b2c
+    L[0, 6] = fan
+    L[0, 4] = as_ * b1c - fan * b1
+    L[0, 5] = as_ * b2c - fan * b2
+    amps.append(0.5 * fabs(lam[0]) * _project(L, 0, du, order))
+    L[1, 0] = 0.5 * (v[T1] * bh2 - v[T2] * bh1)
+    L[1, T1] = -0.5 * bh2
+    L[1, T2] = 0.5 * bh1
+    L[1, 4] = -0.5 * srd * bh2 * sgn
+    L[1, 5] = 0.5 * srd * bh1 * sgn
+    amps.append(0.5 * fabs(lam[1]) * _project(L, 1, du, order))
+    L[2, 0] = san * (vsq - hmb) + css * (cs + vn) + qfn * vbs + afb2
+    L[2, N] = -san * vn - css
+    L[2, T1] = -san * v[T1] - qfn * b1c
+    L[2, T2] = -san * v[T2] - qfn * b2c
+    L[2, 6] = san
+    L[2, 4] = -af_ * b1c - san * b1
+    L[2, 5] = -af_ * b2c - san * b2
+    amps.append(0.5 * fabs(lam[2]) * _project(L, 2, du, order))
+    L[3, 0] = 1.0 - nf * (0.5 * vsq - (gamma - 2.0) * btc / (gamma - 1.0))
+    L[3, 1] = nf * v[1]
+    L[3, 2] = nf * v[2]
+    L[3, 3] = nf * v[3]
+    L[3, 6] = -1.0 * nf
+    L[3, 4] = nf * b1
+    L[3, 5] = nf * b2
+    amps.append(0.5 * fabs(lam[3]) * _project(L, 3, du, order))
+    L[4, 0] = san * (vsq - hmb) + css * (cs - vn) - qfn * vbs + afb2
+    L[4, N] = -san * vn + css
+    L[4, T1] = -san * v[T1] + qfn * b1c
+    L[4, T2] = -san * v[T2] + qfn * b2c
+    L[4, 6] = san
+    L[4, 4] = L[2, 4]
+    L[4, 5] = L[2, 5]
+    amps.append(0.5 * fabs(lam[4]) * _project(L, 4, du, order))
+    L[5, 0] = -L[1, 0]
+    L[5, T1] = -L[1, T1]
+    L[5, T2] = -L[1, T2]
+    L[5, 4] = L[1, 4]
+    L[5, 5] = L[1, 5]
+    amps.append(0.5 * fabs(lam[5]) * _project(L, 5, du, order))
+    L[6, 0] = fan * (vsq - hmb) + cff * (cf - vn) + qsn * vbs - asb2
+    L[6, N] = -fan * vn + cff
+    L[6, T1] = -fan * v[T1] - qsn * b1c
+    L[6, T2] = -fan * v[T2] - qsn * b2c
+    L[6, 6] = fan
+    L[6, 4] = L[0, 4]
+    L[6, 5] = L[0, 5]
+    amps.append(0.5 * fabs(lam[6]) * _project(L, 6, du, order))
+    # R where it is used (after L and the amplitudes): the same values, with its
+    # entries' adjoints held only across the flux rows in the reverse sweep
     R = {}
     R[0, 0] = fa; R[0, 2] = sa; R[0, 3] = 1.0; R[0, 4] = sa; R[0, 6] = fa
     R[N, 0] = fa * lam[0]; R[N, 2] = sa * lam[2]; R[N, 3] = vn; R[N, 4] = sa * lam[4]; R[N, 6] = fa * lam[6]
@@ -455,73 +533,6 @@ def roe_flux(wl, wr, ul, ur, bn, gamma, eps, efix, axis):
     R[4, 4] = R[4, 2]; R[4, 5] = R[4, 1]; R[4, 6] = R[4, 0]
     R[5, 0] = asp * b2s; R[5, 1] = bh1 * sgn * isrd; R[5, 2] = -afp * b2s
     R[5, 4] = R[5, 2]; R[5, 5] = R[5, 1]; R[5, 6] = R[5, 0]
-    nf = 0.5 / a2
-    cff = nf * fa * cf
-    css = nf * sa * cs
-    qfn = qf * nf
-    qsn = qs * nf
-    af_ = nf * afp * rd
-    as_ = nf * asp * rd
-    afb2 = nf * afp * bts
-    asb2 = nf * asp * bts
-    nf = nf * (gamma - 1.0)
-    fan = fa * nf
-    san = sa * nf
-    b1c = b1s / bs2
-    b2c = b2s / bs2
-    vbs = v[T1] * b1c + v[T2] * b2c
-    nf = nf * 2.0
-    L = {}
-    L[0, 0] = fan * (vsq - hmb) + cff * (cf + vn) - qsn * vbs - asb2
-    L[0, N] = -1.0 * fan * vn - cff
-    L[0, T1] = -1.0 * fan * v[T1] + qsn * b1c
-    L[0, T2] = -1.0 * fan * v[T2] + qsn * b2c
-    L[0, 6] = fan
-    L[0, 4] = as_ * b1c - fan * b1
-    L[0, 5] = as_ * b2c - fan * b2
-    L[1, 0] = 0.5 * (v[T1] * bh2 - v[T2] * bh1)
-    L[1, T1] = -0.5 * bh2
-    L[1, T2] = 0.5 * bh1
-    L[1, 4] = -0.5 * srd * bh2 * sgn
-    L[1, 5] = 0.5 * srd * bh1 * sgn
-    L[2, 0] = san * (vsq - hmb) + css * (cs + vn) + qfn * vbs + afb2
-    L[2, N] = -san * vn - css
-    L[2, T1] = -san * v[T1] - qfn * b1c
-    L[2, T2] = -san * v[T2] - qfn * b2c
-    L[2, 6] = san
-    L[2, 4] = -af_ * b1c - san * b1
-    L[2, 5] = -af_ * b2c - san * b2
-    L[3, 0] = 1.0 - nf * (0.5 * vsq - (gamma - 2.0) * btc / (gamma - 1.0))
-    L[3, 1] = nf * v[1]
-    L[3, 2] = nf * v[2]
-    L[3, 3] = nf * v[3]
-    L[3, 6] = -1.0 * nf
-    L[3, 4] = nf * b1
-    L[3, 5] = nf * b2
-    L[4, 0] = san * (vsq - hmb) + css * (cs - vn) - qfn * vbs + afb2
-    L[4, N] = -san * vn + css
-    L[4, T1] = -san * v[T1] + qfn * b1c
-    L[4, T2] = -san * v[T2] + qfn * b2c
-    L[4, 6] = san
-    L[4, 4] = L[2, 4]
-    L[4, 5] = L[2, 5]
-    L[5, 0] = -L[1, 0]
-    L[5, T1] = -L[1, T1]
-    L[5, T2] = -L[1, T2]
-    L[5, 4] = L[1, 4]
-    L[5, 5] = L[1, 5]
-    L[6, 0] = fan * (vsq - hmb) + cff * (cf - vn) + qsn * vbs - asb2
-    L[6, N] = -fan * vn + cff
-    L[6, T1] = -fan * v[T1] - qsn * b1c
-    L[6, T2] = -fan * v[T2] - qsn * b2c
-    L[6, 6] = fan
-    L[6, 4] = L[0, 4]
-    L[6, 5] = L[0, 5]
-    fl = _cell_flux(wl, ul, bn, hbl, axis)
-    fr = _cell_flux(wr, ur, bn, hbr, axis)
-    du = [ur[i] - ul[i] for i in range(7)]
-    order = _order(axis)
-    amps = [0.5 * fabs(lam[i]) * _project(L, i, du, order) for i in range(7)]
     flux = []
     for i in range(7):
         acc = 0.5 * (fl[i] + fr[i])
