@@ -46,7 +46,7 @@ EIG_BASE = 16   # words of eig_base
 def eig_base(w, bn, gamma):
     """The costly part of the primitive eigensystem of one cell state: its square
     roots, divisions and signs, as the list [a2, a, ca, cf, cs, fa, sa, b1, b2, sgn,
-    sqrt_d, inv_d, nf, l14, l15, l36].  ``LazyEig`` builds lam, L and R from
+    sqrt_d, inv_d, nf, l14, l15, l36].  ``eig_from_base`` builds lam, L and R from
     them with multiplies only, so a stage can take them as inputs from the stage that
     formed them instead of recomputing them."""
     bt2 = w[4] * w[4] + w[5] * w[5]
@@ -81,85 +81,53 @@ def eig_base(w, bn, gamma):
     return [a2, a, ca, cf, cs, fa, sa, b1, b2, sgn, sqrt_d, inv_d, nf, l14, l15, l36]
 
 
-class LazyEig:
+def eig_from_base(base, w, axis):
     """lam, L and R (mhd_math.cuh: prim_eigensystem) of the cell state w from its
-    ``eig_base`` words, in the same operation order, with each entry of L and R formed
-    on its first use (and kept for later ones).  A stage that uses row i of L and
-    column i of R only for wave i then holds few of their adjoints at a time in its
-    reverse sweep; the values are those of the eager form, bit for bit."""
-
-    def __init__(self, base, w, axis):
-        (self.a2, self.a, self.ca, self.cf, self.cs, self.fa, self.sa, self.b1, self.b2, self.sgn,
-         self.sqrt_d, self.inv_d, self.nf, self.l14, self.l15, self.l36) = base
-        self.w = w
-        self.N, self.T1, self.T2 = FRAMES[axis]
-        vn = w[self.N]
-        self.lam = [vn - self.cf, vn - self.ca, vn - self.cs, vn, vn + self.cs, vn + self.ca, vn + self.cf]
-        self._m = {}
-        N, T1, T2 = self.N, self.T1, self.T2
-        v = self._v
-        R = {(0, 0): "r00", (0, 2): "r02", (0, 3): 1.0, (0, 4): "r02", (0, 6): "r00",
-             (N, 0): "rn0", (N, 2): "rn2", (N, 4): "-rn2", (N, 6): "-rn0",
-             (T1, 0): "qsb1", (T1, 1): "-b2", (T1, 2): "-qfb1", (T1, 4): "qfb1", (T1, 5): "b2", (T1, 6): "-qsb1",
-             (T2, 0): "qsb2", (T2, 1): "b1", (T2, 2): "-qfb2", (T2, 4): "qfb2", (T2, 5): "-b1", (T2, 6): "-qsb2",
-             (6, 0): "r60", (6, 2): "r62", (6, 4): "r62", (6, 6): "r60",
-             (4, 0): "r40", (4, 1): "r41", (4, 2): "r42", (4, 4): "r42", (4, 5): "r41", (4, 6): "r40",
-             (5, 0): "r50", (5, 1): "r51", (5, 2): "r52", (5, 4): "r52", (5, 5): "r51", (5, 6): "r50"}
-        L = {(0, N): "l0n", (0, T1): "l0t1", (0, T2): "l0t2", (0, 6): "l06", (0, 4): "l04", (0, 5): "l05",
-             (6, N): "-l0n", (6, T1): "-l0t1", (6, T2): "-l0t2", (6, 6): "l06", (6, 4): "l04", (6, 5): "l05",
-             (1, T1): "l1t1", (1, T2): "l1t2", (1, 4): "l14", (1, 5): "l15",
-             (5, T1): "-l1t1", (5, T2): "-l1t2", (5, 4): "l14", (5, 5): "l15",
-             (2, N): "l2n", (2, T1): "l2t1", (2, T2): "l2t2", (2, 6): "l26", (2, 4): "l24", (2, 5): "l25",
-             (4, N): "-l2n", (4, T1): "-l2t1", (4, T2): "-l2t2", (4, 6): "l26", (4, 4): "l24", (4, 5): "l25",
-             (3, 0): 1.0, (3, 6): "l36"}
-        self._R, self._L = R, L
-        self.R_keys, self.L_keys = set(R), set(L)
-        w0 = w[0]
-        # the named values, as the eager form writes them (operands left to right)
-        self._defs = {
-            "qf": lambda: self.cf * self.fa * self.sgn, "qs": lambda: self.cs * self.sa * self.sgn,
-            "af": lambda: self.a * self.fa * self.sqrt_d, "as_": lambda: self.a * self.sa * self.sqrt_d,
-            "r00": lambda: w0 * self.fa, "r02": lambda: w0 * self.sa,
-            "rn0": lambda: -self.cf * self.fa, "rn2": lambda: -self.cs * self.sa,
-            "qsb1": lambda: v("qs") * self.b1, "qfb1": lambda: v("qf") * self.b1,
-            "qsb2": lambda: v("qs") * self.b2, "qfb2": lambda: v("qf") * self.b2,
-            "r60": lambda: w0 * self.a2 * self.fa, "r62": lambda: w0 * self.a2 * self.sa,
-            "r40": lambda: v("as_") * self.b1, "r41": lambda: -self.b2 * self.sgn * self.sqrt_d,
-            "r42": lambda: -v("af") * self.b1,
-            "r50": lambda: v("as_") * self.b2, "r51": lambda: self.b1 * self.sgn * self.sqrt_d,
-            "r52": lambda: -v("af") * self.b2,
-            "b1": lambda: self.b1, "b2": lambda: self.b2,
-            "qf_n": lambda: self.nf * v("qf"), "qs_n": lambda: self.nf * v("qs"),
-            "afp": lambda: self.nf * v("af") * self.inv_d, "asp": lambda: self.nf * v("as_") * self.inv_d,
-            "l0n": lambda: -self.nf * self.cf * self.fa, "l0t1": lambda: v("qs_n") * self.b1,
-            "l0t2": lambda: v("qs_n") * self.b2, "l06": lambda: self.nf * self.fa * self.inv_d,
-            "l04": lambda: v("asp") * self.b1, "l05": lambda: v("asp") * self.b2,
-            "l1t1": lambda: -0.5 * self.b2, "l1t2": lambda: 0.5 * self.b1,
-            "l14": lambda: self.l14, "l15": lambda: self.l15, "l36": lambda: self.l36,
-            "l2n": lambda: -self.nf * self.cs * self.sa, "l2t1": lambda: -v("qf_n") * self.b1,
-            "l2t2": lambda: -v("qf_n") * self.b2, "l26": lambda: self.nf * self.sa * self.inv_d,
-            "l24": lambda: -v("afp") * self.b1, "l25": lambda: -v("afp") * self.b2,
-        }
-
-    def _v(self, name):
-        if name.startswith("-"):
-            key = name
-            if key not in self._m:
-                self._m[key] = -self._v(name[1:])
-            return self._m[key]
-        if name not in self._m:
-            self._m[name] = self._defs[name]()
-        return self._m[name]
-
-    def _entry(self, table, i, j):
-        e = table[i, j]
-        return e if isinstance(e, float) else self._v(e)
-
-    def R(self, i, j):
-        return self._entry(self._R, i, j)
-
-    def L(self, i, j):
-        return self._entry(self._L, i, j)
+    ``eig_base`` words, in the same operation order."""
+    N, T1, T2 = FRAMES[axis]
+    a2, a, ca, cf, cs, fa, sa, b1, b2, sgn, sqrt_d, inv_d, nf, l14, l15, l36 = base
+    qf = cf * fa * sgn
+    qs = cs * sa * sgn
+    af = a * fa * sqrt_d
+    as_ = a * sa * sqrt_d
+    vn = w[N]
+    lam = [vn - cf, vn - ca, vn - cs, vn, vn + cs, vn + ca, vn + cf]
+    R = {}
+    r00 = w[0] * fa
+    r02 = w[0] * sa
+    R[0, 0] = r00; R[0, 2] = r02; R[0, 3] = 1.0; R[0, 4] = r02; R[0, 6] = r00
+    rn0 = -cf * fa
+    rn2 = -cs * sa
+    R[N, 0] = rn0; R[N, 2] = rn2; R[N, 4] = -rn2; R[N, 6] = -rn0
+    qsb1 = qs * b1; qfb1 = qf * b1; qsb2 = qs * b2; qfb2 = qf * b2
+    R[T1, 0] = qsb1; R[T1, 1] = -b2; R[T1, 2] = -qfb1; R[T1, 4] = qfb1; R[T1, 5] = b2; R[T1, 6] = -qsb1
+    R[T2, 0] = qsb2; R[T2, 1] = b1; R[T2, 2] = -qfb2; R[T2, 4] = qfb2; R[T2, 5] = -b1; R[T2, 6] = -qsb2
+    r60 = w[0] * a2 * fa
+    r62 = w[0] * a2 * sa
+    R[6, 0] = r60; R[6, 2] = r62; R[6, 4] = r62; R[6, 6] = r60
+    r40 = as_ * b1; r41 = -b2 * sgn * sqrt_d; r42 = -af * b1
+    R[4, 0] = r40; R[4, 1] = r41; R[4, 2] = r42; R[4, 4] = r42; R[4, 5] = r41; R[4, 6] = r40
+    r50 = as_ * b2; r51 = b1 * sgn * sqrt_d; r52 = -af * b2
+    R[5, 0] = r50; R[5, 1] = r51; R[5, 2] = r52; R[5, 4] = r52; R[5, 5] = r51; R[5, 6] = r50
+    qf_n = nf * qf
+    qs_n = nf * qs
+    afp = nf * af * inv_d
+    asp = nf * as_ * inv_d
+    L = {}
+    l0n = -nf * cf * fa; l0t1 = qs_n * b1; l0t2 = qs_n * b2; l06 = nf * fa * inv_d
+    l04 = asp * b1; l05 = asp * b2
+    L[0, N] = l0n; L[0, T1] = l0t1; L[0, T2] = l0t2; L[0, 6] = l06; L[0, 4] = l04; L[0, 5] = l05
+    L[6, N] = -l0n; L[6, T1] = -l0t1; L[6, T2] = -l0t2; L[6, 6] = l06; L[6, 4] = l04; L[6, 5] = l05
+    l1t1 = -0.5 * b2; l1t2 = 0.5 * b1
+    L[1, T1] = l1t1; L[1, T2] = l1t2; L[1, 4] = l14; L[1, 5] = l15
+    L[5, T1] = -l1t1; L[5, T2] = -l1t2; L[5, 4] = l14; L[5, 5] = l15
+    l2n = -nf * cs * sa; l2t1 = -qf_n * b1; l2t2 = -qf_n * b2; l26 = nf * sa * inv_d
+    l24 = -afp * b1; l25 = -afp * b2
+    L[2, N] = l2n; L[2, T1] = l2t1; L[2, T2] = l2t2; L[2, 6] = l26; L[2, 4] = l24; L[2, 5] = l25
+    L[4, N] = -l2n; L[4, T1] = -l2t1; L[4, T2] = -l2t2; L[4, 6] = l26; L[4, 4] = l24; L[4, 5] = l25
+    L[3, 0] = 1.0
+    L[3, 6] = l36
+    return lam, L, R
 
 
 def _order(axis):
@@ -167,18 +135,15 @@ def _order(axis):
     return (0, N, T1, T2, 6, 4, 5)
 
 
-def _project(e, i, v, order):
-    """Row i of L times v in the reference order (e a LazyEig, or a dict of L's entries)."""
-    if isinstance(e, dict):
-        return _sum_first([e[i, j] * v[j] for j in order if (i, j) in e])
-    return _sum_first([e.L(i, j) * v[j] for j in order if (i, j) in e.L_keys])
+def _project(L, i, v, order):
+    return _sum_first([L[i, j] * v[j] for j in order if (i, j) in L])
 
 
 def char_slopes(wl, wc, wr, bn, gamma, axis):
-    """The reference's limited slope of one cell (k_ppm_slopes), its eigensystem (lazy)
-    and the eigensystem's base words."""
+    """The reference's limited slope of one cell (k_ppm_slopes), its eigensystem and
+    the eigensystem's base words."""
     base = eig_base(wc, bn, gamma)
-    e = LazyEig(base, wc, axis)
+    lam, L, R = eig_from_base(base, wc, axis)
     order = _order(axis)
     dc = [wr[k] - wl[k] for k in range(7)]
     dl = [wc[k] - wl[k] for k in range(7)]
@@ -186,15 +151,15 @@ def char_slopes(wl, wc, wr, bn, gamma, axis):
     wt = [select(dl[k] * dr[k] > 0.0, (2.0 * dl[k] * dr[k]) / (dl[k] + dr[k]), 0.0) for k in range(7)]
     sc = []
     for i in range(7):
-        cc = _project(e, i, dc, order)
-        cl = _project(e, i, dl, order)
-        cr = _project(e, i, dr, order)
-        cw = _project(e, i, wt, order)
+        cc = _project(L, i, dc, order)
+        cl = _project(L, i, dl, order)
+        cr = _project(L, i, dr, order)
+        cw = _project(L, i, wt, order)
         lim1 = dmin(fabs(cl), fabs(cr))
         lim2 = dmin(0.5 * fabs(cc), fabs(cw))
         sc.append(select(cl * cr > 0.0, signed_mag(cc, dmin(2.0 * lim1, lim2)), 0.0))
-    s = [_sum_first([sc[j] * e.R(i, j) for j in range(7) if (i, j) in e.R_keys]) for i in range(7)]
-    return s, e, base
+    s = [_sum_first([sc[j] * R[i, j] for j in range(7) if (i, j) in R]) for i in range(7)]
+    return s, lam, L, R, base
 
 
 def plm_cell(ins, pars, axis):
@@ -205,8 +170,7 @@ def plm_cell(ins, pars, axis):
     """
     wl, wc, wr, bn = ins[0:7], ins[7:14], ins[14:21], ins[21]
     gamma, dtdx = pars
-    s, e, _ = char_slopes(wl, wc, wr, bn, gamma, axis)
-    lam = e.lam
+    s, lam, L, R, _ = char_slopes(wl, wc, wr, bn, gamma, axis)
     order = _order(axis)
     lia, ria = [], []
     for k in range(7):
@@ -223,16 +187,15 @@ def plm_cell(ins, pars, axis):
     c4 = -0.5 * dmin(lam[0], 0.0) * dtdx
     lia = [lia[k] + c4 * c1[k] for k in range(7)]
     ria = [ria[k] - c3 * c1[k] for k in range(7)]
-    # wave by wave, both sides (each edge value still takes its terms in wave order)
-    for i in range(7):
-        for side in (0, 1):
-            edge = lia if side == 0 else ria
+    for side in (0, 1):
+        edge = lia if side == 0 else ria
+        for i in range(7):
             active = (lam[i] <= 0.0) if side == 0 else (lam[i] >= 0.0)
             v3 = 0.5 * dtdx * lam[0 if side == 0 else 6] - 0.5 * dtdx * lam[i]
-            fac = _sum_first([e.L(i, j) * (v3 * c1[j]) for j in order if (i, j) in e.L_keys])
+            fac = _sum_first([L[i, j] * (v3 * c1[j]) for j in order if (i, j) in L])
             for j in range(7):
-                if (j, i) in e.R_keys:
-                    edge[j] = select(active, edge[j] + fac * e.R(j, i), edge[j])
+                if (j, i) in R:
+                    edge[j] = select(active, edge[j] + fac * R[j, i], edge[j])
     return lia + ria
 
 
@@ -243,7 +206,7 @@ def ppm_slope(ins, pars, axis):
     ins = wl(7) + wc(7) + wr(7) + bn ; pars = [gamma] -> s(7) + base(EIG_BASE)
     """
     wl, wc, wr, bn = ins[0:7], ins[7:14], ins[14:21], ins[21]
-    s, _, base = char_slopes(wl, wc, wr, bn, pars[0], axis)
+    s, _, _, _, base = char_slopes(wl, wc, wr, bn, pars[0], axis)
     return s + base
 
 
@@ -286,8 +249,7 @@ def ppm_trace(ins, pars, axis):
     wc, lia, ria = ins[0:7], list(ins[7:14]), list(ins[14:21])
     base = ins[21:21 + EIG_BASE]
     dtdx = pars[1]
-    e = LazyEig(base, wc, axis)
-    lam = e.lam
+    lam, L, R = eig_from_base(base, wc, axis)
     order = _order(axis)
     c1 = [ria[k] - lia[k] for k in range(7)]
     c2 = [6.0 * (wc[k] - 0.5 * (lia[k] + ria[k])) for k in range(7)]
@@ -295,23 +257,22 @@ def ppm_trace(ins, pars, axis):
     c4 = -0.5 * dmin(lam[0], 0.0) * dtdx
     lia = [lia[k] + c4 * (c1[k] + (1.0 - FOUR_THIRDS * c4) * c2[k]) for k in range(7)]
     ria = [ria[k] - c3 * (c1[k] - (1.0 - FOUR_THIRDS * c3) * c2[k]) for k in range(7)]
-    # wave by wave, both sides (each edge value still takes its terms in wave order)
-    for i in range(7):
-        for side in (0, 1):
-            edge = lia if side == 0 else ria
+    for side in (0, 1):
+        edge = lia if side == 0 else ria
+        for i in range(7):
             active = (lam[i] <= 0.0) if side == 0 else (lam[i] >= 0.0)
             v1 = 0.5 * dtdx * lam[0 if side == 0 else 6]
             v2 = 0.5 * dtdx * lam[i]
             v3 = v1 - v2
             v4 = FOUR_THIRDS * (v1 * v1 - v2 * v2)
             if side == 0:
-                terms = [e.L(i, j) * (v3 * (c1[j] + c2[j]) + v4 * c2[j]) for j in order if (i, j) in e.L_keys]
+                terms = [L[i, j] * (v3 * (c1[j] + c2[j]) + v4 * c2[j]) for j in order if (i, j) in L]
             else:
-                terms = [e.L(i, j) * (v3 * (c1[j] - c2[j]) + v4 * c2[j]) for j in order if (i, j) in e.L_keys]
+                terms = [L[i, j] * (v3 * (c1[j] - c2[j]) + v4 * c2[j]) for j in order if (i, j) in L]
             fac = _sum_first(terms)
             for j in range(7):
-                if (j, i) in e.R_keys:
-                    edge[j] = select(active, edge[j] + fac * e.R(j, i), edge[j])
+                if (j, i) in R:
+                    edge[j] = select(active, edge[j] + fac * R[j, i], edge[j])
     return lia + ria
 
 
