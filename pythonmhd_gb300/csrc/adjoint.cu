@@ -120,6 +120,8 @@ constexpr int kFirstOutput = kNumSlots - 4;
 struct Handle {
   Adj A{};
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;              // the second kernel of each x/y pair (Pair)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   size_t off[kNumSlots] = {};  // word offset of each array in an arena
   size_t ps[kNumSlots] = {};   // plane stride of each array
   size_t W = 0;                // words of one arena (all arrays of one cycle)
@@ -279,31 +281,45 @@ int unpack(Handle* h, const double* src, Arr& P, Arr& C, Arr& FX, Arr& FY, bool 
 }
 
 
+// the handle's streams and events as a Pair (x/y kernels of a stage side by side)
+Pair pair_of(Handle* h, cudaError_t* err) {
+  Pair p;
+  p.s = h->stream;
+  p.s2 = h->stream2;
+  p.fork = h->ev_fork;
+  p.join = h->ev_join;
+  p.err = err;
+  return p;
+}
+
 // forward sweep of one cycle from the input arrays (P, C, FX, FY) with A.dt set;
 // TAPE: the PLM and Roe stages also write the tapes their reverse sweeps read
 template <bool TAPE>
 int fwd_cycle_t(Handle* h) {
   Adj& A = h->A;
-  cudaStream_t s = h->stream;
   const int nx = A.nx, ny = A.ny;
-  launch_recon<false, TAPE>(A, s);
-  k_face<0, false><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
-  k_face<1, false><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
-  k_roe<0, 1, false, TAPE><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
-  k_roe<1, 1, false, TAPE><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  cudaError_t err = cudaSuccess;
+  const Pair pair = pair_of(h, &err);
+  cudaStream_t s = h->stream;
+  launch_recon<false, TAPE>(A, pair);
+  pair([&](cudaStream_t t) { k_face<0, false><<<g2(nx + 1, ny, 2), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_face<1, false><<<g2(nx, ny + 1, 2), kT, 0, t>>>(A); });
+  pair([&](cudaStream_t t) { k_roe<0, 1, false, TAPE><<<g1((size_t)(nx + 1) * ny), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_roe<1, 1, false, TAPE><<<g1((size_t)nx * (ny + 1)), kT, 0, t>>>(A); });
   k_ez<false><<<g2(nx, ny), kT, 0, s>>>(A);
   k_emf<1, false><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
-  k_fhalf<0, false, false><<<g2(nx + 1, ny), kT, 0, s>>>(A);
-  k_fhalf<1, false, false><<<g2(nx, ny + 1), kT, 0, s>>>(A);
-  k_ctu<0, false, TAPE><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
-  k_ctu<1, false, TAPE><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
+  pair([&](cudaStream_t t) { k_fhalf<0, false, false><<<g2(nx + 1, ny), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_fhalf<1, false, false><<<g2(nx, ny + 1), kT, 0, t>>>(A); });
+  pair([&](cudaStream_t t) { k_ctu<0, false, TAPE><<<g2(nx + 1, ny, 2), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_ctu<1, false, TAPE><<<g2(nx, ny + 1, 2), kT, 0, t>>>(A); });
   k_half<false><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_roe<0, 2, false, TAPE><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
-  k_roe<1, 2, false, TAPE><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
+  pair([&](cudaStream_t t) { k_roe<0, 2, false, TAPE><<<g1((size_t)(nx + 1) * ny), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_roe<1, 2, false, TAPE><<<g1((size_t)nx * (ny + 1)), kT, 0, t>>>(A); });
   k_emf<2, false><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
   k_final<false><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_fhalf<0, true, false><<<g2(nx + 1, ny), kT, 0, s>>>(A);
-  k_fhalf<1, true, false><<<g2(nx, ny + 1), kT, 0, s>>>(A);
+  pair([&](cudaStream_t t) { k_fhalf<0, true, false><<<g2(nx + 1, ny), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_fhalf<1, true, false><<<g2(nx, ny + 1), kT, 0, t>>>(A); });
+  CK(err);
   CK(cudaGetLastError());
   return MHD_OK;
 }
@@ -324,26 +340,29 @@ int rev_cycle(Handle* h) {
   Adj& A = h->A;
   cudaStream_t s = h->stream;
   const int nx = A.nx, ny = A.ny;
+  cudaError_t err = cudaSuccess;
+  const Pair pair = pair_of(h, &err);
   // zero every adjoint except the outputs' (they sit at the end of the arena)
   CK(cudaMemsetAsync(h->bars, 0, h->off[kFirstOutput] * sizeof(double), s));
-  k_fhalf<1, true, true><<<g2(nx, ny + 1), kT, 0, s>>>(A);
-  k_fhalf<0, true, true><<<g2(nx + 1, ny), kT, 0, s>>>(A);
+  pair([&](cudaStream_t t) { k_fhalf<1, true, true><<<g2(nx, ny + 1), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_fhalf<0, true, true><<<g2(nx + 1, ny), kT, 0, t>>>(A); });
   k_final<true><<<g2(nx, ny), kT, 0, s>>>(A);
   k_emf<2, true><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
-  k_roe<1, 2, true, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
-  k_roe<0, 2, true, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
+  pair([&](cudaStream_t t) { k_roe<1, 2, true, true><<<g1((size_t)nx * (ny + 1)), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_roe<0, 2, true, true><<<g1((size_t)(nx + 1) * ny), kT, 0, t>>>(A); });
   k_half<true><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_ctu<1, true, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
-  k_ctu<0, true, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
-  k_fhalf<1, false, true><<<g2(nx, ny + 1), kT, 0, s>>>(A);
-  k_fhalf<0, false, true><<<g2(nx + 1, ny), kT, 0, s>>>(A);
+  pair([&](cudaStream_t t) { k_ctu<1, true, true><<<g2(nx, ny + 1, 2), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_ctu<0, true, true><<<g2(nx + 1, ny, 2), kT, 0, t>>>(A); });
+  pair([&](cudaStream_t t) { k_fhalf<1, false, true><<<g2(nx, ny + 1), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_fhalf<0, false, true><<<g2(nx + 1, ny), kT, 0, t>>>(A); });
   k_emf<1, true><<<g2(nx + 1, ny + 1), kT, 0, s>>>(A);
   k_ez<true><<<g2(nx, ny), kT, 0, s>>>(A);
-  k_roe<1, 1, true, true><<<g1((size_t)nx * (ny + 1)), kT, 0, s>>>(A);
-  k_roe<0, 1, true, true><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);
-  k_face<1, true><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
-  k_face<0, true><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
-  launch_recon<true, true>(A, s);
+  pair([&](cudaStream_t t) { k_roe<1, 1, true, true><<<g1((size_t)nx * (ny + 1)), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_roe<0, 1, true, true><<<g1((size_t)(nx + 1) * ny), kT, 0, t>>>(A); });
+  pair([&](cudaStream_t t) { k_face<1, true><<<g2(nx, ny + 1, 2), kT, 0, t>>>(A); },
+       [&](cudaStream_t t) { k_face<0, true><<<g2(nx + 1, ny, 2), kT, 0, t>>>(A); });
+  launch_recon<true, true>(A, pair);
+  CK(err);
   CK(cudaGetLastError());
   return MHD_OK;
 }
@@ -623,6 +642,9 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
   h->bars_cap = e == cudaSuccess ? h->W : 0;
   if (e == cudaSuccess) e = cudaMalloc(&h->red, 4 * sizeof(double));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->red, 0, 4 * sizeof(double), h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) rc = fail(e);
@@ -633,6 +655,9 @@ int mhd2d_adj_create(int ny, int nx, double dx, double dy, int bcx, int bcy, dou
     cudaFree(h->red);
     cudaFree(h->vals);
     cudaFree(h->tapes);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->stream2) cudaStreamDestroy(h->stream2);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return rc;
@@ -654,6 +679,10 @@ void mhd2d_adj_destroy(void* handle) {
   cudaFree(h->seg);
   cudaFree(h->br);
   if (h->solver) mhd2d_destroy(h->solver);
+  if (h->stream2) cudaStreamSynchronize(h->stream2);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->stream2) cudaStreamDestroy(h->stream2);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }

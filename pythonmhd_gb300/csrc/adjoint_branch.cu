@@ -9,7 +9,9 @@ namespace mhdadj {
 template <int BR>
 cudaError_t launch_fwd_branch(const Adj& A, cudaStream_t s) {
   const int nx = A.nx, ny = A.ny;
-  launch_recon<false, false, BR>(A, s);
+  Pair serial;
+  serial.s = s;
+  launch_recon<false, false, BR>(A, serial);
   k_face<0, false, BR><<<g2(nx + 1, ny, 2), kT, 0, s>>>(A);
   k_face<1, false, BR><<<g2(nx, ny + 1, 2), kT, 0, s>>>(A);
   k_roe<0, 1, false, false, BR><<<g1((size_t)(nx + 1) * ny), kT, 0, s>>>(A);

@@ -281,37 +281,65 @@ __global__ void __launch_bounds__(kT, REV ? kRevMinBlocks : 1) k_trace(Adj A) {
   else MHD_ADJ_RUN(ppmt1, REV, TAPE, BR, in, out, par, tp, st, bt);
 }
 
+// The x and y kernels of a stage are independent: each writes its own outputs (or,
+// in the reverse sweep, reads its own outputs' adjoints and adds into its inputs'
+// with atomics).  A Pair runs the second on s2 beside the first and joins it back
+// into s, so one kernel's last partial wave overlaps the other; without s2 they run
+// one after the other on s.  The first failing stream call is kept in *err.
+struct Pair {
+  cudaStream_t s = nullptr, s2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaError_t* err = nullptr;
+  template <class F, class G>
+  void operator()(F first, G second) const {
+    if (!s2) {
+      first(s);
+      second(s);
+      return;
+    }
+    keep(cudaEventRecord(fork, s));
+    keep(cudaStreamWaitEvent(s2, fork, 0));
+    first(s);
+    second(s2);
+    keep(cudaEventRecord(join, s2));
+    keep(cudaStreamWaitEvent(s, join, 0));
+  }
+  void keep(cudaError_t e) const {
+    if (e != cudaSuccess && err && *err == cudaSuccess) *err = e;
+  }
+};
+
 // launch the reconstruction of both sweeps (PPM: slopes, interface values, tracing)
 template <bool REV, bool TAPE, int BR = 0>
-void launch_recon(const Adj& A, cudaStream_t s) {
+void launch_recon(const Adj& A, const Pair& pair) {
   const int nx = A.nx, ny = A.ny;
   const dim3 gc((unsigned)((nx + kT - 1) / kT), (unsigned)ny);
   const dim3 gsx((unsigned)((nx + 2 + kT - 1) / kT), (unsigned)ny);
   const dim3 gsy((unsigned)((nx + kT - 1) / kT), (unsigned)(ny + 2));
   switch (A.recon) {
     case 0:
-      k_recon<0, REV, TAPE, 0, BR><<<gc, kT, 0, s>>>(A);
-      k_recon<1, REV, TAPE, 0, BR><<<gc, kT, 0, s>>>(A);
+      pair([&](cudaStream_t s) { k_recon<0, REV, TAPE, 0, BR><<<gc, kT, 0, s>>>(A); },
+           [&](cudaStream_t s) { k_recon<1, REV, TAPE, 0, BR><<<gc, kT, 0, s>>>(A); });
       break;
     case 1:
-      k_recon<0, REV, TAPE, 1, BR><<<gc, kT, 0, s>>>(A);
-      k_recon<1, REV, TAPE, 1, BR><<<gc, kT, 0, s>>>(A);
+      pair([&](cudaStream_t s) { k_recon<0, REV, TAPE, 1, BR><<<gc, kT, 0, s>>>(A); },
+           [&](cudaStream_t s) { k_recon<1, REV, TAPE, 1, BR><<<gc, kT, 0, s>>>(A); });
       break;
     default:
       if constexpr (!REV) {
-        k_slope<0, false, TAPE, BR><<<gsx, kT, 0, s>>>(A);
-        k_slope<1, false, TAPE, BR><<<gsy, kT, 0, s>>>(A);
-        k_recon<0, false, TAPE, 2, BR><<<gc, kT, 0, s>>>(A);
-        k_recon<1, false, TAPE, 2, BR><<<gc, kT, 0, s>>>(A);
-        k_trace<0, false, TAPE, BR><<<gc, kT, 0, s>>>(A);
-        k_trace<1, false, TAPE, BR><<<gc, kT, 0, s>>>(A);
+        pair([&](cudaStream_t s) { k_slope<0, false, TAPE, BR><<<gsx, kT, 0, s>>>(A); },
+             [&](cudaStream_t s) { k_slope<1, false, TAPE, BR><<<gsy, kT, 0, s>>>(A); });
+        pair([&](cudaStream_t s) { k_recon<0, false, TAPE, 2, BR><<<gc, kT, 0, s>>>(A); },
+             [&](cudaStream_t s) { k_recon<1, false, TAPE, 2, BR><<<gc, kT, 0, s>>>(A); });
+        pair([&](cudaStream_t s) { k_trace<0, false, TAPE, BR><<<gc, kT, 0, s>>>(A); },
+             [&](cudaStream_t s) { k_trace<1, false, TAPE, BR><<<gc, kT, 0, s>>>(A); });
       } else {
-        k_trace<1, true, TAPE><<<gc, kT, 0, s>>>(A);
-        k_trace<0, true, TAPE><<<gc, kT, 0, s>>>(A);
-        k_recon<1, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
-        k_recon<0, true, TAPE, 2><<<gc, kT, 0, s>>>(A);
-        k_slope<1, true, TAPE><<<gsy, kT, 0, s>>>(A);
-        k_slope<0, true, TAPE><<<gsx, kT, 0, s>>>(A);
+        pair([&](cudaStream_t s) { k_trace<1, true, TAPE><<<gc, kT, 0, s>>>(A); },
+             [&](cudaStream_t s) { k_trace<0, true, TAPE><<<gc, kT, 0, s>>>(A); });
+        pair([&](cudaStream_t s) { k_recon<1, true, TAPE, 2><<<gc, kT, 0, s>>>(A); },
+             [&](cudaStream_t s) { k_recon<0, true, TAPE, 2><<<gc, kT, 0, s>>>(A); });
+        pair([&](cudaStream_t s) { k_slope<1, true, TAPE><<<gsy, kT, 0, s>>>(A); },
+             [&](cudaStream_t s) { k_slope<0, true, TAPE><<<gsx, kT, 0, s>>>(A); });
       }
   }
 }
