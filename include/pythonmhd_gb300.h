@@ -348,6 +348,13 @@ int mhd2d_adj_quotient(const double* b, const double* v, double* q, long long n)
  * (Markstein's remainder correction), correctly rounded, so equal bit for bit to
  * the IEEE division.  Exposed so that the equality can be tested. */
 int mhd_quotient6(const double* x, double* q, long long n);
+/* out[i] = x[i] op y[i] (op 0 add, 1 subtract, 2 multiply, 3 divide) or sqrt(x[i])
+ * (op 4; y unused) as the step kernels compute them on the integer pipes (n
+ * elements, device pointers; blocks until done).  Each equals the IEEE-754
+ * operation rounded to nearest even bit for bit; exposed so that can be tested.
+ * No counterpart in the reference: it tests arithmetic the reference leaves to
+ * NumPy. */
+int mhd_softfp(int op, const double* x, const double* y, double* out, long long n);
 /* Install a forward record made elsewhere (e.g. by the batched step): `steps`
  * cycles with the host dts `dt`, and the packed device states at cycles 0,
  * every, 2*every, ... in `checkpoints` (ceil(steps/every) states, one after the

@@ -113,6 +113,7 @@ SIGNATURES = {
     "mhd2d_adj_destroy": (None, [ctypes.c_void_p]),
     "mhd2d_adj_quotient": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]),
     "mhd_quotient6": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]),
+    "mhd_softfp": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]),
     "mhd3d_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),

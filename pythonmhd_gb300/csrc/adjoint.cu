@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_cfl(Adj A) {
   const double* c = A.C.v;
   double mx = 0.0, my = 0.0;
   for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
-    const double inv_d = 1.0 / c[idx];
+    const double inv_d = mhdk::ddiv(1.0, c[idx]);
     const double vx = M(c[plane + idx], inv_d);
     const double vy = M(c[2 * plane + idx], inv_d);
     const double vz = M(c[3 * plane + idx], inv_d);
@@ -64,10 +64,10 @@ __global__ void __launch_bounds__(256) k_cfl(Adj A) {
     const double ssum = Ad(bd, a2);
     const double sdiff = Sb(bd, a2);
     const double dd = M(sdiff, sdiff);
-    const double cfx2 = M(0.5, Ad(ssum, __dsqrt_rn(Ad(dd, M(M(M(4.0, a2), Ad(M(by, by), M(bz, bz))), inv_d)))));
-    const double cfy2 = M(0.5, Ad(ssum, __dsqrt_rn(Ad(dd, M(M(M(4.0, a2), Ad(M(bx, bx), M(bz, bz))), inv_d)))));
-    mx = dmax2(mx, Ad(fabs(vx), __dsqrt_rn(cfx2)));
-    my = dmax2(my, Ad(fabs(vy), __dsqrt_rn(cfy2)));
+    const double cfx2 = M(0.5, Ad(ssum, mhdk::sqrt(Ad(dd, M(M(M(4.0, a2), Ad(M(by, by), M(bz, bz))), inv_d)))));
+    const double cfy2 = M(0.5, Ad(ssum, mhdk::sqrt(Ad(dd, M(M(M(4.0, a2), Ad(M(bx, bx), M(bz, bz))), inv_d)))));
+    mx = dmax2(mx, Ad(fabs(vx), mhdk::sqrt(cfx2)));
+    my = dmax2(my, Ad(fabs(vy), mhdk::sqrt(cfy2)));
   }
   for (int o = 16; o > 0; o >>= 1) {
     mx = dmax2(mx, __shfl_xor_sync(0xffffffffu, mx, o));

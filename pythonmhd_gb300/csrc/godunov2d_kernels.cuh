@@ -214,7 +214,7 @@ __device__ __forceinline__ void limited_slopes(const double* wl, const double* w
     dc[k] = wr[k] - wl[k];
     dl[k] = wc[k] - wl[k];
     dr[k] = wr[k] - wc[k];
-    wt[k] = is_pos(dl[k] * dr[k]) ? (2.0 * dl[k] * dr[k]) / (dl[k] + dr[k]) : 0.0;
+    wt[k] = is_pos(dl[k] * dr[k]) ? ddiv(2.0 * dl[k] * dr[k], dl[k] + dr[k]) : 0.0;
   }
   double sc[NV];
 #pragma unroll
@@ -922,8 +922,8 @@ __device__ __forceinline__ void b_half_ez(const Grid& G, const StateBuf& in, int
   }
   const double hbx = (G.nfbx[xlf] + G.nfbx[xr]) * 0.5;   // x / 2 exactly
   const double hby = (G.nfby[yt] + G.nfby[yb]) * 0.5;
-  const double hvx = hu[1] / hu[0];
-  const double hvy = hu[2] / hu[0];
+  const double hvx = ddiv(hu[1], hu[0]);
+  const double hvy = ddiv(hu[2], hu[0]);
   G.hez[idx] = hvy * hbx - hvx * hby;
 }
 
@@ -1064,7 +1064,7 @@ __device__ __forceinline__ void b_dt_cell(const Grid& G, const StateBuf& in, siz
     MHD_GUARD(G, in.fbx, (size_t)(idx / nx) * (nx + 1) + idx % nx);
     MHD_GUARD(G, in.fby, idx);
   }
-  const double inv_d = 1.0 / c[idx];
+  const double inv_d = ddiv(1.0, c[idx]);
   const double vx = c[plane + idx] * inv_d;
   const double vy = c[2 * plane + idx] * inv_d;
   const double vz = c[3 * plane + idx] * inv_d;
@@ -1132,11 +1132,11 @@ __device__ __forceinline__ void b_begin(const Grid& G) {
     if (is_pos(L->dt_fixed)) {
       dt = L->dt_fixed;
     } else if (PHYS == MHD) {
-      const double inv = dmax(mx / G.dx, my / G.dy);
-      dt = L->cfl / inv;
+      const double inv = dmax(ddiv(mx, G.dx), ddiv(my, G.dy));
+      dt = ddiv(L->cfl, inv);
     } else {
-      const double dtx = L->cfl / (mx / G.dx);
-      const double dty = L->cfl / (my / G.dy);
+      const double dtx = ddiv(L->cfl, ddiv(mx, G.dx));
+      const double dty = ddiv(L->cfl, ddiv(my, G.dy));
       dt = dmin(dtx, dty);
     }
     if (L->t + dt > L->t_end) dt = L->t_end - L->t;
@@ -1235,7 +1235,7 @@ __device__ __forceinline__ void b_dt_cell_1d(const Grid& G, const StateBuf& in, 
   const double gamma = G.gamma;
   const double* c = in.cons;
   MHD_GUARD(G, c, i);
-  const double inv_d = 1.0 / c[i];
+  const double inv_d = ddiv(1.0, c[i]);
   const double vx = c[plane + i] * inv_d;
   const double vy = c[2 * plane + i] * inv_d;
   const double vz = c[3 * plane + i] * inv_d;

@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(256) k3_dt_reduce_hydro(Grid3 G, StateBuf3 in)
   const double* c = in.cons;
   double m[3] = {0.0, 0.0, 0.0};
   for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
-    const double inv_d = 1.0 / c[idx];
+    const double inv_d = ddiv(1.0, c[idx]);
     const double vx = c[n + idx] * inv_d;
     const double vy = c[2 * n + idx] * inv_d;
     const double vz = c[3 * n + idx] * inv_d;
@@ -302,9 +302,9 @@ __global__ void k3_begin_hydro(Grid3 G) {
     const double mx = __longlong_as_double((long long)L->max_sx);
     const double my = __longlong_as_double((long long)L->max_sy);
     const double mz = __longlong_as_double((long long)L->max_sz);
-    const double dtx = L->cfl / (mx / G.d[0]);
-    const double dty = L->cfl / (my / G.d[1]);
-    const double dtz = L->cfl / (mz / G.d[2]);
+    const double dtx = ddiv(L->cfl, ddiv(mx, G.d[0]));
+    const double dty = ddiv(L->cfl, ddiv(my, G.d[1]));
+    const double dtz = ddiv(L->cfl, ddiv(mz, G.d[2]));
     double dt = dmin(dtx, dmin(dty, dtz));
     if (L->t + dt > L->t_end) dt = L->t_end - L->t;
     L->dt = dt;

@@ -29,12 +29,12 @@ __device__ __forceinline__ void p2c_frame(const double w[7], double bn, double g
   u[3] = w[0] * w[3];
   u[4] = w[4];
   u[5] = w[5];
-  u[6] = w[6] / (gamma - 1.0) + 0.5 * w[0] * (w[N] * w[N] + w[T1] * w[T1] + w[T2] * w[T2]);
+  u[6] = ddiv(w[6], gamma - 1.0) + 0.5 * w[0] * (w[N] * w[N] + w[T1] * w[T1] + w[T2] * w[T2]);
   u[6] = u[6] + 0.5 * (bn * bn + w[4] * w[4] + w[5] * w[5]);
 }
 template <int N, int T1, int T2>
 __device__ __forceinline__ void c2p_frame(const double u[7], double bn, double gamma, double w[7]) {
-  const double inv_d = 1.0 / u[0];
+  const double inv_d = ddiv(1.0, u[0]);
   w[0] = u[0];
   w[1] = u[1] * inv_d;
   w[2] = u[2] * inv_d;
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(256) k3m_dt_reduce(Grid3 G, StateBuf3 in) {
   for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
     int p[3];
     unlin3<0, 0>(G, (unsigned)idx, p);
-    const double inv_d = 1.0 / c[idx];
+    const double inv_d = ddiv(1.0, c[idx]);
     const double vx = c[n + idx] * inv_d;
     const double vy = c[2 * n + idx] * inv_d;
     const double vz = c[3 * n + idx] * inv_d;
@@ -118,8 +118,8 @@ __global__ void k3m_begin(Grid3 G) {
     const double mx = __longlong_as_double((long long)L->max_sx);
     const double my = __longlong_as_double((long long)L->max_sy);
     const double mz = __longlong_as_double((long long)L->max_sz);
-    const double inv = dmax(mx / G.d[0], dmax(my / G.d[1], mz / G.d[2]));
-    double dt = L->cfl / inv;
+    const double inv = dmax(ddiv(mx, G.d[0]), dmax(ddiv(my, G.d[1]), ddiv(mz, G.d[2])));
+    double dt = ddiv(L->cfl, inv);
     if (L->t_end - L->t < dt) dt = L->t_end - L->t;
     L->dt = dt;
   }
@@ -151,7 +151,7 @@ template <int A>
 __device__ __forceinline__ double own_change(const Grid3& G, const double* fb, const int* p, double h, bool divide) {
   const size_t lo = face3<A>(G, p);
   const double d = fb[lo + stride3<A, 1, A>(G)] - fb[lo];
-  return divide ? d / h : d * h;
+  return divide ? ddiv(d, h) : d * h;
 }
 
 // normal change of face B of direction D at the sweep-extended cell e (-1..L) of the
@@ -171,7 +171,7 @@ __device__ __forceinline__ double normal_change(const Grid3& G, const double* fb
   q[D] = hi;
   const double b_hi = fb[face3<D>(G, q)];
   const double d = b_hi - b_lo;
-  return divide ? d / h : d * h;
+  return divide ? ddiv(d, h) : d * h;
 }
 
 __device__ __forceinline__ double own_change_dyn(const Grid3& G, const double* const* fb, int a, const int* p,
@@ -197,7 +197,7 @@ __device__ __forceinline__ void b3_corr(const Grid3& G, const StateBuf3& in, con
   for (int s = 0; s < 2; ++s) {
     const int a = (s == 0 ? S::T1 : S::T2) - 1;
     const double tch = own_change_dyn(G, in.fb, a, q, 1.0 / G.d[a], false);
-    const double v = __ldg(in.cons + (size_t)(1 + a) * plane + cell) / dens;
+    const double v = ddiv(__ldg(in.cons + (size_t)(1 + a) * plane + cell), dens);
     const double term = b3_limit(nch, tch, D == 1 && s == 0);
     out[s] = 0.5 * dt * (v * term);
   }
@@ -316,9 +316,9 @@ __global__ void __launch_bounds__(kBlock) k3m_cell_e(Grid3 G, StateBuf3 in) {
   const double* p = in.prim;
   const double* c = in.cons;
   const double d = c[i];
-  G.ce[0][i] = (p[5 * n + i] * c[3 * n + i] - p[6 * n + i] * c[2 * n + i]) / d;
-  G.ce[1][i] = (p[6 * n + i] * c[n + i] - p[4 * n + i] * c[3 * n + i]) / d;
-  G.ce[2][i] = (p[4 * n + i] * c[2 * n + i] - p[5 * n + i] * c[n + i]) / d;
+  G.ce[0][i] = ddiv(p[5 * n + i] * c[3 * n + i] - p[6 * n + i] * c[2 * n + i], d);
+  G.ce[1][i] = ddiv(p[6 * n + i] * c[n + i] - p[4 * n + i] * c[3 * n + i], d);
+  G.ce[2][i] = ddiv(p[4 * n + i] * c[2 * n + i] - p[5 * n + i] * c[n + i], d);
 }
 
 // ----------------------------------------------------------------------------
@@ -566,9 +566,9 @@ __global__ void __launch_bounds__(kBlock) k3m_half_e(Grid3 G, StateBuf3 in) {
     h[k] = v;
   }
   const double bx = favg3<0>(G, G.nfb[0], p), by = favg3<1>(G, G.nfb[1], p), bz = favg3<2>(G, G.nfb[2], p);
-  G.ce[0][i] = (by * h[3] - bz * h[2]) / h[0];
-  G.ce[1][i] = (bz * h[1] - bx * h[3]) / h[0];
-  G.ce[2][i] = (bx * h[2] - by * h[1]) / h[0];
+  G.ce[0][i] = ddiv(by * h[3] - bz * h[2], h[0]);
+  G.ce[1][i] = ddiv(bz * h[1] - bx * h[3], h[0]);
+  G.ce[2][i] = ddiv(bx * h[2] - by * h[1], h[0]);
 }
 
 // ----------------------------------------------------------------------------

@@ -16,12 +16,24 @@
 #pragma once
 #include <cstdint>
 
+#include "softfp.cuh"
+
 namespace mhdk {
 
 constexpr double SMALL_VALUE = 0.000000000001;   // Source/PythonMHD_Constants.py:7
 constexpr double FOUR_THIRDS = 1.333333333333333;  // Source/PythonMHD_Constants.py:8 (truncated)
 
 __device__ __forceinline__ double sq(double x) { return x * x; }
+
+// ---------------------------------------------------------------------------
+// Division and square root, correctly rounded.  As FP64 instructions each costs
+// about ten FP64-pipe slots, and that pipe bounds every kernel of the step; these
+// compute the same bits by integer Newton-Raphson with an exact remainder check
+// (softfp.cuh), on the integer pipes.  The unqualified sqrt() of every kernel in
+// this namespace resolves here.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ double ddiv(double a, double b) { return sfp::div(a, b); }
+__host__ __device__ __forceinline__ double sqrt(double x) { return sfp::sqrt(x); }
 
 // ---------------------------------------------------------------------------
 // Operations the compiler never fuses into a multiply-add.  The fast build lets
@@ -218,7 +230,7 @@ __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, d
   const double bt2 = nadd(nsq(w[4]), nsq(w[5]));
   const double bt = sqrt(bt2);
   const double gp = gamma * w[6];
-  const double inv_d = 1.0 / w[0];
+  const double inv_d = ddiv(1.0, w[0]);
   const double sqrt_d = sqrt(w[0]);
   const double red_bt2 = bt2 * inv_d;
   const double a2 = gp * inv_d;
@@ -230,12 +242,12 @@ __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, d
   const double ssqrt = sqrt(nadd(nsq(sdiff), nmul(4.0 * a2, red_bt2)));
   const double cf2 = 0.5 * (ssum + ssqrt);
   const double cf = sqrt(cf2);
-  const double cs2 = a2 * ca2 / cf2;
+  const double cs2 = ddiv(a2 * ca2, cf2);
   const double cs = sqrt(cs2);
 
   double b1 = 0.0, b2 = 0.0;
   if (is_zero(bt)) b1 = 1.0;
-  if (is_pos(bt)) { b1 = w[4] / bt; b2 = w[5] / bt; }
+  if (is_pos(bt)) { b1 = ddiv(w[4], bt); b2 = ddiv(w[5], bt); }
 
   double fa = 0.0, sa = 0.0;
   if (is_zero(ssqrt)) {
@@ -245,8 +257,8 @@ __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, d
   } else if (is_nonpos(cf2 - a2)) {
     fa = 1.0;
   } else {
-    fa = sqrt((a2 - cs2) / ssqrt);
-    sa = sqrt((cf2 - a2) / ssqrt);
+    fa = sqrt(ddiv(a2 - cs2, ssqrt));
+    sa = sqrt(ddiv(cf2 - a2, ssqrt));
   }
   const double sgn = sign_one(bn);
   const double qf = cf * fa * sgn;
@@ -277,7 +289,7 @@ __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, d
   e.r51 = b1 * sgn * sqrt_d;
   e.r52 = -af * b2;
 
-  const double nf = 0.5 / a2;
+  const double nf = ddiv(0.5, a2);
   const double qf_n = nf * qf;
   const double qs_n = nf * qs;
   const double afp = nf * af * inv_d;
@@ -290,15 +302,15 @@ __device__ __forceinline__ void prim_eigensystem(const double w[7], double bn, d
   e.l05 = asp * b2;
   e.l1t1 = -0.5 * b2;
   e.l1t2 = 0.5 * b1;
-  e.l14 = -0.5 * b2 * sgn / sqrt_d;
-  e.l15 = 0.5 * b1 * sgn / sqrt_d;
+  e.l14 = ddiv(-0.5 * b2 * sgn, sqrt_d);
+  e.l15 = ddiv(0.5 * b1 * sgn, sqrt_d);
   e.l2n = -nf * cs * sa;
   e.l2t1 = -qf_n * b1;
   e.l2t2 = -qf_n * b2;
   e.l26 = nf * sa * inv_d;
   e.l24 = -afp * b1;
   e.l25 = -afp * b2;
-  e.l36 = -1.0 / a2;
+  e.l36 = ddiv(-1.0, a2);
 }
 
 // Row i of L times v, accumulated in the reference order (0, N, T1, T2, 6, 4, 5).
@@ -329,13 +341,13 @@ __device__ __forceinline__ void prim_to_cons7(const double w[7], double bn, doub
   u[3] = w[0] * w[3];
   u[4] = w[4];
   u[5] = w[5];
-  double e = w[6] / (gamma - 1.0) + 0.5 * w[0] * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+  double e = ddiv(w[6], gamma - 1.0) + 0.5 * w[0] * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
   e = e + 0.5 * (bn * bn + w[4] * w[4] + w[5] * w[5]);
   u[6] = e;
 }
 
 __device__ __forceinline__ void cons_to_prim7(const double u[7], double bn, double gamma, double w[7]) {
-  const double inv_d = 1.0 / u[0];
+  const double inv_d = ddiv(1.0, u[0]);
   w[0] = u[0];
   w[1] = u[1] * inv_d;
   w[2] = u[2] * inv_d;
@@ -372,7 +384,7 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
                                          double eps, double flux[7]) {
   const double sl = sqrt(wl[0]);
   const double sr = sqrt(wr[0]);
-  const double isum = 1.0 / (sl + sr);
+  const double isum = ddiv(1.0, sl + sr);
   const double rd = sl * sr;
   double v[4];
 #pragma unroll
@@ -382,11 +394,11 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   const double b2 = nadd(nmul(sr, wl[5]), nmul(sl, wr[5])) * isum;
   const double hbl = 0.5 * nadd(nadd(nsq(bn), nsq(wl[4])), nsq(wl[5]));
   const double hbr = 0.5 * nadd(nadd(nsq(bn), nsq(wr[4])), nsq(wr[5]));
-  const double H = ((ul[6] + wl[6] + hbl) / sl + (ur[6] + wr[6] + hbr) / sr) * isum;
+  const double H = (ddiv(ul[6] + wl[6] + hbl, sl) + ddiv(ur[6] + wr[6] + hbr, sr)) * isum;
 
-  const double ird = 1.0 / rd;
-  const double btc = 0.5 * nadd(nsq(wl[4] - wr[4]), nsq(wl[5] - wr[5])) / sq(sl + sr);
-  const double rc = 0.5 * (wl[0] + wr[0]) / rd;
+  const double ird = ddiv(1.0, rd);
+  const double btc = ddiv(0.5 * nadd(nsq(wl[4] - wr[4]), nsq(wl[5] - wr[5])), sq(sl + sr));
+  const double rc = ddiv(0.5 * (wl[0] + wr[0]), rd);
   const double bt2 = nadd(nsq(b1), nsq(b2));
   const double bt = sqrt(bt2);
   const double bts2 = nsub(gamma - 1.0, nmul(gamma - 2.0, rc)) * bt2;
@@ -402,7 +414,7 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   const double ssqrt = sqrt(nadd(nsq(sdiff), nmul(4.0 * a2, rbts2)));
   const double cf2 = 0.5 * (ssum + ssqrt);
   const double cf = sqrt(cf2);
-  const double cs2 = a2 * ca2 / cf2;
+  const double cs2 = ddiv(a2 * ca2, cf2);
   const double cs = sqrt(cs2);
 
   const double vn = v[N];
@@ -412,7 +424,7 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
     for (int k = 0; k < 7; ++k) {
       const double x = lam[k];
       if (dlt(fabs(x), 2.0 * eps) && !is_zero(x)) {
-        const double corr = eps + sq(x) / (4.0 * eps);
+        const double corr = eps + ddiv(sq(x), 4.0 * eps);
         lam[k] = is_pos(x) ? x + corr : x - corr;
       }
     }
@@ -426,12 +438,12 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   } else if (is_nonpos(cf2 - a2)) {
     fa = 1.0;
   } else {
-    fa = sqrt((a2 - cs2) / (cf2 - cs2));
-    sa = sqrt((cf2 - a2) / (cf2 - cs2));
+    fa = sqrt(ddiv(a2 - cs2, cf2 - cs2));
+    sa = sqrt(ddiv(cf2 - a2, cf2 - cs2));
   }
   const double sgn = sign_one(bn);
   const double srd = sqrt(rd);
-  const double isrd = 1.0 / srd;
+  const double isrd = ddiv(1.0, srd);
   const double qf = cf * fa * sgn;
   const double qs = cs * sa * sgn;
   const double afp = a * fa * isrd;
@@ -439,10 +451,10 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
 
   double bh1 = 0.0, bh2 = 0.0;
   if (is_zero(bt)) bh1 = 1.0;
-  if (is_pos(bt)) { bh1 = b1 / bt; bh2 = b2 / bt; }
+  if (is_pos(bt)) { bh1 = ddiv(b1, bt); bh2 = ddiv(b2, bt); }
   const double den = sqrt(nsub(gamma - 1.0, nmul(gamma - 2.0, rc)));
-  const double b1s = bh1 / den;
-  const double b2s = bh2 / den;
+  const double b1s = ddiv(bh1, den);
+  const double b2s = ddiv(bh2, den);
   const double vb = v[T1] * b1s + v[T2] * b2s;
   const double bs2 = b1s * b1s + b2s * b2s;
   const double afb = afp * bts * bs2;
@@ -463,7 +475,7 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   }
   // L, the wave amplitudes, then R: each matrix is formed where it is used, after
   // the supersonic exits (the same expressions, so the same roundings)
-  double nf = 0.5 / a2;
+  double nf = ddiv(0.5, a2);
   const double cff = nf * fa * cf;
   const double css = nf * sa * cs;
   const double qfn = qf * nf;
@@ -475,8 +487,8 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   nf = nf * (gamma - 1.0);
   const double fan = fa * nf;
   const double san = sa * nf;
-  const double b1c = b1s / bs2;
-  const double b2c = b2s / bs2;
+  const double b1c = ddiv(b1s, bs2);
+  const double b2c = ddiv(b2s, bs2);
   const double vbs = v[T1] * b1c + v[T2] * b2c;
   nf = nf * 2.0;
 
@@ -500,7 +512,7 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   L[2][6] = san;
   L[2][4] = -af_ * b1c - san * b1;
   L[2][5] = -af_ * b2c - san * b2;
-  L[3][0] = 1.0 - nf * (0.5 * vsq - (gamma - 2.0) * btc / (gamma - 1.0));
+  L[3][0] = 1.0 - nf * (0.5 * vsq - ddiv((gamma - 2.0) * btc, gamma - 1.0));
   L[3][1] = nf * v[1];
   L[3][2] = nf * v[2];
   L[3][3] = nf * v[3];
@@ -563,7 +575,7 @@ __device__ __forceinline__ void roe_flux(const double wl[7], const double wr[7],
   R[6][0] = fa * (hmb - vn * cf) + qs * vb + asb;
   R[6][1] = -(v[T1] * bh2 - v[T2] * bh1);
   R[6][2] = sa * (hmb - vn * cs) - qf * vb - afb;
-  R[6][3] = 0.5 * vsq + (gamma - 2.0) * btc / (gamma - 1.0);
+  R[6][3] = 0.5 * vsq + ddiv((gamma - 2.0) * btc, gamma - 1.0);
   R[6][4] = sa * (hmb + vn * cs) + qf * vb - afb;
   R[6][5] = -R[6][1];
   R[6][6] = fa * (hmb + vn * cf) - qs * vb + asb;
@@ -600,13 +612,13 @@ __device__ __forceinline__ void hprim_to_cons(const double w[5], double gamma, d
   u[2] = w[0] * w[2];
   u[3] = w[0] * w[3];
   const double ke = hkin<A>(w[1], w[2], w[3]);
-  u[4] = (w[4] / (gamma - 1.0)) + 0.5 * w[0] * ke;
+  u[4] = ddiv(w[4], gamma - 1.0) + 0.5 * w[0] * ke;
 }
 
 template <int A>
 __device__ __forceinline__ void hcons_to_prim(const double u[5], double gamma, double w[5]) {
   w[0] = u[0];
-  const double inv_d = 1.0 / w[0];
+  const double inv_d = ddiv(1.0, w[0]);
   w[1] = u[1] * inv_d;
   w[2] = u[2] * inv_d;
   w[3] = u[3] * inv_d;
@@ -656,15 +668,15 @@ template <int A>
 __device__ __forceinline__ void hprim_eigensystem(const double w[5], double gamma, HPrimEig& e) {
   const int n = A + 1;
   const double gp = gamma * w[4];
-  const double a2 = gp / w[0];
+  const double a2 = ddiv(gp, w[0]);
   const double a = sqrt(a2);
   const double vn = w[n];
   e.lam[0] = vn - a; e.lam[1] = vn; e.lam[2] = vn; e.lam[3] = vn; e.lam[4] = vn + a;
-  e.rn0 = -a / w[0];
+  e.rn0 = ddiv(-a, w[0]);
   e.a2 = a2;
-  e.l0n = -0.5 * w[0] / a;
-  e.l04 = 0.5 / a2;
-  e.le4 = -1.0 / a2;
+  e.l0n = ddiv(-0.5 * w[0], a);
+  e.l04 = ddiv(0.5, a2);
+  e.le4 = ddiv(-1.0, a2);
 }
 template <int A>
 __device__ __forceinline__ double hprim_project(const HPrimEig& e, int i, const double v[5]) {
@@ -693,14 +705,14 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
   hprim_to_cons<A>(wr, gamma, ur);
   const double sl = sqrt(wl[0]);
   const double sr = sqrt(wr[0]);
-  const double isum = 1.0 / (sl + sr);
+  const double isum = ddiv(1.0, sl + sr);
   double v[4];
 #pragma unroll
   for (int k = 1; k <= 3; ++k) v[k] = (sl * wl[k] + sr * wr[k]) * isum;
   const double vsq = A == 2 ? (v[3] * v[3] + v[1] * v[1] + v[2] * v[2])
                    : A == 1 ? (v[2] * v[2] + v[3] * v[3] + v[1] * v[1])
                             : (v[1] * v[1] + v[2] * v[2] + v[3] * v[3]);
-  const double H = ((ul[4] + wl[4]) / sl + (ur[4] + wr[4]) / sr) * isum;
+  const double H = (ddiv(ul[4] + wl[4], sl) + ddiv(ur[4] + wr[4], sr)) * isum;
   const double a2 = (gamma - 1.0) * dmax(H - 0.5 * vsq, SMALL_VALUE);
   const double a = sqrt(a2);
   const double vn = v[n];
@@ -710,7 +722,7 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
     for (int k = 0; k < 5; ++k) {
       const double x = lam[k];
       if (dlt(fabs(x), 2.0 * eps) && !is_zero(x)) {
-        const double corr = eps + sq(x) / (4.0 * eps);
+        const double corr = eps + ddiv(sq(x), 4.0 * eps);
         lam[k] = is_pos(x) ? x + corr : x - corr;
       }
     }
@@ -732,9 +744,9 @@ __device__ __forceinline__ void hroe_flux(const double wl[5], const double wr[5]
     for (int i = 0; i < 5; ++i) flux[i] = fl[i];
     return;
   }
-  const double nf = 0.5 / a2;
+  const double nf = ddiv(0.5, a2);
   const double g1 = gamma - 1.0;
-  const double gn = g1 / a2;
+  const double gn = ddiv(g1, a2);
   double du[5];
 #pragma unroll
   for (int i = 0; i < 5; ++i) du[i] = ur[i] - ul[i];

@@ -68,6 +68,29 @@ __global__ void k_quotient6(const double* __restrict__ x, double* __restrict__ q
 }
 }  // namespace
 
+// The integer-pipe add, subtract, multiply, divide and square root (softfp.cuh),
+// elementwise, so that they can be compared bit for bit with the IEEE operations.
+namespace {
+__global__ void k_softfp(int op, const double* __restrict__ x, const double* __restrict__ y,
+                         double* __restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double a = x[i];
+    const double b = op == 4 ? 0.0 : y[i];
+    out[i] = op == 0 ? sfp::add(a, b) : op == 1 ? sfp::sub(a, b) : op == 2 ? sfp::mul(a, b)
+           : op == 3 ? sfp::div(a, b) : sfp::sqrt(a);
+  }
+}
+}  // namespace
+
+extern "C" int mhd_softfp(int op, const double* x, const double* y, double* out, long long n) {
+  if (op < 0 || op > 4 || n < 0 || (n > 0 && (!x || !out || (op != 4 && !y)))) return MHD_ERR_ARG;
+  if (n == 0) return MHD_OK;
+  const long long blocks = (n + 255) / 256 < 152LL * 16 ? (n + 255) / 256 : 152LL * 16;
+  k_softfp<<<(unsigned)blocks, 256>>>(op, x, y, out, n);
+  if (cudaGetLastError() != cudaSuccess) return MHD_ERR_CUDA;
+  return cudaDeviceSynchronize() == cudaSuccess ? MHD_OK : MHD_ERR_CUDA;
+}
+
 extern "C" int mhd_quotient6(const double* x, double* q, long long n) {
   if (n < 0 || (n > 0 && (!x || !q))) return MHD_ERR_ARG;
   if (n == 0) return MHD_OK;
