@@ -222,7 +222,7 @@ def _reverse_needs(t, act):
 # emitters
 # ----------------------------------------------------------------------------
 _PY_BIN = {"add": "+", "sub": "-", "mul": "*", "div": "/"}
-_C_RN = {"add": "__dadd_rn", "sub": "__dsub_rn", "mul": "__dmul_rn", "div": "mhdk::ddiv"}
+_C_RN = {"add": "__dadd_rn", "sub": "__dsub_rn", "mul": "__dmul_rn", "div": "DSL_FDIV"}
 _CMP = {"gt": ">", "ge": ">=", "lt": "<", "le": "<=", "eq": "=="}
 # CUDA comparisons on the IEEE bit pattern (``dsl_*`` in the emitted preamble): an FP64
 # compare issues on the FP64 pipe at the DFMA rate, the pattern test on the integer pipe;
@@ -231,6 +231,7 @@ _C_CMP = {op: f"dsl_{op}" for op in _CMP}
 _C_PREAMBLE = (
     "#ifndef MHD_DSL_NZ\n#define MHD_DSL_NZ\n"
     "#include \"mhd_math.cuh\"\n"
+
     "__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }\n"
     "__device__ __forceinline__ long long dsl_key(double x) {\n"
     "  const long long b = __double_as_longlong(x);\n"
@@ -295,7 +296,7 @@ def _fwd_lines(t, live, lang):
         elif op == "neg":
             L.append((v, f"-{a[0]}", kind))
         elif op == "sqrt":
-            L.append((v, f"np.sqrt({a[0]})" if lang == "py" else f"mhdk::sqrt({a[0]})", kind))
+            L.append((v, f"np.sqrt({a[0]})" if lang == "py" else f"DSL_FSQRT({a[0]})", kind))
         elif op == "abs":
             L.append((v, f"np.abs({a[0]})" if lang == "py" else f"fabs({a[0]})", kind))
         elif op in _CMP:
