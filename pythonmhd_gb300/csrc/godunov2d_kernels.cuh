@@ -28,8 +28,21 @@ constexpr int kBlock = 128;
 #ifndef MHD_MIN_BLOCKS
 #define MHD_MIN_BLOCKS 2
 #endif
-// resident blocks per SM the heavy FP64 kernels are compiled for (caps registers)
+#ifndef MHD_MIN_BLOCKS_SLOPES
+#define MHD_MIN_BLOCKS_SLOPES MHD_MIN_BLOCKS
+#endif
+#ifndef MHD_MIN_BLOCKS_FACES
+#define MHD_MIN_BLOCKS_FACES MHD_MIN_BLOCKS
+#endif
+#ifndef MHD_MIN_BLOCKS_ROE
+#define MHD_MIN_BLOCKS_ROE MHD_MIN_BLOCKS
+#endif
+// resident blocks per SM the heavy FP64 kernels are compiled for (caps registers):
+// the batched kernels, and per kernel the slope, face and Roe kernels of the single grid
 constexpr int kMinBlocks = MHD_MIN_BLOCKS;
+constexpr int kMinBlocksSlopes = MHD_MIN_BLOCKS_SLOPES;
+constexpr int kMinBlocksFaces = MHD_MIN_BLOCKS_FACES;
+constexpr int kMinBlocksRoe = MHD_MIN_BLOCKS_ROE;
 
 __device__ __forceinline__ int wrapc(int c, int L, int bc) {
   if (bc == PERIODIC) {
@@ -1185,15 +1198,15 @@ __global__ void k_begin(Grid G) { b_begin<PHYS>(G); }
 __global__ void k_end(Grid G) { b_end(G); }
 
 template <class S, int AX>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_ppm_slopes(Grid G, StateBuf in) {
+__global__ void __launch_bounds__(kBlock, kMinBlocksSlopes) k_ppm_slopes(Grid G, StateBuf in) {
   b_ppm_slopes<S, AX>(G, in, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 template <class S, int AX, int MODE>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_faces(Grid G, StateBuf in) {
+__global__ void __launch_bounds__(kBlock, kMinBlocksFaces) k_faces(Grid G, StateBuf in) {
   b_faces<S, AX, MODE>(G, in, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 template <int AX, int STAGE>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_roe_mhd(Grid G, StateBuf in) {
+__global__ void __launch_bounds__(kBlock, kMinBlocksRoe) k_roe_mhd(Grid G, StateBuf in) {
   b_roe_mhd<AX, STAGE>(G, in, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 template <int AX>
