@@ -375,7 +375,7 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
     typename S::Eig e;
     eig_at(e);
     const double* lam = S::lam(e);
-    const double dtdx = dt / dn;
+    const double dtdx = ddiv(dt, dn);
     double c1[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) c1[k] = ria[k] - lia[k];
@@ -439,7 +439,7 @@ __device__ __forceinline__ void edge_states(const double* wl, const double* wc, 
     typename S::Eig e;
     eig_at(e);
     const double* lam = S::lam(e);
-    const double dtdx = dt / dn;
+    const double dtdx = ddiv(dt, dn);
     double c1[NV], c2[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -565,7 +565,7 @@ __device__ __forceinline__ void b_faces(const Grid& G, const StateBuf& in, int x
   if (src) {
     const double* fb = AX == 0 ? in.fbx : in.fby;
     const double half_dt = 0.5 * dt;
-    const double inv_dn = 1.0 / dn;
+    const double inv_dn = ddiv(1.0, dn);
     s_mid = bsource<AX>(G, in.prim, fb, plane, c, c, c + 1, t, g.nx, half_dt, inv_dn);
     if (c == 0) {
       if (g.bc == OUTFLOW) s_lo = bsource<AX>(G, in.prim, fb, plane, 0, 0, 0, t, g.nx, half_dt, inv_dn);
@@ -735,8 +735,8 @@ __device__ __forceinline__ void b_ctu_mhd(const Grid& G, const StateBuf& in, siz
   const int bc = AX == 0 ? G.bcx : G.bcy;
   const double dt = G.loop->dt;
   const double half_dt = 0.5 * dt;
-  const double inv_dn = 1.0 / (AX == 0 ? G.dx : G.dy);
-  const double half_dtdt = 0.5 * (dt / (AX == 0 ? G.dy : G.dx));   // transverse
+  const double inv_dn = ddiv(1.0, AX == 0 ? G.dx : G.dy);
+  const double half_dtdt = 0.5 * ddiv(dt, AX == 0 ? G.dy : G.dx);   // transverse
   const size_t plane = cell_plane(G);
   const double* fb = AX == 0 ? in.fbx : in.fby;
   auto fbv = [&](int ff) -> double {
@@ -876,7 +876,7 @@ __device__ __forceinline__ void b_ctu_hydro(const Grid& G, size_t fl) {
   const int Ls = AX == 0 ? G.nx : G.ny;
   const int bc = AX == 0 ? G.bcx : G.bcy;
   const double dt = G.loop->dt;
-  const double half_dtdt = 0.5 * (dt / (AX == 0 ? G.dy : G.dx));
+  const double half_dtdt = 0.5 * ddiv(dt, AX == 0 ? G.dy : G.dx);
   double* Wout[2] = {AX == 0 ? G.xl : G.yl, AX == 0 ? G.xr : G.yr};
   const double* F = AX == 0 ? G.fy : G.fx;
   const size_t tfp = AX == 0 ? yface_plane(G) : xface_plane(G);
@@ -910,7 +910,7 @@ __device__ __forceinline__ void b_half_ez(const Grid& G, const StateBuf& in, int
   const int nx = G.nx;
   if (i >= nx || j >= G.ny) return;
   const double dt = G.loop->dt;
-  const double hx = 0.5 * (dt / G.dx), hy = 0.5 * (dt / G.dy);
+  const double hx = 0.5 * ddiv(dt, G.dx), hy = 0.5 * ddiv(dt, G.dy);
   const size_t plane = cell_plane(G), xfp = xface_plane(G), yfp = yface_plane(G);
   const size_t idx = (size_t)j * nx + i;
   const size_t xr = (size_t)j * (nx + 1) + i + 1, xlf = (size_t)j * (nx + 1) + i;
@@ -949,7 +949,7 @@ __device__ __forceinline__ void b_final_mhd(const Grid& G, const StateBuf& in, c
   const int nx = G.nx, ny = G.ny;
   if (i >= nx || j >= ny) return;
   const double dt = G.loop->dt;
-  const double dtdy = dt / G.dy, dtdx = dt / G.dx;
+  const double dtdy = ddiv(dt, G.dy), dtdx = ddiv(dt, G.dx);
   const size_t plane = cell_plane(G), xfp = xface_plane(G), yfp = yface_plane(G);
   const size_t idx = (size_t)j * nx + i;
   const size_t xlf = (size_t)j * (nx + 1) + i, xr = xlf + 1;
@@ -1023,7 +1023,7 @@ __device__ __forceinline__ void b_final_hydro(const Grid& G, const StateBuf& in,
   const int nx = G.nx;
   if (i >= nx || j >= G.ny) return;
   const double dt = G.loop->dt;
-  const double dtdx = dt / G.dx, dtdy = dt / G.dy;
+  const double dtdx = ddiv(dt, G.dx), dtdy = ddiv(dt, G.dy);
   const size_t plane = cell_plane(G), xfp = xface_plane(G), yfp = yface_plane(G);
   const size_t idx = (size_t)j * nx + i;
   const size_t xlf = (size_t)j * (nx + 1) + i, xr = xlf + 1;
@@ -1283,7 +1283,7 @@ __global__ void __launch_bounds__(kBlock) k_update_1d(Grid G, StateBuf in, State
   if (!G.loop->active) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= G.nx) return;
-  const double dtdx = G.loop->dt / G.dx;
+  const double dtdx = ddiv(G.loop->dt, G.dx);
   const size_t plane = cell_plane(G), fp = xface_plane(G);
   MHD_GUARD(G, in.cons, (size_t)i);
   MHD_GUARD(G, out.prim, (size_t)i);

@@ -195,8 +195,8 @@ __global__ void __launch_bounds__(kBlock) k3_ctu_hydro(Grid3 G) {
   const double dt = G.loop->dt;
   constexpr int E1 = D == 0 ? 1 : 0;
   constexpr int E2 = D == 2 ? 1 : 2;
-  const double h1 = 0.5 * (dt / G.d[E1]);
-  const double h2 = 0.5 * (dt / G.d[E2]);
+  const double h1 = 0.5 * ddiv(dt, G.d[E1]);
+  const double h2 = 0.5 * ddiv(dt, G.d[E2]);
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
     double* W = side == 0 ? G.wl[D] : G.wr[D];
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(kBlock) k3_final_hydro(Grid3 G, StateBuf3 in, 
   int c[3];
   unlin3<0, 0>(G, i, c);
   const double dt = G.loop->dt;
-  const double dtdx = dt / G.d[0], dtdy = dt / G.d[1], dtdz = dt / G.d[2];
+  const double dtdx = ddiv(dt, G.d[0]), dtdy = ddiv(dt, G.d[1]), dtdz = ddiv(dt, G.d[2]);
   double u[5], w[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {

@@ -187,7 +187,7 @@ __device__ __forceinline__ void b3_corr(const Grid3& G, const StateBuf3& in, con
                                         double dt, double out[2]) {
   using S = MhdSweep<D>;
   const int L = G.n[D];
-  const double nch = normal_change<D>(G, in.fb[D], p, e, bc, 1.0 / G.d[D], false, L);
+  const double nch = normal_change<D>(G, in.fb[D], p, e, bc, ddiv(1.0, G.d[D]), false, L);
   int q[3] = {p[0], p[1], p[2]};
   q[D] = wrapc(e, L, bc);
   const size_t cell = lin3<0, 0>(G, q);
@@ -196,7 +196,7 @@ __device__ __forceinline__ void b3_corr(const Grid3& G, const StateBuf3& in, con
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     const int a = (s == 0 ? S::T1 : S::T2) - 1;
-    const double tch = own_change_dyn(G, in.fb, a, q, 1.0 / G.d[a], false);
+    const double tch = own_change_dyn(G, in.fb, a, q, ddiv(1.0, G.d[a]), false);
     const double v = ddiv(__ldg(in.cons + (size_t)(1 + a) * plane + cell), dens);
     const double term = b3_limit(nch, tch, D == 1 && s == 0);
     out[s] = 0.5 * dt * (v * term);
@@ -412,9 +412,9 @@ __global__ void __launch_bounds__(kBlock) k3m_ct(Grid3 G, StateBuf3 in, StateBuf
   unlin3<D, 1>(G, i, p);
   const int x = p[0], y = p[1], z = p[2];
   const double dt = G.loop->dt;
-  const double h0 = FULL ? dt / G.d[0] : 0.5 * (dt / G.d[0]);
-  const double h1 = FULL ? dt / G.d[1] : 0.5 * (dt / G.d[1]);
-  const double h2 = FULL ? dt / G.d[2] : 0.5 * (dt / G.d[2]);
+  const double h0 = FULL ? ddiv(dt, G.d[0]) : 0.5 * ddiv(dt, G.d[0]);
+  const double h1 = FULL ? ddiv(dt, G.d[1]) : 0.5 * ddiv(dt, G.d[1]);
+  const double h2 = FULL ? ddiv(dt, G.d[2]) : 0.5 * ddiv(dt, G.d[2]);
   const double* ex = G.emf[0];
   const double* ey = G.emf[1];
   const double* ez = G.emf[2];
@@ -485,8 +485,8 @@ __global__ void __launch_bounds__(kBlock) k3m_ctu(Grid3 G, StateBuf3 in) {
   // (slot, sign) of each step's EMF term: x: (5, +), (4, -); y: (4, -), (5, +); z: (5, +), (4, -)
   constexpr int SL1 = D == 1 ? 4 : 5, SL2 = D == 1 ? 5 : 4;
   constexpr double SG1 = D == 1 ? -1.0 : 1.0, SG2 = D == 1 ? 1.0 : -1.0;
-  const double h1 = 0.5 * (dt / G.d[E1]);
-  const double h2 = 0.5 * (dt / G.d[E2]);
+  const double h1 = 0.5 * ddiv(dt, G.d[E1]);
+  const double h2 = 0.5 * ddiv(dt, G.d[E2]);
   // the source vector's changes: x with products by 1/dn, y and z with quotients by dn
   const bool divide = D != 0;
   const size_t n = cells3(G);
@@ -503,11 +503,11 @@ __global__ void __launch_bounds__(kBlock) k3m_ctu(Grid3 G, StateBuf3 in) {
     ctu3m_step<D, E2>(G, p, h2, SL2, SG2, u);
     // source vector of the sweep-extended cell e = f - 1 + side
     const int e = f - 1 + side;
-    const double hn = divide ? G.d[D] : 1.0 / G.d[D];
+    const double hn = divide ? G.d[D] : ddiv(1.0, G.d[D]);
     const double nch = normal_change<D>(G, in.fb[D], c, e, bc, hn, divide, D == 2 ? L - 1 : L);
     const int a = S::T1 - 1, b = S::T2 - 1;
-    const double ta = own_change_dyn(G, in.fb, a, p, divide ? G.d[a] : 1.0 / G.d[a], divide);
-    const double tb = own_change_dyn(G, in.fb, b, p, divide ? G.d[b] : 1.0 / G.d[b], divide);
+    const double ta = own_change_dyn(G, in.fb, a, p, divide ? G.d[a] : ddiv(1.0, G.d[a]), divide);
+    const double tb = own_change_dyn(G, in.fb, b, p, divide ? G.d[b] : ddiv(1.0, G.d[b]), divide);
     const size_t cell = lin3<0, 0>(G, p);
     const double bx = pr[4 * n + cell], by = pr[5 * n + cell], bz = pr[6 * n + cell];
     const double va = pr[(size_t)(1 + a) * n + cell], vb = pr[(size_t)(1 + b) * n + cell];
@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(kBlock) k3m_half_e(Grid3 G, StateBuf3 in) {
   int p[3];
   unlin3<0, 0>(G, i, p);
   const double dt = G.loop->dt;
-  const double hx = 0.5 * (dt / G.d[0]), hy = 0.5 * (dt / G.d[1]), hz = 0.5 * (dt / G.d[2]);
+  const double hx = 0.5 * ddiv(dt, G.d[0]), hy = 0.5 * ddiv(dt, G.d[1]), hz = 0.5 * ddiv(dt, G.d[2]);
   double h[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(kBlock) k3m_final(Grid3 G, StateBuf3 in, State
   int p[3];
   unlin3<0, 0>(G, i, p);
   const double dt = G.loop->dt;
-  const double dtdx = dt / G.d[0], dtdy = dt / G.d[1], dtdz = dt / G.d[2];
+  const double dtdx = ddiv(dt, G.d[0]), dtdy = ddiv(dt, G.d[1]), dtdz = ddiv(dt, G.d[2]);
   constexpr int src[7] = {0, 1, 2, 3, 5, 6, 7};
   double u[7];
 #pragma unroll

@@ -62,12 +62,13 @@ __device__ __forceinline__ double nsq(double x) { return __dmul_rn(x, x); }
 // binade of x/6 gives 6m - x = u (6k + 3 - x/u), an odd multiple of u, so
 // |x/6 - m| >= u/6 (and the boundary below the binade is u/4 away from it).  The
 // rounding of q0 + r z therefore equals that of x/6.  The argument needs x/6 and q0
-// in the normal range; other exponents (zeros, subnormals, huge values, inf, NaN)
-// take the IEEE division, which also keeps the sign of a zero.
+// in the normal range; a zero is returned as it is (+-0 / 6 = +-0), and other
+// exponents (subnormals, huge values, inf, NaN) take the IEEE division.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double div6(double x) {
   const unsigned int ex = ((unsigned int)__double2hiint(x) >> 20) & 0x7ffu;
-  if (ex - 24u > 1998u) return x / 6.0;
+  if (ex - 24u > 1998u)
+    return (static_cast<unsigned long long>(__double_as_longlong(x)) << 1) == 0ULL ? x : x / 6.0;
   const double z = 0.16666666666666666;   // RN(1/6)
   const double q0 = __dmul_rn(x, z);
   return __fma_rn(__fma_rn(-6.0, q0, x), z, q0);

@@ -262,7 +262,8 @@ SFP_FN double sub(double x, double y) { return add(x, from_bits(to_bits(y) ^ kSi
 //    computed exactly modulo 2^64 (it is below 3 my < 2^55) and two conditional steps
 //    correct Q0.
 // Fast path: normal operands and a normal result (biased exponent 1..2045 before a
-// rounding carry); everything else takes the FP64 division.
+// rounding carry), and a zero over a normal divisor; everything else takes the FP64
+// division.
 template <class Seed>
 SFP_FN double div_seeded(double x, double y, const Seed& seed) {
   const uint64_t a = to_bits(x), b = to_bits(y);
@@ -271,7 +272,11 @@ SFP_FN double div_seeded(double x, double y, const Seed& seed) {
   const uint64_t mx = (a & kFrac) | kHidden, my = (b & kFrac) | kHidden;
   const uint32_t lt = mx < my ? 1u : 0u;
   const uint32_t e = ex - ey + 1023u - lt;  // wraps below zero
-  if (ex - 1u > 2045u || ey - 1u > 2045u || e - 1u > 2044u) return hw_div(x, y);
+  if (ex - 1u > 2045u || ey - 1u > 2045u || e - 1u > 2044u) {
+    // a zero dividend over a normal divisor: a zero with the sign of the quotient
+    if ((a << 1) == 0u && ey - 1u <= 2045u) return from_bits((a ^ b) & kSign);
+    return hw_div(x, y);
+  }
   // seed: my's top 24 bits as a float (exact), its reciprocal, one FP32 Newton step
   const float f = u2f(static_cast<uint32_t>(my >> 29) - 0x800000u + (150u << 23));
   float r = seed.rcp(f);
@@ -316,13 +321,13 @@ SFP_FN double div_seeded(double x, double y, const Seed& seed) {
 //  * S0 = floor(K Y / 2^116) then lies within two of S from below; K - S0^2 is
 //    computed exactly modulo 2^64 (its magnitude is below 2^57) and two conditional
 //    steps correct S0.
-// Fast path: positive normal x; zeros, negative numbers, subnormals, infinities and
-// NaN take the FP64 square root.
+// Fast path: positive normal x, and zeros (returned as they are); negative numbers,
+// subnormals, infinities and NaN take the FP64 square root.
 template <class Seed>
 SFP_FN double sqrt_seeded(double x, const Seed& seed) {
   const uint64_t a = to_bits(x);
   const uint32_t ex = static_cast<uint32_t>(a >> 52);  // sign included: negative x fails below
-  if (ex - 1u > 2045u) return hw_sqrt(x);
+  if (ex - 1u > 2045u) return (a << 1) == 0u ? x : hw_sqrt(x);  // sqrt(+-0) = +-0
   const uint64_t mx = (a & kFrac) | kHidden;
   const uint32_t odd = (ex & 1u) ^ 1u;  // 1 when ex - 1023 is odd
   const uint64_t M = mx << odd;         // K = M 2^54, u = M / 2^52
