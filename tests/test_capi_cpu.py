@@ -84,6 +84,39 @@ def test_adjoint_entry_points_reject_bad_arguments(lib):
     lib.mhd2d_adj_destroy(None)
 
 
+def test_arithmetic_hooks_reject_bad_arguments_before_touching_the_device(lib):
+    # mhd_softfp: op 0..4 (add, subtract, multiply, divide, sqrt), n >= 0, pointers for n > 0
+    assert lib.mhd_softfp(5, None, None, None, 1) == 1
+    assert lib.mhd_softfp(-1, None, None, None, 1) == 1
+    assert lib.mhd_softfp(0, None, None, None, -1) == 1
+    assert lib.mhd_softfp(3, None, None, None, 4) == 1
+    assert lib.mhd_softfp(2, None, None, None, 0) == 0   # nothing to do: no launch
+    assert lib.mhd_quotient6(None, None, -1) == 1
+    assert lib.mhd_quotient6(None, None, 0) == 0
+
+
+def test_adjoint_codegen_places_the_integer_pipe_division_per_stage():
+    """The generated forward statements divide and take square roots on the integer pipes
+    only in the stages listed in ``codegen.INTEGER_PIPE_DIVSQRT`` (the small CT, half-step
+    and update stages, where that measured faster); the taped reconstruction and Roe
+    stages keep the FP64 instructions."""
+    from pythonmhd_gb300.adjoint import codegen
+    src = codegen.generate()
+    blocks = re.split(r"\n// ---- (\w+): ", src)[1:]
+    seen = {}
+    for name, body in zip(blocks[0::2], blocks[1::2]):
+        m = re.search(r"#define DSL_FDIV (\S+)\n#define DSL_FSQRT (\S+)", body)
+        assert m, name
+        seen[name] = m.groups()
+    assert set(seen) == {n for n, *_ in codegen.STAGES}
+    for name, (div, sq) in seen.items():
+        if name in codegen.INTEGER_PIPE_DIVSQRT:
+            assert (div, sq) == ("mhdk::ddiv", "mhdk::sqrt"), name
+        else:
+            assert (div, sq) == ("__ddiv_rn", "__dsqrt_rn"), name
+    assert {"roe1_0", "plm0", "pslope0", "ppmt0"}.isdisjoint(codegen.INTEGER_PIPE_DIVSQRT)
+
+
 def test_driver_time_precision_follows_the_reference_rule():
     from pythonmhd_gb300 import driver
     assert driver.time_precision(0.01, 0.5) == 2
