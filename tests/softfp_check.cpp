@@ -100,6 +100,21 @@ int main(int argc, char** argv) {
   const char* names[] = {"random bits", "moderate exponents", "close magnitudes", "exponent differences 0-70",
                          "runs of equal bits", "near overflow/underflow", "zeros, subnormals, specials",
                          "small integers and halves", "exact and near-tie quotients, squares"};
+  // fixed operands at known hard spots: halfway cases of the sum and product, rounding carries
+  // into the exponent, overflow and underflow thresholds, exact quotients and squares
+  {
+    const double e = std::ldexp(1.0, -52), m = 1.7976931348623157e308, tiny = std::ldexp(1.0, -1022);
+    const double fixed[] = {1.0, 1.0 + e, 1.0 - e / 2, 1.5, 2.0, 3.0, 1.0 / 3.0, 0.1, 0.2, 0.3, std::ldexp(1.0, -53),
+                            3 * std::ldexp(1.0, -53), m, m / 2, std::ldexp(1.0, 1023), tiny, tiny * (1 + e), 2 * tiny,
+                            std::ldexp(1.0, 511), std::ldexp(1.0, -511), std::ldexp(1.0 + e, 600),
+                            std::ldexp(1.0, -600), 0.0, -0.0, 4.0, 9.0, 1e-300, 1e300, -1.0, -(1.0 + e)};
+    const uint64_t before = mismatches;
+    for (double x : fixed)
+      for (double y : fixed) check(x, y);
+    std::printf("%-30s %llu pairs, %llu mismatches\n", "fixed hard operands",
+                (unsigned long long)(sizeof(fixed) / sizeof(fixed[0]) * (sizeof(fixed) / sizeof(fixed[0]))),
+                (unsigned long long)(mismatches - before));
+  }
   for (int g = 0; g < 9; ++g) {
     const uint64_t before = mismatches;
     for (uint64_t i = 0; i < n; ++i) {
